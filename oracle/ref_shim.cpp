@@ -1,0 +1,223 @@
+// Thin extern "C" shim over the reference library's own C++ API (giao::),
+// compiled together with the reference's hot-path sources by
+// oracle/build_ref.py.  Test infrastructure only: it lets the golden-vector
+// generator and the oracle checks call the reference implementation through
+// ctypes without pybind11.  Nothing in the product links it.
+//
+// Entry points mirror the reference bindings:
+//   ref_boys               <- src/bindings.cpp:444-482 (compute_boys)
+//   ref_primitive_eri      <- src/bindings.cpp:599-614 (primitive_eri)
+//   ref_eri_shell          <- src/bindings.cpp:616-639 (compute_eri)
+//   ref_eri_batch          <- src/bindings.cpp:672-731 (evaluate_eri_shell_quartets)
+//   ref_eri_full           <- src/bindings.cpp:640-671 (compute_eri_tensor)
+//   ref_schwarz            <- src/bindings.cpp:409-425 (EriSchwarzBounds)
+//   ref_cholesky_diagonal  <- src/bindings.cpp:2306-2314
+//   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
+#include "giao_integrals/boys.hpp"
+#include "giao_integrals/eri.hpp"
+#include "giao_integrals/types.hpp"
+#include "cholesky.hpp"
+
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <exception>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(const std::exception& e, int code) {
+    g_error = e.what();
+    return code;
+}
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (const giao::BoysNumericalError& e) {
+        return fail(e, -4);
+    } catch (const std::invalid_argument& e) {
+        return fail(e, -1);
+    } catch (const std::out_of_range& e) {
+        return fail(e, -2);
+    } catch (const std::length_error& e) {
+        return fail(e, -3);
+    } catch (const std::exception& e) {
+        return fail(e, -5);
+    }
+}
+
+giao::Basis make_basis(int ns, const double* centers, const int* ls,
+                       const int* nprims, const int* ncontrs,
+                       const double* exps, const double* coefs,
+                       const int* normalize) {
+    std::vector<giao::Shell> shells;
+    std::size_t e = 0, c = 0;
+    for (int s = 0; s < ns; ++s) {
+        std::vector<double> ex(exps + e, exps + e + nprims[s]);
+        std::vector<double> co(coefs + c, coefs + c + (std::size_t)nprims[s] * ncontrs[s]);
+        e += nprims[s];
+        c += (std::size_t)nprims[s] * ncontrs[s];
+        shells.emplace_back(giao::Vec3{centers[3 * s], centers[3 * s + 1], centers[3 * s + 2]},
+                            (std::uint16_t)ls[s], std::move(ex), std::move(co),
+                            (std::size_t)ncontrs[s],
+                            normalize[s] ? giao::ContractionNormalization::normalize
+                                         : giao::ContractionNormalization::as_provided);
+    }
+    return giao::Basis(std::move(shells));
+}
+
+giao::MagneticField make_field(const double* B, const double* O) {
+    return giao::MagneticField(giao::Vec3{B[0], B[1], B[2]}, giao::Vec3{O[0], O[1], O[2]});
+}
+
+struct Packer {
+    double* out;
+    std::size_t pos;
+};
+
+void pack_block(const giao::ShellQuartetBlockView& block, void* user) {
+    auto* p = static_cast<Packer*>(user);
+    std::memcpy(p->out + 2 * p->pos, block.values.data(), block.values.size() * sizeof(giao::Complex));
+    p->pos += block.values.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_error.c_str(); }
+
+int ref_boys(double zr, double zi, int nmax, int scaled, double* out, int* region,
+             double* est_error, long* segments) {
+    return guarded([&] {
+        std::vector<giao::Complex> v((std::size_t)nmax + 1);
+        auto d = giao::compute_boys({zr, zi}, v, scaled ? giao::BoysScaling::exp_z
+                                                         : giao::BoysScaling::unscaled);
+        std::memcpy(out, v.data(), v.size() * sizeof(giao::Complex));
+        *region = (int)d.region;
+        *est_error = d.estimated_absolute_error;
+        *segments = (long)d.quadrature_segments;
+    });
+}
+
+int ref_primitive_eri(const double* exps, const double* centers, const int* angular,
+                      const double* coefs, const int* normalized, const double* B,
+                      const double* O, double* out) {
+    return guarded([&] {
+        std::vector<giao::PrimitiveGaussian> p;
+        for (int i = 0; i < 4; ++i) {
+            p.emplace_back(exps[i], giao::Vec3{centers[3 * i], centers[3 * i + 1], centers[3 * i + 2]},
+                           giao::CartesianExponent{(std::uint16_t)angular[3 * i],
+                                                   (std::uint16_t)angular[3 * i + 1],
+                                                   (std::uint16_t)angular[3 * i + 2]},
+                           coefs[i], normalized[i] != 0);
+        }
+        auto v = giao::primitive_eri(p[0], p[1], p[2], p[3], make_field(B, O));
+        out[0] = v.real();
+        out[1] = v.imag();
+    });
+}
+
+int ref_shell_coefficients(int ns, const double* centers, const int* ls, const int* nprims,
+                           const int* ncontrs, const double* exps, const double* coefs,
+                           const int* normalize, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        std::size_t c = 0;
+        for (const auto& s : basis.shells()) {
+            for (double v : s.coefficients()) out[c++] = v;
+        }
+    });
+}
+
+int ref_eri_batch(int ns, const double* centers, const int* ls, const int* nprims,
+                  const int* ncontrs, const double* exps, const double* coefs,
+                  const int* normalize, const std::uint32_t* quartets, long nq,
+                  const double* B, const double* O, int threads, double screening,
+                  double* out, long* stats) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        auto field = make_field(B, O);
+        std::vector<giao::ShellQuartetIndex> q((std::size_t)nq);
+        for (long i = 0; i < nq; ++i) {
+            q[i] = {quartets[4 * i], quartets[4 * i + 1], quartets[4 * i + 2], quartets[4 * i + 3]};
+        }
+        std::vector<giao::EriSchwarzBounds> bounds;
+        if (screening > 0.0) bounds.emplace_back(basis, field);
+        Packer packer{out, 0};
+        auto st = giao::evaluate_eri_shell_quartets(
+            basis, q, field, {screening, (std::size_t)threads},
+            bounds.empty() ? nullptr : &bounds[0], pack_block, &packer);
+        stats[0] = (long)st.requested_quartets;
+        stats[1] = (long)st.computed_quartets;
+        stats[2] = (long)st.screened_quartets;
+    });
+}
+
+int ref_eri_full(int ns, const double* centers, const int* ls, const int* nprims,
+                 const int* ncontrs, const double* exps, const double* coefs,
+                 const int* normalize, const double* B, const double* O, int threads,
+                 double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        const std::size_t n = basis.ao_count();
+        auto span = std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out), n * n * n * n);
+        [[maybe_unused]] auto st =
+            giao::compute_eri_tensor(basis, make_field(B, O), {0.0, (std::size_t)threads}, nullptr, span);
+    });
+}
+
+int ref_schwarz(int ns, const double* centers, const int* ls, const int* nprims,
+                const int* ncontrs, const double* exps, const double* coefs,
+                const int* normalize, const double* B, const double* O, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        giao::EriSchwarzBounds b(basis, make_field(B, O));
+        std::memcpy(out, b.values().data(), b.values().size() * sizeof(double));
+    });
+}
+
+int ref_cholesky_diagonal(int ns, const double* centers, const int* ls, const int* nprims,
+                          const int* ncontrs, const double* exps, const double* coefs,
+                          const int* normalize, const long* pairs, long npairs,
+                          const double* B, const double* O, int threads, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        std::vector<std::array<std::size_t, 2>> p((std::size_t)npairs);
+        for (long i = 0; i < npairs; ++i) p[i] = {(std::size_t)pairs[2 * i], (std::size_t)pairs[2 * i + 1]};
+        const std::size_t n = basis.ao_count();
+        giao::detail::cholesky_diagonal(basis, p, make_field(B, O), std::span<double>(out, n * n),
+                                        (std::size_t)threads);
+    });
+}
+
+int ref_cholesky_columns(int ns, const double* centers, const int* ls, const int* nprims,
+                         const int* ncontrs, const double* exps, const double* coefs,
+                         const int* normalize, const long* pivots, long npiv,
+                         const double* B, const double* O, int threads, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        std::vector<std::array<std::size_t, 2>> p((std::size_t)npiv);
+        for (long i = 0; i < npiv; ++i) p[i] = {(std::size_t)pivots[2 * i], (std::size_t)pivots[2 * i + 1]};
+        const std::size_t n = basis.ao_count();
+        auto field = make_field(B, O);
+        if (B[0] == 0.0 && B[1] == 0.0 && B[2] == 0.0) {
+            giao::detail::cholesky_columns(basis, p, field, std::span<double>(out, p.size() * n * n),
+                                           (std::size_t)threads);
+        } else {
+            giao::detail::cholesky_columns(
+                basis, p, field,
+                std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out), p.size() * n * n),
+                (std::size_t)threads);
+        }
+    });
+}
+
+}  // extern "C"
