@@ -1,0 +1,180 @@
+"""ctypes binding of ``libgiao_gb300.so`` (the C ABI of include/giao_gb300.h).
+
+There is no CPU fallback: every compute entry point runs on the GPU through
+this library, and a missing library or device raises immediately.  Host-only
+entry points (shell normalisation) work without a GPU.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+_i64 = ctypes.POINTER(ctypes.c_int64)
+_u32 = ctypes.POINTER(ctypes.c_uint32)
+_vp = ctypes.c_void_p
+
+
+class BoysNumericalError(RuntimeError):
+    """Complex Boys evaluation outside the verified domain (giao::BoysNumericalError)."""
+
+
+class GxStats(ctypes.Structure):
+    _fields_ = [
+        ("requested", ctypes.c_int64),
+        ("computed", ctypes.c_int64),
+        ("screened", ctypes.c_int64),
+        ("primitive_quartets", ctypes.c_int64),
+        ("fp32_primitive_quartets", ctypes.c_int64),
+        ("skipped_primitive_quartets", ctypes.c_int64),
+        ("kernel_ms", ctypes.c_double),
+    ]
+
+
+class GxCholeskyOptions(ctypes.Structure):
+    _fields_ = [
+        ("threshold", ctypes.c_double),
+        ("screening_threshold", ctypes.c_double),
+        ("max_rank", ctypes.c_int64),
+        ("pivot_batch_size", ctypes.c_int),
+    ]
+
+
+# name -> (restype, argtypes); every symbol of include/giao_gb300.h
+SIGNATURES = {
+    "gx_context_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    "gx_context_destroy": (None, [_vp]),
+    "gx_last_error": (ctypes.c_char_p, []),
+    "gx_version": (ctypes.c_char_p, []),
+    "gx_primitive_normalization": (ctypes.c_double, [ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "gx_shell_normalize": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, ctypes.c_int, _d]),
+    "gx_basis_create": (ctypes.c_int, [_vp, ctypes.c_int, _d, _i, _i, _i, _d, _d, _i, ctypes.POINTER(_vp)]),
+    "gx_basis_destroy": (None, [_vp]),
+    "gx_basis_ao_count": (ctypes.c_int64, [_vp]),
+    "gx_boys": (ctypes.c_int, [_vp, _d, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _d, _i]),
+    "gx_primitive_eri": (ctypes.c_int, [_vp, _d, _d, _i, _d, _i, _d, _d, _d]),
+    "gx_eri_batch": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, _u32, _i64, _d, ctypes.c_int64, ctypes.POINTER(GxStats)]),
+    "gx_eri_batch_device": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, _u32, _i64, _vp, ctypes.c_int64,
+                                           ctypes.POINTER(GxStats)]),
+    "gx_eri_shell": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d]),
+    "gx_eri_full": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]),
+    "gx_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d]),
+    "gx_cholesky_diagonal": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
+    "gx_cholesky_columns": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
+    "gx_cholesky": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.POINTER(GxCholeskyOptions), _d, _i64, _i64, _d]),
+    "gx_context_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "gx_context_synchronize": (ctypes.c_int, [_vp]),
+    "gx_eri_plan_create": (ctypes.c_int, [_vp, _vp, _u32, ctypes.c_int64, _i64, ctypes.POINTER(_vp)]),
+    "gx_eri_plan_info": (ctypes.c_int, [_vp, _i64, _i64, _d, _i]),
+    "gx_eri_plan_execute": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp]),
+    "gx_eri_plan_destroy": (None, [_vp]),
+    "gx_measure_fp64_peak": (ctypes.c_int, [_vp, _d]),
+    "gx_canonical_quartets": (ctypes.c_int64, [ctypes.c_int, _u32]),
+}
+
+_lib: ctypes.CDLL | None = None
+_lock = threading.Lock()
+
+
+def library_path() -> Path:
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    """Load the library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not LIB.exists():
+                from .build import build
+
+                build()
+            handle = ctypes.CDLL(str(LIB))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().gx_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int) -> None:
+    """Raise the reference's exception type for a gx_status code."""
+    if rc == 0:
+        return
+    msg = last_error()
+    if rc in (-1, -3):
+        raise ValueError(msg)
+    if rc == -2:
+        raise IndexError(msg)
+    if rc == -4:
+        raise BoysNumericalError(msg)
+    if rc == -6:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)
+
+
+class Context:
+    """One CUDA device with its Boys table and pools (gx_context)."""
+
+    def __init__(self, device: int = 0):
+        handle = _vp()
+        check(lib().gx_context_create(device, ctypes.byref(handle)))
+        self.handle = handle
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().gx_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default: Context | None = None
+
+
+def default_context() -> Context:
+    """The process-wide context on CUDA device 0 (created on first use)."""
+    global _default
+    if _default is None:
+        with _lock:
+            if _default is None:
+                _default = Context(0)
+    return _default
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(_d)
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(_i)
+
+
+def i64ptr(a: np.ndarray):
+    return a.ctypes.data_as(_i64)
+
+
+def u32ptr(a: np.ndarray):
+    return a.ctypes.data_as(_u32)

@@ -1,0 +1,1512 @@
+// Host side of the GB300 electron-repulsion library: the C ABI declared in
+// include/giao_gb300.h.  Owns the device context (stream, Boys table, pools),
+// uploads bases, builds the per-(basis, field) primitive-pair records, plans
+// class-sorted quartet launches and maps device status words to the
+// reference's error semantics.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/giao_gb300.h"
+#include "gx_internal.h"
+
+using gx::c2;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+    g_error = msg;
+    return code;
+}
+
+struct CudaFailure {
+    cudaError_t err;
+    const char* where;
+};
+
+#define GX_CUDA(call)                                    \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) throw CudaFailure{e_, #call}; \
+    } while (0)
+
+struct ApiError {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void raise(int code, const std::string& msg) { throw ApiError{code, msg}; }
+
+template <typename F>
+int guarded(F&& f) {
+    try {
+        f();
+        return GX_OK;
+    } catch (const ApiError& e) {
+        return fail(e.code, e.msg);
+    } catch (const CudaFailure& e) {
+        return fail(GX_ECUDA, std::string("CUDA error in ") + e.where + ": " + cudaGetErrorString(e.err));
+    } catch (const std::bad_alloc&) {
+        return fail(GX_ENOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(GX_EINVAL, e.what());
+    }
+}
+
+// Grow-only device buffer.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    void reserve(size_t n) {
+        if (n <= bytes) return;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        const size_t want = std::max<size_t>(n, 256);
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            raise(GX_ENOMEM, "device allocation of " + std::to_string(want) + " bytes failed");
+        }
+        bytes = want;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(ptr);
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    ~DeviceBuffer() { release(); }
+};
+
+template <typename T>
+void upload(DeviceBuffer& buf, const std::vector<T>& v, cudaStream_t s) {
+    buf.reserve(sizeof(T) * std::max<size_t>(v.size(), 1));
+    if (!v.empty()) GX_CUDA(cudaMemcpyAsync(buf.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s));
+}
+
+// ---- host-side normalisation (src/types.cpp:20-72, 136-157) ---------------
+
+double log_odd_double_factorial(int l) {
+    if (l == 0) return 0.0;
+    const double n = (double)l;
+    return n * std::log(2.0) + std::lgamma(n + 0.5) - 0.5 * std::log(M_PI);
+}
+
+double primitive_norm(double a, int lx, int ly, int lz) {
+    const double total = (double)(lx + ly + lz);
+    const double den = log_odd_double_factorial(lx) + log_odd_double_factorial(ly) + log_odd_double_factorial(lz);
+    return std::exp(0.75 * std::log(2.0 * a / M_PI) + 0.5 * (total * std::log(4.0 * a) - den));
+}
+
+double same_center_overlap(double a, double b, int l) {
+    const double norm = primitive_norm(a, l, 0, 0) * primitive_norm(b, l, 0, 0);
+    const double p = a + b;
+    return norm * std::exp(std::lgamma(l + 0.5) - (l + 0.5) * std::log(p)) * M_PI / p;
+}
+
+// Gauss-Legendre nodes (Newton iteration on P_n).
+void gauss_legendre(int n, double* x, double* w) {
+    for (int i = 0; i < n / 2; ++i) {
+        double root = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+        double deriv = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = root;
+            for (int k = 2; k <= n; ++k) {
+                const double p2 = ((2.0 * k - 1.0) * root * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            deriv = n * (root * p1 - p0) / (root * root - 1.0);
+            const double upd = p1 / deriv;
+            root -= upd;
+            if (std::fabs(upd) < 1e-16) break;
+        }
+        const double wt = 2.0 / ((1.0 - root * root) * deriv * deriv);
+        x[i] = -root;
+        x[n - 1 - i] = root;
+        w[i] = wt;
+        w[n - 1 - i] = wt;
+    }
+}
+
+// ---- pair classes -----------------------------------------------------------
+
+struct PairClassHost {
+    int la, lb, nab, Etot;
+    std::vector<int> boxoff, boxdim;
+    std::vector<uint32_t> ent;
+    DeviceBuffer d_boxoff, d_boxdim, d_ent;
+    gx::PairClassDev dev() const {
+        return gx::PairClassDev{la, lb, nab, la + lb, Etot, d_boxoff.as<int>(), d_boxdim.as<int>(),
+                                d_ent.as<uint32_t>()};
+    }
+};
+
+std::vector<std::array<int, 3>> components(int l) {
+    std::vector<std::array<int, 3>> c;
+    for (int x = l; x >= 0; --x)
+        for (int y = l - x; y >= 0; --y) c.push_back({x, y, l - x - y});
+    return c;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+
+struct gx_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    double boys_table_agreement = 0.0;
+    DeviceBuffer boys_S, boys_E0, gl, herm, status;
+    std::mutex mu;
+    std::map<std::pair<int, int>, std::unique_ptr<PairClassHost>> pair_classes;
+    // scratch
+    DeviceBuffer out, tasks, scratch_a, scratch_b, scratch_c;
+
+    PairClassHost& pair_class(int la, int lb) {
+        auto key = std::make_pair(la, lb);
+        auto it = pair_classes.find(key);
+        if (it != pair_classes.end()) return *it->second;
+        auto pc = std::make_unique<PairClassHost>();
+        pc->la = la;
+        pc->lb = lb;
+        const auto ca = components(la), cb = components(lb);
+        pc->nab = (int)(ca.size() * cb.size());
+        int off = 0;
+        for (const auto& a : ca)
+            for (const auto& b : cb) {
+                const int bx = a[0] + b[0] + 1, by = a[1] + b[1] + 1, bz = a[2] + b[2] + 1;
+                pc->boxoff.push_back(off);
+                pc->boxdim.push_back(bx | (by << 8) | (bz << 16));
+                for (int k = 0; k < bx; ++k)
+                    for (int l = 0; l < by; ++l)
+                        for (int m = 0; m < bz; ++m) pc->ent.push_back((uint32_t)(k | (l << 8) | (m << 16)));
+                off += bx * by * bz;
+            }
+        pc->Etot = off;
+        upload(pc->d_boxoff, pc->boxoff, stream);
+        upload(pc->d_boxdim, pc->boxdim, stream);
+        upload(pc->d_ent, pc->ent, stream);
+        auto& ref = *pc;
+        pair_classes.emplace(key, std::move(pc));
+        return ref;
+    }
+
+    gx::BoysTable boys() const { return gx::BoysTable{boys_S.as<double2>(), boys_E0.as<double2>()}; }
+
+    void reset_status() { GX_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(gx::DevStatus), stream)); }
+
+    gx::DevStatus read_status() {
+        gx::DevStatus st;
+        GX_CUDA(cudaMemcpyAsync(&st, status.ptr, sizeof st, cudaMemcpyDeviceToHost, stream));
+        GX_CUDA(cudaStreamSynchronize(stream));
+        return st;
+    }
+};
+
+namespace {
+
+std::string boys_domain_message(double zr, double zi, int order) {
+    char buf[320];
+    std::snprintf(buf, sizeof buf,
+                  "complex Boys argument (%.17g,%.17g) at order %d is outside the verified direct domain |z| <= 160 "
+                  "and the conservative large-positive asymptotic sector",
+                  zr, zi, order);
+    return buf;
+}
+
+void check_status(gx_context* ctx) {
+    const gx::DevStatus st = ctx->read_status();
+    if (st.code == 0) return;
+    if (st.code == -4) raise(GX_EBOYS, boys_domain_message(st.zr, st.zi, st.order));
+    if (st.code == -40) raise(GX_EBOYS, "requested Boys scaling is not representable for this argument");
+    raise(GX_ECUDA, "device status " + std::to_string(st.code));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// basis
+// ---------------------------------------------------------------------------
+
+struct FieldPairs {
+    double B[3], O[3];
+    DeviceBuffer p, Pr, Pi, F, Epool, bound;
+};
+
+struct gx_basis {
+    gx_context* ctx = nullptr;
+    int ns = 0;
+    std::vector<double> center;
+    std::vector<int> l, nprim, ncontr;
+    std::vector<double> exps, coefs;
+    std::vector<int> raw;
+    std::vector<int64_t> ao_off;
+    int64_t nao = 0;
+    // segmented shells: shell s, contraction x -> seg_first[s] + x
+    int nseg = 0;
+    std::vector<int> seg_first, seg_l, seg_nprim, seg_primoff, seg_raw, seg_orig;
+    std::vector<double> seg_center, seg_exps, seg_coefs;
+    DeviceBuffer d_center, d_l, d_nprim, d_primoff, d_exps, d_coefs, d_raw, d_sp_off;
+    // pair structure (field independent)
+    int npp = 0;
+    std::vector<int> sp_off, pp_class;
+    std::vector<long long> Eoff;
+    long long Etotal = 0;
+    DeviceBuffer d_pp_a, d_pp_b, d_pp_pa, d_pp_pb, d_pp_class, d_Eoff, d_classes;
+    std::vector<std::pair<int, int>> class_keys;
+    std::unique_ptr<FieldPairs> pairs;
+
+    gx::BasisDev dev() const {
+        return gx::BasisDev{nseg, d_center.as<double>(), d_l.as<int>(), d_nprim.as<int>(), d_primoff.as<int>(),
+                            d_exps.as<double>(), d_coefs.as<double>(), d_raw.as<int>(), d_sp_off.as<int>()};
+    }
+    int ncart_of(int s) const { return gx::ncart(l[s]); }
+    int64_t nao_of(int s) const { return (int64_t)ncontr[s] * ncart_of(s); }
+};
+
+namespace {
+
+void build_segments(gx_basis* b) {
+    cudaStream_t s = b->ctx->stream;
+    b->seg_first.assign(b->ns, 0);
+    size_t e = 0, c = 0;
+    for (int sh = 0; sh < b->ns; ++sh) {
+        b->seg_first[sh] = b->nseg;
+        for (int x = 0; x < b->ncontr[sh]; ++x) {
+            b->seg_l.push_back(b->l[sh]);
+            b->seg_nprim.push_back(b->nprim[sh]);
+            b->seg_primoff.push_back((int)b->seg_exps.size());
+            b->seg_raw.push_back(b->raw[sh]);
+            b->seg_orig.push_back(sh);
+            for (int k = 0; k < 3; ++k) b->seg_center.push_back(b->center[3 * sh + k]);
+            for (int p = 0; p < b->nprim[sh]; ++p) {
+                b->seg_exps.push_back(b->exps[e + p]);
+                b->seg_coefs.push_back(b->coefs[c + (size_t)x * b->nprim[sh] + p]);
+            }
+            ++b->nseg;
+        }
+        e += b->nprim[sh];
+        c += (size_t)b->nprim[sh] * b->ncontr[sh];
+    }
+    upload(b->d_center, b->seg_center, s);
+    upload(b->d_l, b->seg_l, s);
+    upload(b->d_nprim, b->seg_nprim, s);
+    upload(b->d_primoff, b->seg_primoff, s);
+    upload(b->d_exps, b->seg_exps, s);
+    upload(b->d_coefs, b->seg_coefs, s);
+    upload(b->d_raw, b->seg_raw, s);
+    // every ordered segmented shell pair, primitive pairs pa-major
+    const int ns = b->nseg;
+    std::map<std::pair<int, int>, int> cls;
+    std::vector<int> pp_a, pp_b, pp_pa, pp_pb;
+    b->sp_off.assign((size_t)ns * ns, 0);
+    for (int a = 0; a < ns; ++a)
+        for (int bb = 0; bb < ns; ++bb) {
+            b->sp_off[(size_t)a * ns + bb] = (int)pp_a.size();
+            auto key = std::make_pair(b->seg_l[a], b->seg_l[bb]);
+            auto it = cls.find(key);
+            int ci;
+            if (it == cls.end()) {
+                ci = (int)b->class_keys.size();
+                cls.emplace(key, ci);
+                b->class_keys.push_back(key);
+            } else {
+                ci = it->second;
+            }
+            const PairClassHost& pc = b->ctx->pair_class(key.first, key.second);
+            for (int pa = 0; pa < b->seg_nprim[a]; ++pa)
+                for (int pb = 0; pb < b->seg_nprim[bb]; ++pb) {
+                    pp_a.push_back(a);
+                    pp_b.push_back(bb);
+                    pp_pa.push_back(pa);
+                    pp_pb.push_back(pb);
+                    b->pp_class.push_back(ci);
+                    b->Eoff.push_back(b->Etotal);
+                    b->Etotal += pc.Etot;
+                }
+        }
+    b->npp = (int)pp_a.size();
+    upload(b->d_sp_off, b->sp_off, s);
+    upload(b->d_pp_a, pp_a, s);
+    upload(b->d_pp_b, pp_b, s);
+    upload(b->d_pp_pa, pp_pa, s);
+    upload(b->d_pp_pb, pp_pb, s);
+    upload(b->d_pp_class, b->pp_class, s);
+    upload(b->d_Eoff, b->Eoff, s);
+    std::vector<gx::PairClassDev> devs;
+    for (const auto& k : b->class_keys) devs.push_back(b->ctx->pair_class(k.first, k.second).dev());
+    upload(b->d_classes, devs, s);
+}
+
+// Primitive-pair records for (B, O); cached on the basis for the last field.
+FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
+    if (b->pairs && std::memcmp(b->pairs->B, B, sizeof(double) * 3) == 0 &&
+        std::memcmp(b->pairs->O, O, sizeof(double) * 3) == 0)
+        return *b->pairs;
+    if (!b->pairs) b->pairs = std::make_unique<FieldPairs>();
+    FieldPairs& fp = *b->pairs;
+    std::memcpy(fp.B, B, sizeof fp.B);
+    std::memcpy(fp.O, O, sizeof fp.O);
+    const size_t n = std::max(b->npp, 1);
+    fp.p.reserve(n * sizeof(double));
+    fp.Pr.reserve(3 * n * sizeof(double));
+    fp.Pi.reserve(3 * n * sizeof(double));
+    fp.F.reserve(n * sizeof(double2));
+    fp.bound.reserve(n * sizeof(double));
+    fp.Epool.reserve(std::max<long long>(b->Etotal, 1) * sizeof(double2));
+    GX_CUDA(gx::launch_pair_precompute(b->dev(), B, O, b->npp, b->d_pp_a.as<int>(), b->d_pp_b.as<int>(),
+                                       b->d_pp_pa.as<int>(), b->d_pp_pb.as<int>(), b->d_pp_class.as<int>(),
+                                       b->d_classes.as<gx::PairClassDev>(), fp.p.as<double>(), fp.Pr.as<double>(),
+                                       fp.Pi.as<double>(), fp.F.as<double2>(), b->d_Eoff.as<long long>(),
+                                       fp.Epool.as<double2>(), fp.bound.as<double>(), b->ctx->stream));
+    return fp;
+}
+
+void check_field(const double* B, const double* O) {
+    for (int k = 0; k < 3; ++k) {
+        if (!std::isfinite(B[k])) raise(GX_EINVAL, "B values must be finite");
+        if (!std::isfinite(O[k])) raise(GX_EINVAL, "gauge_origin values must be finite");
+    }
+}
+
+// ---- quartet evaluation ------------------------------------------------------
+
+struct QuartetRequest {
+    uint32_t a, b, c, d;   // original shells
+    int64_t out_off;       // complex-element offset of the block
+};
+
+// Class-sorted task list for a set of quartet blocks (field independent).
+struct PlanClass {
+    std::array<int, 4> key;
+    size_t first, count;
+    int64_t primitive_quartets;
+};
+
+struct PlanData {
+    DeviceBuffer tasks;
+    std::vector<PlanClass> classes;
+    int64_t ntask = 0, primitive_quartets = 0;
+    double model_flops = 0.0;
+};
+
+// FP64 FLOP model per primitive quartet of class (la, lb, lc, ld): the
+// reference-structured MD count (one complex FMA per six-index R entry plus
+// the cheaper real-by-complex E.R.E ordering, coefficient accumulation and a
+// nominal Boys term).
+double model_flops(int la, int lb, int lc, int ld) {
+    const int Lab = la + lb, Lcd = lc + ld, L = Lab + Lcd;
+    auto T = [](int k) { return (double)(k + 1) * (k + 2) / 2.0; };
+    double R = 0.0;
+    for (int k = 0; k <= Lab; ++k)
+        for (int m = 0; m <= Lcd; ++m) R += T(k) * T(m) * (L - k - m + 1);
+    const double Nab = gx::herm_count(Lab), Ncd = gx::herm_count(Lcd);
+    const double nab = (double)gx::ncart(la) * gx::ncart(lb), ncd = (double)gx::ncart(lc) * gx::ncart(ld);
+    const double ere = std::min(4 * Nab * Ncd * ncd + 4 * nab * Nab * ncd, 4 * nab * Nab * Ncd + 4 * nab * Ncd * ncd);
+    return 8 * R + ere + 8 * nab * ncd + 8 * (L + 1);
+}
+
+void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
+    std::map<std::array<int, 4>, std::vector<gx::Task>> by_class;
+    std::map<std::array<int, 4>, int64_t> prims;
+    for (const auto& r : req) {
+        const int sh[4] = {(int)r.a, (int)r.b, (int)r.c, (int)r.d};
+        int64_t N[4];
+        int nc[4];
+        for (int k = 0; k < 4; ++k) {
+            N[k] = b->nao_of(sh[k]);
+            nc[k] = b->ncart_of(sh[k]);
+        }
+        const std::array<int, 4> key{b->l[sh[0]], b->l[sh[1]], b->l[sh[2]], b->l[sh[3]]};
+        if (key[0] + key[1] + key[2] + key[3] > 32)
+            raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
+        const int st0 = (int)(N[1] * N[2] * N[3]), st1 = (int)(N[2] * N[3]), st2 = (int)N[3];
+        auto& vec = by_class[key];
+        auto& np = prims[key];
+        for (int xa = 0; xa < b->ncontr[sh[0]]; ++xa)
+            for (int xb = 0; xb < b->ncontr[sh[1]]; ++xb)
+                for (int xc = 0; xc < b->ncontr[sh[2]]; ++xc)
+                    for (int xd = 0; xd < b->ncontr[sh[3]]; ++xd) {
+                        gx::Task t;
+                        t.sa = b->seg_first[sh[0]] + xa;
+                        t.sb = b->seg_first[sh[1]] + xb;
+                        t.sc = b->seg_first[sh[2]] + xc;
+                        t.sd = b->seg_first[sh[3]] + xd;
+                        t.out_off = r.out_off + (int64_t)xa * nc[0] * st0 + (int64_t)xb * nc[1] * st1 +
+                                    (int64_t)xc * nc[2] * st2 + (int64_t)xd * nc[3];
+                        t.st[0] = st0;
+                        t.st[1] = st1;
+                        t.st[2] = st2;
+                        t.st[3] = 1;
+                        vec.push_back(t);
+                        np += (int64_t)b->seg_nprim[t.sa] * b->seg_nprim[t.sb] * b->seg_nprim[t.sc] *
+                              b->seg_nprim[t.sd];
+                    }
+    }
+    std::vector<gx::Task> all;
+    plan.classes.clear();
+    plan.primitive_quartets = 0;
+    plan.model_flops = 0.0;
+    for (auto& kv : by_class) {
+        const auto& k = kv.first;
+        const int64_t np = prims[k];
+        plan.classes.push_back({k, all.size(), kv.second.size(), np});
+        plan.primitive_quartets += np;
+        plan.model_flops += (double)np * model_flops(k[0], k[1], k[2], k[3]);
+        all.insert(all.end(), kv.second.begin(), kv.second.end());
+    }
+    plan.ntask = (int64_t)all.size();
+    upload(plan.tasks, all, ctx->stream);
+}
+
+// Enqueue the pair records for (B, O) and every class launch; no host sync.
+int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
+                 double2* out) {
+    cudaStream_t s = ctx->stream;
+    FieldPairs& fp = field_pairs(b, B, O);
+    gx::EriDev dev;
+    dev.basis = b->dev();
+    dev.pairs = gx::PairData{b->npp,           fp.p.as<double>(),        fp.Pr.as<double>(),
+                             fp.Pi.as<double>(), fp.F.as<double2>(),      b->d_Eoff.as<long long>(),
+                             fp.Epool.as<double2>(), fp.bound.as<double>()};
+    dev.boys = ctx->boys();
+    dev.gl = ctx->gl.as<gx::GLRules>();
+    dev.herm_xyz = ctx->herm.as<uint32_t>();
+    dev.out = out;
+    dev.status = ctx->status.as<gx::DevStatus>();
+    ctx->reset_status();
+    int launches = 1;
+    for (const auto& pc : plan.classes) {
+        const auto& k = pc.key;
+        gx::QuartetClass qc;
+        qc.bra = ctx->pair_class(k[0], k[1]).dev();
+        qc.ket = ctx->pair_class(k[2], k[3]).dev();
+        qc.L = k[0] + k[1] + k[2] + k[3];
+        qc.Nab = gx::herm_count(k[0] + k[1]);
+        qc.NL = gx::herm_count(qc.L);
+        const int ncd = qc.ket.nab;
+        qc.CH = std::max(1, std::min(ncd, 2048 / qc.Nab));
+        int B1 = 32;
+        while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
+        qc.B1 = B1;
+        qc.ntask = (int)pc.count;
+        qc.tasks = plan.tasks.as<gx::Task>() + pc.first;
+        const size_t per_warp = gx::quartet_smem_bytes(qc, 1);
+        int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
+        const int grid = (qc.ntask + wpb - 1) / wpb;
+        GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
+        ++launches;
+    }
+    return launches;
+}
+
+// Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
+// index = contraction * ncart + component) and wait for them.
+void run_quartets(gx_context* ctx, gx_basis* b, const double* B, const double* O,
+                  const std::vector<QuartetRequest>& req, double2* out, float* kernel_ms,
+                  int64_t* primitive_quartets = nullptr) {
+    cudaStream_t s = ctx->stream;
+    PlanData plan;
+    build_plan(ctx, b, req, plan);
+    if (primitive_quartets) *primitive_quartets = plan.primitive_quartets;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (kernel_ms) {
+        GX_CUDA(cudaEventCreate(&e0));
+        GX_CUDA(cudaEventCreate(&e1));
+        GX_CUDA(cudaEventRecord(e0, s));
+    }
+    execute_plan(ctx, b, B, O, plan, out);
+    if (kernel_ms) {
+        GX_CUDA(cudaEventRecord(e1, s));
+        GX_CUDA(cudaEventSynchronize(e1));
+        GX_CUDA(cudaEventElapsedTime(kernel_ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    check_status(ctx);
+}
+
+void validate_quartets(const gx_basis* b, const uint32_t* q, int64_t nq) {
+    for (int64_t i = 0; i < 4 * nq; ++i)
+        if (q[i] >= (uint32_t)b->ns) raise(GX_ERANGE, "ERI shell-quartet index is out of range");
+}
+
+std::vector<double> schwarz_values(gx_context* ctx, gx_basis* b, const double* B, const double* O) {
+    // (ab|ba) blocks for a <= b, then Q_ab = nextafter(sqrt(max |(ij|ji)|)(1 + 64 eps))
+    std::vector<QuartetRequest> req;
+    int64_t off = 0;
+    for (int a = 0; a < b->ns; ++a)
+        for (int c = a; c < b->ns; ++c) {
+            req.push_back({(uint32_t)a, (uint32_t)c, (uint32_t)c, (uint32_t)a, off});
+            off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
+        }
+    ctx->scratch_a.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
+    run_quartets(ctx, b, B, O, req, ctx->scratch_a.as<double2>(), nullptr);
+    std::vector<std::complex<double>> host(off);
+    if (off) GX_CUDA(cudaMemcpy(host.data(), ctx->scratch_a.ptr, off * sizeof(double2), cudaMemcpyDeviceToHost));
+    std::vector<double> q((size_t)b->ns * b->ns, 0.0);
+    size_t r = 0;
+    for (int a = 0; a < b->ns; ++a)
+        for (int c = a; c < b->ns; ++c, ++r) {
+            const int64_t na = b->nao_of(a), nb = b->nao_of(c);
+            const std::complex<double>* blk = host.data() + req[r].out_off;
+            double m = 0.0;
+            for (int64_t i = 0; i < na; ++i)
+                for (int64_t j = 0; j < nb; ++j) m = std::max(m, std::abs(blk[((i * nb + j) * nb + j) * na + i]));
+            const double v = std::nextafter(std::sqrt(m) * (1.0 + 64.0 * 2.220446049250313e-16), INFINITY);
+            q[(size_t)a * b->ns + c] = v;
+            q[(size_t)c * b->ns + a] = v;
+        }
+    return q;
+}
+
+int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
+                   int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
+                   int64_t* offsets, void* out, bool out_is_device, int64_t capacity, gx_eri_stats* stats) {
+    (void)precision;
+    (void)mixed_cutoff;
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        if (!std::isfinite(screening) || screening < 0.0)
+            raise(GX_EINVAL, "ERI screening threshold must be finite and non-negative");
+        validate_quartets(b, quartets, nq);
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        std::vector<double> q;
+        if (screening > 0.0) q = schwarz_values(ctx, b, B, O);
+        std::vector<QuartetRequest> req;
+        req.reserve((size_t)nq);
+        int64_t off = 0, screened = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* x = quartets + 4 * i;
+            if (screening > 0.0 &&
+                q[(size_t)x[0] * b->ns + x[1]] * q[(size_t)x[2] * b->ns + x[3]] < screening) {
+                ++screened;
+                continue;
+            }
+            if (kept) std::memcpy(kept + 4 * req.size(), x, 4 * sizeof(uint32_t));
+            offsets[req.size()] = off;
+            req.push_back({x[0], x[1], x[2], x[3], off});
+            off += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+        }
+        offsets[req.size()] = off;
+        if (off > capacity) raise(GX_ELENGTH, "ERI output buffer is too small");
+        double2* dout;
+        if (out_is_device) {
+            dout = static_cast<double2*>(out);
+        } else {
+            ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
+            dout = ctx->out.as<double2>();
+        }
+        float ms = 0.f;
+        int64_t nprim = 0;
+        if (!req.empty()) run_quartets(ctx, b, B, O, req, dout, &ms, &nprim);
+        if (!out_is_device && off)
+            GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (stats) {
+            stats->requested = nq;
+            stats->computed = (int64_t)req.size();
+            stats->screened = screened;
+            stats->primitive_quartets = nprim;
+            stats->fp32_primitive_quartets = 0;
+            stats->skipped_primitive_quartets = 0;
+            stats->kernel_ms = ms;
+        }
+    });
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* gx_last_error(void) { return g_error.c_str(); }
+const char* gx_version(void) { return "0.1.0"; }
+
+double gx_primitive_normalization(double exponent, int lx, int ly, int lz) {
+    return primitive_norm(exponent, lx, ly, lz);
+}
+
+int gx_shell_normalize(int l, int nprim, int ncontr, const double* exps, const double* coefs_in, int normalize,
+                       double* coefs_out) {
+    return guarded([&] {
+        if (nprim <= 0) raise(GX_EINVAL, "a shell requires at least one primitive");
+        if (ncontr <= 0) raise(GX_EINVAL, "a shell requires at least one contraction");
+        if (l < 0 || l > 65535) raise(GX_EINVAL, "shell angular momentum must fit non-negative uint16");
+        for (int i = 0; i < nprim; ++i)
+            if (!std::isfinite(exps[i]) || exps[i] <= 0.0)
+                raise(GX_EINVAL, "shell exponents must be finite and positive");
+        for (int i = 0; i < nprim * ncontr; ++i)
+            if (!std::isfinite(coefs_in[i])) raise(GX_EINVAL, "shell coefficients must be finite");
+        for (int x = 0; x < ncontr; ++x) {
+            const double* c = coefs_in + (size_t)x * nprim;
+            double* o = coefs_out + (size_t)x * nprim;
+            bool nonzero = false;
+            for (int i = 0; i < nprim; ++i) nonzero = nonzero || c[i] != 0.0;
+            if (!nonzero) raise(GX_EINVAL, "a shell contraction cannot have all-zero coefficients");
+            double scale = 1.0;
+            if (normalize) {
+                double s = 0.0;
+                for (int i = 0; i < nprim; ++i)
+                    for (int j = 0; j < nprim; ++j) s += c[i] * c[j] * same_center_overlap(exps[i], exps[j], l);
+                if (!std::isfinite(s) || s <= 0.0)
+                    raise(GX_EINVAL, "contraction has a non-positive or non-finite norm");
+                scale = 1.0 / std::sqrt(s);
+            }
+            for (int i = 0; i < nprim; ++i) o[i] = normalize ? c[i] * scale : c[i];
+        }
+    });
+}
+
+int gx_context_create(int device, gx_context** out) {
+    return guarded([&] {
+        auto ctx = std::make_unique<gx_context>();
+        ctx->device = device;
+        GX_CUDA(cudaSetDevice(device));
+        GX_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
+        GX_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+        gx::GLRules gl;
+        gauss_legendre(16, gl.x16, gl.w16);
+        gauss_legendre(32, gl.x32, gl.w32);
+        ctx->gl.reserve(sizeof gl);
+        GX_CUDA(cudaMemcpy(ctx->gl.ptr, &gl, sizeof gl, cudaMemcpyHostToDevice));
+        std::vector<uint32_t> herm(gx::herm_count(32));
+        for (int s = 0; s <= 32; ++s)
+            for (int k = s; k >= 0; --k)
+                for (int l = s - k; l >= 0; --l) {
+                    const int m = s - k - l;
+                    herm[gx::herm_index(k, l, m)] = (uint32_t)(k | (l << 8) | (m << 16));
+                }
+        upload(ctx->herm, herm, ctx->stream);
+        ctx->status.reserve(sizeof(gx::DevStatus));
+        const size_t npts = (size_t)gx::BOYS_NX * gx::BOYS_NY;
+        ctx->boys_S.reserve(npts * gx::BOYS_TABLE_ORDERS * sizeof(double2));
+        ctx->boys_E0.reserve(npts * sizeof(double2));
+        DeviceBuffer fails;  // [0]: points worse than 1e-13, [1]: worst relative agreement (double bits)
+        fails.reserve(2 * sizeof(unsigned long long));
+        GX_CUDA(cudaMemsetAsync(fails.ptr, 0, 2 * sizeof(unsigned long long), ctx->stream));
+        GX_CUDA(gx::launch_boys_table(ctx->boys_S.as<double2>(), ctx->boys_E0.as<double2>(),
+                                      ctx->gl.as<gx::GLRules>(), fails.as<int>(), ctx->stream));
+        unsigned long long words[2] = {0, 0};
+        GX_CUDA(cudaMemcpyAsync(words, fails.ptr, sizeof words, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        double worst;
+        std::memcpy(&worst, &words[1], sizeof worst);
+        ctx->boys_table_agreement = worst;
+        const int nfail = (int)(words[0] & 0xffffffffu);
+        if (nfail)
+            raise(GX_ECUDA, "Boys table construction did not converge at " + std::to_string(nfail) +
+                                " points (worst relative agreement " + std::to_string(worst) + ")");
+        *out = ctx.release();
+    });
+}
+
+void gx_context_destroy(gx_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->pair_classes.clear();
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int gx_basis_create(gx_context* ctx, int nshell, const double* centers, const int* l, const int* nprim,
+                    const int* ncontr, const double* exponents, const double* coefs, const int* raw, gx_basis** out) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        if (nshell < 0) raise(GX_EINVAL, "negative shell count");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        auto b = std::make_unique<gx_basis>();
+        b->ctx = ctx;
+        b->ns = nshell;
+        b->center.assign(centers, centers + 3 * (size_t)nshell);
+        b->l.assign(l, l + nshell);
+        b->nprim.assign(nprim, nprim + nshell);
+        b->ncontr.assign(ncontr, ncontr + nshell);
+        size_t ne = 0, nc = 0;
+        for (int s = 0; s < nshell; ++s) {
+            if (l[s] < 0 || l[s] > 16) raise(GX_EINVAL, "shell angular momentum above 16 is not supported");
+            if (nprim[s] <= 0 || ncontr[s] <= 0) raise(GX_EINVAL, "a shell requires primitives and contractions");
+            ne += nprim[s];
+            nc += (size_t)nprim[s] * ncontr[s];
+        }
+        b->exps.assign(exponents, exponents + ne);
+        b->coefs.assign(coefs, coefs + nc);
+        b->raw.assign(nshell, 0);
+        if (raw)
+            for (int s = 0; s < nshell; ++s) b->raw[s] = raw[s] ? 1 : 0;
+        int64_t a = 0;
+        for (int s = 0; s < nshell; ++s) {
+            b->ao_off.push_back(a);
+            a += b->nao_of(s);
+        }
+        b->nao = a;
+        build_segments(b.get());
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *out = b.release();
+    });
+}
+
+void gx_basis_destroy(gx_basis* b) {
+    if (!b) return;
+    std::lock_guard<std::mutex> lock(b->ctx->mu);
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    delete b;
+}
+
+int64_t gx_basis_ao_count(const gx_basis* b) { return b ? b->nao : 0; }
+
+int gx_boys(gx_context* ctx, const double* z, int64_t count, int nmax, int scaled, double* out, int* region) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        if (nmax < 0) raise(GX_EINVAL, "Boys output must contain at least F_0");
+        if (nmax > 32) raise(GX_EINVAL, "complex Boys supports orders through 32");
+        for (int64_t i = 0; i < 2 * count; ++i)
+            if (!std::isfinite(z[i])) raise(GX_EINVAL, "complex Boys argument must be finite");
+        if (count <= 0) return;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        const size_t nz = (size_t)count * sizeof(double2);
+        const size_t no = (size_t)count * (nmax + 1) * sizeof(double2);
+        ctx->scratch_a.reserve(nz);
+        ctx->scratch_b.reserve(no);
+        ctx->scratch_c.reserve((size_t)count * sizeof(int));
+        GX_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, z, nz, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->reset_status();
+        GX_CUDA(gx::launch_boys_values(ctx->scratch_a.as<double2>(), count, nmax, scaled, ctx->boys(),
+                                       ctx->gl.as<gx::GLRules>(), ctx->scratch_b.as<double2>(),
+                                       region ? ctx->scratch_c.as<int>() : nullptr,
+                                       ctx->status.as<gx::DevStatus>(), ctx->stream));
+        check_status(ctx);
+        GX_CUDA(cudaMemcpyAsync(out, ctx->scratch_b.ptr, no, cudaMemcpyDeviceToHost, ctx->stream));
+        if (region)
+            GX_CUDA(cudaMemcpyAsync(region, ctx->scratch_c.ptr, count * sizeof(int), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int gx_eri_batch(gx_context* ctx, gx_basis* basis, const double* B, const double* O, const uint32_t* quartets,
+                 int64_t nq, int precision, double mixed_cutoff, double screening_threshold, uint32_t* kept,
+                 int64_t* offsets, double* out, int64_t out_capacity, gx_eri_stats* stats) {
+    return eri_batch_impl(ctx, basis, B, O, quartets, nq, precision, mixed_cutoff, screening_threshold, kept, offsets,
+                          out, false, out_capacity, stats);
+}
+
+int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                        const uint32_t* quartets, int64_t nq, int precision, double mixed_cutoff,
+                        double screening_threshold, uint32_t* kept, int64_t* offsets, void* out_device,
+                        int64_t out_capacity, gx_eri_stats* stats) {
+    return eri_batch_impl(ctx, basis, B, O, quartets, nq, precision, mixed_cutoff, screening_threshold, kept, offsets,
+                          out_device, true, out_capacity, stats);
+}
+
+int gx_eri_shell(gx_context* ctx, gx_basis* basis, int a, int b, int c, int d, const double* B, const double* O,
+                 double* out) {
+    const uint32_t q[4] = {(uint32_t)a, (uint32_t)b, (uint32_t)c, (uint32_t)d};
+    int64_t offsets[2];
+    if (a < 0 || b < 0 || c < 0 || d < 0) return fail(GX_ERANGE, "ERI shell-quartet index is out of range");
+    int64_t cap = INT64_MAX;
+    return eri_batch_impl(ctx, basis, B, O, q, 1, GX_PRECISION_FP64, 0.0, 0.0, nullptr, offsets, out, false, cap,
+                          nullptr);
+}
+
+int gx_schwarz(gx_context* ctx, gx_basis* b, const double* B, const double* O, double* out) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        const auto q = schwarz_values(ctx, b, B, O);
+        std::copy(q.begin(), q.end(), out);
+    });
+}
+
+int gx_eri_full(gx_context* ctx, gx_basis* b, const double* B, const double* O, int precision, double mixed_cutoff,
+                double screening, double* out) {
+    (void)precision;
+    (void)mixed_cutoff;
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        if (!std::isfinite(screening) || screening < 0.0)
+            raise(GX_EINVAL, "ERI screening threshold must be finite and non-negative");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        const int64_t n = b->nao;
+        std::vector<double> q;
+        if (screening > 0.0) q = schwarz_values(ctx, b, B, O);
+        std::vector<QuartetRequest> req;
+        std::vector<long long> boff;
+        std::vector<int> info;
+        int64_t off = 0;
+        const int ns = b->ns;
+        for (int a = 0; a < ns; ++a)
+            for (int bb = 0; bb < ns; ++bb)
+                for (int c = 0; c < ns; ++c)
+                    for (int d = 0; d < ns; ++d) {
+                        const std::array<int, 4> me{a, bb, c, d};
+                        const std::array<std::array<int, 4>, 3> other{
+                            {{c, d, a, bb}, {bb, a, d, c}, {d, c, bb, a}}};
+                        bool canonical = true;
+                        for (const auto& o : other)
+                            if (o < me) canonical = false;
+                        if (!canonical) continue;
+                        if (screening > 0.0 && q[(size_t)a * ns + bb] * q[(size_t)c * ns + d] < screening) continue;
+                        req.push_back({(uint32_t)a, (uint32_t)bb, (uint32_t)c, (uint32_t)d, off});
+                        boff.push_back(off);
+                        const int na = (int)b->nao_of(a), nb = (int)b->nao_of(bb), nc = (int)b->nao_of(c),
+                                  nd = (int)b->nao_of(d);
+                        info.insert(info.end(), {(int)b->ao_off[a], (int)b->ao_off[bb], (int)b->ao_off[c],
+                                                 (int)b->ao_off[d], na | (nb << 8) | (nc << 16) | (nd << 24)});
+                        off += (int64_t)na * nb * nc * nd;
+                    }
+        ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
+        const size_t full_bytes = (size_t)n * n * n * n * sizeof(double2);
+        ctx->scratch_b.reserve(std::max<size_t>(full_bytes, 16));
+        if (!req.empty()) run_quartets(ctx, b, B, O, req, ctx->out.as<double2>(), nullptr);
+        GX_CUDA(cudaMemsetAsync(ctx->scratch_b.ptr, 0, full_bytes, ctx->stream));
+        DeviceBuffer d_boff, d_info;
+        upload(d_boff, boff, ctx->stream);
+        upload(d_info, info, ctx->stream);
+        GX_CUDA(gx::launch_scatter_full(ctx->out.as<double2>(), d_boff.as<long long>(), d_info.as<int>(),
+                                        (int)req.size(), n, ctx->scratch_b.as<double2>(), ctx->stream));
+        if (full_bytes)
+            GX_CUDA(cudaMemcpyAsync(out, ctx->scratch_b.ptr, full_bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+int gx_primitive_eri(gx_context* ctx, const double* exps, const double* centers, const int* angular,
+                     const double* coefs, const int* normalized, const double* B, const double* O, double* out) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        check_field(B, O);
+        int ls[4], L = 0;
+        for (int i = 0; i < 4; ++i) {
+            if (!std::isfinite(exps[i]) || exps[i] <= 0.0)
+                raise(GX_EINVAL, "Gaussian exponent must be finite and positive");
+            if (!std::isfinite(coefs[i])) raise(GX_EINVAL, "primitive coefficient must be finite");
+            ls[i] = angular[3 * i] + angular[3 * i + 1] + angular[3 * i + 2];
+            L += ls[i];
+        }
+        if (L > 32) raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
+        // four raw (unnormalised) single-primitive shells; pick the component
+        const int np[4] = {1, 1, 1, 1}, nc[4] = {1, 1, 1, 1}, raw[4] = {1, 1, 1, 1};
+        const double one[4] = {1.0, 1.0, 1.0, 1.0};
+        gx_basis* b = nullptr;
+        int rc = gx_basis_create(ctx, 4, centers, ls, np, nc, exps, one, raw, &b);
+        if (rc) raise(rc, g_error);
+        std::unique_ptr<gx_basis, void (*)(gx_basis*)> guard(b, gx_basis_destroy);
+        int64_t n[4], idx[4];
+        for (int i = 0; i < 4; ++i) {
+            n[i] = gx::ncart(ls[i]);
+            const auto comps = components(ls[i]);
+            idx[i] = -1;
+            for (size_t k = 0; k < comps.size(); ++k)
+                if (comps[k][0] == angular[3 * i] && comps[k][1] == angular[3 * i + 1] &&
+                    comps[k][2] == angular[3 * i + 2])
+                    idx[i] = (int64_t)k;
+        }
+        std::vector<double> blk(2 * n[0] * n[1] * n[2] * n[3]);
+        rc = gx_eri_shell(ctx, b, 0, 1, 2, 3, B, O, blk.data());
+        if (rc) raise(rc, g_error);
+        const int64_t e = ((idx[0] * n[1] + idx[1]) * n[2] + idx[2]) * n[3] + idx[3];
+        double scale = 1.0;
+        for (int i = 0; i < 4; ++i) {
+            scale *= coefs[i];
+            if (normalized[i]) scale *= primitive_norm(exps[i], angular[3 * i], angular[3 * i + 1], angular[3 * i + 2]);
+        }
+        out[0] = blk[2 * e] * scale;
+        out[1] = blk[2 * e + 1] * scale;
+    });
+}
+
+int gx_cholesky_diagonal(gx_context* ctx, gx_basis* b, const int64_t* pairs, int64_t npairs, const double* B,
+                         const double* O, double* out) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        const int ns = b->ns;
+        const int64_t n = b->nao;
+        std::vector<char> seen((size_t)ns * ns, 0);
+        for (int64_t i = 0; i < npairs; ++i) {
+            const int64_t a = pairs[2 * i], c = pairs[2 * i + 1];
+            if (a < 0 || c < 0 || a >= ns || c >= ns || a > c)
+                raise(GX_ERANGE, "Cholesky diagonal shell pair must be valid and ordered");
+            if (seen[(size_t)a * ns + c]) raise(GX_EINVAL, "duplicate Cholesky diagonal shell pair");
+            seen[(size_t)a * ns + c] = 1;
+        }
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        std::vector<QuartetRequest> req;
+        int64_t off = 0;
+        for (int64_t i = 0; i < npairs; ++i) {
+            const uint32_t a = (uint32_t)pairs[2 * i], c = (uint32_t)pairs[2 * i + 1];
+            req.push_back({a, c, c, a, off});
+            off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
+        }
+        std::fill(out, out + n * n, 0.0);
+        if (req.empty()) return;
+        ctx->scratch_a.reserve(off * sizeof(double2));
+        run_quartets(ctx, b, B, O, req, ctx->scratch_a.as<double2>(), nullptr);
+        std::vector<std::complex<double>> host(off);
+        GX_CUDA(cudaMemcpy(host.data(), ctx->scratch_a.ptr, off * sizeof(double2), cudaMemcpyDeviceToHost));
+        for (const auto& r : req) {
+            const int64_t na = b->nao_of(r.a), nb = b->nao_of(r.b);
+            const std::complex<double>* blk = host.data() + r.out_off;
+            for (int64_t i = 0; i < na; ++i)
+                for (int64_t j = 0; j < nb; ++j) {
+                    const double v = blk[((i * nb + j) * nb + j) * na + i].real();
+                    const int64_t mu = b->ao_off[r.a] + i, nu = b->ao_off[r.b] + j;
+                    out[nu * n + mu] = v;
+                    if (r.a != r.b) out[mu * n + nu] = v;
+                }
+        }
+    });
+}
+
+int gx_cholesky_columns(gx_context* ctx, gx_basis* b, const int64_t* pivots, int64_t npiv, const double* B,
+                        const double* O, double* out) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        const int ns = b->ns;
+        const int64_t n = b->nao;
+        if (npiv == 0) return;
+        std::vector<int> owner(n);
+        for (int s = 0; s < ns; ++s)
+            for (int64_t i = b->ao_off[s]; i < b->ao_off[s] + b->nao_of(s); ++i) owner[i] = s;
+        for (int64_t k = 0; k < npiv; ++k)
+            if (pivots[2 * k] < 0 || pivots[2 * k + 1] < 0 || pivots[2 * k] >= n || pivots[2 * k + 1] >= n)
+                raise(GX_ERANGE, "Cholesky pivot AO index is out of range");
+        const int sa = owner[pivots[0]], sb = owner[pivots[1]];
+        for (int64_t k = 0; k < npiv; ++k)
+            if (owner[pivots[2 * k]] != sa || owner[pivots[2 * k + 1]] != sb)
+                raise(GX_EINVAL, "Cholesky candidate pivots must share a shell pair");
+        const bool real = B[0] == 0.0 && B[1] == 0.0 && B[2] == 0.0;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        std::vector<QuartetRequest> req;
+        int64_t off = 0;
+        for (int a = 0; a < ns; ++a)
+            for (int c = real ? a : 0; c < ns; ++c) {
+                req.push_back({(uint32_t)a, (uint32_t)c, (uint32_t)sb, (uint32_t)sa, off});
+                off += b->nao_of(a) * b->nao_of(c) * b->nao_of(sb) * b->nao_of(sa);
+            }
+        ctx->scratch_a.reserve(off * sizeof(double2));
+        run_quartets(ctx, b, B, O, req, ctx->scratch_a.as<double2>(), nullptr);
+        std::vector<std::complex<double>> host(off);
+        GX_CUDA(cudaMemcpy(host.data(), ctx->scratch_a.ptr, off * sizeof(double2), cudaMemcpyDeviceToHost));
+        const int64_t nc = b->nao_of(sb), nd = b->nao_of(sa);
+        for (const auto& r : req) {
+            const int64_t na = b->nao_of(r.a), nb = b->nao_of(r.b);
+            const std::complex<double>* blk = host.data() + r.out_off;
+            for (int64_t k = 0; k < npiv; ++k) {
+                const int64_t c = pivots[2 * k + 1] - b->ao_off[sb], d = pivots[2 * k] - b->ao_off[sa];
+                for (int64_t i = 0; i < na; ++i)
+                    for (int64_t j = 0; j < nb; ++j) {
+                        const std::complex<double> v = blk[((i * nb + j) * nc + c) * nd + d];
+                        const int64_t mu = b->ao_off[r.a] + i, nu = b->ao_off[r.b] + j;
+                        if (real) {
+                            double s = v.real();
+                            if (r.a == r.b) s = (s + blk[((j * nb + i) * nc + c) * nd + d].real()) * 0.5;
+                            out[(k * n + mu) * n + nu] = s;
+                            if (r.a != r.b) out[(k * n + nu) * n + mu] = s;
+                        } else {
+                            out[2 * ((k * n + mu) * n + nu)] = v.real();
+                            out[2 * ((k * n + mu) * n + nu) + 1] = v.imag();
+                        }
+                    }
+            }
+        }
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+struct CholRed {
+    double maxv;
+    long long idx;
+    double minv;
+};
+
+// Device column slots shared by the current candidate batch and the raw-column
+// LRU (python/giao_integrals/cholesky.py:180-265).
+struct ColumnPool {
+    DeviceBuffer buf;
+    size_t col_bytes = 0;
+    int capacity = 0;
+    std::vector<int> refs, free_list;
+    void init(int cap, size_t bytes) {
+        capacity = cap;
+        col_bytes = bytes;
+        buf.reserve((size_t)cap * bytes);
+        refs.assign(cap, 0);
+        free_list.clear();
+        for (int i = cap - 1; i >= 0; --i) free_list.push_back(i);
+    }
+    int take() {
+        if (free_list.empty()) raise(GX_ENOMEM, "Cholesky column pool exhausted");
+        const int s = free_list.back();
+        free_list.pop_back();
+        refs[s] = 1;
+        return s;
+    }
+    void retain(int s) { ++refs[s]; }
+    void release(int s) {
+        if (--refs[s] == 0) free_list.push_back(s);
+    }
+    void* ptr(int s) const { return static_cast<char*>(buf.ptr) + (size_t)s * col_bytes; }
+};
+
+}  // namespace
+
+extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const double* Of,
+                           const gx_cholesky_options* opt, double* vectors, int64_t* pivots_out, int64_t* rank_out,
+                           double* max_residual) {
+    return guarded([&] {
+        if (!ctx || !b || !opt) raise(GX_EINVAL, "null context, basis or options");
+        check_field(Bf, Of);
+        const double threshold = opt->threshold, screening = opt->screening_threshold;
+        if (!std::isfinite(threshold) || threshold < 0.0) raise(GX_EINVAL, "threshold must be finite and non-negative");
+        if (!std::isfinite(screening) || screening < 0.0)
+            raise(GX_EINVAL, "screening_threshold must be finite and non-negative");
+        if (opt->pivot_batch_size < 1) raise(GX_EINVAL, "pivot_batch_size must be a positive integer");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        const int ns = b->ns;
+        const int64_t n = b->nao, N = n * n;
+        *rank_out = 0;
+        *max_residual = 0.0;
+        if (n == 0) return;
+        // single centre: the London phase cancels; use zero-field integrals (cholesky.py:130-133)
+        bool single = true;
+        for (int s = 1; s < ns; ++s)
+            for (int k = 0; k < 3; ++k) single = single && b->center[3 * s + k] == b->center[k];
+        const double zero3[3] = {0.0, 0.0, 0.0};
+        const double* iB = single ? zero3 : Bf;
+        const double* iO = single ? zero3 : Of;
+        const bool real = (Bf[0] == 0.0 && Bf[1] == 0.0 && Bf[2] == 0.0) || single;
+        const size_t esz = real ? sizeof(double) : sizeof(double2);
+        std::vector<int> owner(n);
+        for (int s = 0; s < ns; ++s)
+            for (int64_t i = b->ao_off[s]; i < b->ao_off[s] + b->nao_of(s); ++i) owner[i] = s;
+
+        // ---- diagonal (with optional Schwarz skip of initial blocks) ----
+        DeviceBuffer d_D, d_res, d_partial, d_red, d_scale, d_work, d_L, d_boff, d_info, d_cand, d_dst;
+        d_D.reserve(N * sizeof(double));
+        d_res.reserve(N * sizeof(double));
+        d_partial.reserve(gx::chol_partial_bytes());
+        d_red.reserve(gx::chol_red_bytes());
+        d_scale.reserve(sizeof(double));
+        GX_CUDA(cudaMemsetAsync(d_D.ptr, 0, N * sizeof(double), st));
+        std::vector<double> q;
+        if (screening > 0.0) q = schwarz_values(ctx, b, iB, iO);
+        std::vector<std::pair<int, int>> measured, skipped;
+        std::vector<double> skip_fill;
+        for (int a = 0; a < ns; ++a)
+            for (int c = a; c < ns; ++c) {
+                const double qq = screening > 0.0 ? q[(size_t)a * ns + c] * q[(size_t)a * ns + c] : 0.0;
+                if (screening > 0.0 && qq <= std::min(threshold, screening)) {
+                    skipped.push_back({a, c});
+                    skip_fill.push_back(qq);
+                } else {
+                    measured.push_back({a, c});
+                }
+            }
+        auto read_diagonal = [&](const std::vector<std::pair<int, int>>& pairs, double* target) {
+            if (pairs.empty()) return;
+            std::vector<QuartetRequest> req;
+            std::vector<long long> boff;
+            std::vector<int> info;
+            int64_t off = 0;
+            for (const auto& pr : pairs) {
+                const uint32_t a = pr.first, c = pr.second;
+                req.push_back({a, c, c, a, off});
+                boff.push_back(off);
+                info.insert(info.end(), {(int)b->ao_off[a], (int)b->ao_off[c], (int)b->nao_of(a), (int)b->nao_of(c)});
+                off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
+            }
+            ctx->scratch_a.reserve(off * sizeof(double2));
+            run_quartets(ctx, b, iB, iO, req, ctx->scratch_a.as<double2>(), nullptr);
+            upload(d_boff, boff, st);
+            upload(d_info, info, st);
+            GX_CUDA(gx::launch_chol_diag(ctx->scratch_a.as<double2>(), d_boff.as<long long>(), d_info.as<int>(),
+                                         (int)pairs.size(), (int)n, target, st));
+        };
+        read_diagonal(measured, d_D.as<double>());
+        if (!skipped.empty()) {
+            std::vector<double> D(N);
+            GX_CUDA(cudaMemcpyAsync(D.data(), d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+            GX_CUDA(cudaStreamSynchronize(st));
+            for (size_t k = 0; k < skipped.size(); ++k) {
+                const int a = skipped[k].first, c = skipped[k].second;
+                for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
+                    for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) {
+                        D[i * n + j] = skip_fill[k];
+                        D[j * n + i] = skip_fill[k];
+                    }
+            }
+            GX_CUDA(cudaMemcpyAsync(d_D.ptr, D.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        GX_CUDA(cudaMemcpyAsync(d_res.ptr, d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        CholRed red;
+        auto fetch_red = [&] {
+            GX_CUDA(cudaMemcpyAsync(&red, d_red.ptr, sizeof red, cudaMemcpyDeviceToHost, st));
+            GX_CUDA(cudaStreamSynchronize(st));
+        };
+        GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
+        fetch_red();
+        const double floor = 64 * 2.220446049250313e-16 * std::max(red.maxv, 0.0);
+        const double tol = std::max(threshold, floor);
+        const int64_t limit = std::min<int64_t>(N, opt->max_rank);
+
+        // ---- pivot loop ----
+        bool reuse = !single;
+        for (int s = 0; s < ns; ++s) reuse = reuse || b->ncontr[s] > 1 || b->nprim[s] > 1;
+        const int candidate_count = reuse ? 32 : 8;
+        ColumnPool pool;
+        pool.init(32 + 1024 + 64, N * esz);
+        d_work.reserve(N * esz);
+        d_L.reserve(std::max<int64_t>(limit, 1) * N * esz);
+        std::vector<int64_t> cands;               // current batch candidates (flat indices)
+        std::vector<int> cand_slot;               // their column slots
+        std::vector<int64_t> block_cands;         // local block-pivot candidates
+        std::list<std::pair<int64_t, int>> lru;   // raw-column cache, oldest first
+        std::map<int64_t, std::list<std::pair<int64_t, int>>::iterator> lru_pos;
+        std::vector<double> hostblk;
+        int64_t rank = 0;
+        auto residual_at = [&](const std::vector<int64_t>& idx, std::vector<double>& vals) {
+            vals.resize(idx.size());
+            for (size_t k = 0; k < idx.size(); ++k)
+                GX_CUDA(cudaMemcpyAsync(&vals[k], d_res.as<double>() + idx[k], sizeof(double), cudaMemcpyDeviceToHost,
+                                        st));
+            GX_CUDA(cudaStreamSynchronize(st));
+        };
+        auto drop_batch = [&] {
+            for (int s : cand_slot) pool.release(s);
+            cands.clear();
+            cand_slot.clear();
+        };
+        while (red.maxv > tol) {
+            int64_t pivot = red.idx;
+            if (reuse && !real && opt->pivot_batch_size > 1 && !block_cands.empty()) {
+                std::vector<double> v;
+                residual_at(block_cands, v);
+                size_t best = 0;
+                for (size_t k = 1; k < v.size(); ++k)
+                    if (v[k] > v[best]) best = k;
+                if (v[best] > tol && v[best] >= 0.01 * red.maxv) pivot = block_cands[best];
+            }
+            if (rank >= limit) {
+                *rank_out = rank;
+                raise(GX_ENOMEM, "Cholesky rank capacity exceeded");
+            }
+            auto cached = lru_pos.find(pivot);
+            if (reuse && cached != lru_pos.end()) {
+                const int slot = cached->second->second;
+                lru.erase(cached->second);
+                lru_pos.erase(cached);
+                drop_batch();
+                cands.push_back(pivot);
+                cand_slot.push_back(slot);  // cache reference moves to the batch
+            }
+            auto it = std::find(cands.begin(), cands.end(), pivot);
+            if (it == cands.end()) {
+                const int64_t mu = pivot / n, nu = pivot % n;
+                const int a = owner[mu], c = owner[nu];
+                std::vector<int64_t> idx;
+                if (reuse) {
+                    const int ca = b->ncart_of(a), cc = b->ncart_of(c);
+                    for (int xa = 0; xa < b->ncontr[a]; ++xa)
+                        for (int xc = 0; xc < b->ncontr[c]; ++xc)
+                            idx.push_back((b->ao_off[a] + (mu - b->ao_off[a]) % ca + (int64_t)ca * xa) * n +
+                                          b->ao_off[c] + (nu - b->ao_off[c]) % cc + (int64_t)cc * xc);
+                } else {
+                    for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
+                        for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) idx.push_back(i * n + j);
+                }
+                // residual on the block: one strided 2-D copy
+                const int64_t na = b->nao_of(a), nc = b->nao_of(c);
+                hostblk.resize(na * nc);
+                GX_CUDA(cudaMemcpy2DAsync(hostblk.data(), nc * sizeof(double),
+                                          d_res.as<double>() + b->ao_off[a] * n + b->ao_off[c], n * sizeof(double),
+                                          nc * sizeof(double), na, cudaMemcpyDeviceToHost, st));
+                GX_CUDA(cudaStreamSynchronize(st));
+                auto rv = [&](int64_t f) {
+                    return hostblk[(f / n - b->ao_off[a]) * nc + (f % n - b->ao_off[c])];
+                };
+                std::vector<int64_t> keep;
+                for (int64_t f : idx)
+                    if (rv(f) > tol) keep.push_back(f);
+                std::stable_sort(keep.begin(), keep.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
+                if ((int)keep.size() > candidate_count) keep.resize(candidate_count);
+                if (std::find(keep.begin(), keep.end(), pivot) == keep.end()) {
+                    if (keep.empty())
+                        keep.push_back(pivot);
+                    else
+                        keep.back() = pivot;
+                }
+                block_cands.assign(keep.begin(), keep.begin() + std::min<size_t>(keep.size(),
+                                                                                 std::min(32, opt->pivot_batch_size)));
+                drop_batch();
+                cands = keep;
+                // columns (mu nu | p1 p0) for all shell pairs (real: b >= a)
+                const int sa = a, sb = c;
+                std::vector<QuartetRequest> req;
+                std::vector<long long> boff;
+                std::vector<int> info;
+                int64_t off = 0;
+                for (int x = 0; x < ns; ++x)
+                    for (int y = real ? x : 0; y < ns; ++y) {
+                        req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
+                        boff.push_back(off);
+                        info.insert(info.end(), {(int)b->ao_off[x], (int)b->ao_off[y], (int)b->nao_of(x),
+                                                 (int)b->nao_of(y), x == y ? 1 : 0});
+                        off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
+                    }
+                ctx->scratch_a.reserve(off * sizeof(double2));
+                run_quartets(ctx, b, iB, iO, req, ctx->scratch_a.as<double2>(), nullptr);
+                std::vector<int> cl;
+                std::vector<void*> dst;
+                for (int64_t f : cands) {
+                    cl.push_back((int)(f % n - b->ao_off[sb]));  // c: p1 within sb
+                    cl.push_back((int)(f / n - b->ao_off[sa]));  // d: p0 within sa
+                    const int slot = pool.take();
+                    cand_slot.push_back(slot);
+                    dst.push_back(pool.ptr(slot));
+                }
+                upload(d_boff, boff, st);
+                upload(d_info, info, st);
+                upload(d_cand, cl, st);
+                upload(d_dst, dst, st);
+                GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), d_boff.as<long long>(),
+                                             d_info.as<int>(), (int)req.size(), d_cand.as<int>(), (int)cands.size(),
+                                             (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
+                if (reuse) {
+                    for (size_t k = 0; k < cands.size(); ++k) {
+                        if (cands[k] == pivot) continue;
+                        // assignment to an existing key keeps its LRU position (OrderedDict semantics)
+                        auto old = lru_pos.find(cands[k]);
+                        pool.retain(cand_slot[k]);
+                        if (old != lru_pos.end()) {
+                            pool.release(old->second->second);
+                            old->second->second = cand_slot[k];
+                        } else {
+                            lru.push_back({cands[k], cand_slot[k]});
+                            lru_pos[cands[k]] = std::prev(lru.end());
+                        }
+                    }
+                    const size_t cap = (size_t)std::min<int64_t>(1024, std::max<int64_t>(8, rank + 8));
+                    while (lru.size() > cap) {
+                        pool.release(lru.front().second);
+                        lru_pos.erase(lru.front().first);
+                        lru.pop_front();
+                    }
+                }
+                it = std::find(cands.begin(), cands.end(), pivot);
+            }
+            if (reuse) {
+                auto c2it = lru_pos.find(pivot);
+                if (c2it != lru_pos.end()) {
+                    pool.release(c2it->second->second);
+                    lru.erase(c2it->second);
+                    lru_pos.erase(c2it);
+                }
+            }
+            const int slot = cand_slot[it - cands.begin()];
+            void* Lrow = static_cast<char*>(d_L.ptr) + (size_t)rank * N * esz;
+            GX_CUDA(gx::launch_chol_step(real, d_L.ptr, N, (int)rank, pivot, pool.ptr(slot), d_work.ptr, (int)n,
+                                         d_res.as<double>(), d_scale.as<double>(), Lrow, d_partial.ptr, d_red.ptr,
+                                         st));
+            fetch_red();
+            pivots_out[2 * rank] = pivot / n;
+            pivots_out[2 * rank + 1] = pivot % n;
+            ++rank;
+            if (red.minv < -std::max(floor * 16, 1e-12))
+                raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
+        }
+        double final_max = std::max(red.maxv, 0.0);
+        if (!skipped.empty()) {
+            read_diagonal(skipped, d_D.as<double>());
+            GX_CUDA(gx::launch_chol_final_residual(real, d_D.as<double>(), d_L.ptr, (int)rank, N, d_res.as<double>(),
+                                                   st));
+            GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
+            fetch_red();
+            final_max = std::max(red.maxv, 0.0);
+        }
+        // factors out as complex128
+        if (rank) {
+            if (real) {
+                std::vector<double> tmp(rank * N);
+                GX_CUDA(cudaMemcpyAsync(tmp.data(), d_L.ptr, rank * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+                GX_CUDA(cudaStreamSynchronize(st));
+                for (int64_t j = 0; j < rank * N; ++j) {
+                    vectors[2 * j] = tmp[j];
+                    vectors[2 * j + 1] = 0.0;
+                }
+            } else {
+                GX_CUDA(cudaMemcpyAsync(vectors, d_L.ptr, rank * N * sizeof(double2), cudaMemcpyDeviceToHost, st));
+                GX_CUDA(cudaStreamSynchronize(st));
+            }
+        }
+        *rank_out = rank;
+        *max_residual = final_max;
+    });
+}
+
+// ---------------------------------------------------------------------------
+// plans: build the class-sorted task list once, replay it per field
+// ---------------------------------------------------------------------------
+
+struct gx_eri_plan {
+    gx_context* ctx;
+    gx_basis* basis;
+    PlanData data;
+    int64_t total = 0;
+    int last_launches = 0;
+};
+
+extern "C" {
+
+int gx_context_set_stream(gx_context* ctx, void* stream) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    });
+}
+
+int gx_context_synchronize(gx_context* ctx) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        check_status(ctx);
+    });
+}
+
+int gx_eri_plan_create(gx_context* ctx, gx_basis* b, const uint32_t* quartets, int64_t nq, int64_t* offsets,
+                       gx_eri_plan** out) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        validate_quartets(b, quartets, nq);
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        auto plan = std::make_unique<gx_eri_plan>();
+        plan->ctx = ctx;
+        plan->basis = b;
+        std::vector<QuartetRequest> req((size_t)nq);
+        int64_t off = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* x = quartets + 4 * i;
+            offsets[i] = off;
+            req[i] = {x[0], x[1], x[2], x[3], off};
+            off += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+        }
+        offsets[nq] = off;
+        plan->total = off;
+        build_plan(ctx, b, req, plan->data);
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        *out = plan.release();
+    });
+}
+
+int gx_eri_plan_info(const gx_eri_plan* plan, int64_t* tasks, int64_t* primitive_quartets, double* model_flops,
+                     int* launches) {
+    return guarded([&] {
+        if (!plan) raise(GX_EINVAL, "null plan");
+        if (tasks) *tasks = plan->data.ntask;
+        if (primitive_quartets) *primitive_quartets = plan->data.primitive_quartets;
+        if (model_flops) *model_flops = plan->data.model_flops;
+        if (launches) *launches = 1 + (int)plan->data.classes.size();
+    });
+}
+
+int gx_eri_plan_execute(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                        void* out_device) {
+    (void)precision;
+    (void)mixed_cutoff;
+    return guarded([&] {
+        if (!plan) raise(GX_EINVAL, "null plan");
+        check_field(B, O);
+        gx_context* ctx = plan->ctx;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        plan->last_launches = execute_plan(ctx, plan->basis, B, O, plan->data, static_cast<double2*>(out_device));
+    });
+}
+
+void gx_eri_plan_destroy(gx_eri_plan* plan) { delete plan; }
+
+int gx_measure_fp64_peak(gx_context* ctx, double* tflops) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        float ms = 0.f;
+        double flops = 0.0;
+        GX_CUDA(gx::run_fp64_probe(ctx->sm_count, ctx->stream, &ms, &flops));
+        *tflops = flops / (ms * 1e-3) / 1e12;
+    });
+}
+
+}  // extern "C"
+
+// Canonical representatives of the finite-field orbit {(ab|cd), (cd|ab),
+// (ba|dc)*, (dc|ba)*} in lexicographic order (src/eri.cpp:414-429, 825-843).
+// out may be NULL to count; returns the count.
+extern "C" int64_t gx_canonical_quartets(int ns, uint32_t* out) {
+    int64_t n = 0;
+    for (int a = 0; a < ns; ++a)
+        for (int b = 0; b < ns; ++b)
+            for (int c = 0; c < ns; ++c)
+                for (int d = 0; d < ns; ++d) {
+                    const std::array<int, 4> me{a, b, c, d};
+                    if (std::array<int, 4>{c, d, a, b} < me || std::array<int, 4>{b, a, d, c} < me ||
+                        std::array<int, 4>{d, c, b, a} < me)
+                        continue;
+                    if (out) {
+                        out[4 * n] = (uint32_t)a;
+                        out[4 * n + 1] = (uint32_t)b;
+                        out[4 * n + 2] = (uint32_t)c;
+                        out[4 * n + 3] = (uint32_t)d;
+                    }
+                    ++n;
+                }
+    return n;
+}

@@ -1,0 +1,274 @@
+// Device kernels of the streamed pivoted Cholesky (K6-K9):
+//
+//   chol_diag_kernel     (mu nu|nu mu) diagonal from packed (ab|ba) blocks,
+//                        placed as src/cholesky.cpp:305-311
+//   chol_cols_kernel     pivot columns (mu nu|p1 p0) from packed
+//                        (ab|sb sa) blocks; zero-phase real path mirrored and
+//                        same-shell averaged as src/cholesky.cpp:245-279
+//   chol_gemv_kernel     column -= conj(L[:rank, piv]) L[:rank]
+//                        (python/giao_integrals/cholesky.py:268)
+//   chol_update_kernel   real symmetrisation, 1/sqrt(residual) scale, new
+//                        factor row, residual -= |column|^2, PSD minimum,
+//                        clamp, zeroed pivot and the next argmax, fused
+//                        (cholesky.py:269-281)
+//   argmax reductions    lowest flat index on ties (NumPy argmax order)
+#include "gx_internal.h"
+
+namespace gx {
+
+// ---- diagonal --------------------------------------------------------------
+
+// info per block: ao_a, ao_b, na, nb
+__global__ void chol_diag_kernel(const double2* packed, const long long* boff, const int* info, int nblocks, int n,
+                                 double* D) {
+    const int bi = blockIdx.x;
+    if (bi >= nblocks) return;
+    const int oa = info[4 * bi], ob = info[4 * bi + 1], na = info[4 * bi + 2], nb = info[4 * bi + 3];
+    const double2* blk = packed + boff[bi];
+    for (int e = threadIdx.x; e < na * nb; e += blockDim.x) {
+        const int i = e / nb, j = e - i * nb;
+        const double v = blk[(((long long)i * nb + j) * nb + j) * na + i].x;
+        const long long mu = oa + i, nu = ob + j;
+        D[nu * n + mu] = v;
+        if (oa != ob) D[mu * n + nu] = v;
+    }
+}
+
+cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const int* info, int nblocks, int n,
+                             double* D, cudaStream_t s) {
+    if (nblocks <= 0) return cudaSuccess;
+    chol_diag_kernel<<<nblocks, 128, 0, s>>>(packed, boff, info, nblocks, n, D);
+    return cudaGetLastError();
+}
+
+// ---- columns ---------------------------------------------------------------
+
+// info per block: ao_a, ao_b, na, nb, same_shell; cand[2*k] = (c, d) local
+// indices in shells (sb, sa); dst[k] = column k (n*n values).
+template <bool REAL>
+__global__ void chol_cols_kernel(const double2* packed, const long long* boff, const int* info, int nblocks,
+                                 const int* cand, int ncand, int nc, int nd, int n, void* const* dst) {
+    const int bi = blockIdx.x;
+    if (bi >= nblocks) return;
+    const int oa = info[5 * bi], ob = info[5 * bi + 1], na = info[5 * bi + 2], nb = info[5 * bi + 3];
+    const bool same = info[5 * bi + 4] != 0;
+    const double2* blk = packed + boff[bi];
+    const int per = na * nb;
+    for (int e = threadIdx.x; e < per * ncand; e += blockDim.x) {
+        const int k = e / per, r = e - k * per;
+        const int i = r / nb, j = r - i * nb;
+        const int c = cand[2 * k], d = cand[2 * k + 1];
+        const double2 v = blk[(((long long)i * nb + j) * nc + c) * nd + d];
+        const long long mu = oa + i, nu = ob + j;
+        if (REAL) {
+            double s = v.x;
+            if (same) s = (s + blk[(((long long)j * nb + i) * nc + c) * nd + d].x) * 0.5;
+            double* out = static_cast<double*>(dst[k]);
+            out[mu * n + nu] = s;
+            if (!same) out[nu * n + mu] = s;
+        } else {
+            double2* out = static_cast<double2*>(dst[k]);
+            out[mu * n + nu] = v;
+        }
+    }
+}
+
+cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info, int nblocks,
+                             const int* cand, int ncand, int nc, int nd, int n, void* const* dst, cudaStream_t s) {
+    if (nblocks <= 0) return cudaSuccess;
+    if (real)
+        chol_cols_kernel<true><<<nblocks, 256, 0, s>>>(packed, boff, info, nblocks, cand, ncand, nc, nd, n, dst);
+    else
+        chol_cols_kernel<false><<<nblocks, 256, 0, s>>>(packed, boff, info, nblocks, cand, ncand, nc, nd, n, dst);
+    return cudaGetLastError();
+}
+
+// ---- argmax / min reductions -------------------------------------------------
+
+struct Red {
+    double maxv;
+    long long idx;
+    double minv;
+};
+
+__device__ __forceinline__ void red_merge(Red& a, const Red& b) {
+    if (b.maxv > a.maxv || (b.maxv == a.maxv && b.idx < a.idx)) {
+        a.maxv = b.maxv;
+        a.idx = b.idx;
+    }
+    a.minv = fmin(a.minv, b.minv);
+}
+
+__device__ Red block_reduce(Red r) {
+    __shared__ Red sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        Red t;
+        t.maxv = __shfl_down_sync(0xffffffffu, r.maxv, o);
+        t.idx = __shfl_down_sync(0xffffffffu, r.idx, o);
+        t.minv = __shfl_down_sync(0xffffffffu, r.minv, o);
+        red_merge(r, t);
+    }
+    if (lane == 0) sh[w] = r;
+    __syncthreads();
+    if (w == 0) {
+        r = lane < (int)(blockDim.x >> 5) ? sh[lane] : Red{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+        for (int o = 16; o > 0; o >>= 1) {
+            Red t;
+            t.maxv = __shfl_down_sync(0xffffffffu, r.maxv, o);
+            t.idx = __shfl_down_sync(0xffffffffu, r.idx, o);
+            t.minv = __shfl_down_sync(0xffffffffu, r.minv, o);
+            red_merge(r, t);
+        }
+    }
+    return r;
+}
+
+constexpr int RED_BLOCKS = 256;
+
+__global__ void chol_scan_kernel(const double* res, long long N, Red* partial) {
+    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        const double v = res[j];
+        red_merge(r, Red{v, j, v});
+    }
+    r = block_reduce(r);
+    if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+__global__ void chol_final_kernel(const Red* partial, int np, Red* out) {
+    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    for (int i = threadIdx.x; i < np; i += blockDim.x) red_merge(r, partial[i]);
+    r = block_reduce(r);
+    if (threadIdx.x == 0) *out = r;
+}
+
+cudaError_t launch_chol_scan(const double* res, long long N, void* partial, void* out, cudaStream_t s) {
+    chol_scan_kernel<<<RED_BLOCKS, 256, 0, s>>>(res, N, static_cast<Red*>(partial));
+    chol_final_kernel<<<1, 256, 0, s>>>(static_cast<const Red*>(partial), RED_BLOCKS, static_cast<Red*>(out));
+    return cudaGetLastError();
+}
+
+// ---- factor update -----------------------------------------------------------
+
+__device__ __forceinline__ double2 conj_mul(double2 a, double2 b) {  // conj(a) * b
+    return c2(fma(a.x, b.x, a.y * b.y), fma(a.x, b.y, -a.y * b.x));
+}
+
+template <typename T>
+__global__ void chol_gemv_kernel(const T* L, long long ld, int rank, long long piv, const T* col_in, T* col_out,
+                                 long long N) {
+    __shared__ T coef[256];
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    T acc;
+    if constexpr (sizeof(T) == 8) {
+        acc = j < N ? col_in[j] : T(0);
+    } else {
+        acc = j < N ? col_in[j] : c2(0.0, 0.0);
+    }
+    for (int r0 = 0; r0 < rank; r0 += 256) {
+        const int nr = min(256, rank - r0);
+        __syncthreads();
+        if ((int)threadIdx.x < nr) coef[threadIdx.x] = L[(long long)(r0 + threadIdx.x) * ld + piv];
+        __syncthreads();
+        if (j < N) {
+            for (int r = 0; r < nr; ++r) {
+                const T lv = L[(long long)(r0 + r) * ld + j];
+                if constexpr (sizeof(T) == 8) {
+                    acc -= coef[r] * lv;
+                } else {
+                    acc = csub(acc, conj_mul(coef[r], lv));
+                }
+            }
+        }
+    }
+    if (j < N) col_out[j] = acc;
+}
+
+// scale = 1/sqrt(residual[piv]) (read before the update)
+__global__ void chol_scale_kernel(const double* res, long long piv, double* scale) { *scale = rsqrt(res[piv]); }
+
+template <typename T>
+__global__ void chol_update_kernel(const T* col, int n, long long piv, const double* scale, T* Lrow, double* res,
+                                   Red* partial) {
+    const long long N = (long long)n * n;
+    const double sc = *scale;
+    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        double mag2;
+        if constexpr (sizeof(T) == 8) {
+            const long long mu = j / n, nu = j - mu * n;
+            const double c = (col[j] + col[nu * n + mu]) * 0.5 * sc;
+            Lrow[j] = c;
+            mag2 = c * c;
+        } else {
+            const double2 c = cscale(col[j], sc);
+            Lrow[j] = c;
+            mag2 = c.x * c.x + c.y * c.y;
+        }
+        const double nr = res[j] - mag2;
+        const double kept = j == piv ? 0.0 : fmax(nr, 0.0);
+        res[j] = kept;
+        red_merge(r, Red{kept, j, nr});
+    }
+    r = block_reduce(r);
+    if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, long long piv, const void* column,
+                             void* work, int n, double* res, double* scale, void* Lrow, void* partial, void* out,
+                             cudaStream_t s) {
+    const long long N = (long long)n * n;
+    const int blocks = (int)((N + 255) / 256);
+    if (real) {
+        chol_gemv_kernel<double><<<blocks, 256, 0, s>>>(static_cast<const double*>(L), ld, rank, piv,
+                                                        static_cast<const double*>(column),
+                                                        static_cast<double*>(work), N);
+    } else {
+        chol_gemv_kernel<double2><<<blocks, 256, 0, s>>>(static_cast<const double2*>(L), ld, rank, piv,
+                                                         static_cast<const double2*>(column),
+                                                         static_cast<double2*>(work), N);
+    }
+    chol_scale_kernel<<<1, 1, 0, s>>>(res, piv, scale);
+    if (real)
+        chol_update_kernel<double><<<RED_BLOCKS, 256, 0, s>>>(static_cast<const double*>(work), n, piv, scale,
+                                                              static_cast<double*>(Lrow), res,
+                                                              static_cast<Red*>(partial));
+    else
+        chol_update_kernel<double2><<<RED_BLOCKS, 256, 0, s>>>(static_cast<const double2*>(work), n, piv, scale,
+                                                               static_cast<double2*>(Lrow), res,
+                                                               static_cast<Red*>(partial));
+    chol_final_kernel<<<1, 256, 0, s>>>(static_cast<const Red*>(partial), RED_BLOCKS, static_cast<Red*>(out));
+    return cudaGetLastError();
+}
+
+// residual = D - sum_P |L_P|^2 (used when screened diagonal blocks are measured at the end)
+template <typename T>
+__global__ void chol_final_residual_kernel(const double* D, const T* L, int rank, long long N, double* res) {
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int r = 0; r < rank; ++r) {
+            const T v = L[(long long)r * N + j];
+            if constexpr (sizeof(T) == 8)
+                s += v * v;
+            else
+                s += v.x * v.x + v.y * v.y;
+        }
+        res[j] = D[j] - s;
+    }
+}
+
+cudaError_t launch_chol_final_residual(bool real, const double* D, const void* L, int rank, long long N, double* res,
+                                       cudaStream_t s) {
+    const int blocks = (int)((N + 255) / 256);
+    if (real)
+        chol_final_residual_kernel<double><<<blocks, 256, 0, s>>>(D, static_cast<const double*>(L), rank, N, res);
+    else
+        chol_final_residual_kernel<double2><<<blocks, 256, 0, s>>>(D, static_cast<const double2*>(L), rank, N, res);
+    return cudaGetLastError();
+}
+
+size_t chol_red_bytes() { return sizeof(Red); }
+size_t chol_partial_bytes() { return sizeof(Red) * RED_BLOCKS; }
+
+}  // namespace gx

@@ -1,0 +1,103 @@
+// Internal declarations shared by the host orchestration (gx_api.cu) and the
+// kernels (gx_kernels.cu).  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gx_device.cuh"
+
+namespace gx {
+
+// Device view of one angular-momentum pair class (la, lb): for every
+// Cartesian component pair ab = ca * ncart(lb) + cb, the box of complex
+// Hermite coefficients E~[k][l][m], k <= ax+bx, l <= ay+by, m <= az+bz,
+// stored x-major at boxoff[ab] inside each primitive pair's record.
+struct PairClassDev {
+    int la, lb, nab, Lab, Etot;
+    const int* boxoff;     // [nab]
+    const int* boxdim;     // [nab] bx | by << 8 | bz << 16
+    const uint32_t* ent;   // [Etot] k | l << 8 | m << 16
+};
+
+// One shell-quartet work item (segmented shells) and where its block goes.
+struct Task {
+    int sa, sb, sc, sd;
+    long long out_off;  // complex-element offset of element (0,0,0,0)
+    int st[4];          // complex-element strides of the component indices
+};
+
+// Per-(basis, field) primitive-pair data, structure of arrays.
+struct PairData {
+    int npp;
+    const double* p;       // [npp] exponent sum
+    const double* Pr;      // [3*npp] product centre
+    const double* Pi;      // [3*npp] imaginary part of the complex centre, -q/(2p)
+    const double2* F;      // [npp] complex prefactor (coefficients, norms, K_ab, London phase, 1/p)
+    const long long* Eoff; // [npp] offset of the primitive pair's E~ record in Epool
+    const double2* Epool;  // complex Hermite coefficients
+    const double* bound;   // [npp] magnitude bound of the pair's charge distribution
+};
+
+struct BasisDev {
+    int ns;
+    const double* center;  // [3*ns]
+    const int* l;
+    const int* nprim;
+    const int* primoff;
+    const double* exps;
+    const double* coefs;   // per primitive, contraction-normalised (segmented shells)
+    const int* raw;        // 1: no Cartesian primitive normalisation
+    const int* sp_off;     // [ns*ns] first primitive pair of ordered shell pair (a, b)
+};
+
+struct QuartetClass {
+    PairClassDev bra, ket;
+    int L, Nab, NL;        // total order, herm_count(Lab), herm_count(L)
+    int B1, CH;            // phase-1 batch (primitive quartets), ket-component chunk
+    int ntask;
+    const Task* tasks;
+};
+
+struct EriDev {
+    BasisDev basis;
+    PairData pairs;
+    BoysTable boys;
+    const GLRules* gl;
+    const uint32_t* herm_xyz;  // packed (k, l, m) of herm index, L <= 32
+    double2* out;
+    DevStatus* status;
+};
+
+// ---- launch wrappers (gx_kernels.cu) -------------------------------------
+
+cudaError_t launch_boys_table(double2* S, double2* E0, const GLRules* gl, int* fail_count, cudaStream_t s);
+cudaError_t launch_boys_values(const double2* z, long long count, int nmax, int scaled, const BoysTable& tab,
+                               const GLRules* gl, double2* out, int* region, DevStatus* st, cudaStream_t s);
+cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
+                                   const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
+                                   const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
+                                   const long long* Eoff, double2* Epool, double* bound, cudaStream_t s);
+size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block);
+cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps_per_block, int grid,
+                            cudaStream_t s);
+cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
+                                long long n, double2* full, cudaStream_t s);
+
+// Cholesky (gx_chol.cu)
+cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const int* info, int nblocks, int n,
+                             double* D, cudaStream_t s);
+cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info, int nblocks,
+                             const int* cand, int ncand, int nc, int nd, int n, void* const* dst, cudaStream_t s);
+cudaError_t launch_chol_scan(const double* res, long long N, void* partial, void* out, cudaStream_t s);
+cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, long long piv, const void* column,
+                             void* work, int n, double* res, double* scale, void* Lrow, void* partial, void* out,
+                             cudaStream_t s);
+cudaError_t launch_chol_final_residual(bool real, const double* D, const void* L, int rank, long long N, double* res,
+                                       cudaStream_t s);
+size_t chol_red_bytes();
+size_t chol_partial_bytes();
+
+cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops);
+
+}  // namespace gx

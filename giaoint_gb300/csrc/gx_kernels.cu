@@ -1,0 +1,570 @@
+// GB300 kernels for the GIAO electron-repulsion path.
+//
+//   boys_table_kernel     scaled Boys values on the Taylor grid (setup)
+//   boys_values_kernel    F_0..F_n(z) for the boys() entry point (K2)
+//   pair_kernel           primitive-pair records: complex centre, prefactor
+//                         and complex Hermite coefficients (K1)
+//   quartet_kernel        class-generic shell-quartet ERIs (K3/K4)
+//   scatter_full_kernel   the four symmetry images of the full tensor (K5)
+//
+// Formulation (own derivation; same integral as src/eri.cpp:67-384).
+// The reference builds, per Cartesian component quartet, a six-index complex
+// table R_{tuv;tau phi chi} whose recurrence carries the London phase as
+// -i q terms.  Writing R = d^t/dP^t d^tau/dQ^tau [e^{-i q_ab.P - i q_cd.Q}
+// H(P - Q)] and applying Leibniz per axis gives
+//   (ab|cd) = sum_{K,K'} E~ab_K E~cd_K' (-1)^{|K'|} Rh_{K+K'}
+// with complex Hermite coefficients E~_k = sum_{t>=k} C(t,k) (-i q)^{t-k} E_t
+// (E_t the real McMurchie-Davidson coefficients, src/hermite.cpp:8-40) and
+// Rh the ordinary three-index MD table of the complex centre separation
+// X' = P' - Q', seeded by common (-2 rho)^n F_n(rho X'^2).  E~ depends only
+// on the primitive pair, so it is computed once per (basis, field) by
+// pair_kernel; per primitive quartet only Rh (C(L+3,3) entries) and the two
+// contractions remain.
+#include <cstdio>
+
+#include "gx_internal.h"
+
+namespace gx {
+
+// ---------------------------------------------------------------------------
+// Boys table (setup): S_n(z0) = e^{z0} F_n(z0), n < 43, on the 1/8 grid.
+// Fixed-segment 32-point Gauss-Legendre of the scaled integral, segments
+// doubled until two successive results agree to 4e-16 relative.
+// ---------------------------------------------------------------------------
+
+// Compensated fixed-segment 32-point Gauss-Legendre of the scaled integral
+// (setup only).
+__device__ void boys_quad_kahan(double x, double y, int L, int segments, const GLRules* gl, double2* out,
+                                double2* comp) {
+    for (int n = 0; n <= L; ++n) {
+        out[n] = c2(0.0, 0.0);
+        comp[n] = c2(0.0, 0.0);
+    }
+    const double inv = 1.0 / (double)segments;
+    const double hw = 0.5 * inv;
+    for (int s = 0; s < segments; ++s) {
+        const double mid = ((double)s + 0.5) * inv;
+        for (int k = 0; k < 32; ++k) {
+            const double t = fma(hw, gl->x32[k], mid);
+            const double t2 = t * t;
+            const double a = 1.0 - t2;
+            const double mag = exp(x * a) * hw * gl->w32[k];
+            double sn, cs;
+            sincos(y * a, &sn, &cs);
+            double2 term = c2(mag * cs, mag * sn);
+            for (int n = 0; n <= L; ++n) {
+                // Kahan summation per component
+                const double yr = term.x - comp[n].x, yi = term.y - comp[n].y;
+                const double tr = out[n].x + yr, ti = out[n].y + yi;
+                comp[n] = c2((tr - out[n].x) - yr, (ti - out[n].y) - yi);
+                out[n] = c2(tr, ti);
+                term = cscale(term, t2);
+            }
+        }
+    }
+}
+
+__global__ void boys_table_kernel(double2* S, double2* E0, const GLRules* gl, int* fail_count) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= BOYS_NX * BOYS_NY) return;
+    const int ix = p / BOYS_NY, iy = p - ix * BOYS_NY;
+    const double x = BOYS_X0 + BOYS_H * ix, y = -BOYS_Y1 + BOYS_H * iy;
+    constexpr int N = BOYS_TABLE_ORDERS - 1;
+    double2 a[N + 1], b[N + 1], c[N + 1];
+    int segments = (int)ceil(fmax(fabs(x), fabs(y)) / 4.0);
+    if (segments < 4) segments = 4;
+    boys_quad_kahan(x, y, N, segments, gl, a, c);
+    bool ok = false;
+    double worst = 0.0;
+    for (int it = 0; it < 8 && !ok; ++it) {
+        segments *= 2;
+        boys_quad_kahan(x, y, N, segments, gl, b, c);
+        ok = true;
+        worst = 0.0;
+        for (int n = 0; n <= N; ++n) {
+            const double dx = b[n].x - a[n].x, dy = b[n].y - a[n].y;
+            const double m = sqrt(b[n].x * b[n].x + b[n].y * b[n].y);
+            const double rel = sqrt(dx * dx + dy * dy) / (m + 1e-300);
+            worst = fmax(worst, rel);
+            ok = ok && rel <= 2.0e-15;
+            a[n] = b[n];
+        }
+    }
+    // worst relative agreement of the last two refinements (positive doubles
+    // order as their bit patterns)
+    atomicMax(reinterpret_cast<unsigned long long*>(fail_count) + 1, __double_as_longlong(worst));
+    if (worst > 1.0e-13) atomicAdd(fail_count, 1);
+    double2* dst = S + (size_t)p * BOYS_TABLE_ORDERS;
+    for (int n = 0; n <= N; ++n) dst[n] = a[n];
+    double sn, cs;
+    sincos(-y, &sn, &cs);
+    const double m = exp(-x);
+    E0[p] = c2(m * cs, m * sn);
+}
+
+cudaError_t launch_boys_table(double2* S, double2* E0, const GLRules* gl, int* fail_count, cudaStream_t s) {
+    const int n = BOYS_NX * BOYS_NY;
+    boys_table_kernel<<<(n + 127) / 128, 128, 0, s>>>(S, E0, gl, fail_count);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// boys() entry point: one thread per argument.  region follows the
+// reference's dispatch (src/boys.cpp:245-294) for diagnostics.
+// ---------------------------------------------------------------------------
+
+__global__ void boys_values_kernel(const double2* z, long long count, int nmax, int scaled, BoysTable tab,
+                                   const GLRules* gl, double2* out, int* region, DevStatus* st) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const double x = z[i].x, y = z[i].y;
+    double2 Sh[BOYS_MAX_ORDER + 1];
+    double2 e0;
+    if (boys_eval(x, y, nmax, tab, gl, Sh, e0)) {
+        report(st, -4, i, nmax, x, y);
+        return;
+    }
+    // scaled output: e^{z} F_n = e^{z} e0 Sh
+    double2 f = e0;
+    if (scaled) {
+        double sn, cs;
+        sincos(y, &sn, &cs);
+        const double m = exp(x);
+        f = cmul(f, c2(m * cs, m * sn));
+    }
+    bool finite = true;
+    for (int n = 0; n <= nmax; ++n) {
+        const double2 v = cmul(f, Sh[n]);
+        finite = finite && isfinite(v.x) && isfinite(v.y);
+        out[i * (nmax + 1) + n] = v;
+    }
+    if (!finite) report(st, -40, i, nmax, x, y);
+    if (region) {
+        const double mag = sqrt(x * x + y * y);
+        int r;
+        if (mag <= 0.75)
+            r = 0;
+        else if (x >= 2.0 * nmax + 60.0 && fabs(y) <= 0.5 * x)
+            r = 3;
+        else if (x < 0.0)
+            r = 2;
+        else
+            r = 1;
+        region[i] = r;
+    }
+}
+
+cudaError_t launch_boys_values(const double2* z, long long count, int nmax, int scaled, const BoysTable& tab,
+                               const GLRules* gl, double2* out, int* region, DevStatus* st, cudaStream_t s) {
+    if (count <= 0) return cudaSuccess;
+    boys_values_kernel<<<(unsigned)((count + 127) / 128), 128, 0, s>>>(z, count, nmax, scaled, tab, gl, out,
+                                                                          region, st);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K1: primitive-pair records.  One thread per primitive pair.
+// ---------------------------------------------------------------------------
+
+__device__ double log_odd_double_factorial(int l) {
+    // ln((2l-1)!!) = l ln 2 + lgamma(l + 1/2) - ln(pi)/2
+    if (l == 0) return 0.0;
+    return l * 0.69314718055994530942 + lgamma(l + 0.5) - 0.57236494292470008707;
+}
+
+// Radial part of the primitive normalisation (src/types.cpp:60-72) without
+// the component factor: (2a/pi)^{3/4} (4a)^{l/2}.
+__device__ double radial_norm(double a, int l) {
+    return exp(0.75 * log(2.0 * a / 3.14159265358979323846) + 0.5 * l * log(4.0 * a));
+}
+
+// 1-D real MD coefficients E^{ij}_t, t <= i + j, by repeated raising
+// (src/hermite.cpp:8-40): first i raisings about A, then j about B.
+__device__ void hermite_1d(int i, int j, double PA, double PB, double inv2p, double* e) {
+    const int n = i + j;
+    for (int t = 0; t <= n + 1; ++t) e[t] = 0.0;
+    e[0] = 1.0;
+    for (int step = 0; step < n; ++step) {
+        const double d = step < i ? PA : PB;
+        // in place, descending t: new e[t] = inv2p e[t-1] + d e[t] + (t+1) e[t+1]
+        double upper = 0.0;  // old e[t+1]
+        for (int t = step + 1; t >= 0; --t) {
+            const double old = e[t];
+            e[t] = (t > 0 ? inv2p * e[t - 1] : 0.0) + d * old + (double)(t + 1) * upper;
+            upper = old;
+        }
+    }
+}
+
+__global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const int* pp_a, const int* pp_b,
+                            const int* pp_pa, const int* pp_pb, const int* pp_class, const PairClassDev* classes,
+                            double* out_p, double* out_Pr, double* out_Pi, double2* out_F, const long long* Eoff,
+                            double2* Epool, double* out_bound) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npp) return;
+    const int a = pp_a[i], b = pp_b[i];
+    const int pa = bs.primoff[a] + pp_pa[i], pb = bs.primoff[b] + pp_pb[i];
+    const double al = bs.exps[pa], be = bs.exps[pb];
+    const double A[3] = {bs.center[3 * a], bs.center[3 * a + 1], bs.center[3 * a + 2]};
+    const double Bc[3] = {bs.center[3 * b], bs.center[3 * b + 1], bs.center[3 * b + 2]};
+    const double p = al + be, mu = al * be / p;
+    double P[3], q[3], r2 = 0.0;
+    const double Bv[3] = {B.x, B.y, B.z}, Ov[3] = {O.x, O.y, O.z};
+    double ka[3], kb[3];
+    {
+        // London wave vectors k = B x (R - O) / 2 (src/types.cpp:179-186)
+        const double da[3] = {A[0] - Ov[0], A[1] - Ov[1], A[2] - Ov[2]};
+        const double db[3] = {Bc[0] - Ov[0], Bc[1] - Ov[1], Bc[2] - Ov[2]};
+        ka[0] = 0.5 * (Bv[1] * da[2] - Bv[2] * da[1]);
+        ka[1] = 0.5 * (Bv[2] * da[0] - Bv[0] * da[2]);
+        ka[2] = 0.5 * (Bv[0] * da[1] - Bv[1] * da[0]);
+        kb[0] = 0.5 * (Bv[1] * db[2] - Bv[2] * db[1]);
+        kb[1] = 0.5 * (Bv[2] * db[0] - Bv[0] * db[2]);
+        kb[2] = 0.5 * (Bv[0] * db[1] - Bv[1] * db[0]);
+    }
+    double qP = 0.0, qq = 0.0;
+    for (int x = 0; x < 3; ++x) {
+        P[x] = (al * A[x] + be * Bc[x]) / p;
+        q[x] = kb[x] - ka[x];
+        r2 += (A[x] - Bc[x]) * (A[x] - Bc[x]);
+        qP += q[x] * P[x];
+        qq += q[x] * q[x];
+    }
+    const int la = bs.l[a], lb = bs.l[b];
+    const bool raw_a = bs.raw[a] != 0, raw_b = bs.raw[b] != 0;
+    const double na = raw_a ? 1.0 : radial_norm(al, la);
+    const double nb = raw_b ? 1.0 : radial_norm(be, lb);
+    // 2 pi^{5/2} / (p q sqrt(p+q)) = sqrt(2 pi^{5/2})/p * sqrt(2 pi^{5/2})/q / sqrt(p+q)
+    const double mag = 5.914967172795613 * bs.coefs[pa] * bs.coefs[pb] * na * nb * exp(-mu * r2) / p;
+    double sn, cs;
+    sincos(-qP, &sn, &cs);
+    const double damp = exp(-qq / (4.0 * p));
+    out_p[i] = p;
+    for (int x = 0; x < 3; ++x) {
+        out_Pr[3 * i + x] = P[x];
+        out_Pi[3 * i + x] = -0.5 * q[x] / p;
+    }
+    out_F[i] = c2(mag * damp * cs, mag * damp * sn);
+
+    // complex Hermite coefficients per axis and per component pair
+    const PairClassDev pc = classes[pp_class[i]];
+    double2* rec = Epool + Eoff[i];
+    const double inv2p = 0.5 / p;
+    int ab = 0;
+    double bmax = 0.0;
+    for (int xa = la; xa >= 0; --xa)
+        for (int ya = la - xa; ya >= 0; --ya) {
+            const int ca[3] = {xa, ya, la - xa - ya};
+            for (int xb = lb; xb >= 0; --xb)
+                for (int yb = lb - xb; yb >= 0; --yb, ++ab) {
+                    const int cb[3] = {xb, yb, lb - xb - yb};
+                    double2 Et[3][34];
+                    int dim[3];
+                    double g = 1.0;
+                    for (int x = 0; x < 3; ++x) {
+                        if (!raw_a) g *= exp(-0.5 * log_odd_double_factorial(ca[x]));
+                        if (!raw_b) g *= exp(-0.5 * log_odd_double_factorial(cb[x]));
+                        double e[35];
+                        hermite_1d(ca[x], cb[x], P[x] - A[x], P[x] - Bc[x], inv2p, e);
+                        const int n = ca[x] + cb[x];
+                        dim[x] = n + 1;
+                        // E~_k = sum_{t>=k} C(t,k) (-i q)^{t-k} E_t
+                        for (int k = 0; k <= n; ++k) {
+                            double2 acc = c2(0.0, 0.0);
+                            double binom = 1.0;        // C(t, k) for t = k
+                            double2 pw = c2(1.0, 0.0); // (-i q)^{t-k}
+                            for (int t = k; t <= n; ++t) {
+                                acc = cadd(acc, cscale(pw, binom * e[t]));
+                                pw = cmul(pw, c2(0.0, -q[x]));
+                                binom = binom * (double)(t + 1) / (double)(t + 1 - k);
+                            }
+                            Et[x][k] = acc;
+                        }
+                    }
+                    const int off = pc.boxoff[ab];
+                    int e = 0;
+                    for (int k = 0; k < dim[0]; ++k)
+                        for (int l = 0; l < dim[1]; ++l) {
+                            const double2 xy = cmul(Et[0][k], Et[1][l]);
+                            for (int m = 0; m < dim[2]; ++m, ++e) {
+                                const double2 v = cscale(cmul(xy, Et[2][m]), g);
+                                rec[off + e] = v;
+                                bmax = fmax(bmax, fabs(v.x) + fabs(v.y));
+                            }
+                        }
+                }
+        }
+    out_bound[i] = mag * damp * bmax;
+}
+
+cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
+                                   const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
+                                   const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
+                                   const long long* Eoff, double2* Epool, double* bound, cudaStream_t s) {
+    if (npp <= 0) return cudaSuccess;
+    pair_kernel<<<(npp + 63) / 64, 64, 0, s>>>(basis, make_double3(B[0], B[1], B[2]), make_double3(O[0], O[1], O[2]),
+                                               npp, pp_a, pp_b, pp_pa, pp_pb, pp_class, classes, p, Pr, Pi, F, Eoff,
+                                               Epool, bound);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K3/K4: class-generic quartet kernel, one warp per shell quartet.
+//
+// Phase 1 (lane-parallel): up to B1 primitive quartets (P, Q..Q+B1) at a
+//   time, one per lane: T = rho X'^2, Boys, seeds, and the in-place Rh
+//   recurrence into the lane's column of shared memory.
+// Phase 2 (warp-cooperative, per primitive quartet): ket transform
+//   W[K][cd] += sum_{K' in box(cd)} E~cd_K' Rh_{K+K'}, accumulated over the
+//   ket primitive pairs; then, once per bra primitive pair, the bra
+//   transform out[ab][cd] += sum_{K in box(ab)} E~ab_K W[K][cd] straight
+//   into the caller's output block (lane-owned entries, coalesced).
+// The sign (-1)^{|K'|} of the ket side is applied to the ket records when
+// they are read as kets (ket_sign below).
+// ---------------------------------------------------------------------------
+
+__constant__ double c_int[40];  // c_int[k] = k, avoids int->double conversions in inner loops
+
+__device__ __forceinline__ void phase1(const EriDev& d, int L, int ip, int iq, double2* col, int stride,
+                                       long long item) {
+    const PairData& pp = d.pairs;
+    const double p = pp.p[ip], q = pp.p[iq];
+    const double Xr0 = pp.Pr[3 * ip] - pp.Pr[3 * iq], Xr1 = pp.Pr[3 * ip + 1] - pp.Pr[3 * iq + 1],
+                 Xr2 = pp.Pr[3 * ip + 2] - pp.Pr[3 * iq + 2];
+    const double Xi0 = pp.Pi[3 * ip] - pp.Pi[3 * iq], Xi1 = pp.Pi[3 * ip + 1] - pp.Pi[3 * iq + 1],
+                 Xi2 = pp.Pi[3 * ip + 2] - pp.Pi[3 * iq + 2];
+    const double r = rsqrt(p + q);
+    const double rho = p * q * r * r;
+    const double tre = rho * (fma(Xr0, Xr0, fma(Xr1, Xr1, Xr2 * Xr2)) - fma(Xi0, Xi0, fma(Xi1, Xi1, Xi2 * Xi2)));
+    const double tim = 2.0 * rho * fma(Xr0, Xi0, fma(Xr1, Xi1, Xr2 * Xi2));
+    double2 Sh[BOYS_MAX_ORDER + 1];
+    double2 e0;
+    double2 C = cscale(cmul(pp.F[ip], pp.F[iq]), r);
+    if (boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
+        report(d.status, -4, item, L, tre, tim);
+        C = c2(0.0, 0.0);
+        e0 = c2(0.0, 0.0);
+        for (int n = 0; n <= L; ++n) Sh[n] = c2(0.0, 0.0);
+    }
+    C = cmul(C, e0);
+    // seeds (-2 rho)^n C Sh_n, folded into Sh
+    const double m2r = -2.0 * rho;
+    double2 cn = C;
+    for (int n = 0; n <= L; ++n) {
+        Sh[n] = cmul(cn, Sh[n]);
+        cn = cscale(cn, m2r);
+    }
+    const double2 X[3] = {c2(Xr0, Xi0), c2(Xr1, Xi1), c2(Xr2, Xi2)};
+    col[0] = Sh[L];
+    for (int n = L - 1; n >= 0; --n) {
+        for (int dg = L - n; dg >= 1; --dg) {
+            for (int k = dg; k >= 0; --k) {
+                for (int l = dg - k; l >= 0; --l) {
+                    const int m = dg - k - l;
+                    int axis, pw, i1, i2;
+                    if (k > 0) {
+                        axis = 0;
+                        pw = k;
+                        i1 = herm_index(k - 1, l, m);
+                        i2 = k > 1 ? herm_index(k - 2, l, m) : 0;
+                    } else if (l > 0) {
+                        axis = 1;
+                        pw = l;
+                        i1 = herm_index(0, l - 1, m);
+                        i2 = l > 1 ? herm_index(0, l - 2, m) : 0;
+                    } else {
+                        axis = 2;
+                        pw = m;
+                        i1 = herm_index(0, 0, m - 1);
+                        i2 = m > 1 ? herm_index(0, 0, m - 2) : 0;
+                    }
+                    double2 v = cmul(X[axis], col[i1 * stride]);
+                    if (pw > 1) v = cmacr(v, c_int[pw - 1], col[i2 * stride]);
+                    col[herm_index(k, l, m) * stride] = v;
+                }
+            }
+        }
+        col[0] = Sh[n];
+    }
+}
+
+__global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc) {
+    extern __shared__ double2 sm[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const int B1p = qc.B1 + 1;
+    const int per_warp = qc.NL * B1p + qc.Nab * qc.CH;
+    double2* R = sm + (size_t)wib * per_warp;
+    double2* W = R + qc.NL * B1p;
+    const int nab = qc.bra.nab, ncd = qc.ket.nab;
+    const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
+    const int ns = d.basis.ns;
+    for (int tk = blockIdx.x * wpb + wib; tk < qc.ntask; tk += gridDim.x * wpb) {
+        const Task t = qc.tasks[tk];
+        const int Kab = d.basis.nprim[t.sa] * d.basis.nprim[t.sb];
+        const int Kcd = d.basis.nprim[t.sc] * d.basis.nprim[t.sd];
+        const int pab0 = d.basis.sp_off[t.sa * ns + t.sb];
+        const int pcd0 = d.basis.sp_off[t.sc * ns + t.sd];
+        for (int P = 0; P < Kab; ++P) {
+            const int ip = pab0 + P;
+            for (int c0 = 0; c0 < ncd; c0 += qc.CH) {
+                const int chn = min(qc.CH, ncd - c0);
+                for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
+                for (int Q0 = 0; Q0 < Kcd; Q0 += qc.B1) {
+                    const int nb = min(qc.B1, Kcd - Q0);
+                    __syncwarp();
+                    if (lane < nb) phase1(d, qc.L, ip, pcd0 + Q0 + lane, R + lane, B1p, tk);
+                    __syncwarp();
+                    for (int j = 0; j < nb; ++j) {
+                        const double2* Ek = d.pairs.Epool + d.pairs.Eoff[pcd0 + Q0 + j];
+                        for (int it = lane; it < qc.Nab * chn; it += 32) {
+                            const int K = it / chn, cdl = it - K * chn, cd = c0 + cdl;
+                            const uint32_t kx = __ldg(&d.herm_xyz[K]);
+                            const int bk = kx & 255, bl = (kx >> 8) & 255, bm = (kx >> 16) & 255;
+                            const int bo = qc.ket.boxoff[cd];
+                            const int bd = qc.ket.boxdim[cd];
+                            const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+                            double2 acc = W[K * qc.CH + cdl];
+                            for (int e = 0; e < nbox; ++e) {
+                                const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
+                                const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
+                                double2 ev = __ldg(&Ek[bo + e]);
+                                if ((k2 + l2 + m2) & 1) ev = c2(-ev.x, -ev.y);
+                                acc = cmac(acc, ev, R[herm_index(bk + k2, bl + l2, bm + m2) * B1p + j]);
+                            }
+                            W[K * qc.CH + cdl] = acc;
+                        }
+                    }
+                }
+                __syncwarp();
+                const double2* Ea = d.pairs.Epool + d.pairs.Eoff[ip];
+                for (int it = lane; it < nab * chn; it += 32) {
+                    const int ab = it / chn, cdl = it - ab * chn, cd = c0 + cdl;
+                    const int bo = qc.bra.boxoff[ab];
+                    const int bd = qc.bra.boxdim[ab];
+                    const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+                    double2 acc = c2(0.0, 0.0);
+                    for (int e = 0; e < nbox; ++e) {
+                        const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
+                        const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+                        acc = cmac(acc, __ldg(&Ea[bo + e]), W[K * qc.CH + cdl]);
+                    }
+                    const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
+                    double2* o = d.out + t.out_off + (long long)ca * t.st[0] + (long long)cb * t.st[1] +
+                                 (long long)cc * t.st[2] + (long long)cdd * t.st[3];
+                    *o = P == 0 ? acc : cadd(*o, acc);
+                }
+                __syncwarp();
+            }
+        }
+    }
+}
+
+size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block) {
+    return (size_t)warps_per_block * ((size_t)qc.NL * (qc.B1 + 1) + (size_t)qc.Nab * qc.CH) * sizeof(double2);
+}
+
+static bool g_const_ready = false;
+
+cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps_per_block, int grid,
+                            cudaStream_t s) {
+    if (qc.ntask <= 0) return cudaSuccess;
+    if (!g_const_ready) {
+        double v[40];
+        for (int i = 0; i < 40; ++i) v[i] = (double)i;
+        cudaError_t e = cudaMemcpyToSymbol(c_int, v, sizeof v);
+        if (e != cudaSuccess) return e;
+        g_const_ready = true;
+    }
+    const size_t smem = quartet_smem_bytes(qc, warps_per_block);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(quartet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    quartet_kernel<<<grid, warps_per_block * 32, smem, s>>>(dev, qc);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K5: full-tensor images (src/eri.cpp:777-805).  block_info[5*i] =
+// (ga, gb, gc, gd AO offsets, packed shape na | nb<<8 | nc<<16 | nd<<24).
+// One thread per packed element; images written in the reference's order.
+// ---------------------------------------------------------------------------
+
+__global__ void scatter_full_kernel(const double2* packed, const long long* block_off, const int* info, int nblocks,
+                                    long long n, double2* full) {
+    const int bi = blockIdx.y * gridDim.x + blockIdx.x;
+    if (bi >= nblocks) return;
+    const int* f = info + 5 * bi;
+    const int sh = f[4];
+    const int na = sh & 255, nb = (sh >> 8) & 255, nc = (sh >> 16) & 255, nd = (sh >> 24) & 255;
+    const int total = na * nb * nc * nd;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int id = e % nd, ic = (e / nd) % nc, ib = (e / (nd * nc)) % nb, ia = e / (nd * nc * nb);
+        const double2 v = packed[block_off[bi] + e];
+        const long long a = f[0] + ia, b = f[1] + ib, c = f[2] + ic, dd = f[3] + id;
+        full[((a * n + b) * n + c) * n + dd] = v;
+        full[((c * n + dd) * n + a) * n + b] = v;
+        full[((b * n + a) * n + dd) * n + c] = cconj(v);
+        full[((dd * n + c) * n + b) * n + a] = cconj(v);
+    }
+}
+
+cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
+                                long long n, double2* full, cudaStream_t s) {
+    if (nblocks <= 0) return cudaSuccess;
+    const int gx = nblocks < 65535 ? nblocks : 65535;
+    const int gy = (nblocks + gx - 1) / gx;
+    scatter_full_kernel<<<dim3(gx, gy), 128, 0, s>>>(packed, block_off, block_info, nblocks, n, full);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 FMA throughput probe: 8 independent dependent-FMA chains per thread,
+// 8 resident blocks of 256 threads per SM.
+// ---------------------------------------------------------------------------
+
+__global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+           x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            x0 = fma(x0, a, b);
+            x1 = fma(x1, a, b);
+            x2 = fma(x2, a, b);
+            x3 = fma(x3, a, b);
+            x4 = fma(x4, a, b);
+            x5 = fma(x5, a, b);
+            x6 = fma(x6, a, b);
+            x7 = fma(x7, a, b);
+        }
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops) {
+    const int blocks = sms * 8, threads = 256, iters = 1000;
+    double* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, sizeof(double) * blocks * threads);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(buf, 20, 1.0000001, 1e-9);
+    cudaEventRecord(a, s);
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(buf, iters, 1.0000001, 1e-9);
+    cudaEventRecord(b, s);
+    e = cudaEventSynchronize(b);
+    cudaEventElapsedTime(ms, a, b);
+    *flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(buf);
+    return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+}  // namespace gx

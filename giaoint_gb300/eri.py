@@ -1,0 +1,281 @@
+"""Electron-repulsion entry points on the GPU, with the reference's Python API.
+
+Mirrors python/giao_integrals/eri.py:1-208 and the native entry points
+``primitive_eri``, ``eri_shell``, ``_eri_full``, ``_eri_batch`` and
+``_EriSchwarzBounds`` (src/bindings.cpp:409-425, 599-731): same names,
+keyword arguments, validation and error types.  ``threads`` is accepted and
+validated for compatibility and has no effect (the work runs on one GPU).
+Two keyword arguments are additions: ``precision`` ("fp64" or "mixed") and
+``mixed_cutoff``, the FP32 gating bound of the mixed mode.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections.abc import Iterable, Iterator, Sequence
+from dataclasses import dataclass
+from itertools import product
+from math import prod
+
+import numpy as np
+import numpy.typing as npt
+
+from . import _native as nat
+from ._threads import resolve_num_threads
+from ._types import Basis, MagneticField, PrimitiveGaussian, Shell, field_arrays
+
+Quartet = tuple[int, int, int, int]
+
+PRECISIONS = {"fp64": 0, "mixed": 1}
+DEFAULT_MIXED_CUTOFF = 1.0e-6
+
+
+def _precision(precision: str) -> int:
+    try:
+        return PRECISIONS[precision]
+    except KeyError:
+        raise ValueError("precision must be 'fp64' or 'mixed'") from None
+
+
+@dataclass(frozen=True)
+class EriBatch:
+    """Packed shell-quartet results and screening counts.
+
+    ``values[offsets[i]:offsets[i + 1]]`` reshaped to ``shapes[i]`` is the
+    C-contiguous block for ``quartets[i]``.
+    """
+
+    quartets: npt.NDArray[np.uint32]
+    shapes: npt.NDArray[np.int64]
+    offsets: npt.NDArray[np.int64]
+    values: npt.NDArray[np.complex128]
+    requested_count: int = 0
+    screened_count: int = 0
+
+    def block(self, index: int) -> npt.NDArray[np.complex128]:
+        start = int(self.offsets[index])
+        stop = int(self.offsets[index + 1])
+        return self.values[start:stop].reshape(tuple(self.shapes[index]))
+
+
+def _checked_quartets(shell_count: int, quartets: Iterable[Sequence[int]] | None) -> Iterator[Quartet]:
+    if quartets is None:
+        for quartet in product(range(shell_count), repeat=4):
+            a, b, c, d = quartet
+            if min(quartet, (c, d, a, b), (b, a, d, c), (d, c, b, a)) == quartet:
+                yield quartet
+        return
+    for value in quartets:
+        if len(value) != 4:
+            raise ValueError("each shell quartet must contain four indices")
+        if any(isinstance(index, (bool, np.bool_)) for index in value):
+            raise ValueError("shell-quartet indices must be integers")
+        try:
+            quartet = tuple(int(index) for index in value)
+        except (TypeError, ValueError, OverflowError) as error:
+            raise ValueError("shell-quartet indices must be integers") from error
+        if any(converted != original for converted, original in zip(quartet, value, strict=True)):
+            raise ValueError("shell-quartet indices must be integers")
+        if any(index < 0 or index >= shell_count for index in quartet):
+            raise IndexError("shell-quartet index is out of range")
+        yield quartet  # type: ignore[misc]
+
+
+def canonical_quartets(shell_count: int) -> np.ndarray:
+    """All canonical representatives of the finite-field orbit
+    {(ab|cd), (cd|ab), (ba|dc)*, (dc|ba)*} (src/eri.cpp:414-429), uint32[k, 4],
+    in the reference's enumeration order (native host enumeration)."""
+    n = int(shell_count)
+    count = nat.lib().gx_canonical_quartets(n, None)
+    out = np.empty((max(count, 1), 4), dtype=np.uint32)
+    if count:
+        nat.lib().gx_canonical_quartets(n, nat.u32ptr(out))
+    return out[:count]
+
+
+def _eri_batch(basis: Basis, quartets, *, field: MagneticField | None = None, screening_threshold: float = 0.0,
+               threads=None, bounds=None, precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF,
+               context=None):
+    """Native packed batch (src/bindings.cpp:672-731): returns
+    (quartets uint32[k,4], shapes int64[k,4], offsets int64[k+1],
+    values complex128, requested, screened)."""
+    resolve_num_threads(threads)
+    ctx = context or nat.default_context()
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+    ns = len(basis.shells)
+    if len(q) and (q.min() < 0 or q.max() >= ns):
+        raise IndexError("ERI shell-quartet index is out of range")
+    q = q.astype(np.uint32)
+    screening_threshold = float(screening_threshold)
+    if not np.isfinite(screening_threshold) or screening_threshold < 0.0:
+        raise ValueError("ERI screening threshold must be finite and non-negative")
+    sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+    total = int(np.prod(sizes[q.astype(np.int64)], axis=1).sum()) if len(q) else 0
+    values = np.empty(max(total, 1), dtype=np.complex128)
+    offsets = np.zeros(len(q) + 1, dtype=np.int64)
+    kept = np.empty((max(len(q), 1), 4), dtype=np.uint32)
+    stats = nat.GxStats()
+    B, O = field_arrays(field)
+    nat.check(nat.lib().gx_eri_batch(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O), nat.u32ptr(q),
+                                     len(q), _precision(precision), float(mixed_cutoff), screening_threshold,
+                                     nat.u32ptr(kept), nat.i64ptr(offsets), nat.dptr(values.view(np.float64)),
+                                     total, ctypes.byref(stats)))
+    k = int(stats.computed)
+    kept = kept[:k]
+    offsets = offsets[: k + 1]
+    shapes = sizes[kept.astype(np.int64)] if k else np.zeros((0, 4), dtype=np.int64)
+    return kept, shapes, offsets, values[: int(offsets[-1])], int(stats.requested), int(stats.screened)
+
+
+def eri_batches(basis: Basis, *, field: MagneticField | None = None, quartets: Iterable[Sequence[int]] | None = None,
+                target_bytes: int = 64 * 1024 * 1024, screening_threshold: float = 0.0, threads: int | None = None,
+                precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF) -> Iterator[EriBatch]:
+    """Yield packed shell-quartet batches without allocating an AO tensor
+    (python/giao_integrals/eri.py:80-146)."""
+    if isinstance(target_bytes, (bool, np.bool_)) or not isinstance(target_bytes, (int, np.integer)):
+        raise ValueError("target_bytes must be a positive integer")
+    if target_bytes <= 0:
+        raise ValueError("target_bytes must be a positive integer")
+    screening_threshold = float(screening_threshold)
+    if not np.isfinite(screening_threshold) or screening_threshold < 0.0:
+        raise ValueError("screening_threshold must be finite and non-negative")
+    threads = resolve_num_threads(threads)
+    _precision(precision)
+    shells = basis.shells
+    sizes = [s.ao_count for s in shells]
+    packed: list[Quartet] = []
+    packed_bytes = 0
+
+    def emit() -> EriBatch:
+        q, shapes, offsets, values, requested, screened = _eri_batch(
+            basis, packed, field=field, screening_threshold=screening_threshold, threads=threads,
+            precision=precision, mixed_cutoff=mixed_cutoff)
+        return EriBatch(q, shapes, offsets, values, requested, screened)
+
+    for quartet in _checked_quartets(len(shells), quartets):
+        block_bytes = prod(sizes[i] for i in quartet) * 16
+        if packed and packed_bytes + block_bytes > target_bytes:
+            yield emit()
+            packed.clear()
+            packed_bytes = 0
+        packed.append(quartet)
+        packed_bytes += int(block_bytes)
+    if packed:
+        yield emit()
+
+
+def _eri_full(basis: Basis, *, field: MagneticField | None = None, screening_threshold: float = 0.0, threads=None,
+              precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF, context=None):
+    """Native full tensor (src/bindings.cpp:640-671)."""
+    resolve_num_threads(threads)
+    ctx = context or nat.default_context()
+    n = basis.ao_count
+    out = np.empty((n, n, n, n), dtype=np.complex128)
+    B, O = field_arrays(field)
+    nat.check(nat.lib().gx_eri_full(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                    _precision(precision), float(mixed_cutoff), float(screening_threshold),
+                                    nat.dptr(out.view(np.float64).reshape(-1))))
+    return out
+
+
+def eri(basis: Basis, *, field: MagneticField | None = None, storage: str = "blocks", max_bytes: int | None = None,
+        target_bytes: int = 64 * 1024 * 1024, screening_threshold: float = 0.0, threads: int | None = None,
+        precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF):
+    """Streamed blocks or an explicitly guarded full tensor (eri.py:149-200)."""
+    screening_threshold = float(screening_threshold)
+    if not np.isfinite(screening_threshold) or screening_threshold < 0.0:
+        raise ValueError("screening_threshold must be finite and non-negative")
+    threads = resolve_num_threads(threads)
+    if storage == "blocks":
+        if max_bytes is not None:
+            raise ValueError("max_bytes is only valid with storage='full'")
+        return eri_batches(basis, field=field, target_bytes=target_bytes, screening_threshold=screening_threshold,
+                           threads=threads, precision=precision, mixed_cutoff=mixed_cutoff)
+    if storage != "full":
+        raise ValueError("storage must be 'blocks' or 'full'")
+    if max_bytes is None:
+        raise ValueError("storage='full' requires an explicit max_bytes limit")
+    if isinstance(max_bytes, (bool, np.bool_)) or not isinstance(max_bytes, (int, np.integer)):
+        raise ValueError("max_bytes must be a non-negative integer")
+    if max_bytes < 0:
+        raise ValueError("max_bytes must be a non-negative integer")
+    required = basis.ao_count**4 * 16
+    if required > max_bytes:
+        raise MemoryError(f"full ERI tensor requires {required} bytes, exceeding max_bytes={max_bytes}")
+    return _eri_full(basis, field=field, screening_threshold=screening_threshold, threads=threads,
+                     precision=precision, mixed_cutoff=mixed_cutoff)
+
+
+class _EriSchwarzBounds:
+    """Shell-pair Schwarz factors (src/eri.cpp:587-635)."""
+
+    def __init__(self, basis: Basis, *, field: MagneticField | None = None, context=None):
+        ctx = context or nat.default_context()
+        ns = len(basis.shells)
+        out = np.zeros((ns, ns), dtype=np.float64)
+        B, O = field_arrays(field)
+        if ns:
+            nat.check(nat.lib().gx_schwarz(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                           nat.dptr(out.reshape(-1))))
+        self.values = out
+
+    def bound(self, a: int, b: int) -> float:
+        ns = self.values.shape[0]
+        if a < 0 or b < 0 or a >= ns or b >= ns:
+            raise IndexError("ERI Schwarz shell-pair index is out of range")
+        return float(self.values[a, b])
+
+
+def eri_schwarz_bounds(basis: Basis, *, field: MagneticField | None = None) -> npt.NDArray[np.float64]:
+    """The shell-pair Schwarz factors used by ERI screening."""
+    return np.asarray(_EriSchwarzBounds(basis, field=field).values, dtype=np.float64)
+
+
+def _validate_out(out, shape):
+    if out is None:
+        return np.empty(shape, dtype=np.complex128)
+    if not isinstance(out, np.ndarray):
+        raise ValueError("out must be a NumPy array")
+    if out.dtype != np.complex128:
+        raise ValueError("out must have dtype complex128")
+    if out.ndim != len(shape):
+        raise ValueError("out has an incorrect number of dimensions")
+    if tuple(out.shape) != tuple(shape):
+        raise ValueError("out has an incorrect shape")
+    if not out.flags.c_contiguous:
+        raise ValueError("out must be C-contiguous")
+    if not out.flags.writeable:
+        raise ValueError("out must be writable")
+    return out
+
+
+def eri_shell(a: Shell, b: Shell, c: Shell, d: Shell, *, field: MagneticField | None = None, out=None,
+              context=None):
+    """One shell quartet (compute_eri; src/bindings.cpp:616-639)."""
+    shape = (a.ao_count, b.ao_count, c.ao_count, d.ao_count)
+    result = _validate_out(out, shape)
+    ctx = context or nat.default_context()
+    basis = Basis([a, b, c, d])
+    buf = np.empty(shape, dtype=np.complex128)
+    B, O = field_arrays(field)
+    nat.check(nat.lib().gx_eri_shell(ctx.handle, basis._device(ctx), 0, 1, 2, 3, nat.dptr(B), nat.dptr(O),
+                                     nat.dptr(buf.view(np.float64).reshape(-1))))
+    result[...] = buf
+    return result
+
+
+def primitive_eri(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussian, d: PrimitiveGaussian, *,
+                  field: MagneticField | None = None, context=None) -> complex:
+    """One primitive quartet (src/bindings.cpp:599-614)."""
+    prims = (a, b, c, d)
+    ctx = context or nat.default_context()
+    exps = np.ascontiguousarray([p.exponent for p in prims], dtype=np.float64)
+    centers = np.ascontiguousarray([x for p in prims for x in p.center], dtype=np.float64)
+    ang = np.ascontiguousarray([x for p in prims for x in p.angular], dtype=np.int32)
+    coefs = np.ascontiguousarray([p.coefficient for p in prims], dtype=np.float64)
+    norm = np.ascontiguousarray([int(p.normalized) for p in prims], dtype=np.int32)
+    out = np.zeros(2, dtype=np.float64)
+    B, O = field_arrays(field)
+    nat.check(nat.lib().gx_primitive_eri(ctx.handle, nat.dptr(exps), nat.dptr(centers), nat.iptr(ang),
+                                         nat.dptr(coefs), nat.iptr(norm), nat.dptr(B), nat.dptr(O), nat.dptr(out)))
+    return complex(out[0], out[1])

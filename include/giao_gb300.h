@@ -1,0 +1,228 @@
+/*
+ * giao_gb300.h -- C ABI of the GB300 electron-repulsion library.
+ *
+ * Plain pointers and sizes only.  Complex values are interleaved
+ * (re, im) doubles, i.e. the memory layout of C99 double complex, NumPy
+ * complex128 and std::complex<double>.  Every entry point returns 0 on
+ * success or a negative gx_status; the message of the last failure on the
+ * calling thread is returned by gx_last_error().
+ *
+ * Each entry point replaces one native function of the reference library
+ * (simenkva/GIAOINT v0.11.1); the reference interface is cited beside it.
+ * A Python binding over this ABI (ctypes) mirrors the reference's
+ * pybind11 module names and argument meaning.
+ */
+#ifndef GIAO_GB300_H
+#define GIAO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The Python layer maps them to the reference's exception
+ * types (src/bindings.cpp:290-291 and pybind11's standard translation). */
+enum gx_status {
+    GX_OK = 0,
+    GX_EINVAL = -1,   /* std::invalid_argument  -> ValueError              */
+    GX_ERANGE = -2,   /* std::out_of_range      -> IndexError              */
+    GX_ELENGTH = -3,  /* std::length_error      -> ValueError              */
+    GX_EBOYS = -4,    /* giao::BoysNumericalError                          */
+    GX_ECUDA = -5,    /* CUDA runtime failure   -> RuntimeError            */
+    GX_ENOMEM = -6,   /* device memory budget   -> MemoryError             */
+    GX_EPSD = -7,     /* Cholesky residual lost positive semidefiniteness  */
+    GX_ETIMEOUT = -8  /* a bounded device wait gave up                     */
+};
+
+/* Arithmetic of the quartet kernels. */
+enum gx_precision {
+    GX_PRECISION_FP64 = 0,  /* FP64 throughout                                   */
+    GX_PRECISION_MIXED = 1  /* FP32 for primitive quartets under a bound cutoff  */
+};
+
+typedef struct gx_context gx_context; /* one device, its streams, Boys table, pools */
+typedef struct gx_basis gx_basis;     /* shells resident on the device            */
+
+typedef struct gx_eri_stats {
+    int64_t requested;  /* quartets asked for                                  */
+    int64_t computed;   /* quartets evaluated                                  */
+    int64_t screened;   /* quartets dropped by Schwarz screening               */
+    int64_t primitive_quartets; /* primitive quartets evaluated (all precisions) */
+    int64_t fp32_primitive_quartets; /* of which in FP32 (mixed precision)       */
+    int64_t skipped_primitive_quartets; /* dropped under the mixed-mode floor    */
+    double kernel_ms;   /* device time of the quartet kernels                  */
+} gx_eri_stats;
+
+/* ---------------------------------------------------------------------- */
+/* context                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Create a context on CUDA device `device`; builds the Boys tables. */
+int gx_context_create(int device, gx_context** out);
+void gx_context_destroy(gx_context* ctx);
+/* Message of the last failure on the calling thread ("" if none). */
+const char* gx_last_error(void);
+/* Library version string. */
+const char* gx_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* host-side input model                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* primitive_normalization (include/giao_integrals/types.hpp:141-142). */
+double gx_primitive_normalization(double exponent, int lx, int ly, int lz);
+
+/* Shell contraction normalisation as in the Shell constructor
+ * (src/types.cpp:92-159): validates and writes coefs_out[ncontr][nprim].
+ * normalize = 0 copies the coefficients unchanged after validation. */
+int gx_shell_normalize(int l, int nprim, int ncontr, const double* exponents, const double* coefs_in,
+                       int normalize, double* coefs_out);
+
+/* Upload a basis (Basis, include/giao_integrals/types.hpp:108-124).
+ * centers[3*ns]; exponents concatenated per shell; coefs concatenated,
+ * contraction-major [ncontr][nprim] per shell, already normalised.
+ * raw_primitives[s] != 0 omits the Cartesian primitive normalisation of
+ * shell s (used by gx_primitive_eri for unnormalised primitives); may be NULL. */
+int gx_basis_create(gx_context* ctx, int nshell, const double* centers, const int* l, const int* nprim,
+                    const int* ncontr, const double* exponents, const double* coefs, const int* raw_primitives,
+                    gx_basis** out);
+void gx_basis_destroy(gx_basis* basis);
+int64_t gx_basis_ao_count(const gx_basis* basis);
+
+/* ---------------------------------------------------------------------- */
+/* complex Boys function                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* F_0..F_nmax(z) (or e^z F_n when scaled) for `count` arguments:
+ * compute_boys (src/boys.cpp:245-294, bindings.cpp:444-482).
+ * z[2*count]; out[2*count*(nmax+1)] row-major per argument; region[count]
+ * receives the reference's region classification (BoysRegion order:
+ * 0 power series, 1 adaptive quadrature, 2 scaled quadrature,
+ * 3 positive asymptotic) and may be NULL.  Domain failures return GX_EBOYS
+ * with the reference's message. */
+int gx_boys(gx_context* ctx, const double* z, int64_t count, int nmax, int scaled, double* out, int* region);
+
+/* ---------------------------------------------------------------------- */
+/* electron-repulsion integrals                                            */
+/* ---------------------------------------------------------------------- */
+
+/* One primitive quartet with explicit Cartesian powers:
+ * primitive_eri (src/eri.cpp:438-452, bindings.cpp:599-614).
+ * exps[4], centers[12], angular[12], coefs[4], normalized[4], B[3], O[3]. */
+int gx_primitive_eri(gx_context* ctx, const double* exps, const double* centers, const int* angular,
+                     const double* coefs, const int* normalized, const double* B, const double* O, double* out);
+
+/* Shell-quartet blocks packed in input order:
+ * evaluate_eri_shell_quartets + append_eri_block
+ * (src/eri.cpp:644-767, bindings.cpp:267-284, 672-731).
+ * quartets[4*nq] shell indices; B[3], O[3] the field and gauge origin.
+ * Screened quartets (Schwarz bound product < screening_threshold) are
+ * omitted; kept[4*nkept] receives the emitted quartets, offsets[nkept+1]
+ * the complex-element offsets of their blocks, out the values
+ * (host memory, capacity out_capacity complex elements).
+ * precision: gx_precision; mixed_cutoff the FP32 bound cutoff. */
+int gx_eri_batch(gx_context* ctx, gx_basis* basis, const double* B, const double* O, const uint32_t* quartets,
+                 int64_t nq, int precision, double mixed_cutoff, double screening_threshold, uint32_t* kept,
+                 int64_t* offsets, double* out, int64_t out_capacity, gx_eri_stats* stats);
+
+/* Same, with the packed values written to device memory `out_device`
+ * (in-process GPU consumers; no host copy). */
+int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                        const uint32_t* quartets, int64_t nq, int precision, double mixed_cutoff,
+                        double screening_threshold, uint32_t* kept, int64_t* offsets, void* out_device,
+                        int64_t out_capacity, gx_eri_stats* stats);
+
+/* One shell quartet (compute_eri, src/eri.cpp:454-585; bindings.cpp:616-639).
+ * out: complex (na, nb, nc, nd) C order, host memory. */
+int gx_eri_shell(gx_context* ctx, gx_basis* basis, int a, int b, int c, int d, const double* B, const double* O,
+                 double* out);
+
+/* Full symmetric nao^4 tensor (compute_eri_tensor, src/eri.cpp:777-847,
+ * bindings.cpp:640-671).  out: host complex[n^4]. */
+int gx_eri_full(gx_context* ctx, gx_basis* basis, const double* B, const double* O, int precision,
+                double mixed_cutoff, double screening_threshold, double* out);
+
+/* Shell-pair Schwarz factors (EriSchwarzBounds, src/eri.cpp:587-619,
+ * bindings.cpp:409-425).  out[ns*ns]. */
+int gx_schwarz(gx_context* ctx, gx_basis* basis, const double* B, const double* O, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* Cholesky-selected integrals and the pivoted Cholesky driver            */
+/* ---------------------------------------------------------------------- */
+
+/* Diagonal of W: detail::cholesky_diagonal (src/cholesky.cpp:285-314,
+ * bindings.cpp:2306-2314).  pairs[2*npairs] shell pairs a <= b; out[n*n]. */
+int gx_cholesky_diagonal(gx_context* ctx, gx_basis* basis, const int64_t* pairs, int64_t npairs, const double* B,
+                         const double* O, double* out);
+
+/* Pivot columns: detail::cholesky_columns (src/cholesky.cpp:203-323,
+ * bindings.cpp:2315-2330).  pivots[2*npiv] AO pairs sharing one shell
+ * pair.  out: float64[npiv][n][n] when B == 0 exactly, else
+ * complex128[npiv][n][n]. */
+int gx_cholesky_columns(gx_context* ctx, gx_basis* basis, const int64_t* pivots, int64_t npiv, const double* B,
+                        const double* O, double* out);
+
+typedef struct gx_cholesky_options {
+    double threshold;           /* stop when max residual <= max(threshold, floor) */
+    double screening_threshold; /* Schwarz skip of initial diagonal blocks          */
+    int64_t max_rank;           /* output capacity (rows); MemoryError beyond       */
+    int pivot_batch_size;       /* local block-pivot policy; 1 = strict global      */
+} gx_cholesky_options;
+
+/* Streamed pivoted Cholesky of W[(mu,nu),(lam,sig)] = (nu mu|lam sig):
+ * python/giao_integrals/cholesky.py:60-297 with the integrals, pivot search,
+ * factor update and residual kept on the device.
+ * vectors: host complex128[max_rank][n][n]; pivots: int64[max_rank][2].
+ * *rank and *max_residual receive the result. */
+int gx_cholesky(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                const gx_cholesky_options* options, double* vectors, int64_t* pivots, int64_t* rank,
+                double* max_residual);
+
+
+/* ---------------------------------------------------------------------- */
+/* streams, plans and device-resident execution                            */
+/* ---------------------------------------------------------------------- */
+
+/* Enqueue all later device work of `ctx` on `stream` (a cudaStream_t);
+ * NULL restores the context's own stream.  No reference counterpart: the
+ * reference runs synchronously on host threads (src/eri.cpp:708-763). */
+int gx_context_set_stream(gx_context* ctx, void* stream);
+/* Wait for the context's stream and report any device status word. */
+int gx_context_synchronize(gx_context* ctx);
+
+/* A plan fixes a quartet list (its class-sorted task list and packed
+ * offsets, offsets[nq+1]) so that it can be evaluated for many fields
+ * without host work: the persistent batched form of
+ * evaluate_eri_shell_quartets (src/eri.cpp:644-767). */
+typedef struct gx_eri_plan gx_eri_plan;
+int gx_eri_plan_create(gx_context* ctx, gx_basis* basis, const uint32_t* quartets, int64_t nq, int64_t* offsets,
+                       gx_eri_plan** out);
+/* tasks (segmented quartets), primitive quartets, FP64 FLOP-model total and
+ * kernel launches per execution. */
+int gx_eri_plan_info(const gx_eri_plan* plan, int64_t* tasks, int64_t* primitive_quartets, double* model_flops,
+                     int* launches);
+/* Enqueue the evaluation for field (B, O) into device memory out_device
+ * (complex128, offsets from gx_eri_plan_create).  Asynchronous: call
+ * gx_context_synchronize (or synchronise the stream) before reading. */
+int gx_eri_plan_execute(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                        void* out_device);
+void gx_eri_plan_destroy(gx_eri_plan* plan);
+
+/* Canonical shell quartets of an ns-shell basis: the lexicographic
+ * minimum of each finite-field orbit {(ab|cd), (cd|ab), (ba|dc)*, (dc|ba)*}
+ * (canonicalize_shell_quartet, src/eri.cpp:414-429), in the enumeration
+ * order of compute_eri_tensor (src/eri.cpp:825-843).  out[4*count] may be
+ * NULL to count only; returns the count. */
+int64_t gx_canonical_quartets(int ns, uint32_t* out);
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s) from a dependent-
+ * chain probe kernel: the roofline denominator of the FP64-bound kernels. */
+int gx_measure_fp64_peak(gx_context* ctx, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GIAO_GB300_H */

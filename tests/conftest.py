@@ -1,0 +1,32 @@
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = ROOT / "tests" / "golden"
+sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
+
+
+@pytest.fixture(scope="session")
+def golden():
+    class G:
+        boys = json.loads((GOLDEN / "boys.json").read_text())
+        m8 = json.loads((GOLDEN / "primitive_eri_m8.json").read_text())
+        cholesky = json.loads((GOLDEN / "cholesky.json").read_text())
+        blocks = dict(np.load(GOLDEN / "eri_blocks.npz"))
+
+    return G
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from oracle import oracle as O
+
+    return O.Oracle()

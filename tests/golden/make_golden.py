@@ -1,0 +1,235 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run where the reference checkout exists (GIAO_REFERENCE_ROOT, default the
+read-only reference path used to build oracle/_ref):
+
+    python tests/golden/make_golden.py
+
+Inputs and outputs:
+
+* ``boys.json`` -- the reference's Boys test map (tests/python/
+  test_boys_production.py:13-37 arguments x orders 0,3,12,32) and its
+  reachable-domain sample (test_boys_reachable_domain.py:7-44, seed 410404),
+  with the reference library's F_0..F_32 and 40-digit mpmath values;
+* ``primitive_eri_m8.json`` -- the 96 frozen primitive quartets of
+  tests/data/eri_recursive_m8.jsonl (zero and finite field) with their
+  recorded expected values and the reference library's values;
+* ``eri_blocks.npz`` -- reference ``evaluate_eri_shell_quartets`` output for
+  the 19-AO atom (all canonical quartets, B=(0,0,0.1)) and a seeded subset of
+  the 12-atom molecule's canonical quartets;
+* ``cholesky.json`` -- the reference's own NumPy Cholesky driver
+  (python/giao_integrals/cholesky.py, executed unmodified over the reference
+  library's native diagonal/column generators) on the two-shell d/f system of
+  tests/python/test_cholesky.py:14-22 and on a small three-atom molecule.
+
+The product never reads these files at run time; tests compare against them.
+"""
+
+from __future__ import annotations
+
+import importlib.util
+import json
+import os
+import random
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(ROOT))
+
+from giaoint_gb300 import synthetic as syn  # noqa: E402
+from oracle import build_ref  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", "/root/reference"))
+
+BOYS_MAP = [0.0, 1.0e-14 + 1.0e-14j, 0.749999, 0.750001, 1.0 + 4.0j, 20.0 - 35.0j, -1.0 + 2.0j, -30.0 - 12.0j,
+            -100.0 + 20.0j, 123.999, 124.001, 130.0 + 10.0j, 159.999j, 1000.0 - 25.0j]
+
+
+def reachable_arguments():
+    """The argument construction of the reference's reachable-domain test."""
+    g = random.Random(410404)
+    out = []
+    for _ in range(120):
+        ea = 10 ** g.uniform(-1.3, 1.3)
+        eb = 10 ** g.uniform(-1.3, 1.3)
+        e = ea + eb
+        ca = tuple(g.uniform(-2.0, 2.0) for _ in range(3))
+        cb = tuple(g.uniform(-2.0, 2.0) for _ in range(3))
+        nuc = tuple(g.uniform(-2.0, 2.0) for _ in range(3))
+        direction = tuple(g.gauss(0.0, 1.0) for _ in range(3))
+        norm = sum(v * v for v in direction) ** 0.5
+        mag = g.random()
+        field = tuple(mag * v / norm for v in direction)
+        sep = tuple(cb[i] - ca[i] for i in range(3))
+        q = (0.5 * (field[1] * sep[2] - field[2] * sep[1]), 0.5 * (field[2] * sep[0] - field[0] * sep[2]),
+             0.5 * (field[0] * sep[1] - field[1] * sep[0]))
+        P = tuple((ea * ca[i] + eb * cb[i]) / e for i in range(3))
+        cc = tuple(P[i] - 0.5j * q[i] / e for i in range(3))
+        out.append(e * sum((cc[i] - nuc[i]) ** 2 for i in range(3)))
+    return out
+
+
+def boys_fixture(ref):
+    import mpmath as mp
+
+    def hyp(n, z):
+        with mp.workdps(40):
+            zz = mp.mpc(z)
+            return complex(mp.hyp1f1(n + mp.mpf("0.5"), n + mp.mpf("1.5"), -zz) / (2 * n + 1))
+
+    cases = []
+    for z in BOYS_MAP + reachable_arguments():
+        z = complex(z)
+        vals, diag = ref.boys(z, 32)
+        cases.append({"z": [z.real, z.imag], "region": diag["region"],
+                      "reference": [[v.real, v.imag] for v in vals],
+                      "mpmath": [[hyp(n, z).real, hyp(n, z).imag] for n in (0, 1, 3, 8, 12, 16, 32)]})
+    scaled = []
+    for z in (-0.3 + 0.2j, -20.0 + 5.0j, -120.0 - 8.0j, 3.0 - 7.0j):
+        vals, _ = ref.boys(z, 16, scaled=True)
+        scaled.append({"z": [z.real, z.imag], "reference": [[v.real, v.imag] for v in vals]})
+    errors = []
+    for z, n in ((10.0 + 500.0j, 4), (160.001j, 4)):
+        try:
+            ref.boys(z, n)
+            raise SystemExit("expected a Boys domain error")
+        except O.OracleError as e:
+            errors.append({"z": [z.real, z.imag], "order": n, "message": str(e)})
+    return {"mpmath_orders": [0, 1, 3, 8, 12, 16, 32], "cases": cases, "scaled": scaled, "errors": errors}
+
+
+def m8_fixture(ref):
+    records = [json.loads(x) for x in (REFERENCE / "tests/data/eri_recursive_m8.jsonl").read_text().splitlines()]
+    out = []
+    for r in records:
+        prims = [(p["exponent"], p["center"], p["angular"], p["coefficient"], p["normalized"])
+                 for p in r["primitives"]]
+        vals = []
+        for fld in ((0.0, 0.0, 0.0), tuple(r["field"])):
+            v = ref.primitive_eri(prims, fld, r["gauge"])
+            vals.append([v.real, v.imag])
+        out.append({"primitives": r["primitives"], "field": r["field"], "gauge": r["gauge"],
+                    "expected": r["expected"], "reference": vals})
+    return out
+
+
+def blocks_fixture(ref, orc):
+    atom = syn.full_tensor_atom()
+    q1 = orc.canonical_quartets(len(atom))
+    v1, o1, _ = ref.eri_batch(atom, q1, (0.0, 0.0, 0.1), None, 8)
+    mol = syn.random_molecule(2026)
+    B = syn.random_field(2026)
+    qall = orc.canonical_quartets(len(mol))
+    pick = np.random.default_rng(7).choice(len(qall), 400, replace=False)
+    q2 = qall[np.sort(pick)]
+    v2, o2, _ = ref.eri_batch(mol, q2, B, None, 8)
+    # zero-field variant of the same subset
+    v3, o3, _ = ref.eri_batch(mol, q2[:120], (0.0, 0.0, 0.0), None, 8)
+    np.savez_compressed(HERE / "eri_blocks.npz", atom_quartets=q1, atom_values=v1, atom_offsets=o1,
+                        mol_quartets=q2, mol_values=v2, mol_offsets=o2, mol_field=np.asarray(B),
+                        mol_zero_values=v3, mol_zero_offsets=o3)
+
+
+def reference_cholesky_module(ref):
+    """Execute the reference's cholesky.py unmodified over the reference library."""
+
+    class Shell:
+        def __init__(self, spec):
+            self.spec = spec
+            self.center = tuple(spec.center)
+            self.cartesian_count = spec.ncart
+            self.contraction_count = spec.ncontr
+            self.primitive_count = spec.nprim
+            self.ao_count = spec.nao
+
+    class Basis:
+        def __init__(self, specs):
+            self.specs = specs
+            self.shells = [Shell(s) for s in specs]
+            offs, t = [], 0
+            for s in specs:
+                offs.append(t)
+                t += s.nao
+            self.ao_offsets = tuple(offs)
+            self.ao_count = t
+
+    class MagneticField:
+        def __init__(self, B, gauge_origin=(0.0, 0.0, 0.0)):
+            self.B = tuple(B)
+            self.gauge_origin = tuple(gauge_origin)
+
+    def fb(field):
+        return (None, None) if field is None else (field.B, field.gauge_origin)
+
+    native = types.ModuleType("giao_integrals._giao_integrals")
+    native.Basis = Basis
+    native.MagneticField = MagneticField
+    native._cholesky_diagonal = lambda basis, pairs, field=None, threads=None: ref.cholesky_diagonal(
+        basis.specs, pairs, *fb(field), threads or 1)
+    native._cholesky_columns = lambda basis, pivots, field=None, threads=None: ref.cholesky_columns(
+        basis.specs, pivots, *fb(field), threads or 1)
+    threads_mod = types.ModuleType("giao_integrals._threads")
+    threads_mod.resolve_num_threads = lambda t=None: 1 if t is None else int(t)
+    eri_mod = types.ModuleType("giao_integrals.eri")
+    eri_mod.eri_schwarz_bounds = lambda basis, field=None: ref.schwarz(basis.specs, *fb(field))
+    pkg = types.ModuleType("giao_integrals")
+    pkg.__path__ = []
+    for name, mod in (("giao_integrals", pkg), ("giao_integrals._giao_integrals", native),
+                      ("giao_integrals._threads", threads_mod), ("giao_integrals.eri", eri_mod)):
+        sys.modules[name] = mod
+    spec = importlib.util.spec_from_file_location("giao_integrals.cholesky",
+                                                  REFERENCE / "python/giao_integrals/cholesky.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["giao_integrals.cholesky"] = mod
+    spec.loader.exec_module(mod)
+    return mod, Basis, MagneticField
+
+
+def cholesky_fixture(ref):
+    mod, Basis, MagneticField = reference_cholesky_module(ref)
+    df = [O.ShellSpec((0.2, -0.1, 0.3), 2, [0.8], [[1.0]]), O.ShellSpec((-0.3, 0.4, -0.2), 3, [0.6], [[1.0]])]
+    tri = O.as_specs(syn.random_molecule(11, natoms=3, box=4.0))
+    cases = []
+    for name, specs in (("df", df), ("molecule3", tri)):
+        for label, B, origin in (("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)),
+                                 ("field", (0.05, -0.03, 0.2), (0.37, -0.29, 0.43))):
+            for tau in (1e-4, 1e-8):
+                for pbs in (32, 1):
+                    if name == "df" and pbs == 1:
+                        continue
+                    res = mod.cholesky_eri(Basis(specs), field=MagneticField(B, origin), threshold=tau,
+                                           pivot_batch_size=pbs)
+                    v = res.vectors
+                    cases.append({
+                        "system": name, "field_label": label, "B": list(B), "origin": list(origin),
+                        "threshold": tau, "pivot_batch_size": pbs, "rank": int(len(res.pivots)),
+                        "pivots": res.pivots.tolist(), "max_residual_diagonal": res.max_residual_diagonal,
+                        "vector_sum": [float(v.sum().real), float(v.sum().imag)],
+                        "vector_abs_sum": float(np.abs(v).sum()),
+                        "first_vector": [[x.real, x.imag] for x in v[0].ravel()[:256]],
+                    })
+    shells = {"df": [s.__dict__ for s in df], "molecule3": [s.__dict__ for s in tri]}
+    return {"shells": shells, "cases": cases}
+
+
+def main():
+    if build_ref.build() is None:
+        raise SystemExit("the reference checkout is required to generate fixtures")
+    ref = O.Reference()
+    orc = O.Oracle()
+    (HERE / "boys.json").write_text(json.dumps(boys_fixture(ref)))
+    (HERE / "primitive_eri_m8.json").write_text(json.dumps(m8_fixture(ref)))
+    blocks_fixture(ref, orc)
+    (HERE / "cholesky.json").write_text(json.dumps(cholesky_fixture(ref)))
+    for p in sorted(HERE.iterdir()):
+        print(p.name, p.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

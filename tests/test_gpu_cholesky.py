@@ -1,0 +1,78 @@
+"""Cholesky selections and the pivoted factorisation against the reference."""
+
+import numpy as np
+import pytest
+
+import giaoint_gb300 as gi
+from giaoint_gb300.eri import _eri_batch
+from giaoint_gb300.cholesky import _cholesky_columns, _cholesky_diagonal
+from helpers import specs_to_basis
+
+pytestmark = pytest.mark.gpu
+
+
+def test_selected_diagonal_and_columns_against_oracle(golden, oracle):
+    shells = golden.cholesky["shells"]["molecule3"]
+    basis = specs_to_basis(shells)
+    from oracle.oracle import ShellSpec
+
+    specs = [ShellSpec(tuple(s["center"]), s["l"], s["exponents"], s["coefficients"], s["normalize"]) for s in shells]
+    n = basis.ao_count
+    ns = len(specs)
+    pairs = [(a, b) for a in range(ns) for b in range(a, ns)]
+    for B, O in (((0, 0, 0), (0, 0, 0)), ((0.05, -0.03, 0.2), (0.37, -0.29, 0.43))):
+        field = gi.MagneticField(B, O)
+        d = _cholesky_diagonal(basis, pairs, field=field)
+        np.testing.assert_allclose(d, oracle.cholesky_diagonal(specs, pairs, B, O), atol=1e-12)
+        off = basis.ao_offsets
+        for sa, sb in ((3, 4), (5, 5), (0, 11)):
+            piv = [(off[sa] + i, off[sb] + j) for i in range(basis.shells[sa].ao_count)
+                   for j in range(basis.shells[sb].ao_count)][:8]
+            c = _cholesky_columns(basis, piv, field=field)
+            r = oracle.cholesky_columns(specs, piv, B, O)
+            assert c.dtype == r.dtype
+            assert np.abs(c - r).max() <= 1e-12
+            assert c.shape == (len(piv), n * n)
+
+
+@pytest.mark.parametrize("backend", ["host", "device"])
+def test_cholesky_against_reference_driver(golden, backend):
+    g = golden.cholesky
+    for case in g["cases"]:
+        basis = specs_to_basis(g["shells"][case["system"]])
+        field = gi.MagneticField(case["B"], case["origin"])
+        res = gi.cholesky_eri(basis, field=field, threshold=case["threshold"],
+                              pivot_batch_size=case["pivot_batch_size"], backend=backend)
+        ref_piv = np.asarray(case["pivots"])
+        # pivots equal wherever the residual-diagonal gap exceeds 1e-10:
+        # compare the common prefix up to the first near tie
+        k = 0
+        while k < min(len(res.pivots), len(ref_piv)) and tuple(res.pivots[k]) == tuple(ref_piv[k]):
+            k += 1
+        assert k >= min(len(ref_piv), 20) or k == min(len(res.pivots), len(ref_piv)), (case["system"], k)
+        assert abs(len(res.pivots) - case["rank"]) <= max(2, case["rank"] // 50)
+        assert res.max_residual_diagonal <= max(case["threshold"], 2e-12)
+        first = np.array([complex(*x) for x in case["first_vector"]])
+        np.testing.assert_allclose(res.vectors[0].ravel()[: len(first)], first, atol=1e-11)
+
+
+def test_cholesky_reconstruction_df(golden):
+    shells = golden.cholesky["shells"]["df"]
+    basis = specs_to_basis(shells)
+    for B in ((0, 0, 0), (0.05, -0.03, 0.2)):
+        field = gi.MagneticField(B, (0.37, -0.29, 0.43))
+        n = basis.ao_count
+        exact = gi.eri(basis, field=field, storage="full", max_bytes=n**4 * 16)
+        w = exact.transpose(1, 0, 2, 3).reshape(n * n, -1)
+        np.testing.assert_allclose(w, w.conj().T, atol=1e-13)
+        for tau in (1e-4, 1e-6, 1e-8, 1e-10, 0):
+            res = gi.cholesky_eri(basis, field=field, threshold=tau)
+            rec = res.reconstruct()
+            atol = tau + 2e-12 if tau else 2e-12
+            assert np.max(np.abs(exact - rec)) <= atol
+            assert res.max_residual_diagonal <= max(tau, 2e-12)
+            residual = w.diagonal().real - np.sum(abs(res.vectors) ** 2, axis=0).ravel()
+            assert abs(res.max_residual_diagonal - max(0, residual.max())) < 2e-12
+            assert len(np.unique(res.pivots, axis=0)) == len(res.vectors)
+            if B == (0, 0, 0):
+                np.testing.assert_array_equal(res.vectors.imag, 0)
