@@ -82,7 +82,7 @@ SIGNATURES = {
 }
 
 _lib: ctypes.CDLL | None = None
-_lock = threading.Lock()
+_lock = threading.RLock()
 
 
 def library_path() -> Path:
@@ -140,15 +140,12 @@ class Context:
         self.device = device
 
     def close(self) -> None:
+        """Release the device context.  Bases uploaded to it must not be used
+        afterwards; contexts that are still referenced at interpreter exit are
+        left to the process teardown (no destructor runs then)."""
         if getattr(self, "handle", None):
             lib().gx_context_destroy(self.handle)
             self.handle = None
-
-    def __del__(self):  # pragma: no cover - interpreter shutdown order
-        try:
-            self.close()
-        except Exception:
-            pass
 
 
 _default: Context | None = None

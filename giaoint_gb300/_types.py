@@ -12,6 +12,7 @@ resident for every later call.
 from __future__ import annotations
 
 import ctypes
+import sys
 import threading
 from collections.abc import Sequence
 
@@ -270,7 +271,7 @@ class Basis:
         key = id(ctx)
         h = self._handles.get(key)
         if h is not None:
-            return h
+            return h[0]
         with self._lock:
             h = self._handles.get(key)
             if h is None:
@@ -285,15 +286,19 @@ class Basis:
                 nat.check(nat.lib().gx_basis_create(ctx.handle, len(s), nat.dptr(centers), nat.iptr(ls),
                                                     nat.iptr(nps), nat.iptr(ncs), nat.dptr(exps), nat.dptr(coefs),
                                                     None, ctypes.byref(handle)))
-                self._handles[key] = handle
-                self._ctx_ref = ctx
-                h = handle
-        return h
+                self._handles[key] = (handle, ctx)  # the basis keeps its context alive
+                h = (handle, ctx)
+        return h[0]
 
     def __del__(self):  # pragma: no cover
+        # At interpreter exit the process teardown frees device memory; only
+        # release bases whose context is still open during normal execution.
+        if sys.is_finalizing():
+            return
         try:
-            for h in self._handles.values():
-                nat.lib().gx_basis_destroy(h)
+            for handle, ctx in self._handles.values():
+                if getattr(ctx, "handle", None):
+                    nat.lib().gx_basis_destroy(handle)
         except Exception:
             pass
 

@@ -87,9 +87,11 @@ __device__ __forceinline__ void report(DevStatus* st, int code, long long item, 
 //       recursion is stable (Re z >= 0 and |Im z| <= 3 or Re z >= 2|Im z|:
 //       error growth below 3x), the Taylor sum for every order elsewhere;
 //       e0 = e^{-z0}.
-//   * otherwise (|z| <= 160) adaptive Gauss-Legendre quadrature of the
-//       scaled integral int t^{2n} e^{z(1-t^2)} dt, 16 vs 32 points on
-//       ceil(max|Re|,|Im|)/8) doubling segments; e0 = e^{-z}.
+//   * otherwise (|z| <= 160) adaptive Gauss-Legendre quadrature, 16 vs 32
+//       points on ceil(max(|Re|,|Im|)/8) doubling segments, of the unscaled
+//       integral (e0 = 1) for Re z >= 0 and of the scaled integral
+//       int t^{2n} e^{z(1-t^2)} dt (e0 = e^{-z}) for Re z < 0; a quadrature
+//       that does not reach tolerance in 4096 segments returns -5.
 //   * outside |z| <= 160 and the reference's asymptotic sector
 //       (Re z >= 2L + 60, |Im z| <= Re z / 2): domain error, as
 //       src/boys.cpp:262-270.
@@ -118,27 +120,37 @@ __device__ __forceinline__ bool boys_domain_ok(double x, double y, int L) {
     return x >= 2.0 * L + 60.0 && fabs(y) <= 0.5 * x;
 }
 
-// Scaled quadrature on a fixed number of segments: out[n] = int_0^1 t^{2n} e^{z(1-t^2)}.
+// Gauss-Legendre quadrature of F_n on a fixed number of segments with
+// compensated sums: scaled (int t^{2n} e^{z(1-t^2)}) for Re z < 0, unscaled
+// (int t^{2n} e^{-z t^2}) otherwise, so the integrand never exceeds the
+// result's own scale (the reference's choice, src/boys.cpp:155-179, 272-291).
 static __device__ __noinline__ void boys_quad_fixed(double x, double y, int L, int segments, int rule, const GLRules* gl,
-                                             double2* out) {
-    for (int n = 0; n <= L; ++n) out[n] = c2(0.0, 0.0);
+                                                    double2* out, double2* comp) {
+    for (int n = 0; n <= L; ++n) {
+        out[n] = c2(0.0, 0.0);
+        comp[n] = c2(0.0, 0.0);
+    }
+    const bool scaled = x < 0.0;
     const int npt = rule ? 32 : 16;
     const double* nodes = rule ? gl->x32 : gl->x16;
     const double* weights = rule ? gl->w32 : gl->w16;
     const double inv = 1.0 / (double)segments;
     const double hw = 0.5 * inv;
+    const double ex = scaled ? exp(x) : 1.0;
     for (int s = 0; s < segments; ++s) {
         const double mid = ((double)s + 0.5) * inv;
         for (int k = 0; k < npt; ++k) {
             const double t = fma(hw, nodes[k], mid);
             const double t2 = t * t;
-            const double a = 1.0 - t2;
-            const double mag = exp(x * a) * hw * weights[k];
+            const double mag = ex * exp(-x * t2) * hw * weights[k];
             double sn, cs;
-            sincos(y * a, &sn, &cs);
+            sincos(scaled ? y * (1.0 - t2) : -y * t2, &sn, &cs);
             double2 term = c2(mag * cs, mag * sn);
             for (int n = 0; n <= L; ++n) {
-                out[n] = cadd(out[n], term);
+                const double yr = term.x - comp[n].x, yi = term.y - comp[n].y;
+                const double tr = out[n].x + yr, ti = out[n].y + yi;
+                comp[n] = c2((tr - out[n].x) - yr, (ti - out[n].y) - yi);
+                out[n] = c2(tr, ti);
                 term = cscale(term, t2);
             }
         }
@@ -148,12 +160,13 @@ static __device__ __noinline__ void boys_quad_fixed(double x, double y, int L, i
 // Adaptive GL16/GL32 (tolerance abs 2e-15 + rel 7.5e-14, at most 4096
 // segments); returns 0 or GX_EBOYS.
 static __device__ __noinline__ int boys_quad_adaptive(double x, double y, int L, const GLRules* gl, double2* out,
-                                               double2* scratch) {
+                                                      double2* scratch) {
+    double2 comp[BOYS_MAX_ORDER + 1];
     int segments = (int)ceil(fmax(fabs(x), fabs(y)) / 8.0);
     if (segments < 1) segments = 1;
     for (;;) {
-        boys_quad_fixed(x, y, L, segments, 0, gl, scratch);
-        boys_quad_fixed(x, y, L, segments, 1, gl, out);
+        boys_quad_fixed(x, y, L, segments, 0, gl, scratch, comp);
+        boys_quad_fixed(x, y, L, segments, 1, gl, out, comp);
         bool ok = true;
         for (int n = 0; n <= L; ++n) {
             const double dx = out[n].x - scratch[n].x, dy = out[n].y - scratch[n].y;
@@ -223,12 +236,17 @@ __device__ __forceinline__ int boys_eval(double x, double y, int L, const BoysTa
         }
         return 0;
     }
-    double2 scratch[BOYS_MAX_ORDER + 1];
-    if (boys_quad_adaptive(x, y, L, gl, Sh, scratch)) return -4;
-    double sn, cs;
-    sincos(-y, &sn, &cs);
-    const double m = exp(-x);
-    e0 = c2(m * cs, m * sn);
+    double2 tmp[BOYS_MAX_ORDER + 1], scratch[BOYS_MAX_ORDER + 1];
+    if (boys_quad_adaptive(x, y, L, gl, tmp, scratch)) return -5;
+    for (int n = 0; n <= L; ++n) Sh[n] = tmp[n];
+    if (x < 0.0) {
+        double sn, cs;
+        sincos(-y, &sn, &cs);
+        const double m = exp(-x);
+        e0 = c2(m * cs, m * sn);
+    } else {
+        e0 = c2(1.0, 0.0);
+    }
     return 0;
 }
 

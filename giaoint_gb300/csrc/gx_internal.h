@@ -57,6 +57,8 @@ struct QuartetClass {
     int B1, CH;            // phase-1 batch (primitive quartets), ket-component chunk
     int ntask;
     const Task* tasks;
+    int ngroup;
+    const int2* groups;  // (first task, task count) per warp work unit
 };
 
 struct EriDev {
@@ -83,6 +85,11 @@ cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps
                             cudaStream_t s);
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
                                 long long n, double2* full, cudaStream_t s);
+
+// register-resident small classes (gx_small.cu)
+bool small_class(int la, int lb, int lc, int ld);
+cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const Task* tasks, int ntask,
+                         cudaStream_t s);
 
 // Cholesky (gx_chol.cu)
 cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const int* info, int nblocks, int n,
