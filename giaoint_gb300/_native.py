@@ -79,6 +79,8 @@ SIGNATURES = {
     "gx_eri_plan_destroy": (None, [_vp]),
     "gx_measure_fp64_peak": (ctypes.c_int, [_vp, _d]),
     "gx_canonical_quartets": (ctypes.c_int64, [ctypes.c_int, _u32]),
+    "gx_cholesky_step_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int, ctypes.c_int,
+                                                _vp, _vp, _vp, _vp]),
 }
 
 _lib: ctypes.CDLL | None = None

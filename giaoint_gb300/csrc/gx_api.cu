@@ -1549,3 +1549,7 @@ extern "C" int64_t gx_canonical_quartets(int ns, uint32_t* out) {
                 }
     return n;
 }
+
+namespace gx {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace gx

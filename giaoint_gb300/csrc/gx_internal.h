@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "gx_device.cuh"
 
 namespace gx {
@@ -104,6 +106,9 @@ cudaError_t launch_chol_final_residual(bool real, const double* D, const void* L
                                        cudaStream_t s);
 size_t chol_red_bytes();
 size_t chol_partial_bytes();
+
+// record a failure for gx_last_error() and return its code (gx_api.cu)
+int set_error(int code, const std::string& msg);
 
 cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops);
 

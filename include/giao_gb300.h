@@ -221,6 +221,42 @@ int64_t gx_canonical_quartets(int ns, uint32_t* out);
  * chain probe kernel: the roofline denominator of the FP64-bound kernels. */
 int gx_measure_fp64_peak(gx_context* ctx, double* tflops);
 
+/* ---------------------------------------------------------------------- */
+/* allocation-free Cholesky step                                           */
+/* ---------------------------------------------------------------------- */
+
+/* Largest n*n (ordered AO pairs) the allocation-free step accepts. */
+#define GX_NOALLOC_MAX_ENTRIES 65536
+
+typedef struct gx_cholesky_step_result {
+    double max_residual; /* largest residual diagonal after the step (pivot zeroed) */
+    int64_t argmax;      /* its flat index mu*n+nu, lowest index on ties            */
+    double min_residual; /* smallest residual before clamping (PSD check)           */
+} gx_cholesky_step_result;
+
+/* One pivot step of the pivoted Cholesky that allocates no device memory
+ * and needs no context: new_row = (column - conj(factors[:rank, pivot])
+ * factors[:rank]) / sqrt(residual[pivot]) (symmetrised first when real),
+ * residual -= |new_row|^2, clamped at 0 with the pivot zeroed, and the next
+ * argmax and the PSD minimum written to `result`.  No counterpart in the
+ * reference library: it is the device step of gx_cholesky offered to callers
+ * that cannot let a library call cudaMalloc/cudaFree (they own all device
+ * memory, e.g. through a pooling allocator or a hard memory cap, and cannot
+ * afford the device-wide synchronisation those calls imply).
+ * All pointers are device memory of the caller: factors [rank][n*n],
+ * column [n*n], residual [n*n] float64, new_row [n*n], result one
+ * gx_cholesky_step_result; values are float64 when real != 0, else
+ * complex128.  Work is enqueued on `stream` (a cudaStream_t, NULL = default).
+ * Scratch lives in a fixed device array of GX_NOALLOC_MAX_ENTRIES complex128
+ * plus a few KiB, held by every GPU that loads the library until process
+ * exit; n*n above GX_NOALLOC_MAX_ENTRIES returns GX_ELENGTH.  All calls share
+ * that scratch, so calls that overlap on the GPU (different streams or
+ * threads without ordering) race.  The first call on a device resolves the
+ * scratch address with that device current; make it before any stream
+ * capture. */
+int gx_cholesky_step_noalloc(const void* factors, int64_t rank, int64_t pivot, const void* column, int n, int real,
+                             double* residual, void* new_row, void* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
