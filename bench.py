@@ -38,7 +38,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "GIAO ERIs/s (12-atom config-2 molecule, all canonical quartets)"
+METRIC = "GIAO ERIs/s & Cholesky time, mixed vs FP64 GPU @1e-10; p50/p99 req latency"
 UNIT = "ERIs/s"
 WORKLOAD = "12-atom s6 s1 s1 p3 p1 d1 molecule, seed 2026, |B|<=0.2, all 6722352 canonical quartets, complex128"
 
@@ -49,9 +49,11 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    p.add_argument("--mixed-cutoff", type=float, default=1e-6)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-cholesky", action="store_true")
     p.add_argument("--natoms", type=int, default=12)
     return p.parse_args()
 
@@ -146,6 +148,40 @@ def cpu_sample_rate(recs, B, quartets, target_seconds: float, seed: int = 1):
             "quartets_per_s": count / dt}
 
 
+def cholesky_leg(gi, nat, ctx, run_cpu: bool):
+    """Streamed pivoted Cholesky of the 140-AO atom (10s 8p 6d 4f 2g, ratio
+    2.5 from 0.05) at B = (0, 0, 0.1), threshold 1e-8: device driver time,
+    rank and residual; the oracle port on all host cores beside it."""
+    from giaoint_gb300 import synthetic as syn
+    from giaoint_gb300.cholesky import _cholesky_device
+
+    recs = syn.cholesky_atom()
+    basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
+    field = gi.MagneticField((0.0, 0.0, 0.1))
+    _cholesky_device(basis, field, 1e-4, 0.0, None, 32, context=ctx)  # warm-up (pairs, plans, pools)
+    t0 = time.perf_counter()
+    res = _cholesky_device(basis, field, 1e-8, 0.0, None, 32, context=ctx)
+    gpu_s = time.perf_counter() - t0
+    out = {"workload": "140-AO atom 10s8p6d4f2g, B=(0,0,0.1), threshold 1e-8", "seconds": gpu_s,
+           "rank": int(len(res.pivots)), "max_residual_diagonal": res.max_residual_diagonal}
+    if run_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = O.cholesky_eri(O.Oracle(), recs, (0.0, 0.0, 0.1), None, threshold=1e-8, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        out["cpu_port_seconds"] = cpu_s
+        out["cpu_port_threads"] = threads
+        out["cpu_port_rank"] = int(len(ref.pivots))
+        k = 0
+        while k < min(len(ref.pivots), len(res.pivots)) and tuple(ref.pivots[k]) == tuple(res.pivots[k]):
+            k += 1
+        out["pivots_equal_prefix"] = k
+        out["speedup_vs_cpu_port"] = cpu_s / gpu_s
+    return out
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -206,44 +242,65 @@ def run_gpu(args):
     nat.check(lib.gx_context_set_stream(ctx.handle, ctypes.c_void_p(stream.cuda_stream)))
     Bv = np.ascontiguousarray(B, dtype=np.float64)
     Ov = np.zeros(3)
-    prec = {"fp64": 0, "mixed": 1}[args.precision]
     outp = ctypes.c_void_p(out.data_ptr())
 
-    def step():
-        nat.check(lib.gx_eri_plan_execute(plan, nat.dptr(Bv), nat.dptr(Ov), prec, 1e-6, outp))
+    def step(prec):
+        nat.check(lib.gx_eri_plan_execute(plan, nat.dptr(Bv), nat.dptr(Ov), prec, args.mixed_cutoff, outp))
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
-        torch.cuda.synchronize()
+    def timed(prec):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                step(prec)
+            torch.cuda.synchronize()
+            nat.check(lib.gx_context_synchronize(ctx.handle))
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            clocks = ClockSampler(local)
+            clocks.start()
+            evs = []
+            for _ in range(args.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step(prec)
+                e1.record(stream)
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+            clock_info = clocks.stop()
         nat.check(lib.gx_context_synchronize(ctx.handle))
+        ms = float(sum(a.elapsed_time(b) for a, b in evs) / len(evs))
         if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        clocks = ClockSampler(local)
-        clocks.start()
-        evs = []
-        for _ in range(args.steps):
-            flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            evs.append((e0, e1))
-        torch.cuda.synchronize()
-        clock_info = clocks.stop()
-    nat.check(lib.gx_context_synchronize(ctx.handle))
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = float(sum(step_ms) / len(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+            t = torch.tensor([ms], device=f"cuda:{local}")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        n64, n32 = ctypes.c_int64(), ctypes.c_int64()
+        f64, f32 = ctypes.c_double(), ctypes.c_double()
+        nat.check(lib.gx_eri_plan_counts(plan, ctypes.byref(n64), ctypes.byref(n32), ctypes.byref(f64),
+                                         ctypes.byref(f32)))
+        return ms, clock_info, (n64.value, n32.value, f64.value, f32.value)
+
+    ms_ex, clocks_ex, cnt_ex = timed(2)
+    exact = out.clone()
+    ms64, clocks64, cnt64 = timed(0)
+    d64 = (out - exact).view(-1, 2)
+    err64 = float(torch.sqrt((d64 * d64).sum(dim=1)).max().item())
+    del d64
+    ref64 = out.clone()
+    ms_mx, clocks_mx, cnt_mx = timed(1)
+    diff = (out - exact).view(-1, 2)
+    max_err = float(torch.sqrt((diff * diff).sum(dim=1)).max().item())
+    del diff, ref64, exact
+    headline_mixed = args.precision == "mixed"
+    ms = ms_mx if headline_mixed else ms64
+    clock_info = clocks_mx if headline_mixed else clocks64
     value = world * total / (ms * 1e-3)
     # live FP64 roofline denominator
     peak = ctypes.c_double()
     nat.check(lib.gx_measure_fp64_peak(ctx.handle, ctypes.byref(peak)))
-    achieved = model.value / (ms * 1e-3) / 1e12
+    achieved64 = cnt64[2] / (ms64 * 1e-3) / 1e12
+    achieved = achieved64
+    prec = {"fp64": 0, "mixed": 1}[args.precision]
     # e2e through the host-buffer C ABI call (pinned host memory)
     e2e = None
     if not args.no_e2e:
@@ -279,6 +336,10 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample_rate(recs, B, quartets, target_seconds=10.0)
+    chol = None
+    if rank == 0 and not args.no_cholesky:
+        nat.check(lib.gx_context_set_stream(ctx.handle, None))
+        chol = cholesky_leg(gi, nat, ctx, run_cpu=(world == 1 and not args.no_cpu))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -286,18 +347,33 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "precision": args.precision, "quartets_per_step": nq,
                        "eris_per_step": total, "primitive_quartets_per_step": int(nprim.value),
+                       "mixed_cutoff": args.mixed_cutoff,
                        "parallelism": f"replicas{world} (one field per rank)", "l2": "flushed (256 MB write) "
                        "between timed steps; the 4.2 GB output is also larger than L2"},
             "quartets_per_s": world * nq / (ms * 1e-3),
+            "fp64_exact": {"ms_per_step": ms_ex, "eris_per_s": world * total / (ms_ex * 1e-3),
+                           "primitive_quartets_evaluated": cnt_ex[0], "clocks": clocks_ex,
+                           "note": "every primitive quartet, as the reference evaluates them"},
+            "fp64": {"ms_per_step": ms64, "eris_per_s": world * total / (ms64 * 1e-3),
+                     "max_abs_error_vs_fp64_exact": err64,
+                     "primitive_quartets_evaluated": cnt64[0], "primitive_quartets_skipped": int(nprim.value) - cnt64[0],
+                     "clocks": clocks64},
+            "mixed": {"ms_per_step": ms_mx, "eris_per_s": world * total / (ms_mx * 1e-3),
+                      "fp64_primitive_quartets": cnt_mx[0], "fp32_primitive_quartets": cnt_mx[1],
+                      "max_abs_error_vs_fp64_exact": max_err, "speedup_vs_fp64": ms64 / ms_mx,
+                      "speedup_vs_fp64_exact": ms_ex / ms_mx, "clocks": clocks_mx},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value, "traffic": None,
-                         "achieved_basis": "FP64 FLOP model per primitive quartet x primitive quartets per step "
-                                           "/ event-timed step (all quartet-kernel launches + pair kernel)",
+                         "kernel": "FP64 path (quartet_kernel + small_kernel launches of one step)",
+                         "achieved_basis": "FP64 FLOP model per primitive quartet x primitive quartets evaluated "
+                                           "(screened ones excluded) / event-timed FP64 step",
+                         "model_flops_all_primitive_quartets": model.value,
                          "peak_source": "measured live: FP64 FMA-chain probe kernel (gx_measure_fp64_peak)"},
             "gpu_launches": int(launches.value) * args.steps,
             "clocks": clock_info,
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "cholesky": chol,
         }
         print(json.dumps(line), flush=True)
     lib.gx_eri_plan_destroy(plan)

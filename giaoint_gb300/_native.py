@@ -77,6 +77,7 @@ SIGNATURES = {
     "gx_eri_plan_info": (ctypes.c_int, [_vp, _i64, _i64, _d, _i]),
     "gx_eri_plan_execute": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp]),
     "gx_eri_plan_destroy": (None, [_vp]),
+    "gx_eri_plan_counts": (ctypes.c_int, [_vp, _i64, _i64, _d, _d]),
     "gx_measure_fp64_peak": (ctypes.c_int, [_vp, _d]),
     "gx_canonical_quartets": (ctypes.c_int64, [ctypes.c_int, _u32]),
     "gx_cholesky_step_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int, ctypes.c_int,

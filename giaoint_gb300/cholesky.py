@@ -110,6 +110,7 @@ def cholesky_eri(basis: Basis, *, field: MagneticField | None = None, threshold:
 
 
 def _cholesky_device(basis, field, threshold, screening_threshold, max_bytes, pivot_batch_size, context=None):
+    """gx_cholesky: the pivot loop resident on the device."""
     ctx = context or nat.default_context()
     n = basis.ao_count
     row_bytes = n * n * 16 + 16

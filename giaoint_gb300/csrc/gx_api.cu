@@ -253,7 +253,7 @@ void check_status(gx_context* ctx) {
 
 struct FieldPairs {
     double B[3], O[3];
-    DeviceBuffer p, Pr, Pi, F, Epool, bound;
+    DeviceBuffer p, Pr, Pi, F, Epool, bound, Epool32, order, sbound;
 };
 
 struct gx_basis {
@@ -362,6 +362,25 @@ void build_segments(gx_basis* b) {
 }
 
 // Primitive-pair records for (B, O); cached on the basis for the last field.
+// Primitive-pair records for (B, O); cached on the basis for the last field.
+// After the records, every primitive pair's exact Schwarz factor is computed
+// on the device and each shell pair's primitive pairs are ordered by
+// decreasing factor, so that screened primitive quartets form a suffix of
+// every bra row and ket column.
+gx::PairData pair_view(gx_basis* b, FieldPairs& fp) {
+    return gx::PairData{b->npp,
+                        fp.p.as<double>(),
+                        fp.Pr.as<double>(),
+                        fp.Pi.as<double>(),
+                        fp.F.as<double2>(),
+                        b->d_Eoff.as<long long>(),
+                        fp.Epool.as<double2>(),
+                        fp.bound.as<double>(),
+                        fp.Epool32.as<float2>(),
+                        fp.order.as<int>(),
+                        fp.sbound.as<float>()};
+}
+
 FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
     if (b->pairs && std::memcmp(b->pairs->B, B, sizeof(double) * 3) == 0 &&
         std::memcmp(b->pairs->O, O, sizeof(double) * 3) == 0)
@@ -376,12 +395,42 @@ FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
     fp.Pi.reserve(3 * n * sizeof(double));
     fp.F.reserve(n * sizeof(double2));
     fp.bound.reserve(n * sizeof(double));
+    fp.order.reserve(n * sizeof(int));
+    fp.sbound.reserve(n * sizeof(float));
     fp.Epool.reserve(std::max<long long>(b->Etotal, 1) * sizeof(double2));
+    fp.Epool32.reserve(std::max<long long>(b->Etotal, 1) * sizeof(float2));
+    gx::EriDev dev{};
+    dev.basis = b->dev();
+    dev.pairs = pair_view(b, fp);
+    dev.boys = b->ctx->boys();
+    dev.gl = b->ctx->gl.as<gx::GLRules>();
+    dev.herm_xyz = b->ctx->herm.as<uint32_t>();
     GX_CUDA(gx::launch_pair_precompute(b->dev(), B, O, b->npp, b->d_pp_a.as<int>(), b->d_pp_b.as<int>(),
                                        b->d_pp_pa.as<int>(), b->d_pp_pb.as<int>(), b->d_pp_class.as<int>(),
                                        b->d_classes.as<gx::PairClassDev>(), fp.p.as<double>(), fp.Pr.as<double>(),
                                        fp.Pi.as<double>(), fp.F.as<double2>(), b->d_Eoff.as<long long>(),
-                                       fp.Epool.as<double2>(), fp.bound.as<double>(), b->ctx->stream));
+                                       fp.Epool.as<double2>(), fp.Epool32.as<float2>(), fp.bound.as<double>(), &dev,
+                                       b->ctx->stream));
+    std::vector<double> bound(b->npp);
+    if (b->npp)
+        GX_CUDA(cudaMemcpyAsync(bound.data(), fp.bound.ptr, b->npp * sizeof(double), cudaMemcpyDeviceToHost,
+                                b->ctx->stream));
+    GX_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    std::vector<int> order(b->npp);
+    std::vector<float> sbound(b->npp);
+    const int ns = b->nseg;
+    for (int a = 0; a < ns; ++a)
+        for (int c = 0; c < ns; ++c) {
+            const int first = b->sp_off[(size_t)a * ns + c];
+            const int count = b->seg_nprim[a] * b->seg_nprim[c];
+            std::iota(order.begin() + first, order.begin() + first + count, first);
+            std::stable_sort(order.begin() + first, order.begin() + first + count,
+                             [&](int x, int y) { return bound[x] > bound[y]; });
+            for (int k = first; k < first + count; ++k)
+                sbound[k] = (float)std::min(bound[order[k]], 3.0e38);
+        }
+    upload(fp.order, order, b->ctx->stream);
+    upload(fp.sbound, sbound, b->ctx->stream);
     return fp;
 }
 
@@ -404,10 +453,11 @@ struct PlanClass {
     std::array<int, 4> key;
     size_t first, count;
     int64_t primitive_quartets;
+    double flops_per_primitive_quartet;
 };
 
 struct PlanData {
-    DeviceBuffer tasks, groups;
+    DeviceBuffer tasks, groups, counters;
     std::vector<std::pair<size_t, size_t>> group_range;  // per class: first group, count
     std::vector<PlanClass> classes;
     int64_t ntask = 0, primitive_quartets = 0;
@@ -480,7 +530,7 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
             if (kx != ky) return kx > ky;
             return b->seg_nprim[x.sc] * b->seg_nprim[x.sd] > b->seg_nprim[y.sc] * b->seg_nprim[y.sd];
         });
-        plan.classes.push_back({k, all.size(), kv.second.size(), np});
+        plan.classes.push_back({k, all.size(), kv.second.size(), np, model_flops(k[0], k[1], k[2], k[3])});
         plan.primitive_quartets += np;
         plan.model_flops += (double)np * model_flops(k[0], k[1], k[2], k[3]);
         all.insert(all.end(), kv.second.begin(), kv.second.end());
@@ -514,16 +564,27 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
     upload(plan.groups, groups, ctx->stream);
 }
 
+// Primitive screening thresholds on the Schwarz product B_P B_Q.  FP64: a
+// skipped primitive quartet contributes below 1e-18 to every element, so a
+// shell quartet (at most a few thousand primitive quartets) moves by less
+// than 1e-14 absolute.  Mixed: 1e-15, with FP32 up to the caller's cutoff.
+constexpr double kSkipFP64 = 1e-18;
+constexpr double kSkipMixed = 1e-15;
+
 // Enqueue the pair records for (B, O) and every class launch; no host sync.
+// counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null.
 int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
-                 double2* out) {
+                 double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
+                 unsigned long long* counters = nullptr) {
     cudaStream_t s = ctx->stream;
     FieldPairs& fp = field_pairs(b, B, O);
     gx::EriDev dev;
+    const bool mixed = precision == GX_PRECISION_MIXED;
+    dev.skip_cut = (float)(mixed ? kSkipMixed : (precision == GX_PRECISION_FP64_EXACT ? 0.0 : kSkipFP64));
+    dev.fp32_cut = (float)(mixed ? std::max(mixed_cutoff, kSkipMixed) : 0.0);
+    if (counters) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
     dev.basis = b->dev();
-    dev.pairs = gx::PairData{b->npp,           fp.p.as<double>(),        fp.Pr.as<double>(),
-                             fp.Pi.as<double>(), fp.F.as<double2>(),      b->d_Eoff.as<long long>(),
-                             fp.Epool.as<double2>(), fp.bound.as<double>()};
+    dev.pairs = pair_view(b, fp);
     dev.boys = ctx->boys();
     dev.gl = ctx->gl.as<gx::GLRules>();
     dev.herm_xyz = ctx->herm.as<uint32_t>();
@@ -534,6 +595,7 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
     for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
         const auto& pc = plan.classes[ci];
         const auto& k = pc.key;
+        dev.counters = counters ? counters + 2 * ci : nullptr;
         if (gx::small_class(k[0], k[1], k[2], k[3])) {
             GX_CUDA(gx::launch_small(k[0], k[1], k[2], k[3], dev, plan.tasks.as<gx::Task>() + pc.first,
                                      (int)pc.count, s));
@@ -555,7 +617,7 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
         qc.tasks = plan.tasks.as<gx::Task>() + pc.first;
         qc.ngroup = (int)plan.group_range[ci].second;
         qc.groups = plan.groups.as<int2>() + plan.group_range[ci].first;
-        const size_t per_warp = gx::quartet_smem_bytes(qc, 1);
+        const size_t per_warp = gx::quartet_smem_bytes(qc, 1, dev.fp32_cut > 0.0f);
         int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
         const int grid = (qc.ngroup + wpb - 1) / wpb;
         GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
@@ -568,18 +630,24 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
 // index = contraction * ncart + component) and wait for them.
 void run_quartets(gx_context* ctx, gx_basis* b, const double* B, const double* O,
                   const std::vector<QuartetRequest>& req, double2* out, float* kernel_ms,
-                  int64_t* primitive_quartets = nullptr) {
+                  int64_t* primitive_quartets = nullptr, int precision = GX_PRECISION_FP64,
+                  double mixed_cutoff = 0.0, int64_t* evaluated = nullptr) {
     cudaStream_t s = ctx->stream;
     PlanData plan;
     build_plan(ctx, b, req, plan);
     if (primitive_quartets) *primitive_quartets = plan.primitive_quartets;
+    unsigned long long* counters = nullptr;
+    if (evaluated) {
+        plan.counters.reserve(std::max<size_t>(2 * plan.classes.size(), 2) * sizeof(unsigned long long));
+        counters = plan.counters.as<unsigned long long>();
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (kernel_ms) {
         GX_CUDA(cudaEventCreate(&e0));
         GX_CUDA(cudaEventCreate(&e1));
         GX_CUDA(cudaEventRecord(e0, s));
     }
-    execute_plan(ctx, b, B, O, plan, out);
+    execute_plan(ctx, b, B, O, plan, out, precision, mixed_cutoff, counters);
     if (kernel_ms) {
         GX_CUDA(cudaEventRecord(e1, s));
         GX_CUDA(cudaEventSynchronize(e1));
@@ -588,6 +656,16 @@ void run_quartets(gx_context* ctx, gx_basis* b, const double* B, const double* O
         cudaEventDestroy(e1);
     }
     check_status(ctx);
+    if (evaluated) {
+        std::vector<unsigned long long> c(2 * plan.classes.size());
+        if (!c.empty())
+            GX_CUDA(cudaMemcpy(c.data(), counters, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        evaluated[0] = evaluated[1] = 0;
+        for (size_t i = 0; i < plan.classes.size(); ++i) {
+            evaluated[0] += (int64_t)c[2 * i];
+            evaluated[1] += (int64_t)c[2 * i + 1];
+        }
+    }
 }
 
 void validate_quartets(const gx_basis* b, const uint32_t* q, int64_t nq) {
@@ -605,7 +683,8 @@ std::vector<double> schwarz_values(gx_context* ctx, gx_basis* b, const double* B
             off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
         }
     ctx->scratch_a.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
-    run_quartets(ctx, b, B, O, req, ctx->scratch_a.as<double2>(), nullptr);
+    // bounds must not lose the tiniest pairs: no primitive screening here
+    run_quartets(ctx, b, B, O, req, ctx->scratch_a.as<double2>(), nullptr, nullptr, GX_PRECISION_FP64_EXACT);
     std::vector<std::complex<double>> host(off);
     if (off) GX_CUDA(cudaMemcpy(host.data(), ctx->scratch_a.ptr, off * sizeof(double2), cudaMemcpyDeviceToHost));
     std::vector<double> q((size_t)b->ns * b->ns, 0.0);
@@ -627,9 +706,11 @@ std::vector<double> schwarz_values(gx_context* ctx, gx_basis* b, const double* B
 int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
                    int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
                    int64_t* offsets, void* out, bool out_is_device, int64_t capacity, gx_eri_stats* stats) {
-    (void)precision;
-    (void)mixed_cutoff;
     return guarded([&] {
+        if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
+            raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
+        if (precision == GX_PRECISION_MIXED && !(std::isfinite(mixed_cutoff) && mixed_cutoff >= 0.0))
+            raise(GX_EINVAL, "mixed_cutoff must be finite and non-negative");
         if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
         check_field(B, O);
         if (!std::isfinite(screening) || screening < 0.0)
@@ -664,8 +745,9 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             dout = ctx->out.as<double2>();
         }
         float ms = 0.f;
-        int64_t nprim = 0;
-        if (!req.empty()) run_quartets(ctx, b, B, O, req, dout, &ms, &nprim);
+        int64_t nprim = 0, evaluated[2] = {0, 0};
+        if (!req.empty())
+            run_quartets(ctx, b, B, O, req, dout, &ms, &nprim, precision, mixed_cutoff, stats ? evaluated : nullptr);
         if (!out_is_device && off)
             GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -673,9 +755,9 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             stats->requested = nq;
             stats->computed = (int64_t)req.size();
             stats->screened = screened;
-            stats->primitive_quartets = nprim;
-            stats->fp32_primitive_quartets = 0;
-            stats->skipped_primitive_quartets = 0;
+            stats->primitive_quartets = evaluated[0] + evaluated[1];
+            stats->fp32_primitive_quartets = evaluated[1];
+            stats->skipped_primitive_quartets = nprim - evaluated[0] - evaluated[1];
             stats->kernel_ms = ms;
         }
     });
@@ -893,9 +975,9 @@ int gx_schwarz(gx_context* ctx, gx_basis* b, const double* B, const double* O, d
 
 int gx_eri_full(gx_context* ctx, gx_basis* b, const double* B, const double* O, int precision, double mixed_cutoff,
                 double screening, double* out) {
-    (void)precision;
-    (void)mixed_cutoff;
     return guarded([&] {
+        if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
+            raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
         if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
         check_field(B, O);
         if (!std::isfinite(screening) || screening < 0.0)
@@ -933,7 +1015,8 @@ int gx_eri_full(gx_context* ctx, gx_basis* b, const double* B, const double* O, 
         ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
         const size_t full_bytes = (size_t)n * n * n * n * sizeof(double2);
         ctx->scratch_b.reserve(std::max<size_t>(full_bytes, 16));
-        if (!req.empty()) run_quartets(ctx, b, B, O, req, ctx->out.as<double2>(), nullptr);
+        if (!req.empty())
+            run_quartets(ctx, b, B, O, req, ctx->out.as<double2>(), nullptr, nullptr, precision, mixed_cutoff);
         GX_CUDA(cudaMemsetAsync(ctx->scratch_b.ptr, 0, full_bytes, ctx->stream));
         DeviceBuffer d_boff, d_info;
         upload(d_boff, boff, ctx->stream);
@@ -1498,15 +1581,44 @@ int gx_eri_plan_info(const gx_eri_plan* plan, int64_t* tasks, int64_t* primitive
 
 int gx_eri_plan_execute(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                         void* out_device) {
-    (void)precision;
-    (void)mixed_cutoff;
     return guarded([&] {
         if (!plan) raise(GX_EINVAL, "null plan");
         check_field(B, O);
+        if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
+            raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
         gx_context* ctx = plan->ctx;
         std::lock_guard<std::mutex> lock(ctx->mu);
         GX_CUDA(cudaSetDevice(ctx->device));
-        plan->last_launches = execute_plan(ctx, plan->basis, B, O, plan->data, static_cast<double2*>(out_device));
+        plan->data.counters.reserve(std::max<size_t>(2 * plan->data.classes.size(), 2) * sizeof(unsigned long long));
+        plan->last_launches =
+            execute_plan(ctx, plan->basis, B, O, plan->data, static_cast<double2*>(out_device), precision,
+                         mixed_cutoff, plan->data.counters.as<unsigned long long>());
+    });
+}
+
+int gx_eri_plan_counts(gx_eri_plan* plan, int64_t* fp64_quartets, int64_t* fp32_quartets, double* fp64_flops,
+                       double* fp32_flops) {
+    return guarded([&] {
+        if (!plan) raise(GX_EINVAL, "null plan");
+        std::lock_guard<std::mutex> lock(plan->ctx->mu);
+        const size_t nc = plan->data.classes.size();
+        std::vector<unsigned long long> c(2 * nc);
+        GX_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+        if (nc)
+            GX_CUDA(cudaMemcpy(c.data(), plan->data.counters.ptr, c.size() * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost));
+        int64_t n64 = 0, n32 = 0;
+        double f64 = 0.0, f32 = 0.0;
+        for (size_t i = 0; i < nc; ++i) {
+            n64 += (int64_t)c[2 * i];
+            n32 += (int64_t)c[2 * i + 1];
+            f64 += (double)c[2 * i] * plan->data.classes[i].flops_per_primitive_quartet;
+            f32 += (double)c[2 * i + 1] * plan->data.classes[i].flops_per_primitive_quartet;
+        }
+        if (fp64_quartets) *fp64_quartets = n64;
+        if (fp32_quartets) *fp32_quartets = n32;
+        if (fp64_flops) *fp64_flops = f64;
+        if (fp32_flops) *fp32_flops = f32;
     });
 }
 

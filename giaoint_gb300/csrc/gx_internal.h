@@ -38,7 +38,10 @@ struct PairData {
     const double2* F;      // [npp] complex prefactor (coefficients, norms, K_ab, London phase, 1/p)
     const long long* Eoff; // [npp] offset of the primitive pair's E~ record in Epool
     const double2* Epool;  // complex Hermite coefficients
-    const double* bound;   // [npp] magnitude bound of the pair's charge distribution
+    const double* bound;   // [npp] primitive Schwarz factor sqrt(max |(ab|ba)_PP|)
+    const float2* Epool32; // the same coefficients in FP32 (mixed precision)
+    const int* order;      // [npp] records of each shell pair sorted by decreasing bound
+    const float* sbound;   // [npp] bound of order[i] (FP32, for gating)
 };
 
 struct BasisDev {
@@ -71,6 +74,9 @@ struct EriDev {
     const uint32_t* herm_xyz;  // packed (k, l, m) of herm index, L <= 32
     double2* out;
     DevStatus* status;
+    float skip_cut;   // primitive quartets with bound product below this are skipped
+    float fp32_cut;   // ... below this (and above skip_cut) run in FP32; 0 = FP64 only
+    unsigned long long* counters;  // [0] FP64, [1] FP32 primitive quartets evaluated (may be null)
 };
 
 // ---- launch wrappers (gx_kernels.cu) -------------------------------------
@@ -81,8 +87,9 @@ cudaError_t launch_boys_values(const double2* z, long long count, int nmax, int 
 cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
                                    const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
                                    const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
-                                   const long long* Eoff, double2* Epool, double* bound, cudaStream_t s);
-size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block);
+                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound,
+                                   const EriDev* dev_for_bounds, cudaStream_t s);
+size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed);
 cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps_per_block, int grid,
                             cudaStream_t s);
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,

@@ -181,7 +181,7 @@ __device__ void hermite_1d(int i, int j, double PA, double PB, double inv2p, dou
 __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const int* pp_a, const int* pp_b,
                             const int* pp_pa, const int* pp_pb, const int* pp_class, const PairClassDev* classes,
                             double* out_p, double* out_Pr, double* out_Pi, double2* out_F, const long long* Eoff,
-                            double2* Epool, double* out_bound) {
+                            double2* Epool, float2* Epool32, double* out_bound) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npp) return;
     const int a = pp_a[i], b = pp_b[i];
@@ -231,6 +231,7 @@ __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const in
     // complex Hermite coefficients per axis and per component pair
     const PairClassDev pc = classes[pp_class[i]];
     double2* rec = Epool + Eoff[i];
+    float2* rec32 = Epool32 + Eoff[i];
     const double inv2p = 0.5 / p;
     int ab = 0;
     double bmax = 0.0;
@@ -271,6 +272,7 @@ __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const in
                             for (int m = 0; m < dim[2]; ++m, ++e) {
                                 const double2 v = cscale(cmul(xy, Et[2][m]), g);
                                 rec[off + e] = v;
+                                rec32[off + e] = make_float2((float)v.x, (float)v.y);
                                 bmax = fmax(bmax, fabs(v.x) + fabs(v.y));
                             }
                         }
@@ -279,14 +281,112 @@ __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const in
     out_bound[i] = mag * damp * bmax;
 }
 
+// Exact primitive Schwarz factor of every primitive pair P = (a pa, b pb):
+// bound[P] = sqrt(max over component pairs |(ab|ba)_PP|), from the records of
+// P and of its reversed pair (b pb, a pa).  |(ab|cd)_PQ| <= bound[P] bound[Q]
+// holds for every component of a primitive quartet (Cauchy-Schwarz in the
+// Coulomb metric, the argument of src/eri.cpp:587-619 applied per primitive
+// pair).  Pairs with la+lb > 4 get an infinite bound (never screened).
+constexpr int BOUND_MAX_LAB = 4;
+
+__global__ void pair_bound_kernel(BasisDev bs, EriDev d, int npp, const int* pp_a, const int* pp_b, const int* pp_pa,
+                                  const int* pp_pb, const int* pp_class, const PairClassDev* classes, double* bound) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npp) return;
+    const int a = pp_a[i], b = pp_b[i];
+    const int la = bs.l[a], lb = bs.l[b];
+    if (la + lb > BOUND_MAX_LAB) {
+        bound[i] = 1.0e300;
+        return;
+    }
+    const int j = bs.sp_off[b * bs.ns + a] + pp_pb[i] * bs.nprim[a] + pp_pa[i];
+    const PairData& pp = d.pairs;
+    const int L = 2 * (la + lb);
+    const double p = pp.p[i];
+    double2 X[3];
+    for (int x = 0; x < 3; ++x) X[x] = c2(pp.Pr[3 * i + x] - pp.Pr[3 * j + x], pp.Pi[3 * i + x] - pp.Pi[3 * j + x]);
+    const double rho = 0.5 * p;
+    const double tre = rho * (X[0].x * X[0].x + X[1].x * X[1].x + X[2].x * X[2].x - X[0].y * X[0].y -
+                              X[1].y * X[1].y - X[2].y * X[2].y);
+    const double tim = 2.0 * rho * (X[0].x * X[0].y + X[1].x * X[1].y + X[2].x * X[2].y);
+    double2 Sh[2 * BOUND_MAX_LAB + 1];
+    double2 e0;
+    if (boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
+        bound[i] = 1.0e300;
+        return;
+    }
+    double2 C = cmul(cscale(cmul(pp.F[i], pp.F[j]), rsqrt(2.0 * p)), e0);
+    constexpr int NR = (2 * BOUND_MAX_LAB + 1) * (2 * BOUND_MAX_LAB + 2) * (2 * BOUND_MAX_LAB + 3) / 6;
+    double2 R[NR];
+    for (int n = 0; n <= L; ++n) {
+        Sh[n] = cmul(C, Sh[n]);
+        C = cscale(C, -2.0 * rho);
+    }
+    R[0] = Sh[L];
+    for (int n = L - 1; n >= 0; --n) {
+        for (int dg = L - n; dg >= 1; --dg)
+            for (int k = dg; k >= 0; --k)
+                for (int l = dg - k; l >= 0; --l) {
+                    const int m = dg - k - l;
+                    double2 v;
+                    if (k > 0) {
+                        v = cmul(X[0], R[herm_index(k - 1, l, m)]);
+                        if (k > 1) v = cmacr(v, (double)(k - 1), R[herm_index(k - 2, l, m)]);
+                    } else if (l > 0) {
+                        v = cmul(X[1], R[herm_index(0, l - 1, m)]);
+                        if (l > 1) v = cmacr(v, (double)(l - 1), R[herm_index(0, l - 2, m)]);
+                    } else {
+                        v = cmul(X[2], R[herm_index(0, 0, m - 1)]);
+                        if (m > 1) v = cmacr(v, (double)(m - 1), R[herm_index(0, 0, m - 2)]);
+                    }
+                    R[herm_index(k, l, m)] = v;
+                }
+        R[0] = Sh[n];
+    }
+    const PairClassDev ci = classes[pp_class[i]], cj = classes[pp_class[j]];
+    const double2* Ei = pp.Epool + pp.Eoff[i];
+    const double2* Ej = pp.Epool + pp.Eoff[j];
+    const int nb = ncart(lb), na = ncart(la);
+    double best = 0.0;
+    for (int ab = 0; ab < ci.nab; ++ab) {
+        const int ca = ab / nb, cb = ab - ca * nb;
+        const int ba = cb * na + ca;
+        const int oi = ci.boxoff[ab], di = ci.boxdim[ab];
+        const int oj = cj.boxoff[ba], dj = cj.boxdim[ba];
+        const int ni = (di & 255) * ((di >> 8) & 255) * ((di >> 16) & 255);
+        const int nj = (dj & 255) * ((dj >> 8) & 255) * ((dj >> 16) & 255);
+        double2 acc = c2(0.0, 0.0);
+        for (int e = 0; e < ni; ++e) {
+            const uint32_t ke = ci.ent[oi + e];
+            const int k1 = ke & 255, l1 = (ke >> 8) & 255, m1 = (ke >> 16) & 255;
+            double2 inner = c2(0.0, 0.0);
+            for (int f = 0; f < nj; ++f) {
+                const uint32_t kf = cj.ent[oj + f];
+                const int k2 = kf & 255, l2 = (kf >> 8) & 255, m2 = (kf >> 16) & 255;
+                double2 ev = Ej[oj + f];
+                if ((k2 + l2 + m2) & 1) ev = c2(-ev.x, -ev.y);
+                inner = cmac(inner, ev, R[herm_index(k1 + k2, l1 + l2, m1 + m2)]);
+            }
+            acc = cmac(acc, Ei[oi + e], inner);
+        }
+        best = fmax(best, sqrt(acc.x * acc.x + acc.y * acc.y));
+    }
+    bound[i] = sqrt(best) * (1.0 + 1.0e-10) + 1.0e-300;
+}
+
 cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
                                    const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
                                    const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
-                                   const long long* Eoff, double2* Epool, double* bound, cudaStream_t s) {
+                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound,
+                                   const EriDev* dev_for_bounds, cudaStream_t s) {
     if (npp <= 0) return cudaSuccess;
     pair_kernel<<<(npp + 63) / 64, 64, 0, s>>>(basis, make_double3(B[0], B[1], B[2]), make_double3(O[0], O[1], O[2]),
                                                npp, pp_a, pp_b, pp_pa, pp_pb, pp_class, classes, p, Pr, Pi, F, Eoff,
-                                               Epool, bound);
+                                               Epool, Epool32, bound);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !dev_for_bounds) return e;
+    pair_bound_kernel<<<(npp + 63) / 64, 64, 0, s>>>(basis, *dev_for_bounds, npp, pp_a, pp_b, pp_pa, pp_pb, pp_class,
+                                                     classes, bound);
     return cudaGetLastError();
 }
 
@@ -307,19 +407,19 @@ cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const
 
 __constant__ double c_int[40];  // c_int[k] = k, avoids int->double conversions in inner loops
 
-__device__ __forceinline__ void phase1(const EriDev& d, int L, int ip, int iq, double2* col, int stride,
-                                       long long item) {
+// Seeds C (-2 rho)^n F_n(T) of primitive quartet (ip, iq) into Sh[0..L];
+// X receives the complex centre separation.  Boys failures are reported
+// through the status word and give zero seeds.
+__device__ __forceinline__ void quartet_seeds_rt(const EriDev& d, int L, int ip, int iq, double2* X, double2* Sh,
+                                                 long long item) {
     const PairData& pp = d.pairs;
     const double p = pp.p[ip], q = pp.p[iq];
-    const double Xr0 = pp.Pr[3 * ip] - pp.Pr[3 * iq], Xr1 = pp.Pr[3 * ip + 1] - pp.Pr[3 * iq + 1],
-                 Xr2 = pp.Pr[3 * ip + 2] - pp.Pr[3 * iq + 2];
-    const double Xi0 = pp.Pi[3 * ip] - pp.Pi[3 * iq], Xi1 = pp.Pi[3 * ip + 1] - pp.Pi[3 * iq + 1],
-                 Xi2 = pp.Pi[3 * ip + 2] - pp.Pi[3 * iq + 2];
+    for (int x = 0; x < 3; ++x) X[x] = c2(pp.Pr[3 * ip + x] - pp.Pr[3 * iq + x], pp.Pi[3 * ip + x] - pp.Pi[3 * iq + x]);
     const double r = rsqrt(p + q);
     const double rho = p * q * r * r;
-    const double tre = rho * (fma(Xr0, Xr0, fma(Xr1, Xr1, Xr2 * Xr2)) - fma(Xi0, Xi0, fma(Xi1, Xi1, Xi2 * Xi2)));
-    const double tim = 2.0 * rho * fma(Xr0, Xi0, fma(Xr1, Xi1, Xr2 * Xi2));
-    double2 Sh[BOYS_MAX_ORDER + 1];
+    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
+                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
+    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
     double2 e0;
     double2 C = cscale(cmul(pp.F[ip], pp.F[iq]), r);
     if (const int rc = boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
@@ -329,15 +429,35 @@ __device__ __forceinline__ void phase1(const EriDev& d, int L, int ip, int iq, d
         for (int n = 0; n <= L; ++n) Sh[n] = c2(0.0, 0.0);
     }
     C = cmul(C, e0);
-    // seeds (-2 rho)^n C Sh_n, folded into Sh
     const double m2r = -2.0 * rho;
-    double2 cn = C;
     for (int n = 0; n <= L; ++n) {
-        Sh[n] = cmul(cn, Sh[n]);
-        cn = cscale(cn, m2r);
+        Sh[n] = cmul(C, Sh[n]);
+        C = cscale(C, m2r);
     }
-    const double2 X[3] = {c2(Xr0, Xi0), c2(Xr1, Xi1), c2(Xr2, Xi2)};
-    col[0] = Sh[L];
+}
+
+// In-place descending-level Hermite recurrence into one column (stride
+// apart) of the shared table, FP64 (T = double2) or FP32 (T = float2).
+template <typename T>
+__device__ __forceinline__ T tmul(T a, T b);
+template <>
+__device__ __forceinline__ double2 tmul(double2 a, double2 b) { return cmul(a, b); }
+template <>
+__device__ __forceinline__ float2 tmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 tmacr(double2 c, int k, double2 a) { return cmacr(c, c_int[k], a); }
+__device__ __forceinline__ float2 tmacr(float2 c, int k, float2 a) {
+    return make_float2(fmaf((float)k, a.x, c.x), fmaf((float)k, a.y, c.y));
+}
+__device__ __forceinline__ double2 tmac(double2 c, double2 a, double2 b) { return cmac(c, a, b); }
+__device__ __forceinline__ float2 tmac(float2 c, float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+
+template <typename T>
+__device__ __forceinline__ void hermite_rec(int L, const T* seed, const T* X, T* col, int stride) {
+    col[0] = seed[L];
     for (int n = L - 1; n >= 0; --n) {
         for (int dg = L - n; dg >= 1; --dg) {
             for (int k = dg; k >= 0; --k) {
@@ -360,13 +480,89 @@ __device__ __forceinline__ void phase1(const EriDev& d, int L, int ip, int iq, d
                         i1 = herm_index(0, 0, m - 1);
                         i2 = m > 1 ? herm_index(0, 0, m - 2) : 0;
                     }
-                    double2 v = cmul(X[axis], col[i1 * stride]);
-                    if (pw > 1) v = cmacr(v, c_int[pw - 1], col[i2 * stride]);
+                    T v = tmul(X[axis], col[i1 * stride]);
+                    if (pw > 1) v = tmacr(v, pw - 1, col[i2 * stride]);
                     col[herm_index(k, l, m) * stride] = v;
                 }
             }
         }
-        col[0] = Sh[n];
+        col[0] = seed[n];
+    }
+}
+
+constexpr double FP32_SEED_LIMIT = 1.0e25;
+
+// Per-warp shared layout of quartet_kernel (all offsets in bytes).
+struct WarpSmem {
+    size_t R, W, R32, W32, queue, flag, total;
+};
+__host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed) {
+    WarpSmem w;
+    const size_t B1p = B1 + 1;
+    w.R = 0;
+    w.W = w.R + (size_t)NL * B1p * 16;
+    w.R32 = w.W + (size_t)Nab * CH * 16;
+    w.W32 = w.R32 + (mixed ? (((size_t)NL * B1p * 8 + 15) / 16) * 16 : 0);
+    w.queue = w.W32 + (mixed ? (((size_t)Nab * CH * 8 + 15) / 16) * 16 : 0);
+    w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
+    w.total = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
+    return w;
+}
+
+// Ket transform of batch entry j into W (FP64) or W32 (FP32).
+template <typename T, typename E>
+__device__ __forceinline__ void step_k(const QuartetClass& qc, const uint32_t* herm_xyz, const E* Ek, const T* R,
+                                       int B1p, int j, T* W, int c0, int chn, int lane) {
+    for (int it = lane; it < qc.Nab * chn; it += 32) {
+        const int K = it / chn, cdl = it - K * chn, cd = c0 + cdl;
+        const uint32_t kx = __ldg(&herm_xyz[K]);
+        const int bk = kx & 255, bl = (kx >> 8) & 255, bm = (kx >> 16) & 255;
+        const int bo = qc.ket.boxoff[cd];
+        const int bd = qc.ket.boxdim[cd];
+        const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+        T acc = W[K * qc.CH + cdl];
+        for (int e = 0; e < nbox; ++e) {
+            const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
+            const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
+            E ev = __ldg(&Ek[bo + e]);
+            if ((k2 + l2 + m2) & 1) {
+                ev.x = -ev.x;
+                ev.y = -ev.y;
+            }
+            T evt;
+            evt.x = ev.x;
+            evt.y = ev.y;
+            acc = tmac(acc, evt, R[herm_index(bk + k2, bl + l2, bm + m2) * B1p + j]);
+        }
+        W[K * qc.CH + cdl] = acc;
+    }
+}
+
+// Bra transform of W (FP64) and W32 (FP32) into the task's output block.
+__device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, const Task& tg, int ip, double2* W,
+                                       float2* W32, bool use32, int c0, int chn, int lane) {
+    const int nab = qc.bra.nab;
+    const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
+    const double2* Ea = d.pairs.Epool + d.pairs.Eoff[ip];
+    const float2* Ea32 = d.pairs.Epool32 + d.pairs.Eoff[ip];
+    for (int it = lane; it < nab * chn; it += 32) {
+        const int ab = it / chn, cdl = it - ab * chn, cd = c0 + cdl;
+        const int bo = qc.bra.boxoff[ab];
+        const int bd = qc.bra.boxdim[ab];
+        const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+        double2 acc = c2(0.0, 0.0);
+        float2 acc32 = make_float2(0.0f, 0.0f);
+        for (int e = 0; e < nbox; ++e) {
+            const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
+            const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+            acc = cmac(acc, __ldg(&Ea[bo + e]), W[K * qc.CH + cdl]);
+            if (use32) acc32 = tmac(acc32, __ldg(&Ea32[bo + e]), W32[K * qc.CH + cdl]);
+        }
+        if (use32) acc = cadd(acc, c2((double)acc32.x, (double)acc32.y));  // FP64 final summation
+        const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
+        double2* o = d.out + tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1] +
+                     (long long)cc * tg.st[2] + (long long)cdd * tg.st[3];
+        *o = cadd(*o, acc);
     }
 }
 
@@ -376,16 +572,27 @@ __global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc)
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
     const int B1p = qc.B1 + 1;
-    const int per_warp = qc.NL * B1p + qc.Nab * qc.CH;
-    double2* R = sm + (size_t)wib * per_warp;
-    double2* W = R + qc.NL * B1p;
+    const float skip = d.skip_cut, cut32 = d.fp32_cut;
+    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f);
+    char* base = reinterpret_cast<char*>(sm) + (size_t)wib * lay.total;
+    double2* R = reinterpret_cast<double2*>(base + lay.R);
+    double2* W = reinterpret_cast<double2*>(base + lay.W);
+    float2* R32 = reinterpret_cast<float2*>(base + lay.R32);
+    float2* W32 = reinterpret_cast<float2*>(base + lay.W32);
+    int* queue = reinterpret_cast<int*>(base + lay.queue);
+    int* flag = reinterpret_cast<int*>(base + lay.flag);
     const int nab = qc.bra.nab, ncd = qc.ket.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const int ns = d.basis.ns;
-    // Each warp takes a group of tasks with equal primitive counts and walks
-    // their primitive quartets as one stream (task g, bra pair P, ket pair Q),
-    // B1 at a time through phase 1, so lanes stay busy for any contraction
-    // depth.
+    const PairData& pp = d.pairs;
+    const float cut64 = fmaxf(cut32, skip);
+    const int npass = cut32 > 0.0f ? 2 : 1;
+    unsigned long long cnt64 = 0, cnt32 = 0;
+    // A warp takes a group of tasks with equal primitive counts and walks
+    // their primitive quartets as one stream (task g, bra pair P, ket pair Q;
+    // pairs in decreasing Schwarz order).  Each pass compacts the entries of
+    // its precision into batches of B1 with a ballot, so screened or
+    // other-precision entries cost no FP64 issue slots.
     for (int grp = blockIdx.x * wpb + wib; grp < qc.ngroup; grp += gridDim.x * wpb) {
         const int2 gi = qc.groups[grp];
         const Task t0 = qc.tasks[gi.x];
@@ -393,79 +600,139 @@ __global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc)
         const int Kcd = d.basis.nprim[t0.sc] * d.basis.nprim[t0.sd];
         const int KK = Kab * Kcd;
         const int S = gi.y * KK;
-        for (int c0 = 0; c0 < ncd; c0 += qc.CH) {
-            const int chn = min(qc.CH, ncd - c0);
-            for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
-            for (int s0 = 0; s0 < S; s0 += qc.B1) {
-                const int nb = min(qc.B1, S - s0);
-                __syncwarp();
-                if (lane < nb) {
-                    const int sidx = s0 + lane;
-                    const int g = sidx / KK, r = sidx - g * KK;
-                    const Task tg = qc.tasks[gi.x + g];
-                    const int P = r / Kcd, Q = r - P * Kcd;
-                    phase1(d, qc.L, d.basis.sp_off[tg.sa * ns + tg.sb] + P, d.basis.sp_off[tg.sc * ns + tg.sd] + Q,
-                           R + lane, B1p, gi.x + g);
-                }
-                __syncwarp();
-                for (int j = 0; j < nb; ++j) {
-                    const int sidx = s0 + j;
-                    const int g = sidx / KK, r = sidx - g * KK;
-                    const int P = r / Kcd, Q = r - P * Kcd;
-                    const Task tg = qc.tasks[gi.x + g];
-                    const double2* Ek =
-                        d.pairs.Epool + d.pairs.Eoff[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
-                    for (int it = lane; it < qc.Nab * chn; it += 32) {
-                        const int K = it / chn, cdl = it - K * chn, cd = c0 + cdl;
-                        const uint32_t kx = __ldg(&d.herm_xyz[K]);
-                        const int bk = kx & 255, bl = (kx >> 8) & 255, bm = (kx >> 16) & 255;
-                        const int bo = qc.ket.boxoff[cd];
-                        const int bd = qc.ket.boxdim[cd];
-                        const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-                        double2 acc = W[K * qc.CH + cdl];
-                        for (int e = 0; e < nbox; ++e) {
-                            const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
-                            const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
-                            double2 ev = __ldg(&Ek[bo + e]);
-                            if ((k2 + l2 + m2) & 1) ev = c2(-ev.x, -ev.y);
-                            acc = cmac(acc, ev, R[herm_index(bk + k2, bl + l2, bm + m2) * B1p + j]);
-                        }
-                        W[K * qc.CH + cdl] = acc;
-                    }
-                    if (Q == Kcd - 1) {
-                        // bra transform of this (task, P) into the task's output block
-                        __syncwarp();
-                        const double2* Ea =
-                            d.pairs.Epool + d.pairs.Eoff[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                        for (int it = lane; it < nab * chn; it += 32) {
-                            const int ab = it / chn, cdl = it - ab * chn, cd = c0 + cdl;
-                            const int bo = qc.bra.boxoff[ab];
-                            const int bd = qc.bra.boxdim[ab];
-                            const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-                            double2 acc = c2(0.0, 0.0);
-                            for (int e = 0; e < nbox; ++e) {
-                                const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
-                                const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
-                                acc = cmac(acc, __ldg(&Ea[bo + e]), W[K * qc.CH + cdl]);
-                            }
-                            const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
-                            double2* o = d.out + tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1] +
-                                         (long long)cc * tg.st[2] + (long long)cdd * tg.st[3];
-                            *o = P == 0 ? acc : cadd(*o, acc);
-                        }
-                        __syncwarp();
-                        for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
-                        __syncwarp();
-                    }
-                }
+        for (int g = 0; g < gi.y; ++g) {
+            const Task tg = qc.tasks[gi.x + g];
+            for (int it = lane; it < nab * ncd; it += 32) {
+                const int ab = it / ncd, cd = it - ab * ncd;
+                const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
+                d.out[tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1] + (long long)cc * tg.st[2] +
+                      (long long)cdd * tg.st[3]] = c2(0.0, 0.0);
             }
-            __syncwarp();
+        }
+        __syncwarp();
+        for (int pass = 0; pass < npass; ++pass) {
+            for (int c0 = 0; c0 < ncd; c0 += qc.CH) {
+                const int chn = min(qc.CH, ncd - c0);
+                for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
+                    W[it] = c2(0.0, 0.0);
+                    if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
+                }
+                int cur = -1;  // g * Kab + P of the accumulating bra pair
+                int cursor = 0;
+                while (cursor < S) {
+                    // assemble up to B1 entries of this pass
+                    int nb = 0;
+                    __syncwarp();
+                    while (nb < qc.B1 && cursor < S) {
+                        const int idx = cursor + lane;
+                        bool valid = false;
+                        if (idx < S) {
+                            const int g = idx / KK, r = idx - g * KK;
+                            const int P = r / Kcd, Q = r - P * Kcd;
+                            const Task tg = qc.tasks[gi.x + g];
+                            const float b = pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
+                                            pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                            valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
+                        }
+                        const unsigned mask = __ballot_sync(0xffffffffu, valid);
+                        const int cnt = __popc(mask);
+                        const int take = min(cnt, qc.B1 - nb);
+                        const int rank = __popc(mask & ((1u << lane) - 1u));
+                        if (valid && rank < take) queue[nb + rank] = idx;
+                        if (take < cnt) {
+                            const unsigned m2 = __ballot_sync(0xffffffffu, valid && rank == take);
+                            cursor += __ffs(m2) - 1;
+                        } else {
+                            cursor += 32;
+                        }
+                        nb += take;
+                    }
+                    __syncwarp();
+                    if (nb == 0) break;
+                    if (lane < nb) {
+                        const int idx = queue[lane];
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                        double2 X[3], Sh[BOYS_MAX_ORDER + 1];
+                        quartet_seeds_rt(d, qc.L, ip, iq, X, Sh, gi.x + g);
+                        int f = 1;
+                        if (pass == 1) {
+                            double big = 0.0;
+                            for (int n = 0; n <= qc.L; ++n) big = fmax(big, fabs(Sh[n].x) + fabs(Sh[n].y));
+                            f = big < FP32_SEED_LIMIT ? 0 : 1;
+                        }
+                        if (f) {
+                            hermite_rec<double2>(qc.L, Sh, X, R + lane, B1p);
+                            ++cnt64;
+                        } else {
+                            float2 S32[BOYS_MAX_ORDER + 1];
+                            for (int n = 0; n <= qc.L; ++n) S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
+                            const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
+                                                   make_float2((float)X[1].x, (float)X[1].y),
+                                                   make_float2((float)X[2].x, (float)X[2].y)};
+                            hermite_rec<float2>(qc.L, S32, X32, R32 + lane, B1p);
+                            ++cnt32;
+                        }
+                        flag[lane] = f;
+                    }
+                    __syncwarp();
+                    for (int j = 0; j < nb; ++j) {
+                        const int idx = queue[j];
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const int key = g * Kab + P;
+                        if (key != cur) {
+                            if (cur >= 0) {
+                                __syncwarp();
+                                const int cg = cur / Kab, cP = cur - cg * Kab;
+                                const Task tc = qc.tasks[gi.x + cg];
+                                step_b(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, pass == 1,
+                                       c0, chn, lane);
+                                __syncwarp();
+                                for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
+                                    W[it] = c2(0.0, 0.0);
+                                    if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
+                                }
+                                __syncwarp();
+                            }
+                            cur = key;
+                        }
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                        if (flag[j])
+                            step_k<double2, double2>(qc, d.herm_xyz, pp.Epool + pp.Eoff[iq], R, B1p, j, W, c0, chn,
+                                                     lane);
+                        else
+                            step_k<float2, float2>(qc, d.herm_xyz, pp.Epool32 + pp.Eoff[iq], R32, B1p, j, W32, c0,
+                                                   chn, lane);
+                    }
+                }
+                if (cur >= 0) {
+                    __syncwarp();
+                    const int cg = cur / Kab, cP = cur - cg * Kab;
+                    const Task tc = qc.tasks[gi.x + cg];
+                    step_b(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, pass == 1, c0, chn,
+                           lane);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    if (d.counters) {
+        const unsigned long long a64 = __reduce_add_sync(0xffffffffu, (unsigned)cnt64);
+        const unsigned long long a32 = __reduce_add_sync(0xffffffffu, (unsigned)cnt32);
+        if (lane == 0) {
+            atomicAdd(&d.counters[0], a64);
+            atomicAdd(&d.counters[1], a32);
         }
     }
 }
 
-size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block) {
-    return (size_t)warps_per_block * ((size_t)qc.NL * (qc.B1 + 1) + (size_t)qc.Nab * qc.CH) * sizeof(double2);
+size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed) {
+    return (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed).total;
 }
 
 static bool g_const_ready = false;
@@ -480,7 +747,7 @@ cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps
         if (e != cudaSuccess) return e;
         g_const_ready = true;
     }
-    const size_t smem = quartet_smem_bytes(qc, warps_per_block);
+    const size_t smem = quartet_smem_bytes(qc, warps_per_block, dev.fp32_cut > 0.0f);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(quartet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

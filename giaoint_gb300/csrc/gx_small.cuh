@@ -140,6 +140,57 @@ __host__ __device__ constexpr BMac bmac(int idx) {
     return BMac{0, 0, 0};
 }
 
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 fmac2(float2 c, float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+
+template <int L, int... S>
+__device__ __forceinline__ void run_rec32(float2* R, const float2* seed, const float2* X,
+                                          std::integer_sequence<int, S...>) {
+    (
+        [&] {
+            constexpr RStep st = rstep(L, S);
+            if constexpr (st.kind == 1) {
+                R[0] = seed[st.n];
+            } else {
+                float2 v = fmul2(X[st.axis], R[st.s1]);
+                if constexpr (st.coef > 0) {
+                    v.x = fmaf((float)st.coef, R[st.s2].x, v.x);
+                    v.y = fmaf((float)st.coef, R[st.s2].y, v.y);
+                }
+                R[st.dst] = v;
+            }
+        }(),
+        ...);
+}
+
+template <int LA, int LB, int LC, int LD, int... S>
+__device__ __forceinline__ void run_k32(float2* W, const float2* R, const float2* __restrict__ Ecd,
+                                        std::integer_sequence<int, S...>) {
+    (
+        [&] {
+            constexpr KMac m = kmac<LA, LB, LC, LD>(S);
+            float2 e = __ldg(&Ecd[m.eoff]);
+            if constexpr (m.neg) e = make_float2(-e.x, -e.y);
+            W[m.w] = fmac2(W[m.w], e, R[m.r]);
+        }(),
+        ...);
+}
+
+template <int LA, int LB, int LC, int LD, int... S>
+__device__ __forceinline__ void run_b32(float2* out, const float2* W, const float2* __restrict__ Eab,
+                                        std::integer_sequence<int, S...>) {
+    (
+        [&] {
+            constexpr BMac m = bmac<LA, LB, LC, LD>(S);
+            out[m.o] = fmac2(out[m.o], __ldg(&Eab[m.eoff]), W[m.w]);
+        }(),
+        ...);
+}
+
 template <int L, int... S>
 __device__ __forceinline__ void run_rec(double2* R, const double2* seed, const double2* X,
                                         std::integer_sequence<int, S...>) {
@@ -181,6 +232,36 @@ __device__ __forceinline__ void run_b(double2* out, const double2* W, const doub
         ...);
 }
 
+// Seeds C (-2 rho)^n F_n for one primitive quartet; returns false (and zero
+// seeds) on a Boys failure, which is reported through the status word.
+template <int L>
+__device__ __forceinline__ void quartet_seeds(const EriDev& d, int tk, double p, double q, const double2* X,
+                                              double2 Fab, double2 Fcd, double2* Sh) {
+    const double r = rsqrt(p + q);
+    const double rho = p * q * r * r;
+    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
+                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
+    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+    double2 e0;
+    double2 C = cscale(cmul(Fab, Fcd), r);
+    if (const int rc = boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
+        report(d.status, rc, tk, L, tre, tim);
+        C = c2(0.0, 0.0);
+        e0 = c2(0.0, 0.0);
+    }
+    C = cmul(C, e0);
+    const double m2r = -2.0 * rho;
+#pragma unroll
+    for (int n = 0; n <= L; ++n) {
+        Sh[n] = cmul(C, Sh[n]);
+        C = cscale(C, m2r);
+    }
+}
+
+// FP32 values are safe when every seed is far inside the float range
+// (the recurrence grows entries by at most |X'| + L per level).
+constexpr double FP32_SEED_LIMIT = 1.0e25;
+
 template <int LA, int LB, int LC, int LD>
 __global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks, int ntask) {
     constexpr int L = LA + LB + LC + LD;
@@ -195,11 +276,19 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks,
     const int pab0 = d.basis.sp_off[t.sa * ns + t.sb];
     const int pcd0 = d.basis.sp_off[t.sc * ns + t.sd];
     const PairData& pp = d.pairs;
+    const float skip = d.skip_cut, cut32 = d.fp32_cut;
+    const float cut64 = fmaxf(cut32, skip);
+    const float bq0 = pp.sbound[pcd0];
+    unsigned n64 = 0, n32 = 0;
     double2 out[NAB * NCD];
 #pragma unroll
     for (int i = 0; i < NAB * NCD; ++i) out[i] = c2(0.0, 0.0);
+    // Primitive pairs are visited in decreasing Schwarz order, so screened
+    // quartets form a suffix of every row and the loops can stop early.
     for (int P = 0; P < Kab; ++P) {
-        const int ip = pab0 + P;
+        const float bp = pp.sbound[pab0 + P];
+        if (bp * bq0 < skip) break;
+        const int ip = pp.order[pab0 + P];
         const double p = pp.p[ip];
         const double Pr0 = pp.Pr[3 * ip], Pr1 = pp.Pr[3 * ip + 1], Pr2 = pp.Pr[3 * ip + 2];
         const double Pi0 = pp.Pi[3 * ip], Pi1 = pp.Pi[3 * ip + 1], Pi2 = pp.Pi[3 * ip + 2];
@@ -207,32 +296,8 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks,
         double2 W[NH * NCD];
 #pragma unroll
         for (int i = 0; i < NH * NCD; ++i) W[i] = c2(0.0, 0.0);
-        for (int Q = 0; Q < Kcd; ++Q) {
-            const int iq = pcd0 + Q;
-            const double q = pp.p[iq];
-            const double2 X[3] = {c2(Pr0 - pp.Pr[3 * iq], Pi0 - pp.Pi[3 * iq]),
-                                  c2(Pr1 - pp.Pr[3 * iq + 1], Pi1 - pp.Pi[3 * iq + 1]),
-                                  c2(Pr2 - pp.Pr[3 * iq + 2], Pi2 - pp.Pi[3 * iq + 2])};
-            const double r = rsqrt(p + q);
-            const double rho = p * q * r * r;
-            const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
-                                      fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
-            const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
-            double2 Sh[L + 1];
-            double2 e0;
-            double2 C = cscale(cmul(Fab, pp.F[iq]), r);
-            if (const int rc = boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
-                report(d.status, rc, tk, L, tre, tim);
-                C = c2(0.0, 0.0);
-                e0 = c2(0.0, 0.0);
-            }
-            C = cmul(C, e0);
-            const double m2r = -2.0 * rho;
-#pragma unroll
-            for (int n = 0; n <= L; ++n) {
-                Sh[n] = cmul(C, Sh[n]);
-                C = cscale(C, m2r);
-            }
+        bool any64 = false;
+        auto fp64_quartet = [&](int iq, const double2* X, double2* Sh) {
             double2 R[NL];
             if constexpr (L == 0) {
                 R[0] = Sh[0];
@@ -242,9 +307,72 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks,
             }
             run_k<LA, LB, LC, LD>(W, R, pp.Epool + pp.Eoff[iq],
                                   std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
+            any64 = true;
+            ++n64;
+        };
+        int Q = 0;
+        for (; Q < Kcd; ++Q) {
+            if (bp * pp.sbound[pcd0 + Q] < cut64) break;
+            const int iq = pp.order[pcd0 + Q];
+            const double2 X[3] = {c2(Pr0 - pp.Pr[3 * iq], Pi0 - pp.Pi[3 * iq]),
+                                  c2(Pr1 - pp.Pr[3 * iq + 1], Pi1 - pp.Pi[3 * iq + 1]),
+                                  c2(Pr2 - pp.Pr[3 * iq + 2], Pi2 - pp.Pi[3 * iq + 2])};
+            double2 Sh[L + 1];
+            quartet_seeds<L>(d, tk, p, pp.p[iq], X, Fab, pp.F[iq], Sh);
+            fp64_quartet(iq, X, Sh);
         }
-        run_b<LA, LB, LC, LD>(out, W, pp.Epool + pp.Eoff[ip],
-                              std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
+        if (cut32 > 0.0f) {
+            float2 W32[NH * NCD];
+#pragma unroll
+            for (int i = 0; i < NH * NCD; ++i) W32[i] = make_float2(0.0f, 0.0f);
+            bool any32 = false;
+            for (; Q < Kcd; ++Q) {
+                if (bp * pp.sbound[pcd0 + Q] < skip) break;
+                const int iq = pp.order[pcd0 + Q];
+                const double2 X[3] = {c2(Pr0 - pp.Pr[3 * iq], Pi0 - pp.Pi[3 * iq]),
+                                      c2(Pr1 - pp.Pr[3 * iq + 1], Pi1 - pp.Pi[3 * iq + 1]),
+                                      c2(Pr2 - pp.Pr[3 * iq + 2], Pi2 - pp.Pi[3 * iq + 2])};
+                double2 Sh[L + 1];
+                quartet_seeds<L>(d, tk, p, pp.p[iq], X, Fab, pp.F[iq], Sh);
+                double big = 0.0;
+#pragma unroll
+                for (int n = 0; n <= L; ++n) big = fmax(big, fabs(Sh[n].x) + fabs(Sh[n].y));
+                if (!(big < FP32_SEED_LIMIT)) {
+                    fp64_quartet(iq, X, Sh);  // out of float range: keep FP64
+                    continue;
+                }
+                float2 S32[L + 1];
+#pragma unroll
+                for (int n = 0; n <= L; ++n) S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
+                const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
+                                       make_float2((float)X[1].x, (float)X[1].y),
+                                       make_float2((float)X[2].x, (float)X[2].y)};
+                float2 R32[NL];
+                if constexpr (L == 0) {
+                    R32[0] = S32[0];
+                } else {
+                    R32[0] = S32[L];
+                    run_rec32<L>(R32, S32, X32, std::make_integer_sequence<int, rsteps(L)>{});
+                }
+                run_k32<LA, LB, LC, LD>(W32, R32, pp.Epool32 + pp.Eoff[iq],
+                                        std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
+                any32 = true;
+                ++n32;
+            }
+            if (any32) {
+                float2 o32[NAB * NCD];
+#pragma unroll
+                for (int i = 0; i < NAB * NCD; ++i) o32[i] = make_float2(0.0f, 0.0f);
+                run_b32<LA, LB, LC, LD>(o32, W32, pp.Epool32 + pp.Eoff[ip],
+                                        std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
+                // FP32 accumulation, FP64 final summation
+#pragma unroll
+                for (int i = 0; i < NAB * NCD; ++i) out[i] = cadd(out[i], c2((double)o32[i].x, (double)o32[i].y));
+            }
+        }
+        if (any64)
+            run_b<LA, LB, LC, LD>(out, W, pp.Epool + pp.Eoff[ip],
+                                  std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
     }
     constexpr int NCB = nc(LB), NCDD = nc(LD);
 #pragma unroll
@@ -255,6 +383,14 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks,
             d.out[t.out_off + (long long)ca * t.st[0] + (long long)cb * t.st[1] + (long long)cc * t.st[2] +
                   (long long)cdd * t.st[3]] = out[ab * NCD + cd];
         }
+    if (d.counters) {
+        const unsigned a64 = __reduce_add_sync(__activemask(), n64);
+        const unsigned a32 = __reduce_add_sync(__activemask(), n32);
+        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+            atomicAdd(&d.counters[0], (unsigned long long)a64);
+            atomicAdd(&d.counters[1], (unsigned long long)a32);
+        }
+    }
 }
 
 }  // namespace small

@@ -5,8 +5,13 @@ Mirrors python/giao_integrals/eri.py:1-208 and the native entry points
 ``_EriSchwarzBounds`` (src/bindings.cpp:409-425, 599-731): same names,
 keyword arguments, validation and error types.  ``threads`` is accepted and
 validated for compatibility and has no effect (the work runs on one GPU).
-Two keyword arguments are additions: ``precision`` ("fp64" or "mixed") and
-``mixed_cutoff``, the FP32 gating bound of the mixed mode.
+Two keyword arguments are additions: ``precision`` and ``mixed_cutoff``.
+``precision="fp64"`` (default) skips primitive quartets whose Schwarz
+product is below 1e-18 (they move no result by more than ~1e-15);
+``"fp64_exact"`` evaluates every primitive quartet as the reference does;
+``"mixed"`` evaluates primitive quartets with Schwarz product below
+``mixed_cutoff`` in FP32 (FP64 Boys values, FP64 final summation) and skips
+those below 1e-15.
 """
 
 from __future__ import annotations
@@ -26,7 +31,7 @@ from ._types import Basis, MagneticField, PrimitiveGaussian, Shell, field_arrays
 
 Quartet = tuple[int, int, int, int]
 
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "fp64_exact": 2}
 DEFAULT_MIXED_CUTOFF = 1.0e-6
 
 
@@ -34,7 +39,7 @@ def _precision(precision: str) -> int:
     try:
         return PRECISIONS[precision]
     except KeyError:
-        raise ValueError("precision must be 'fp64' or 'mixed'") from None
+        raise ValueError("precision must be 'fp64', 'mixed' or 'fp64_exact'") from None
 
 
 @dataclass(frozen=True)
@@ -95,10 +100,12 @@ def canonical_quartets(shell_count: int) -> np.ndarray:
 
 def _eri_batch(basis: Basis, quartets, *, field: MagneticField | None = None, screening_threshold: float = 0.0,
                threads=None, bounds=None, precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF,
-               context=None):
+               context=None, stats: dict | None = None):
     """Native packed batch (src/bindings.cpp:672-731): returns
     (quartets uint32[k,4], shapes int64[k,4], offsets int64[k+1],
-    values complex128, requested, screened)."""
+    values complex128, requested, screened).  A ``stats`` dict, when given,
+    receives the primitive-quartet counts (evaluated, FP32, skipped) and the
+    kernel time."""
     resolve_num_threads(threads)
     ctx = context or nat.default_context()
     q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
@@ -114,17 +121,22 @@ def _eri_batch(basis: Basis, quartets, *, field: MagneticField | None = None, sc
     values = np.empty(max(total, 1), dtype=np.complex128)
     offsets = np.zeros(len(q) + 1, dtype=np.int64)
     kept = np.empty((max(len(q), 1), 4), dtype=np.uint32)
-    stats = nat.GxStats()
+    stats_out = stats
+    st = nat.GxStats()
     B, O = field_arrays(field)
     nat.check(nat.lib().gx_eri_batch(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O), nat.u32ptr(q),
                                      len(q), _precision(precision), float(mixed_cutoff), screening_threshold,
                                      nat.u32ptr(kept), nat.i64ptr(offsets), nat.dptr(values.view(np.float64)),
-                                     total, ctypes.byref(stats)))
-    k = int(stats.computed)
+                                     total, ctypes.byref(st)))
+    if stats_out is not None:
+        stats_out.update(primitive_quartets=int(st.primitive_quartets),
+                         fp32_primitive_quartets=int(st.fp32_primitive_quartets),
+                         skipped_primitive_quartets=int(st.skipped_primitive_quartets), kernel_ms=float(st.kernel_ms))
+    k = int(st.computed)
     kept = kept[:k]
     offsets = offsets[: k + 1]
     shapes = sizes[kept.astype(np.int64)] if k else np.zeros((0, 4), dtype=np.int64)
-    return kept, shapes, offsets, values[: int(offsets[-1])], int(stats.requested), int(stats.screened)
+    return kept, shapes, offsets, values[: int(offsets[-1])], int(st.requested), int(st.screened)
 
 
 def eri_batches(basis: Basis, *, field: MagneticField | None = None, quartets: Iterable[Sequence[int]] | None = None,

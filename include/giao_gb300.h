@@ -37,9 +37,15 @@ enum gx_status {
 };
 
 /* Arithmetic of the quartet kernels. */
+/* Arithmetic of the quartet kernels.  Both modes skip primitive quartets
+ * whose Schwarz product B_P B_Q is negligible (below 1e-18 in FP64 mode,
+ * 1e-15 in mixed mode); mixed mode evaluates those under `mixed_cutoff` in
+ * FP32 (FP64 Boys function, FP32 recurrence and contraction, FP64 final
+ * summation). */
 enum gx_precision {
-    GX_PRECISION_FP64 = 0,  /* FP64 throughout                                   */
-    GX_PRECISION_MIXED = 1  /* FP32 for primitive quartets under a bound cutoff  */
+    GX_PRECISION_FP64 = 0,
+    GX_PRECISION_MIXED = 1,
+    GX_PRECISION_FP64_EXACT = 2  /* FP64, every primitive quartet (no screening) */
 };
 
 typedef struct gx_context gx_context; /* one device, its streams, Boys table, pools */
@@ -208,6 +214,10 @@ int gx_eri_plan_info(const gx_eri_plan* plan, int64_t* tasks, int64_t* primitive
  * gx_context_synchronize (or synchronise the stream) before reading. */
 int gx_eri_plan_execute(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                         void* out_device);
+/* Primitive quartets evaluated by the last execution (FP64 and FP32) and
+ * the matching FP64-structured FLOP model totals (waits for the stream). */
+int gx_eri_plan_counts(gx_eri_plan* plan, int64_t* fp64_quartets, int64_t* fp32_quartets, double* fp64_flops,
+                       double* fp32_flops);
 void gx_eri_plan_destroy(gx_eri_plan* plan);
 
 /* Canonical shell quartets of an ns-shell basis: the lexicographic

@@ -154,3 +154,33 @@ def test_screening_and_schwarz_bounds(oracle):
             a, bb, c, d = (int(x) for x in quartet)
             assert q[a, bb] * q[c, d] >= 1e-8
             assert np.abs(b.block(k)).max() <= q[a, bb] * q[c, d] * (1 + 1e-12)
+
+
+def test_primitive_screening_is_exact_and_mixed_precision_within_1e10(golden):
+    """FP64 mode skips primitive quartets with Schwarz product < 1e-18 and
+    stays within 1e-12 of the reference; mixed mode (FP32 below 1e-6, skip
+    below 1e-15) stays within 1e-10 of the reference on every ERI."""
+    g = golden.blocks
+    basis = basis_from_records(syn.random_molecule(2026))
+    field = gi.MagneticField(tuple(g["mol_field"]))
+    st64, stmx = {}, {}
+    _, _, _, v64, _, _ = _eri_batch(basis, g["mol_quartets"], field=field, stats=st64)
+    _, _, _, vmx, _, _ = _eri_batch(basis, g["mol_quartets"], field=field, precision="mixed", stats=stmx)
+    assert np.abs(v64 - g["mol_values"]).max() <= ATOL
+    assert st64["skipped_primitive_quartets"] > 0 and st64["fp32_primitive_quartets"] == 0
+    assert stmx["fp32_primitive_quartets"] > 0
+    assert stmx["primitive_quartets"] - stmx["fp32_primitive_quartets"] < st64["primitive_quartets"]
+    assert np.abs(vmx - g["mol_values"]).max() <= 1e-10
+
+
+def test_mixed_precision_full_tensor_and_zero_field(golden):
+    basis = basis_from_records(syn.full_tensor_atom())
+    n = basis.ao_count
+    f = gi.MagneticField((0, 0, 0.1))
+    full64 = gi.eri(basis, field=f, storage="full", max_bytes=n**4 * 16)
+    fullmx = gi.eri(basis, field=f, storage="full", max_bytes=n**4 * 16, precision="mixed")
+    assert np.abs(full64 - fullmx).max() <= 1e-10
+    g = golden.blocks
+    mol = basis_from_records(syn.random_molecule(2026))
+    _, _, _, v0, _, _ = _eri_batch(mol, g["mol_quartets"][:120], field=gi.MagneticField((0, 0, 0)), precision="mixed")
+    assert np.abs(v0 - g["mol_zero_values"]).max() <= 1e-10
