@@ -47,6 +47,22 @@ class GxCholeskyOptions(ctypes.Structure):
     ]
 
 
+class GxClassProfile(ctypes.Structure):
+    _fields_ = [
+        ("la", ctypes.c_int), ("lb", ctypes.c_int), ("lc", ctypes.c_int), ("ld", ctypes.c_int),
+        ("tasks", ctypes.c_int64),
+        ("primitive_quartets", ctypes.c_int64),
+        ("fp64_quartets", ctypes.c_int64),
+        ("fp32_quartets", ctypes.c_int64),
+        ("model_flops_per_quartet", ctypes.c_double),
+        ("ms", ctypes.c_float),
+        ("per_group", ctypes.c_int),
+        ("warps_per_block", ctypes.c_int),
+        ("batch", ctypes.c_int),
+        ("groups", ctypes.c_int64),
+    ]
+
+
 # name -> (restype, argtypes); every symbol of include/giao_gb300.h
 SIGNATURES = {
     "gx_context_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -78,6 +94,11 @@ SIGNATURES = {
     "gx_eri_plan_execute": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp]),
     "gx_eri_plan_destroy": (None, [_vp]),
     "gx_eri_plan_counts": (ctypes.c_int, [_vp, _i64, _i64, _d, _d]),
+    "gx_eri_plan_class_count": (ctypes.c_int, [_vp]),
+    "gx_eri_plan_graph_replays": (ctypes.c_int, [_vp]),
+    "gx_eri_plan_profile": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp,
+                                           ctypes.POINTER(GxClassProfile)]),
+    "gx_eri_plan_autotune": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp, ctypes.c_int, _d, _d]),
     "gx_measure_fp64_peak": (ctypes.c_int, [_vp, _d]),
     "gx_canonical_quartets": (ctypes.c_int64, [ctypes.c_int, _u32]),
     "gx_cholesky_step_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int, ctypes.c_int,

@@ -213,7 +213,9 @@ struct gx_context {
         return ref;
     }
 
-    gx::BoysTable boys() const { return gx::BoysTable{boys_S.as<double2>(), boys_E0.as<double2>()}; }
+    gx::BoysTable boys() const {
+        return gx::BoysTable{boys_S.as<double2>(), boys_E0.as<double2>()};
+    }
 
     void reset_status() { GX_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(gx::DevStatus), stream)); }
 
@@ -253,7 +255,7 @@ void check_status(gx_context* ctx) {
 
 struct FieldPairs {
     double B[3], O[3];
-    DeviceBuffer p, Pr, Pi, F, Epool, bound, Epool32, order, sbound;
+    DeviceBuffer p, Pr, Pi, F, Epool, bound, Epool32, order, sbound, g32;
 };
 
 struct gx_basis {
@@ -378,7 +380,8 @@ gx::PairData pair_view(gx_basis* b, FieldPairs& fp) {
                         fp.bound.as<double>(),
                         fp.Epool32.as<float2>(),
                         fp.order.as<int>(),
-                        fp.sbound.as<float>()};
+                        fp.sbound.as<float>(),
+                        fp.g32.as<float4>()};
 }
 
 FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
@@ -397,6 +400,7 @@ FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
     fp.bound.reserve(n * sizeof(double));
     fp.order.reserve(n * sizeof(int));
     fp.sbound.reserve(n * sizeof(float));
+    fp.g32.reserve(2 * n * sizeof(float4));
     fp.Epool.reserve(std::max<long long>(b->Etotal, 1) * sizeof(double2));
     fp.Epool32.reserve(std::max<long long>(b->Etotal, 1) * sizeof(float2));
     gx::EriDev dev{};
@@ -409,8 +413,8 @@ FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
                                        b->d_pp_pa.as<int>(), b->d_pp_pb.as<int>(), b->d_pp_class.as<int>(),
                                        b->d_classes.as<gx::PairClassDev>(), fp.p.as<double>(), fp.Pr.as<double>(),
                                        fp.Pi.as<double>(), fp.F.as<double2>(), b->d_Eoff.as<long long>(),
-                                       fp.Epool.as<double2>(), fp.Epool32.as<float2>(), fp.bound.as<double>(), &dev,
-                                       b->ctx->stream));
+                                       fp.Epool.as<double2>(), fp.Epool32.as<float2>(), fp.bound.as<double>(),
+                                       fp.g32.as<float4>(), &dev, b->ctx->stream));
     std::vector<double> bound(b->npp);
     if (b->npp)
         GX_CUDA(cudaMemcpyAsync(bound.data(), fp.bound.ptr, b->npp * sizeof(double), cudaMemcpyDeviceToHost,
@@ -456,12 +460,32 @@ struct PlanClass {
     double flops_per_primitive_quartet;
 };
 
+// Launch configuration of one class: the autotuner's knobs (0 = default).
+struct ClassConf {
+    int per_group = 0;  // primitive quartets per warp work unit (small: 1024, generic: 32)
+    int wpb = 0;        // generic kernel: warps per block cap (4)
+    int b1 = 0;         // generic kernel: phase-1 batch cap (32)
+};
+
+// Warp work units of every class: (first task within the class, task count).
+struct GroupSet {
+    DeviceBuffer dev;
+    std::vector<std::pair<size_t, size_t>> range;  // per class: first group, count
+};
+
 struct PlanData {
-    DeviceBuffer tasks, groups, counters;
-    std::vector<std::pair<size_t, size_t>> group_range;  // per class: first group, count
+    DeviceBuffer tasks, counters;
+    GroupSet base;                  // default configuration
     std::vector<PlanClass> classes;
+    std::vector<int> task_kk;       // per task (class order): Kab << 16 | Kcd, for regrouping
     int64_t ntask = 0, primitive_quartets = 0;
     double model_flops = 0.0;
+    // autotuned configuration per precision mode (GX_PRECISION_*)
+    struct Tuned {
+        bool valid = false;
+        GroupSet groups;
+        std::vector<ClassConf> conf;
+    } tuned[3];
 };
 
 // FP64 FLOP model per primitive quartet of class (la, lb, lc, ld): the
@@ -478,6 +502,44 @@ double model_flops(int la, int lb, int lc, int ld) {
     const double nab = (double)gx::ncart(la) * gx::ncart(lb), ncd = (double)gx::ncart(lc) * gx::ncart(ld);
     const double ere = std::min(4 * Nab * Ncd * ncd + 4 * nab * Nab * ncd, 4 * nab * Nab * Ncd + 4 * nab * Ncd * ncd);
     return 8 * R + ere + 8 * nab * ncd + 8 * (L + 1);
+}
+
+// Warp work units of class ci: runs of tasks with equal primitive counts
+// (Kab, Kcd).  Small classes (one lane per primitive quartet) take up to
+// `per_group` (default 1024) primitive quartets and 128 tasks per unit; the
+// generic kernel about `per_group` (default 32) primitive quartets and at
+// most 128 tasks per unit, fewer tasks when the class is too small to give
+// every SM eight warps.
+std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_t ci, const ClassConf& conf) {
+    const PlanClass& pc = plan.classes[ci];
+    const bool small = gx::small_class(pc.key[0], pc.key[1], pc.key[2], pc.key[3]);
+    const int per = conf.per_group > 0 ? conf.per_group : (small ? 1024 : 32);
+    const int spread = std::max<int>(1, (int)(pc.count / (size_t)(8 * std::max(ctx->sm_count, 1))));
+    std::vector<int2> groups;
+    size_t i = pc.first;
+    const size_t end = pc.first + pc.count;
+    while (i < end) {
+        const int kk_code = plan.task_kk[i];
+        const int kk = (kk_code >> 16) * (kk_code & 0xffff);
+        const int want = small ? std::max(1, std::min(128, per / kk))
+                               : std::max(1, std::min({128, (per + kk - 1) / kk, spread}));
+        size_t j = i + 1;
+        while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
+        groups.push_back(make_int2((int)(i - pc.first), (int)(j - i)));
+        i = j;
+    }
+    return groups;
+}
+
+void make_group_set(gx_context* ctx, const PlanData& plan, const std::vector<ClassConf>& conf, GroupSet& out) {
+    std::vector<int2> all;
+    out.range.clear();
+    for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
+        const auto g = make_groups(ctx, plan, ci, conf[ci]);
+        out.range.push_back({all.size(), g.size()});
+        all.insert(all.end(), g.begin(), g.end());
+    }
+    upload(out.dev, all, ctx->stream);
 }
 
 void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
@@ -537,31 +599,12 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
     }
     plan.ntask = (int64_t)all.size();
     upload(plan.tasks, all, ctx->stream);
-    // warp work units for the generic kernel: runs of tasks with equal
-    // primitive counts, about 32 primitive quartets per unit or more
-    std::vector<int2> groups;
-    plan.group_range.clear();
-    for (const auto& pc : plan.classes) {
-        const size_t g0 = groups.size();
-        size_t i = pc.first;
-        const size_t end = pc.first + pc.count;
-        while (i < end) {
-            const gx::Task& t = all[i];
-            const int kab = b->seg_nprim[t.sa] * b->seg_nprim[t.sb], kcd = b->seg_nprim[t.sc] * b->seg_nprim[t.sd];
-            const int want = std::max(1, std::min(32, (32 + kab * kcd - 1) / (kab * kcd)));
-            size_t j = i + 1;
-            while (j < end && (int)(j - i) < want) {
-                const gx::Task& u = all[j];
-                if (b->seg_nprim[u.sa] * b->seg_nprim[u.sb] != kab || b->seg_nprim[u.sc] * b->seg_nprim[u.sd] != kcd)
-                    break;
-                ++j;
-            }
-            groups.push_back(make_int2((int)i - (int)pc.first, (int)(j - i)));
-            i = j;
-        }
-        plan.group_range.push_back({g0, groups.size() - g0});
-    }
-    upload(plan.groups, groups, ctx->stream);
+    plan.task_kk.resize(all.size());
+    for (size_t t = 0; t < all.size(); ++t)
+        plan.task_kk[t] = (b->seg_nprim[all[t].sa] * b->seg_nprim[all[t].sb]) << 16 |
+                          (b->seg_nprim[all[t].sc] * b->seg_nprim[all[t].sd]);
+    std::vector<ClassConf> defaults(plan.classes.size());
+    make_group_set(ctx, plan, defaults, plan.base);
 }
 
 // Primitive screening thresholds on the Schwarz product B_P B_Q.  FP64: a
@@ -571,18 +614,13 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
 constexpr double kSkipFP64 = 1e-18;
 constexpr double kSkipMixed = 1e-15;
 
-// Enqueue the pair records for (B, O) and every class launch; no host sync.
-// counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null.
-int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
-                 double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
-                 unsigned long long* counters = nullptr) {
-    cudaStream_t s = ctx->stream;
-    FieldPairs& fp = field_pairs(b, B, O);
-    gx::EriDev dev;
+// Device view of one evaluation: pair records for (B, O), thresholds of the
+// precision mode, output and counters.
+gx::EriDev make_dev(gx_context* ctx, gx_basis* b, FieldPairs& fp, double2* out, int precision, double mixed_cutoff) {
+    gx::EriDev dev{};
     const bool mixed = precision == GX_PRECISION_MIXED;
     dev.skip_cut = (float)(mixed ? kSkipMixed : (precision == GX_PRECISION_FP64_EXACT ? 0.0 : kSkipFP64));
     dev.fp32_cut = (float)(mixed ? std::max(mixed_cutoff, kSkipMixed) : 0.0);
-    if (counters) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
     dev.basis = b->dev();
     dev.pairs = pair_view(b, fp);
     dev.boys = ctx->boys();
@@ -590,40 +628,123 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
     dev.herm_xyz = ctx->herm.as<uint32_t>();
     dev.out = out;
     dev.status = ctx->status.as<gx::DevStatus>();
-    ctx->reset_status();
-    int launches = 1;
-    for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
-        const auto& pc = plan.classes[ci];
-        const auto& k = pc.key;
-        dev.counters = counters ? counters + 2 * ci : nullptr;
-        if (gx::small_class(k[0], k[1], k[2], k[3])) {
-            GX_CUDA(gx::launch_small(k[0], k[1], k[2], k[3], dev, plan.tasks.as<gx::Task>() + pc.first,
-                                     (int)pc.count, s));
-            ++launches;
-            continue;
-        }
-        gx::QuartetClass qc;
-        qc.bra = ctx->pair_class(k[0], k[1]).dev();
-        qc.ket = ctx->pair_class(k[2], k[3]).dev();
+    return dev;
+}
+
+// Enqueue the kernel of class ci with configuration conf and work units
+// groups[0..ngroup).  Returns the (batch, warps per block) used through the
+// optional pointers.
+void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t ci, const ClassConf& conf,
+                  const int2* groups, int ngroup, unsigned long long* counters, cudaStream_t s, int* used_b1 = nullptr,
+                  int* used_wpb = nullptr) {
+    const auto& pc = plan.classes[ci];
+    const auto& k = pc.key;
+    dev.counters = counters ? counters + 2 * ci : nullptr;
+    if (gx::small_class(k[0], k[1], k[2], k[3])) {
+        gx::QuartetClass qc{};
         qc.L = k[0] + k[1] + k[2] + k[3];
-        qc.Nab = gx::herm_count(k[0] + k[1]);
-        qc.NL = gx::herm_count(qc.L);
-        const int ncd = qc.ket.nab;
-        qc.CH = std::max(1, std::min(ncd, 2048 / qc.Nab));
-        int B1 = 32;
-        while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
-        qc.B1 = B1;
         qc.ntask = (int)pc.count;
         qc.tasks = plan.tasks.as<gx::Task>() + pc.first;
-        qc.ngroup = (int)plan.group_range[ci].second;
-        qc.groups = plan.groups.as<int2>() + plan.group_range[ci].first;
-        const size_t per_warp = gx::quartet_smem_bytes(qc, 1, dev.fp32_cut > 0.0f);
-        int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
-        const int grid = (qc.ngroup + wpb - 1) / wpb;
-        GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
-        ++launches;
+        qc.ngroup = ngroup;
+        qc.groups = groups;
+        GX_CUDA(gx::launch_small(k[0], k[1], k[2], k[3], dev, qc, s));
+        if (used_b1) *used_b1 = 32;
+        if (used_wpb) *used_wpb = 4;
+        return;
     }
-    return launches;
+    gx::QuartetClass qc;
+    qc.bra = ctx->pair_class(k[0], k[1]).dev();
+    qc.ket = ctx->pair_class(k[2], k[3]).dev();
+    qc.L = k[0] + k[1] + k[2] + k[3];
+    qc.Nab = gx::herm_count(k[0] + k[1]);
+    qc.NL = gx::herm_count(qc.L);
+    const int ncd = qc.ket.nab;
+    qc.CH = std::max(1, std::min(ncd, 2048 / qc.Nab));
+    // Few work units: split the ket components of a group over several
+    // warps (each chunk keeps at least 32 ket-transform rows per warp).
+    const int target_units = 8 * std::max(ctx->sm_count, 1);
+    if (ngroup > 0 && ngroup * ((ncd + qc.CH - 1) / qc.CH) < target_units) {
+        const int want = (target_units + ngroup - 1) / ngroup;
+        const int ch = std::max((ncd + want - 1) / want, (32 + qc.Nab - 1) / qc.Nab);
+        qc.CH = std::max(1, std::min(qc.CH, ch));
+    }
+    // Lane utilisation of a transform with `items` work items per warp.
+    auto util = [](long long items) { return (double)items / (32.0 * (double)((items + 31) / 32)); };
+    // Tiles: rows per lane KT of the ket transform and ket components per lane
+    // CT of the bra transform, chosen for the best lane utilisation (padding
+    // of Nab to a multiple of KT counts as waste), the wider tile on ties.
+    {
+        double best = -1.0;
+        for (int kt : {4, 2, 1}) {
+            const int nkb = (qc.Nab + kt - 1) / kt;
+            const double e = util((long long)nkb * std::min(qc.CH, ncd)) * qc.Nab / (double)(nkb * kt);
+            if (e > best * 1.05) {
+                best = e;
+                qc.KT = kt;
+            }
+        }
+    }
+    {
+        double best = -1.0;
+        qc.CT = 1;
+        for (int ct : {4, 3, 2, 1}) {
+            if (ncd % ct) continue;
+            int ch = qc.CH < ncd ? std::max(ct, qc.CH / ct * ct) : ncd;
+            const double e = util((long long)qc.bra.nab * (std::min(ch, ncd) / ct));
+            if (e > best * 1.05) {
+                best = e;
+                qc.CT = ct;
+            }
+        }
+        if (qc.CH < ncd) qc.CH = std::max(qc.CT, qc.CH / qc.CT * qc.CT);  // chunks hold whole CT tiles
+    }
+    qc.nchunk = (ncd + qc.CH - 1) / qc.CH;
+    int B1 = conf.b1 > 0 ? std::min(32, conf.b1) : 32;
+    while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
+    qc.B1 = B1;
+    {
+        // cooperative recurrence when a batch has fewer entries than the
+        // ratio of the lane-parallel to the cooperative instruction count
+        double lane_cost = 150.0, coop_cost = 180.0;
+        for (int n = 0; n < qc.L; ++n) {
+            const int h = gx::herm_count(qc.L - n);
+            lane_cost += 6.0 * (h - 1);
+            coop_cost += 10.0 * ((h + 31) / 32);
+        }
+        qc.coop = std::min(B1, (int)(lane_cost / coop_cost));
+    }
+    qc.ntask = (int)pc.count;
+    qc.tasks = plan.tasks.as<gx::Task>() + pc.first;
+    qc.ngroup = ngroup;
+    qc.groups = groups;
+    const size_t per_warp = gx::quartet_smem_bytes(qc, 1, dev.fp32_cut > 0.0f);
+    const int cap = conf.wpb > 0 ? std::min(4, conf.wpb) : 4;
+    const int wpb = (int)std::max<size_t>(1, std::min<size_t>(cap, (200 * 1024) / per_warp));
+    const int grid = (int)std::min<long long>(((long long)qc.ngroup * qc.nchunk + wpb - 1) / wpb, 1 << 30);
+    GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
+    if (used_b1) *used_b1 = B1;
+    if (used_wpb) *used_wpb = wpb;
+}
+
+// Enqueue the pair records for (B, O) and every class launch; no host sync
+// unless the field changed (the pair bounds are sorted on the host).  Uses
+// the autotuned configuration of the precision mode when there is one.
+// counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null.
+int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
+                 double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
+                 unsigned long long* counters = nullptr) {
+    cudaStream_t s = ctx->stream;
+    FieldPairs& fp = field_pairs(b, B, O);
+    const gx::EriDev dev = make_dev(ctx, b, fp, out, precision, mixed_cutoff);
+    if (counters) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
+    ctx->reset_status();
+    const auto& tuned = plan.tuned[precision];
+    const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
+    static const ClassConf kDefault{};
+    for (size_t ci = 0; ci < plan.classes.size(); ++ci)
+        launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+                     gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s);
+    return 1 + (int)plan.classes.size();
 }
 
 // Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
@@ -1515,12 +1636,32 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
 // plans: build the class-sorted task list once, replay it per field
 // ---------------------------------------------------------------------------
 
+// Replay of a plan's class launches as one CUDA graph.  The graph is
+// captured on the second execution with the same (stream, output, precision,
+// cutoff, pair buffers, configuration) and replayed from then on; a new field
+// only rewrites the pair records the graph reads.
+struct PlanGraph {
+    cudaGraphExec_t exec = nullptr;
+    std::array<uintptr_t, 8> key{}, pending{};
+    bool disabled = false;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key = {};
+        pending = {};
+    }
+    ~PlanGraph() { reset(); }
+};
+
 struct gx_eri_plan {
     gx_context* ctx;
     gx_basis* basis;
     PlanData data;
     int64_t total = 0;
     int last_launches = 0;
+    PlanGraph graph;
+    int generation = 0;  // bumped when the launch configuration changes
+    int graph_replays = 0;
 };
 
 extern "C" {
@@ -1579,20 +1720,226 @@ int gx_eri_plan_info(const gx_eri_plan* plan, int64_t* tasks, int64_t* primitive
     });
 }
 
+namespace {
+
+void check_precision(int precision) {
+    if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
+        raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
+}
+
+// Enqueue one execution of the plan, replaying its CUDA graph when the
+// launch parameters repeat (see PlanGraph).
+void plan_enqueue(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                  double2* out) {
+    gx_context* ctx = plan->ctx;
+    PlanData& pd = plan->data;
+    pd.counters.reserve(std::max<size_t>(2 * pd.classes.size(), 2) * sizeof(unsigned long long));
+    FieldPairs& fp = field_pairs(plan->basis, B, O);  // host work only when the field changes
+    double cut = mixed_cutoff;
+    uint64_t cut_bits;
+    std::memcpy(&cut_bits, &cut, sizeof cut_bits);
+    const std::array<uintptr_t, 8> key{(uintptr_t)ctx->stream, (uintptr_t)out, (uintptr_t)precision,
+                                       (uintptr_t)cut_bits, (uintptr_t)fp.p.ptr, (uintptr_t)fp.Epool.ptr,
+                                       (uintptr_t)fp.order.ptr, (uintptr_t)plan->generation};
+    PlanGraph& g = plan->graph;
+    const bool capturable = !g.disabled && ctx->stream != nullptr;
+    if (capturable && g.exec && g.key == key) {
+        GX_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+        ++plan->graph_replays;
+        plan->last_launches = 1 + (int)pd.classes.size();
+        return;
+    }
+    if (capturable && g.pending == key) {
+        g.reset();
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            try {
+                plan->last_launches = execute_plan(ctx, plan->basis, B, O, pd, out, precision, mixed_cutoff,
+                                                   pd.counters.as<unsigned long long>());
+            } catch (...) {
+                cudaStreamEndCapture(ctx->stream, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                throw;
+            }
+            e = cudaStreamEndCapture(ctx->stream, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e == cudaSuccess) {
+            g.key = key;
+            GX_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+            ++plan->graph_replays;
+            return;
+        }
+        // capture is not available on this stream: run eagerly from now on
+        cudaGetLastError();
+        g.reset();
+        g.disabled = true;
+    }
+    plan->last_launches = execute_plan(ctx, plan->basis, B, O, pd, out, precision, mixed_cutoff,
+                                       pd.counters.as<unsigned long long>());
+    if (capturable) g.pending = key;
+}
+
+}  // namespace
+
 int gx_eri_plan_execute(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                         void* out_device) {
     return guarded([&] {
         if (!plan) raise(GX_EINVAL, "null plan");
         check_field(B, O);
-        if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
-            raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
+        check_precision(precision);
+        if (!out_device) raise(GX_EINVAL, "null output pointer");
         gx_context* ctx = plan->ctx;
         std::lock_guard<std::mutex> lock(ctx->mu);
         GX_CUDA(cudaSetDevice(ctx->device));
-        plan->data.counters.reserve(std::max<size_t>(2 * plan->data.classes.size(), 2) * sizeof(unsigned long long));
-        plan->last_launches =
-            execute_plan(ctx, plan->basis, B, O, plan->data, static_cast<double2*>(out_device), precision,
-                         mixed_cutoff, plan->data.counters.as<unsigned long long>());
+        plan_enqueue(plan, B, O, precision, mixed_cutoff, static_cast<double2*>(out_device));
+    });
+}
+
+int gx_eri_plan_class_count(const gx_eri_plan* plan) {
+    if (!plan) return gx::set_error(GX_EINVAL, "null plan");
+    return (int)plan->data.classes.size();
+}
+
+int gx_eri_plan_graph_replays(const gx_eri_plan* plan) {
+    if (!plan) return gx::set_error(GX_EINVAL, "null plan");
+    return plan->graph_replays;
+}
+
+int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                        void* out_device, gx_class_profile* out) {
+    return guarded([&] {
+        if (!plan || !out) raise(GX_EINVAL, "null plan or profile array");
+        check_field(B, O);
+        check_precision(precision);
+        if (!out_device) raise(GX_EINVAL, "null output pointer");
+        gx_context* ctx = plan->ctx;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        PlanData& pd = plan->data;
+        const size_t nc = pd.classes.size();
+        pd.counters.reserve(std::max<size_t>(2 * nc, 2) * sizeof(unsigned long long));
+        auto* counters = pd.counters.as<unsigned long long>();
+        FieldPairs& fp = field_pairs(plan->basis, B, O);
+        const gx::EriDev dev = make_dev(ctx, plan->basis, fp, static_cast<double2*>(out_device), precision,
+                                        mixed_cutoff);
+        cudaStream_t s = ctx->stream;
+        GX_CUDA(cudaMemsetAsync(counters, 0, std::max<size_t>(2 * nc, 2) * sizeof(unsigned long long), s));
+        ctx->reset_status();
+        const auto& tuned = pd.tuned[precision];
+        const GroupSet& gs = tuned.valid ? tuned.groups : pd.base;
+        std::vector<cudaEvent_t> ev(nc + 1);
+        for (auto& e : ev) GX_CUDA(cudaEventCreate(&e));
+        std::vector<int> b1(nc), wpb(nc);
+        GX_CUDA(cudaEventRecord(ev[0], s));
+        for (size_t ci = 0; ci < nc; ++ci) {
+            launch_class(ctx, dev, pd, ci, tuned.valid ? tuned.conf[ci] : ClassConf{},
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, &b1[ci],
+                         &wpb[ci]);
+            GX_CUDA(cudaEventRecord(ev[ci + 1], s));
+        }
+        GX_CUDA(cudaEventSynchronize(ev[nc]));
+        std::vector<unsigned long long> c(2 * nc);
+        if (nc) GX_CUDA(cudaMemcpy(c.data(), counters, c.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        for (size_t ci = 0; ci < nc; ++ci) {
+            const PlanClass& pc = pd.classes[ci];
+            gx_class_profile& o = out[ci];
+            o.la = pc.key[0];
+            o.lb = pc.key[1];
+            o.lc = pc.key[2];
+            o.ld = pc.key[3];
+            o.tasks = (int64_t)pc.count;
+            o.primitive_quartets = pc.primitive_quartets;
+            o.fp64_quartets = (int64_t)c[2 * ci];
+            o.fp32_quartets = (int64_t)c[2 * ci + 1];
+            o.model_flops_per_quartet = pc.flops_per_primitive_quartet;
+            float ms = 0.0f;
+            GX_CUDA(cudaEventElapsedTime(&ms, ev[ci], ev[ci + 1]));
+            o.ms = ms;
+            o.per_group = tuned.valid ? tuned.conf[ci].per_group : 0;
+            o.warps_per_block = wpb[ci];
+            o.batch = b1[ci];
+            o.groups = (int64_t)gs.range[ci].second;
+        }
+        for (auto& e : ev) cudaEventDestroy(e);
+        check_status(ctx);
+    });
+}
+
+int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                         void* out_device, int repeats, double* default_ms, double* tuned_ms) {
+    return guarded([&] {
+        if (!plan) raise(GX_EINVAL, "null plan");
+        check_field(B, O);
+        check_precision(precision);
+        if (!out_device) raise(GX_EINVAL, "null output pointer");
+        if (repeats < 1 || repeats > 100) raise(GX_EINVAL, "repeats must be in [1, 100]");
+        gx_context* ctx = plan->ctx;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        PlanData& pd = plan->data;
+        const size_t nc = pd.classes.size();
+        FieldPairs& fp = field_pairs(plan->basis, B, O);
+        const gx::EriDev dev = make_dev(ctx, plan->basis, fp, static_cast<double2*>(out_device), precision,
+                                        mixed_cutoff);
+        cudaStream_t s = ctx->stream;
+        ctx->reset_status();
+        cudaEvent_t e0, e1;
+        GX_CUDA(cudaEventCreate(&e0));
+        GX_CUDA(cudaEventCreate(&e1));
+        std::vector<ClassConf> best(nc);
+        double tot_default = 0.0, tot_best = 0.0;
+        DeviceBuffer tmp;
+        for (size_t ci = 0; ci < nc; ++ci) {
+            const auto& k = pd.classes[ci].key;
+            std::vector<ClassConf> cands{ClassConf{}};
+            if (gx::small_class(k[0], k[1], k[2], k[3])) {
+                for (int per : {256, 4096}) cands.push_back(ClassConf{per, 0, 0});
+            } else {
+                for (int per : {16, 32, 64, 128, 256})
+                    for (int w : {2, 4})
+                        for (int b1 : {16, 32})
+                            if (!(per == 32 && w == 4 && b1 == 32)) cands.push_back(ClassConf{per, w, b1});
+            }
+            double best_ms = 0.0, def_ms = 0.0;
+            for (size_t c = 0; c < cands.size(); ++c) {
+                const auto groups = make_groups(ctx, pd, ci, cands[c]);
+                upload(tmp, groups, s);
+                double t = 1e30;
+                for (int r = 0; r <= repeats; ++r) {  // first launch warms caches
+                    GX_CUDA(cudaEventRecord(e0, s));
+                    launch_class(ctx, dev, pd, ci, cands[c], tmp.as<int2>(), (int)groups.size(), nullptr, s);
+                    GX_CUDA(cudaEventRecord(e1, s));
+                    GX_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.0f;
+                    GX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (r > 0) t = std::min(t, (double)ms);
+                }
+                if (c == 0) {
+                    def_ms = best_ms = t;
+                } else if (t < 0.97 * best_ms) {  // keep the default unless clearly faster
+                    best_ms = t;
+                    best[ci] = cands[c];
+                }
+            }
+            tot_default += def_ms;
+            tot_best += best_ms;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        check_status(ctx);
+        auto& tuned = pd.tuned[precision];
+        make_group_set(ctx, pd, best, tuned.groups);
+        tuned.conf = best;
+        tuned.valid = true;
+        GX_CUDA(cudaStreamSynchronize(s));
+        ++plan->generation;
+        plan->graph.reset();
+        if (default_ms) *default_ms = tot_default;
+        if (tuned_ms) *tuned_ms = tot_best;
     });
 }
 

@@ -250,4 +250,63 @@ __device__ __forceinline__ int boys_eval(double x, double y, int L, const BoysTa
     return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// FP32 Boys values for the mixed-precision path, large |T| only: the
+// asymptotic form F_0 = sqrt(pi)/(2 sqrt z), F_{n+1} = F_n (n + 1/2)/z (an
+// upward recurrence) for Re z >= 2L + 24, |Im z| <= Re z / 2.  The dropped
+// tail is e^{-Re z} |z|^{n-1/2}/Gamma(n+1/2) relative, below 5e-8 there for
+// every order.  Small and moderate |T| (the Taylor grid with its downward
+// recursion, the quadrature) stay in FP64: the function returns false and
+// the caller uses boys_eval, which also reports every domain error exactly
+// as without mixed precision.  z itself is formed in FP64 by the caller.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+
+__device__ __forceinline__ bool boys_eval32(double x, double y, int L, float2* Sh) {
+    if (!(x >= 2.0 * L + 24.0 && fabs(y) <= 0.5 * x && (x * x + y * y <= 160.0 * 160.0 || x >= 2.0 * L + 60.0)))
+        return false;
+    const float xf = (float)x, yf = (float)y;
+    const float r2 = fmaf(xf, xf, yf * yf);
+    const float ir = rsqrtf(r2);
+    const float r = r2 * ir;
+    const float s = sqrtf(0.5f * (r + xf));
+    const float t = 0.5f * yf / s;
+    const float k0 = 0.886226925452758f * ir;  // sqrt(pi)/2 / |z|
+    float2 f = make_float2(k0 * s, -k0 * t);
+    const float ir2 = ir * ir;
+    const float2 iz = make_float2(xf * ir2, -yf * ir2);
+    Sh[0] = f;
+    for (int n = 0; n < L; ++n) {
+        f = f2mul(f, iz);
+        f.x *= (float)n + 0.5f;
+        f.y *= (float)n + 0.5f;
+        Sh[n + 1] = f;
+    }
+    return true;
+}
+
+// FP32 seeds C (-2 rho)^n F_n for a primitive quartet whose C = F_ab F_cd /
+// sqrt(p + q) and T = (tre, tim) were formed in FP64.  False (use FP64 Boys)
+// outside the asymptotic sector or when a seed would leave the range in
+// which the FP32 recurrence is safe (|seed| < 1e25, |C| in [1e-30, 1e30]).
+__device__ __forceinline__ bool seeds32(double2 C, double rho, double tre, double tim, int L, float2* S32) {
+    if (!boys_eval32(tre, tim, L, S32)) return false;
+    float2 c = make_float2((float)C.x, (float)C.y);
+    const float mag = fabsf(c.x) + fabsf(c.y);
+    if (!(mag >= 1.0e-30f && mag <= 1.0e30f)) return false;
+    const float m2r = (float)(-2.0 * rho);
+    bool ok = true;
+    for (int n = 0; n <= L; ++n) {
+        S32[n] = f2mul(c, S32[n]);
+        ok = ok && fabsf(S32[n].x) + fabsf(S32[n].y) < 1.0e25f;  // false for NaN too
+        c.x *= m2r;
+        c.y *= m2r;
+    }
+    return ok;
+}
+
 }  // namespace gx

@@ -42,7 +42,23 @@ struct PairData {
     const float2* Epool32; // the same coefficients in FP32 (mixed precision)
     const int* order;      // [npp] records of each shell pair sorted by decreasing bound
     const float* sbound;   // [npp] bound of order[i] (FP32, for gating)
+    const float4* g32;     // [2*npp] (P, p) and (Im P', 0) in FP32, for classifying Boys arguments
 };
+
+// True when the Boys argument T of primitive quartet (ip, iq) lies in the
+// FP32 asymptotic sector of boys_eval32 with a margin, judged from the FP32
+// pair geometry (a misjudged quartet is still exact: seeds32 rechecks T in
+// FP64 and the caller falls back to the FP64 Boys function).
+__device__ __forceinline__ bool boys_asymptotic32(const PairData& pp, int ip, int iq, int L) {
+    const float4 a = pp.g32[2 * ip], b = pp.g32[2 * iq];
+    const float4 ai = pp.g32[2 * ip + 1], bi = pp.g32[2 * iq + 1];
+    const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    const float ex = ai.x - bi.x, ey = ai.y - bi.y, ez = ai.z - bi.z;
+    const float rho = __fdividef(a.w * b.w, a.w + b.w);
+    const float x = rho * (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) - fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
+    const float y = 2.0f * rho * fmaf(dx, ex, fmaf(dy, ey, dz * ez));
+    return x >= 2.0f * L + 25.0f && fabsf(y) <= 0.45f * x && (x * x + y * y <= 150.0f * 150.0f || x >= 2.0f * L + 61.0f);
+}
 
 struct BasisDev {
     int ns;
@@ -60,6 +76,9 @@ struct QuartetClass {
     PairClassDev bra, ket;
     int L, Nab, NL;        // total order, herm_count(Lab), herm_count(L)
     int B1, CH;            // phase-1 batch (primitive quartets), ket-component chunk
+    int nchunk;            // ket chunks per task group, run by separate warps
+    int coop;              // batches of at most this many entries use the warp-cooperative recurrence
+    int KT, CT;            // Hermite rows per lane in the ket transform, ket components per lane in the bra transform
     int ntask;
     const Task* tasks;
     int ngroup;
@@ -75,7 +94,9 @@ struct EriDev {
     double2* out;
     DevStatus* status;
     float skip_cut;   // primitive quartets with bound product below this are skipped
-    float fp32_cut;   // ... below this (and above skip_cut) run in FP32; 0 = FP64 only
+    float fp32_cut;   // ... below this (and above skip_cut) run in FP32; 0 = FP64 only.
+                      // The FP32 quartets use FP32 Boys values in the asymptotic
+                      // sector and FP64 ones elsewhere, then the FP32 recurrence.
     unsigned long long* counters;  // [0] FP64, [1] FP32 primitive quartets evaluated (may be null)
 };
 
@@ -87,7 +108,7 @@ cudaError_t launch_boys_values(const double2* z, long long count, int nmax, int 
 cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
                                    const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
                                    const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
-                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound,
+                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound, float4* g32,
                                    const EriDev* dev_for_bounds, cudaStream_t s);
 size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed);
 cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps_per_block, int grid,
@@ -97,8 +118,7 @@ cudaError_t launch_scatter_full(const double2* packed, const long long* block_of
 
 // register-resident small classes (gx_small.cu)
 bool small_class(int la, int lb, int lc, int ld);
-cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const Task* tasks, int ntask,
-                         cudaStream_t s);
+cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s);
 
 // Cholesky (gx_chol.cu)
 cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const int* info, int nblocks, int n,

@@ -90,6 +90,7 @@ cudaError_t launch_boys_table(double2* S, double2* E0, const GLRules* gl, int* f
     return cudaGetLastError();
 }
 
+
 // ---------------------------------------------------------------------------
 // boys() entry point: one thread per argument.  region follows the
 // reference's dispatch (src/boys.cpp:245-294) for diagnostics.
@@ -181,7 +182,7 @@ __device__ void hermite_1d(int i, int j, double PA, double PB, double inv2p, dou
 __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const int* pp_a, const int* pp_b,
                             const int* pp_pa, const int* pp_pb, const int* pp_class, const PairClassDev* classes,
                             double* out_p, double* out_Pr, double* out_Pi, double2* out_F, const long long* Eoff,
-                            double2* Epool, float2* Epool32, double* out_bound) {
+                            double2* Epool, float2* Epool32, double* out_bound, float4* out_g32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npp) return;
     const int a = pp_a[i], b = pp_b[i];
@@ -227,6 +228,8 @@ __global__ void pair_kernel(BasisDev bs, double3 B, double3 O, int npp, const in
         out_Pi[3 * i + x] = -0.5 * q[x] / p;
     }
     out_F[i] = c2(mag * damp * cs, mag * damp * sn);
+    out_g32[2 * i] = make_float4((float)P[0], (float)P[1], (float)P[2], (float)p);
+    out_g32[2 * i + 1] = make_float4((float)(-0.5 * q[0] / p), (float)(-0.5 * q[1] / p), (float)(-0.5 * q[2] / p), 0.0f);
 
     // complex Hermite coefficients per axis and per component pair
     const PairClassDev pc = classes[pp_class[i]];
@@ -377,12 +380,12 @@ __global__ void pair_bound_kernel(BasisDev bs, EriDev d, int npp, const int* pp_
 cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const double* O, int npp, const int* pp_a,
                                    const int* pp_b, const int* pp_pa, const int* pp_pb, const int* pp_class,
                                    const PairClassDev* classes, double* p, double* Pr, double* Pi, double2* F,
-                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound,
+                                   const long long* Eoff, double2* Epool, float2* Epool32, double* bound, float4* g32,
                                    const EriDev* dev_for_bounds, cudaStream_t s) {
     if (npp <= 0) return cudaSuccess;
     pair_kernel<<<(npp + 63) / 64, 64, 0, s>>>(basis, make_double3(B[0], B[1], B[2]), make_double3(O[0], O[1], O[2]),
                                                npp, pp_a, pp_b, pp_pa, pp_pb, pp_class, classes, p, Pr, Pi, F, Eoff,
-                                               Epool, Epool32, bound);
+                                               Epool, Epool32, bound, g32);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !dev_for_bounds) return e;
     pair_bound_kernel<<<(npp + 63) / 64, 64, 0, s>>>(basis, *dev_for_bounds, npp, pp_a, pp_b, pp_pa, pp_pb, pp_class,
@@ -407,29 +410,42 @@ cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const
 
 __constant__ double c_int[40];  // c_int[k] = k, avoids int->double conversions in inner loops
 
-// Seeds C (-2 rho)^n F_n(T) of primitive quartet (ip, iq) into Sh[0..L];
-// X receives the complex centre separation.  Boys failures are reported
-// through the status word and give zero seeds.
-__device__ __forceinline__ void quartet_seeds_rt(const EriDev& d, int L, int ip, int iq, double2* X, double2* Sh,
-                                                 long long item) {
-    const PairData& pp = d.pairs;
+// FP64 quantities of primitive quartet (ip, iq): the complex centre
+// separation X' = P' - Q', rho = pq / (p + q), the Boys argument
+// T = rho X'.X' and C = F_ab F_cd / sqrt(p + q).
+struct QuartetArgs {
+    double2 X[3], C;
+    double rho, tre, tim;
+};
+__device__ __forceinline__ QuartetArgs quartet_args(const PairData& pp, int ip, int iq) {
+    QuartetArgs a;
     const double p = pp.p[ip], q = pp.p[iq];
-    for (int x = 0; x < 3; ++x) X[x] = c2(pp.Pr[3 * ip + x] - pp.Pr[3 * iq + x], pp.Pi[3 * ip + x] - pp.Pi[3 * iq + x]);
+    for (int x = 0; x < 3; ++x)
+        a.X[x] = c2(pp.Pr[3 * ip + x] - pp.Pr[3 * iq + x], pp.Pi[3 * ip + x] - pp.Pi[3 * iq + x]);
     const double r = rsqrt(p + q);
-    const double rho = p * q * r * r;
-    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
-                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
-    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+    a.rho = p * q * r * r;
+    const double2* X = a.X;
+    a.tre = a.rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
+                     fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
+    a.tim = 2.0 * a.rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+    a.C = cscale(cmul(pp.F[ip], pp.F[iq]), r);
+    return a;
+}
+
+// FP64 seeds C (-2 rho)^n F_n(T) into Sh[0..L].  Boys failures are reported
+// through the status word and give zero seeds.
+__device__ __forceinline__ void quartet_seeds_rt(const EriDev& d, int L, const QuartetArgs& a, double2* Sh,
+                                                 long long item) {
     double2 e0;
-    double2 C = cscale(cmul(pp.F[ip], pp.F[iq]), r);
-    if (const int rc = boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
-        report(d.status, rc, item, L, tre, tim);
+    double2 C = a.C;
+    if (const int rc = boys_eval(a.tre, a.tim, L, d.boys, d.gl, Sh, e0)) {
+        report(d.status, rc, item, L, a.tre, a.tim);
         C = c2(0.0, 0.0);
         e0 = c2(0.0, 0.0);
         for (int n = 0; n <= L; ++n) Sh[n] = c2(0.0, 0.0);
     }
     C = cmul(C, e0);
-    const double m2r = -2.0 * rho;
+    const double m2r = -2.0 * a.rho;
     for (int n = 0; n <= L; ++n) {
         Sh[n] = cmul(C, Sh[n]);
         C = cscale(C, m2r);
@@ -490,11 +506,11 @@ __device__ __forceinline__ void hermite_rec(int L, const T* seed, const T* X, T*
     }
 }
 
-constexpr double FP32_SEED_LIMIT = 1.0e25;
-
-// Per-warp shared layout of quartet_kernel (all offsets in bytes).
+// Per-warp shared layout of quartet_kernel (all offsets in bytes).  R holds
+// B1 + 1 columns (the last one is the cooperative recurrence's second
+// buffer); `seed` holds one entry's seeds and X' for the cooperative path.
 struct WarpSmem {
-    size_t R, W, R32, W32, queue, flag, total;
+    size_t R, W, R32, W32, queue, flag, eoff, seed, total;
 };
 __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed) {
     WarpSmem w;
@@ -505,68 +521,293 @@ __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, b
     w.W32 = w.R32 + (mixed ? (((size_t)NL * B1p * 8 + 15) / 16) * 16 : 0);
     w.queue = w.W32 + (mixed ? (((size_t)Nab * CH * 8 + 15) / 16) * 16 : 0);
     w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
-    w.total = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
+    w.eoff = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
+    w.seed = w.eoff + (((size_t)B1 * 8 + 15) / 16) * 16;
+    w.total = w.seed + (size_t)(BOYS_MAX_ORDER + 1 + 3) * 16;
     return w;
 }
 
-// Ket transform of batch entry j into W (FP64) or W32 (FP32).
-template <typename T, typename E>
-__device__ __forceinline__ void step_k(const QuartetClass& qc, const uint32_t* herm_xyz, const E* Ek, const T* R,
-                                       int B1p, int j, T* W, int c0, int chn, int lane) {
-    for (int it = lane; it < qc.Nab * chn; it += 32) {
-        const int K = it / chn, cdl = it - K * chn, cd = c0 + cdl;
-        const uint32_t kx = __ldg(&herm_xyz[K]);
-        const int bk = kx & 255, bl = (kx >> 8) & 255, bm = (kx >> 16) & 255;
-        const int bo = qc.ket.boxoff[cd];
-        const int bd = qc.ket.boxdim[cd];
-        const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-        T acc = W[K * qc.CH + cdl];
-        for (int e = 0; e < nbox; ++e) {
-            const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
-            const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
-            E ev = __ldg(&Ek[bo + e]);
-            if ((k2 + l2 + m2) & 1) {
-                ev.x = -ev.x;
-                ev.y = -ev.y;
+// Warp-cooperative Hermite recurrence of one primitive quartet: level n
+// (entries of total degree <= L - n) from level n + 1, all entries of a
+// level in parallel across the lanes, ping-ponging between columns j and s
+// of the shared table so that level 0 ends in column j.
+template <typename T>
+__device__ __forceinline__ void coop_rec(int L, const T* seed, const T* X, T* R, int B1p, int j, int s,
+                                         const uint32_t* herm_xyz, int lane) {
+    int cur = (L % 2 == 0) ? j : s;
+    if (lane == 0) R[cur] = seed[L];
+    __syncwarp();
+    for (int n = L - 1; n >= 0; --n) {
+        const int nxt = cur == j ? s : j;
+        const int cnt = herm_count(L - n);
+        for (int e = lane; e < cnt; e += 32) {
+            T v;
+            if (e == 0) {
+                v = seed[n];
+            } else {
+                const uint32_t kx = __ldg(&herm_xyz[e]);
+                const int k = kx & 255, l = (kx >> 8) & 255, m = (kx >> 16) & 255;
+                int axis, pw, i1, i2;
+                if (k > 0) {
+                    axis = 0;
+                    pw = k;
+                    i1 = herm_index(k - 1, l, m);
+                    i2 = k > 1 ? herm_index(k - 2, l, m) : 0;
+                } else if (l > 0) {
+                    axis = 1;
+                    pw = l;
+                    i1 = herm_index(0, l - 1, m);
+                    i2 = l > 1 ? herm_index(0, l - 2, m) : 0;
+                } else {
+                    axis = 2;
+                    pw = m;
+                    i1 = herm_index(0, 0, m - 1);
+                    i2 = m > 1 ? herm_index(0, 0, m - 2) : 0;
+                }
+                v = tmul(X[axis], R[i1 * B1p + cur]);
+                if (pw > 1) v = tmacr(v, pw - 1, R[i2 * B1p + cur]);
             }
-            T evt;
-            evt.x = ev.x;
-            evt.y = ev.y;
-            acc = tmac(acc, evt, R[herm_index(bk + k2, bl + l2, bm + m2) * B1p + j]);
+            R[e * B1p + nxt] = v;
         }
-        W[K * qc.CH + cdl] = acc;
+        __syncwarp();
+        cur = nxt;
     }
 }
 
-// Bra transform of W (FP64) and W32 (FP32) into the task's output block.
+// Work split of a transform with `items` work items: J lanes share an item
+// (the largest power of two with items * J <= 32; 1 when items >= 16), so
+// that small classes still fill the warp.  Groups of J lanes are aligned.
+__device__ __forceinline__ int lanes_per_item(int items) {
+    int J = 1;
+    while (J < 32 && items * J * 2 <= 32) J *= 2;
+    return J;
+}
+__device__ __forceinline__ double2 group_sum(double2 v, int J) {
+    for (int off = J >> 1; off > 0; off >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    }
+    return v;
+}
+__device__ __forceinline__ float2 group_sum(float2 v, int J) {
+    for (int off = J >> 1; off > 0; off >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    }
+    return v;
+}
+
+// Ket transform of the batch entries j0..j1-1 (one run with the same bra
+// pair) into W (FP64 entries) and W32 (FP32 entries):
+//   W[K][cd] += sum_j sum_{K' in box(cd)} (-1)^{|K'|} E~cd_j[K'] Rh_j[K + K'].
+// A work item is KT consecutive Hermite rows K of one ket component cd (KT
+// independent accumulators); its (entry, box entry) terms are split over the
+// item's J lanes and summed by a butterfly.  eoff[j]: E~ record of the
+// entry's ket pair; flag[j]: 0 FP32, else FP64.
+template <int KT>
+__device__ __forceinline__ void step_k_run(const QuartetClass& qc, const uint32_t* herm_xyz, const PairData& pp,
+                                           const double2* R, const float2* R32, int B1p, const int* flag,
+                                           const long long* eoff, int j0, int j1, bool has64, bool has32,
+                                           double2* W, float2* W32, int c0, int chn, int lane) {
+    const int nkb = (qc.Nab + KT - 1) / KT;
+    const int I = nkb * chn;
+    const int J = lanes_per_item(I);
+    const int rounds = (I * J + 31) / 32;
+    for (int rd = 0; rd < rounds; ++rd) {
+        const int slot = rd * 32 + lane;
+        const int it = slot / J, sub = slot - it * J;
+        const bool act = it < I;
+        double2 a64[KT];
+        float2 a32[KT];
+#pragma unroll
+        for (int u = 0; u < KT; ++u) {
+            a64[u] = c2(0.0, 0.0);
+            a32[u] = make_float2(0.0f, 0.0f);
+        }
+        int kb = 0, cdl = 0;
+        if (act) {
+            kb = it / chn;
+            cdl = it - kb * chn;
+            const int cd = c0 + cdl;
+            int bk[KT], bl[KT], bm[KT];
+#pragma unroll
+            for (int u = 0; u < KT; ++u) {
+                const int K = kb * KT + u;
+                const uint32_t kx = __ldg(&herm_xyz[K < qc.Nab ? K : 0]);
+                bk[u] = kx & 255;
+                bl[u] = (kx >> 8) & 255;
+                bm[u] = (kx >> 16) & 255;
+            }
+            const int bo = qc.ket.boxoff[cd];
+            const int bd = qc.ket.boxdim[cd];
+            const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+            const int tot = (j1 - j0) * nbox;
+            for (int t = sub; t < tot; t += J) {
+                const int jr = t / nbox;
+                const int e = t - jr * nbox;
+                const int jj = j0 + jr;
+                const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
+                const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
+                const bool neg = (k2 + l2 + m2) & 1;
+                if (flag[jj]) {
+                    double2 ev = __ldg(&pp.Epool[eoff[jj] + bo + e]);
+                    if (neg) ev = c2(-ev.x, -ev.y);
+#pragma unroll
+                    for (int u = 0; u < KT; ++u)
+                        a64[u] = cmac(a64[u], ev, R[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                } else {
+                    float2 ev = __ldg(&pp.Epool32[eoff[jj] + bo + e]);
+                    if (neg) ev = make_float2(-ev.x, -ev.y);
+#pragma unroll
+                    for (int u = 0; u < KT; ++u)
+                        a32[u] = tmac(a32[u], ev, R32[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                }
+            }
+        }
+        if (J > 1) {
+#pragma unroll
+            for (int u = 0; u < KT; ++u) {
+                if (has64) a64[u] = group_sum(a64[u], J);
+                if (has32) a32[u] = group_sum(a32[u], J);
+            }
+        }
+        if (act && sub == 0) {
+#pragma unroll
+            for (int u = 0; u < KT; ++u) {
+                const int K = kb * KT + u;
+                if (K < qc.Nab) {
+                    if (has64) W[K * qc.CH + cdl] = cadd(W[K * qc.CH + cdl], a64[u]);
+                    if (has32) {
+                        float2& w = W32[K * qc.CH + cdl];
+                        w.x += a32[u].x;
+                        w.y += a32[u].y;
+                    }
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void step_k_any(const QuartetClass& qc, const uint32_t* herm_xyz, const PairData& pp,
+                                           const double2* R, const float2* R32, int B1p, const int* flag,
+                                           const long long* eoff, int j0, int j1, bool has64, bool has32,
+                                           double2* W, float2* W32, int c0, int chn, int lane) {
+    if (qc.KT == 4)
+        step_k_run<4>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+    else if (qc.KT == 2)
+        step_k_run<2>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+    else
+        step_k_run<1>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+}
+
+// Bra transform of W (FP64) and W32 (FP32) into the task's output block:
+//   out[ab][cd] += sum_{K in box(ab)} E~ab[K] W[K][cd].
+// A work item is CT consecutive ket components of one bra component ab (the
+// chunk length is a multiple of CT); its box entries are split over the
+// item's J lanes.  FP32 partial sums are added in FP64.
+template <int CT>
 __device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, const Task& tg, int ip, double2* W,
-                                       float2* W32, bool use32, int c0, int chn, int lane) {
+                                       float2* W32, bool use64, bool use32, int c0, int chn, int lane) {
     const int nab = qc.bra.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const double2* Ea = d.pairs.Epool + d.pairs.Eoff[ip];
     const float2* Ea32 = d.pairs.Epool32 + d.pairs.Eoff[ip];
-    for (int it = lane; it < nab * chn; it += 32) {
-        const int ab = it / chn, cdl = it - ab * chn, cd = c0 + cdl;
-        const int bo = qc.bra.boxoff[ab];
-        const int bd = qc.bra.boxdim[ab];
-        const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-        double2 acc = c2(0.0, 0.0);
-        float2 acc32 = make_float2(0.0f, 0.0f);
-        for (int e = 0; e < nbox; ++e) {
-            const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
-            const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
-            acc = cmac(acc, __ldg(&Ea[bo + e]), W[K * qc.CH + cdl]);
-            if (use32) acc32 = tmac(acc32, __ldg(&Ea32[bo + e]), W32[K * qc.CH + cdl]);
+    const int nct = chn / CT;
+    const int I = nab * nct;
+    const int J = lanes_per_item(I);
+    const int rounds = (I * J + 31) / 32;
+    for (int rd = 0; rd < rounds; ++rd) {
+        const int slot = rd * 32 + lane;
+        const int it = slot / J, sub = slot - it * J;
+        const bool act = it < I;
+        double2 acc[CT];
+        float2 acc32[CT];
+#pragma unroll
+        for (int u = 0; u < CT; ++u) {
+            acc[u] = c2(0.0, 0.0);
+            acc32[u] = make_float2(0.0f, 0.0f);
         }
-        if (use32) acc = cadd(acc, c2((double)acc32.x, (double)acc32.y));  // FP64 final summation
-        const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
-        double2* o = d.out + tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1] +
-                     (long long)cc * tg.st[2] + (long long)cdd * tg.st[3];
-        *o = cadd(*o, acc);
+        int ab = 0, cdl0 = 0;
+        if (act) {
+            ab = it / nct;
+            cdl0 = (it - ab * nct) * CT;
+            const int bo = qc.bra.boxoff[ab];
+            const int bd = qc.bra.boxdim[ab];
+            const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+            if (use32) {
+                for (int e = sub; e < nbox; e += J) {
+                    const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
+                    const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+                    const float2 ea32 = __ldg(&Ea32[bo + e]);
+#pragma unroll
+                    for (int u = 0; u < CT; ++u) acc32[u] = tmac(acc32[u], ea32, W32[K * qc.CH + cdl0 + u]);
+                }
+            }
+            if (use64) {
+                for (int e = sub; e < nbox; e += J) {
+                    const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
+                    const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+                    const double2 ea = __ldg(&Ea[bo + e]);
+#pragma unroll
+                    for (int u = 0; u < CT; ++u) acc[u] = cmac(acc[u], ea, W[K * qc.CH + cdl0 + u]);
+                }
+            }
+        }
+        if (J > 1) {
+#pragma unroll
+            for (int u = 0; u < CT; ++u) {
+                if (use64) acc[u] = group_sum(acc[u], J);
+                if (use32) acc32[u] = group_sum(acc32[u], J);
+            }
+        }
+        if (act && sub == 0) {
+            const int ca = ab / ncb, cb = ab - ca * ncb;
+            double2* ob = d.out + tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1];
+#pragma unroll
+            for (int u = 0; u < CT; ++u) {
+                const int cd = c0 + cdl0 + u;
+                const int cc = cd / ncdd, cdd = cd - cc * ncdd;
+                const double2 a = use32 ? cadd(acc[u], c2((double)acc32[u].x, (double)acc32[u].y)) : acc[u];
+                double2* o = ob + (long long)cc * tg.st[2] + (long long)cdd * tg.st[3];
+                *o = cadd(*o, a);
+            }
+        }
     }
 }
 
-__global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc) {
+__device__ __forceinline__ void step_b_any(const EriDev& d, const QuartetClass& qc, const Task& tg, int ip,
+                                           double2* W, float2* W32, bool use64, bool use32, int c0, int chn,
+                                           int lane) {
+    switch (qc.CT) {
+        case 4: step_b<4>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
+        case 3: step_b<3>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
+        case 2: step_b<2>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
+        default: step_b<1>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
+    }
+}
+
+// Seeds of primitive quartet (ip, iq) for pass `pass`: returns 1 (FP64 seeds
+// in Sh), 0 (FP32 seeds in S32) or 2 (FP32 pass falling back to FP64, seeds
+// in Sh).  Pass 0 is FP64; in pass 1 (FP32 quartets) the Boys function runs
+// in FP32 in its asymptotic sector and in FP64 elsewhere, and the seeds go to
+// the FP32 recurrence when they fit its range.
+__device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int pass, const QuartetArgs& qa, double2* Sh,
+                                           float2* S32, long long item) {
+    if (pass == 0) {
+        quartet_seeds_rt(d, L, qa, Sh, item);
+        return 1;
+    }
+    if (pass == 1 && seeds32(qa.C, qa.rho, qa.tre, qa.tim, L, S32)) return 0;
+    quartet_seeds_rt(d, L, qa, Sh, item);
+    bool ok = true;
+    for (int n = 0; n <= L; ++n) {
+        ok = ok && fabs(Sh[n].x) + fabs(Sh[n].y) < 1.0e25;
+        S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
+    }
+    return ok ? 0 : 2;
+}
+
+__global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass qc) {
     extern __shared__ double2 sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -581,19 +822,30 @@ __global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc)
     float2* W32 = reinterpret_cast<float2*>(base + lay.W32);
     int* queue = reinterpret_cast<int*>(base + lay.queue);
     int* flag = reinterpret_cast<int*>(base + lay.flag);
+    long long* eoff = reinterpret_cast<long long*>(base + lay.eoff);  // E~ record of each entry's ket pair
+    double2* sseed = reinterpret_cast<double2*>(base + lay.seed);  // [L+1] seeds, then X'[3]
     const int nab = qc.bra.nab, ncd = qc.ket.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const int ns = d.basis.ns;
     const PairData& pp = d.pairs;
     const float cut64 = fmaxf(cut32, skip);
+    // Mixed precision: pass 0 evaluates the FP64 quartets, pass 1 the FP32
+    // ones (FP32 Boys in the asymptotic sector, FP64 Boys elsewhere), so that
+    // both passes fill their batches densely.
     const int npass = cut32 > 0.0f ? 2 : 1;
     unsigned long long cnt64 = 0, cnt32 = 0;
-    // A warp takes a group of tasks with equal primitive counts and walks
-    // their primitive quartets as one stream (task g, bra pair P, ket pair Q;
-    // pairs in decreasing Schwarz order).  Each pass compacts the entries of
-    // its precision into batches of B1 with a ballot, so screened or
+    // A warp takes one work unit: a group of tasks with equal primitive
+    // counts and one chunk of ket components (chunks of a group run on
+    // different warps and write disjoint output entries).  It walks the
+    // group's primitive quartets as one stream (task g, bra pair P, ket pair
+    // Q; pairs in decreasing Schwarz order); each pass compacts the entries
+    // of its precision into batches of up to B1 with a ballot, so screened or
     // other-precision entries cost no FP64 issue slots.
-    for (int grp = blockIdx.x * wpb + wib; grp < qc.ngroup; grp += gridDim.x * wpb) {
+    const int nunit = qc.ngroup * qc.nchunk;
+    for (int unit = blockIdx.x * wpb + wib; unit < nunit; unit += gridDim.x * wpb) {
+        const int grp = unit / qc.nchunk;
+        const int c0 = (unit - grp * qc.nchunk) * qc.CH;
+        const int chn = min(qc.CH, ncd - c0);
         const int2 gi = qc.groups[grp];
         const Task t0 = qc.tasks[gi.x];
         const int Kab = d.basis.nprim[t0.sa] * d.basis.nprim[t0.sb];
@@ -602,8 +854,8 @@ __global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc)
         const int S = gi.y * KK;
         for (int g = 0; g < gi.y; ++g) {
             const Task tg = qc.tasks[gi.x + g];
-            for (int it = lane; it < nab * ncd; it += 32) {
-                const int ab = it / ncd, cd = it - ab * ncd;
+            for (int it = lane; it < nab * chn; it += 32) {
+                const int ab = it / chn, cd = c0 + (it - ab * chn);
                 const int ca = ab / ncb, cb = ab - ca * ncb, cc = cd / ncdd, cdd = cd - cc * ncdd;
                 d.out[tg.out_off + (long long)ca * tg.st[0] + (long long)cb * tg.st[1] + (long long)cc * tg.st[2] +
                       (long long)cdd * tg.st[3]] = c2(0.0, 0.0);
@@ -611,114 +863,148 @@ __global__ void __launch_bounds__(128) quartet_kernel(EriDev d, QuartetClass qc)
         }
         __syncwarp();
         for (int pass = 0; pass < npass; ++pass) {
-            for (int c0 = 0; c0 < ncd; c0 += qc.CH) {
-                const int chn = min(qc.CH, ncd - c0);
-                for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
-                    W[it] = c2(0.0, 0.0);
-                    if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
+            for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
+                W[it] = c2(0.0, 0.0);
+                if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
+            }
+            int cur = -1;  // g * Kab + P of the accumulating bra pair
+            bool any64 = false, any32 = false;  // precisions accumulated into W / W32 for `cur`
+            int cursor = 0;
+            while (cursor < S) {
+                // assemble up to B1 entries of this pass
+                int nb = 0;
+                __syncwarp();
+                while (nb < qc.B1 && cursor < S) {
+                    const int idx = cursor + lane;
+                    bool valid = false;
+                    if (idx < S) {
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
+                        const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
+                        const float b = pp.sbound[op] * pp.sbound[oq];
+                        valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, valid);
+                    const int cnt = __popc(mask);
+                    const int take = min(cnt, qc.B1 - nb);
+                    const int rank = __popc(mask & ((1u << lane) - 1u));
+                    if (valid && rank < take) queue[nb + rank] = idx;
+                    if (take < cnt) {
+                        const unsigned m2 = __ballot_sync(0xffffffffu, valid && rank == take);
+                        cursor += __ffs(m2) - 1;
+                    } else {
+                        cursor += 32;
+                    }
+                    nb += take;
                 }
-                int cur = -1;  // g * Kab + P of the accumulating bra pair
-                int cursor = 0;
-                while (cursor < S) {
-                    // assemble up to B1 entries of this pass
-                    int nb = 0;
-                    __syncwarp();
-                    while (nb < qc.B1 && cursor < S) {
-                        const int idx = cursor + lane;
-                        bool valid = false;
-                        if (idx < S) {
+                __syncwarp();
+                if (nb == 0) break;
+                if (nb <= qc.coop) {
+                    // few entries: one lane forms the seeds, the warp runs the
+                    // recurrence level-parallel
+                    for (int j = 0; j < nb; ++j) {
+                        if (lane == 0) {
+                            const int idx = queue[j];
                             const int g = idx / KK, r = idx - g * KK;
                             const int P = r / Kcd, Q = r - P * Kcd;
                             const Task tg = qc.tasks[gi.x + g];
-                            const float b = pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
-                                            pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
-                            valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
-                        }
-                        const unsigned mask = __ballot_sync(0xffffffffu, valid);
-                        const int cnt = __popc(mask);
-                        const int take = min(cnt, qc.B1 - nb);
-                        const int rank = __popc(mask & ((1u << lane) - 1u));
-                        if (valid && rank < take) queue[nb + rank] = idx;
-                        if (take < cnt) {
-                            const unsigned m2 = __ballot_sync(0xffffffffu, valid && rank == take);
-                            cursor += __ffs(m2) - 1;
-                        } else {
-                            cursor += 32;
-                        }
-                        nb += take;
-                    }
-                    __syncwarp();
-                    if (nb == 0) break;
-                    if (lane < nb) {
-                        const int idx = queue[lane];
-                        const int g = idx / KK, r = idx - g * KK;
-                        const int P = r / Kcd, Q = r - P * Kcd;
-                        const Task tg = qc.tasks[gi.x + g];
-                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
-                        double2 X[3], Sh[BOYS_MAX_ORDER + 1];
-                        quartet_seeds_rt(d, qc.L, ip, iq, X, Sh, gi.x + g);
-                        int f = 1;
-                        if (pass == 1) {
-                            double big = 0.0;
-                            for (int n = 0; n <= qc.L; ++n) big = fmax(big, fabs(Sh[n].x) + fabs(Sh[n].y));
-                            f = big < FP32_SEED_LIMIT ? 0 : 1;
-                        }
-                        if (f) {
-                            hermite_rec<double2>(qc.L, Sh, X, R + lane, B1p);
-                            ++cnt64;
-                        } else {
+                            const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                            const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                            const QuartetArgs qa = quartet_args(pp, ip, iq);
+                            double2 Sh[BOYS_MAX_ORDER + 1];
                             float2 S32[BOYS_MAX_ORDER + 1];
-                            for (int n = 0; n <= qc.L; ++n) S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
-                            const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
-                                                   make_float2((float)X[1].x, (float)X[1].y),
-                                                   make_float2((float)X[2].x, (float)X[2].y)};
-                            hermite_rec<float2>(qc.L, S32, X32, R32 + lane, B1p);
-                            ++cnt32;
-                        }
-                        flag[lane] = f;
-                    }
-                    __syncwarp();
-                    for (int j = 0; j < nb; ++j) {
-                        const int idx = queue[j];
-                        const int g = idx / KK, r = idx - g * KK;
-                        const int P = r / Kcd, Q = r - P * Kcd;
-                        const int key = g * Kab + P;
-                        if (key != cur) {
-                            if (cur >= 0) {
-                                __syncwarp();
-                                const int cg = cur / Kab, cP = cur - cg * Kab;
-                                const Task tc = qc.tasks[gi.x + cg];
-                                step_b(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, pass == 1,
-                                       c0, chn, lane);
-                                __syncwarp();
-                                for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
-                                    W[it] = c2(0.0, 0.0);
-                                    if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
-                                }
-                                __syncwarp();
+                            const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
+                            if (f) {
+                                for (int n = 0; n <= qc.L; ++n) sseed[n] = Sh[n];
+                                for (int x = 0; x < 3; ++x) sseed[qc.L + 1 + x] = qa.X[x];
+                                ++cnt64;
+                            } else {
+                                float2* s32 = reinterpret_cast<float2*>(sseed);
+                                for (int n = 0; n <= qc.L; ++n) s32[n] = S32[n];
+                                for (int x = 0; x < 3; ++x)
+                                    s32[qc.L + 1 + x] = make_float2((float)qa.X[x].x, (float)qa.X[x].y);
+                                ++cnt32;
                             }
-                            cur = key;
+                            flag[j] = f;
+                            eoff[j] = pp.Eoff[iq];
                         }
-                        const Task tg = qc.tasks[gi.x + g];
-                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
-                        if (flag[j])
-                            step_k<double2, double2>(qc, d.herm_xyz, pp.Epool + pp.Eoff[iq], R, B1p, j, W, c0, chn,
-                                                     lane);
-                        else
-                            step_k<float2, float2>(qc, d.herm_xyz, pp.Epool32 + pp.Eoff[iq], R32, B1p, j, W32, c0,
-                                                   chn, lane);
+                        __syncwarp();
+                        if (flag[j]) {
+                            coop_rec<double2>(qc.L, sseed, sseed + qc.L + 1, R, B1p, j, qc.B1, d.herm_xyz, lane);
+                        } else {
+                            const float2* s32 = reinterpret_cast<const float2*>(sseed);
+                            coop_rec<float2>(qc.L, s32, s32 + qc.L + 1, R32, B1p, j, qc.B1, d.herm_xyz, lane);
+                        }
                     }
-                }
-                if (cur >= 0) {
-                    __syncwarp();
-                    const int cg = cur / Kab, cP = cur - cg * Kab;
-                    const Task tc = qc.tasks[gi.x + cg];
-                    step_b(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, pass == 1, c0, chn,
-                           lane);
+                } else if (lane < nb) {
+                    const int idx = queue[lane];
+                    const int g = idx / KK, r = idx - g * KK;
+                    const int P = r / Kcd, Q = r - P * Kcd;
+                    const Task tg = qc.tasks[gi.x + g];
+                    const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                    const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                    const QuartetArgs qa = quartet_args(pp, ip, iq);
+                    double2 Sh[BOYS_MAX_ORDER + 1];
+                    float2 S32[BOYS_MAX_ORDER + 1];
+                    const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
+                    if (f) {
+                        hermite_rec<double2>(qc.L, Sh, qa.X, R + lane, B1p);
+                        ++cnt64;
+                    } else {
+                        const float2 X32[3] = {make_float2((float)qa.X[0].x, (float)qa.X[0].y),
+                                               make_float2((float)qa.X[1].x, (float)qa.X[1].y),
+                                               make_float2((float)qa.X[2].x, (float)qa.X[2].y)};
+                        hermite_rec<float2>(qc.L, S32, X32, R32 + lane, B1p);
+                        ++cnt32;
+                    }
+                    flag[lane] = f;
+                    eoff[lane] = pp.Eoff[iq];
                 }
                 __syncwarp();
+                // phase 2: runs of entries with the same bra pair
+                for (int j0 = 0; j0 < nb;) {
+                    const int key = queue[j0] / Kcd;  // g * Kab + P
+                    int j1 = j0 + 1;
+                    while (j1 < nb && queue[j1] / Kcd == key) ++j1;
+                    if (key != cur) {
+                        if (cur >= 0) {
+                            __syncwarp();
+                            const int cg = cur / Kab, cP = cur - cg * Kab;
+                            const Task tc = qc.tasks[gi.x + cg];
+                            step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64,
+                                       any32, c0, chn, lane);
+                            __syncwarp();
+                            for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
+                                if (any64) W[it] = c2(0.0, 0.0);
+                                if (any32) W32[it] = make_float2(0.0f, 0.0f);
+                            }
+                            __syncwarp();
+                        }
+                        cur = key;
+                        any64 = any32 = false;
+                    }
+                    bool has64 = false, has32 = false;
+                    for (int jj = j0; jj < j1; ++jj) {
+                        has64 = has64 || flag[jj] != 0;
+                        has32 = has32 || flag[jj] == 0;
+                    }
+                    step_k_any(qc, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn,
+                               lane);
+                    any64 = any64 || has64;
+                    any32 = any32 || has32;
+                    j0 = j1;
+                }
             }
+            if (cur >= 0) {
+                __syncwarp();
+                const int cg = cur / Kab, cP = cur - cg * Kab;
+                const Task tc = qc.tasks[gi.x + cg];
+                step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64, any32, c0,
+                           chn, lane);
+            }
+            __syncwarp();
         }
     }
     if (d.counters) {

@@ -6,22 +6,21 @@ namespace gx {
 
 namespace {
 template <int A, int B, int C, int D>
-cudaError_t go(const EriDev& d, const Task* tasks, int ntask, cudaStream_t s) {
-    const int threads = 128;
-    small::small_kernel<A, B, C, D><<<(ntask + threads - 1) / threads, threads, 0, s>>>(d, tasks, ntask);
+cudaError_t go(const EriDev& d, const QuartetClass& qc, cudaStream_t s) {
+    // one warp per task group, four warps per block
+    small::small_kernel<A, B, C, D><<<(qc.ngroup + 3) / 4, 128, 0, s>>>(d, qc);
     return cudaGetLastError();
 }
 }  // namespace
 
 bool small_class(int la, int lb, int lc, int ld) { return la + lb + lc + ld <= 2; }
 
-cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const Task* tasks, int ntask,
-                         cudaStream_t s) {
-    if (ntask <= 0) return cudaSuccess;
+cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s) {
+    if (qc.ntask <= 0 || qc.ngroup <= 0) return cudaSuccess;
     const int key = ((la * 3 + lb) * 3 + lc) * 3 + ld;
     switch (key) {
 #define GX_CASE(A, B, C, D) \
-    case ((A * 3 + B) * 3 + C) * 3 + D: return go<A, B, C, D>(d, tasks, ntask, s);
+    case ((A * 3 + B) * 3 + C) * 3 + D: return go<A, B, C, D>(d, qc, s);
         GX_CASE(0, 0, 0, 0)
         GX_CASE(1, 0, 0, 0)
         GX_CASE(0, 1, 0, 0)

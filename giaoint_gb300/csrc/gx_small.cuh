@@ -1,13 +1,16 @@
 // Register-resident kernel for the small quartet classes (L = la+lb+lc+ld <= 2).
 //
-// One lane evaluates one whole shell quartet: every primitive quartet's
-// Boys values, Hermite table Rh, ket transform W[K][cd] (accumulated over the
-// ket primitive pairs) and bra transform into out[ab][cd], all in registers.
-// Lanes of a warp run quartets with equal primitive counts (tasks are sorted
-// by (Kab, Kcd) within a class), so no lane idles and no FP64 instruction is
-// issued for a masked-off lane.  Every loop is expanded at compile time from
-// constexpr plans (index-sequence folds), so all register indices are
-// constants.
+// One lane evaluates one primitive quartet completely: Boys values, Hermite
+// table Rh, ket transform W[K][cd] and bra transform into its contribution
+// v[ab][cd], all in registers.  A warp walks the primitive quartets of a
+// group of shell quartets with equal primitive counts as one stream and
+// compacts the ones that survive screening (and belong to the current
+// precision pass) into full batches of 32 with a ballot, so screening removes
+// issue slots instead of idling lanes.  Lanes of a batch that belong to the
+// same shell quartet are summed by a segmented warp reduction and the first
+// lane of each segment adds the sum to the output block.  Every loop is
+// expanded at compile time from constexpr plans (index-sequence folds), so
+// all register indices are constants.
 #pragma once
 
 #include <utility>
@@ -232,20 +235,14 @@ __device__ __forceinline__ void run_b(double2* out, const double2* W, const doub
         ...);
 }
 
-// Seeds C (-2 rho)^n F_n for one primitive quartet; returns false (and zero
-// seeds) on a Boys failure, which is reported through the status word.
+// Seeds C (-2 rho)^n F_n for one primitive quartet; zero seeds on a Boys
+// failure, which is reported through the status word.
 template <int L>
-__device__ __forceinline__ void quartet_seeds(const EriDev& d, int tk, double p, double q, const double2* X,
-                                              double2 Fab, double2 Fcd, double2* Sh) {
-    const double r = rsqrt(p + q);
-    const double rho = p * q * r * r;
-    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
-                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
-    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+__device__ __forceinline__ void quartet_seeds(const EriDev& d, long long item, double2 C, double rho, double tre,
+                                              double tim, double2* Sh) {
     double2 e0;
-    double2 C = cscale(cmul(Fab, Fcd), r);
     if (const int rc = boys_eval(tre, tim, L, d.boys, d.gl, Sh, e0)) {
-        report(d.status, rc, tk, L, tre, tim);
+        report(d.status, rc, item, L, tre, tim);
         C = c2(0.0, 0.0);
         e0 = c2(0.0, 0.0);
     }
@@ -258,135 +255,219 @@ __device__ __forceinline__ void quartet_seeds(const EriDev& d, int tk, double p,
     }
 }
 
-// FP32 values are safe when every seed is far inside the float range
-// (the recurrence grows entries by at most |X'| + L per level).
-constexpr double FP32_SEED_LIMIT = 1.0e25;
+// Segmented sum over lanes with equal key (keys non-decreasing along the
+// warp): afterwards the first lane of each run holds the run's total.
+template <int N>
+__device__ __forceinline__ void seg_sum(double2* v, int key, int lane) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int ko = __shfl_down_sync(0xffffffffu, key, off);
+        const bool take = lane + off < 32 && ko == key;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const double ox = __shfl_down_sync(0xffffffffu, v[i].x, off);
+            const double oy = __shfl_down_sync(0xffffffffu, v[i].y, off);
+            if (take) v[i] = c2(v[i].x + ox, v[i].y + oy);
+        }
+    }
+}
+template <int N>
+__device__ __forceinline__ void seg_sum(float2* v, int key, int lane) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int ko = __shfl_down_sync(0xffffffffu, key, off);
+        const bool take = lane + off < 32 && ko == key;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float ox = __shfl_down_sync(0xffffffffu, v[i].x, off);
+            const float oy = __shfl_down_sync(0xffffffffu, v[i].y, off);
+            if (take) v[i] = make_float2(v[i].x + ox, v[i].y + oy);
+        }
+    }
+}
 
 template <int LA, int LB, int LC, int LD>
-__global__ void __launch_bounds__(128) small_kernel(EriDev d, const Task* tasks, int ntask) {
+__global__ void __launch_bounds__(128) small_kernel(EriDev d, QuartetClass qc) {
     constexpr int L = LA + LB + LC + LD;
     constexpr int NL = hc(L), NH = hc(LA + LB);
-    constexpr int NAB = nc(LA) * nc(LB), NCD = nc(LC) * nc(LD);
-    const int tk = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tk >= ntask) return;
-    const Task t = tasks[tk];
-    const int ns = d.basis.ns;
-    const int Kab = d.basis.nprim[t.sa] * d.basis.nprim[t.sb];
-    const int Kcd = d.basis.nprim[t.sc] * d.basis.nprim[t.sd];
-    const int pab0 = d.basis.sp_off[t.sa * ns + t.sb];
-    const int pcd0 = d.basis.sp_off[t.sc * ns + t.sd];
+    constexpr int NAB = nc(LA) * nc(LB), NCD = nc(LC) * nc(LD), NOUT = NAB * NCD;
+    constexpr int NCB = nc(LB), NCDD = nc(LD);
+    __shared__ int s_queue[4][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    int* queue = s_queue[wib];
+    const int nwarp = gridDim.x * (blockDim.x >> 5);
     const PairData& pp = d.pairs;
+    const int ns = d.basis.ns;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
     const float cut64 = fmaxf(cut32, skip);
-    const float bq0 = pp.sbound[pcd0];
+    // Mixed precision: pass 0 evaluates the FP64 quartets, pass 1 the FP32
+    // quartets whose Boys argument lies in the asymptotic sector (FP32 Boys),
+    // pass 2 the other FP32 quartets (FP64 Boys, FP32 recurrence), so that
+    // every batch follows one Boys path.
+    const int npass = cut32 > 0.0f ? 3 : 1;
     unsigned n64 = 0, n32 = 0;
-    double2 out[NAB * NCD];
-#pragma unroll
-    for (int i = 0; i < NAB * NCD; ++i) out[i] = c2(0.0, 0.0);
-    // Primitive pairs are visited in decreasing Schwarz order, so screened
-    // quartets form a suffix of every row and the loops can stop early.
-    for (int P = 0; P < Kab; ++P) {
-        const float bp = pp.sbound[pab0 + P];
-        if (bp * bq0 < skip) break;
-        const int ip = pp.order[pab0 + P];
-        const double p = pp.p[ip];
-        const double Pr0 = pp.Pr[3 * ip], Pr1 = pp.Pr[3 * ip + 1], Pr2 = pp.Pr[3 * ip + 2];
-        const double Pi0 = pp.Pi[3 * ip], Pi1 = pp.Pi[3 * ip + 1], Pi2 = pp.Pi[3 * ip + 2];
-        const double2 Fab = pp.F[ip];
-        double2 W[NH * NCD];
-#pragma unroll
-        for (int i = 0; i < NH * NCD; ++i) W[i] = c2(0.0, 0.0);
-        bool any64 = false;
-        auto fp64_quartet = [&](int iq, const double2* X, double2* Sh) {
-            double2 R[NL];
-            if constexpr (L == 0) {
-                R[0] = Sh[0];
-            } else {
-                R[0] = Sh[L];
-                run_rec<L>(R, Sh, X, std::make_integer_sequence<int, rsteps(L)>{});
-            }
-            run_k<LA, LB, LC, LD>(W, R, pp.Epool + pp.Eoff[iq],
-                                  std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
-            any64 = true;
-            ++n64;
-        };
-        int Q = 0;
-        for (; Q < Kcd; ++Q) {
-            if (bp * pp.sbound[pcd0 + Q] < cut64) break;
-            const int iq = pp.order[pcd0 + Q];
-            const double2 X[3] = {c2(Pr0 - pp.Pr[3 * iq], Pi0 - pp.Pi[3 * iq]),
-                                  c2(Pr1 - pp.Pr[3 * iq + 1], Pi1 - pp.Pi[3 * iq + 1]),
-                                  c2(Pr2 - pp.Pr[3 * iq + 2], Pi2 - pp.Pi[3 * iq + 2])};
-            double2 Sh[L + 1];
-            quartet_seeds<L>(d, tk, p, pp.p[iq], X, Fab, pp.F[iq], Sh);
-            fp64_quartet(iq, X, Sh);
+    auto out_ptr = [&](const Task& t, int o) {
+        const int ab = o / NCD, cd = o - ab * NCD;
+        const int ca = ab / NCB, cb = ab - ca * NCB, cc = cd / NCDD, cdd = cd - cc * NCDD;
+        return d.out + t.out_off + (long long)ca * t.st[0] + (long long)cb * t.st[1] + (long long)cc * t.st[2] +
+               (long long)cdd * t.st[3];
+    };
+    for (int grp = blockIdx.x * (blockDim.x >> 5) + wib; grp < qc.ngroup; grp += nwarp) {
+        const int2 gi = qc.groups[grp];
+        const Task t0 = qc.tasks[gi.x];
+        const int Kab = d.basis.nprim[t0.sa] * d.basis.nprim[t0.sb];
+        const int Kcd = d.basis.nprim[t0.sc] * d.basis.nprim[t0.sd];
+        const int KK = Kab * Kcd;
+        const int S = gi.y * KK;
+        for (int it = lane; it < gi.y * NOUT; it += 32) {
+            const int g = it / NOUT;
+            *out_ptr(qc.tasks[gi.x + g], it - g * NOUT) = c2(0.0, 0.0);
         }
-        if (cut32 > 0.0f) {
-            float2 W32[NH * NCD];
-#pragma unroll
-            for (int i = 0; i < NH * NCD; ++i) W32[i] = make_float2(0.0f, 0.0f);
-            bool any32 = false;
-            for (; Q < Kcd; ++Q) {
-                if (bp * pp.sbound[pcd0 + Q] < skip) break;
-                const int iq = pp.order[pcd0 + Q];
-                const double2 X[3] = {c2(Pr0 - pp.Pr[3 * iq], Pi0 - pp.Pi[3 * iq]),
-                                      c2(Pr1 - pp.Pr[3 * iq + 1], Pi1 - pp.Pi[3 * iq + 1]),
-                                      c2(Pr2 - pp.Pr[3 * iq + 2], Pi2 - pp.Pi[3 * iq + 2])};
-                double2 Sh[L + 1];
-                quartet_seeds<L>(d, tk, p, pp.p[iq], X, Fab, pp.F[iq], Sh);
-                double big = 0.0;
-#pragma unroll
-                for (int n = 0; n <= L; ++n) big = fmax(big, fabs(Sh[n].x) + fabs(Sh[n].y));
-                if (!(big < FP32_SEED_LIMIT)) {
-                    fp64_quartet(iq, X, Sh);  // out of float range: keep FP64
-                    continue;
+        __syncwarp();
+        for (int pass = 0; pass < npass; ++pass) {
+            int cursor = 0;
+            while (cursor < S) {
+                // compact up to 32 surviving entries of this pass
+                int nb = 0;
+                while (nb < 32 && cursor < S) {
+                    const int idx = cursor + lane;
+                    bool valid = false;
+                    if (idx < S) {
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
+                        const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
+                        const float b = pp.sbound[op] * pp.sbound[oq];
+                        valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
+                        if (valid && pass > 0)
+                            valid = (pass == 1) == boys_asymptotic32(pp, pp.order[op], pp.order[oq], L);
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, valid);
+                    const int cnt = __popc(mask);
+                    const int take = min(cnt, 32 - nb);
+                    const int rank = __popc(mask & ((1u << lane) - 1u));
+                    if (valid && rank < take) queue[nb + rank] = idx;
+                    if (take < cnt) {
+                        const unsigned m2 = __ballot_sync(0xffffffffu, valid && rank == take);
+                        cursor += __ffs(m2) - 1;
+                    } else {
+                        cursor += 32;
+                    }
+                    nb += take;
                 }
-                float2 S32[L + 1];
+                __syncwarp();
+                if (nb == 0) break;
+                const bool active = lane < nb;
+                int key = -1 - lane;  // idle lanes never match another lane
+                double2 v[NOUT];
+                float2 v32[NOUT];
 #pragma unroll
-                for (int n = 0; n <= L; ++n) S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
-                const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
-                                       make_float2((float)X[1].x, (float)X[1].y),
-                                       make_float2((float)X[2].x, (float)X[2].y)};
-                float2 R32[NL];
-                if constexpr (L == 0) {
-                    R32[0] = S32[0];
-                } else {
-                    R32[0] = S32[L];
-                    run_rec32<L>(R32, S32, X32, std::make_integer_sequence<int, rsteps(L)>{});
+                for (int i = 0; i < NOUT; ++i) {
+                    v[i] = c2(0.0, 0.0);
+                    v32[i] = make_float2(0.0f, 0.0f);
                 }
-                run_k32<LA, LB, LC, LD>(W32, R32, pp.Epool32 + pp.Eoff[iq],
-                                        std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
-                any32 = true;
-                ++n32;
-            }
-            if (any32) {
-                float2 o32[NAB * NCD];
+                bool used64 = false;
+                if (active) {
+                    const int idx = queue[lane];
+                    const int g = idx / KK, r = idx - g * KK;
+                    const int P = r / Kcd, Q = r - P * Kcd;
+                    key = g;
+                    const Task tg = qc.tasks[gi.x + g];
+                    const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                    const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                    const double p = pp.p[ip], q = pp.p[iq];
+                    const double2 X[3] = {c2(pp.Pr[3 * ip] - pp.Pr[3 * iq], pp.Pi[3 * ip] - pp.Pi[3 * iq]),
+                                          c2(pp.Pr[3 * ip + 1] - pp.Pr[3 * iq + 1], pp.Pi[3 * ip + 1] - pp.Pi[3 * iq + 1]),
+                                          c2(pp.Pr[3 * ip + 2] - pp.Pr[3 * iq + 2], pp.Pi[3 * ip + 2] - pp.Pi[3 * iq + 2])};
+                    const double rs = rsqrt(p + q);
+                    const double rho = p * q * rs * rs;
+                    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
+                                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
+                    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+                    const double2 C = cscale(cmul(pp.F[ip], pp.F[iq]), rs);
+                    double2 Sh[L + 1];
+                    bool ok32 = false;
+                    if (pass > 0) {
+                        float2 S32[L + 1];
+                        ok32 = pass == 1 && seeds32(C, rho, tre, tim, L, S32);
+                        if (!ok32) {
+                            // FP64 Boys; FP32 recurrence when the seeds fit
+                            quartet_seeds<L>(d, gi.x + g, C, rho, tre, tim, Sh);
+                            ok32 = true;
 #pragma unroll
-                for (int i = 0; i < NAB * NCD; ++i) o32[i] = make_float2(0.0f, 0.0f);
-                run_b32<LA, LB, LC, LD>(o32, W32, pp.Epool32 + pp.Eoff[ip],
-                                        std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
-                // FP32 accumulation, FP64 final summation
+                            for (int n = 0; n <= L; ++n) {
+                                ok32 = ok32 && fabs(Sh[n].x) + fabs(Sh[n].y) < 1.0e25;
+                                S32[n] = make_float2((float)Sh[n].x, (float)Sh[n].y);
+                            }
+                        }
+                        if (ok32) {
+                            const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
+                                                   make_float2((float)X[1].x, (float)X[1].y),
+                                                   make_float2((float)X[2].x, (float)X[2].y)};
+                            float2 R32[NL];
+                            if constexpr (L == 0) {
+                                R32[0] = S32[0];
+                            } else {
+                                R32[0] = S32[L];
+                                run_rec32<L>(R32, S32, X32, std::make_integer_sequence<int, rsteps(L)>{});
+                            }
+                            float2 W32[NH * NCD];
 #pragma unroll
-                for (int i = 0; i < NAB * NCD; ++i) out[i] = cadd(out[i], c2((double)o32[i].x, (double)o32[i].y));
+                            for (int i = 0; i < NH * NCD; ++i) W32[i] = make_float2(0.0f, 0.0f);
+                            run_k32<LA, LB, LC, LD>(W32, R32, pp.Epool32 + pp.Eoff[iq],
+                                                    std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
+                            run_b32<LA, LB, LC, LD>(v32, W32, pp.Epool32 + pp.Eoff[ip],
+                                                    std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
+                            ++n32;
+                        }
+                    } else {
+                        quartet_seeds<L>(d, gi.x + g, C, rho, tre, tim, Sh);
+                    }
+                    if (!ok32) {
+                        double2 R[NL];
+                        if constexpr (L == 0) {
+                            R[0] = Sh[0];
+                        } else {
+                            R[0] = Sh[L];
+                            run_rec<L>(R, Sh, X, std::make_integer_sequence<int, rsteps(L)>{});
+                        }
+                        double2 W[NH * NCD];
+#pragma unroll
+                        for (int i = 0; i < NH * NCD; ++i) W[i] = c2(0.0, 0.0);
+                        run_k<LA, LB, LC, LD>(W, R, pp.Epool + pp.Eoff[iq],
+                                              std::make_integer_sequence<int, kmacs<LA, LB, LC, LD>()>{});
+                        run_b<LA, LB, LC, LD>(v, W, pp.Epool + pp.Eoff[ip],
+                                              std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
+                        used64 = true;
+                        ++n64;
+                    }
+                }
+                // FP32 contributions are reduced in FP32, FP64 ones in FP64, and
+                // the first lane of each segment adds both in FP64.
+                if (pass == 0 || __any_sync(0xffffffffu, used64)) seg_sum<NOUT>(v, key, lane);
+                if (pass > 0) {
+                    seg_sum<NOUT>(v32, key, lane);
+#pragma unroll
+                    for (int i = 0; i < NOUT; ++i) v[i] = cadd(v[i], c2((double)v32[i].x, (double)v32[i].y));
+                }
+                const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+                if (active && (lane == 0 || kprev != key)) {
+                    const Task tg = qc.tasks[gi.x + key];
+#pragma unroll
+                    for (int i = 0; i < NOUT; ++i) {
+                        double2* o = out_ptr(tg, i);
+                        *o = cadd(*o, v[i]);
+                    }
+                }
+                __syncwarp();
             }
         }
-        if (any64)
-            run_b<LA, LB, LC, LD>(out, W, pp.Epool + pp.Eoff[ip],
-                                  std::make_integer_sequence<int, bmacs<LA, LB, LC, LD>()>{});
     }
-    constexpr int NCB = nc(LB), NCDD = nc(LD);
-#pragma unroll
-    for (int ab = 0; ab < NAB; ++ab)
-#pragma unroll
-        for (int cd = 0; cd < NCD; ++cd) {
-            const int ca = ab / NCB, cb = ab % NCB, cc = cd / NCDD, cdd = cd % NCDD;
-            d.out[t.out_off + (long long)ca * t.st[0] + (long long)cb * t.st[1] + (long long)cc * t.st[2] +
-                  (long long)cdd * t.st[3]] = out[ab * NCD + cd];
-        }
     if (d.counters) {
-        const unsigned a64 = __reduce_add_sync(__activemask(), n64);
-        const unsigned a32 = __reduce_add_sync(__activemask(), n32);
-        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+        const unsigned a64 = __reduce_add_sync(0xffffffffu, n64);
+        const unsigned a32 = __reduce_add_sync(0xffffffffu, n32);
+        if (lane == 0) {
             atomicAdd(&d.counters[0], (unsigned long long)a64);
             atomicAdd(&d.counters[1], (unsigned long long)a32);
         }

@@ -1,0 +1,303 @@
+"""Persistent request loop for ERI-block and Cholesky requests on one GPU.
+
+The reference evaluates one call at a time on host threads
+(src/eri.cpp:708-763, python/giao_integrals/cholesky.py:95-297); there is no
+serving layer.  This loop serves a stream of requests for molecules and
+fields of different sizes with continuous batching:
+
+* ``slots`` workers each own a device context (its own CUDA stream, Boys
+  table and pools), so the kernels of up to ``slots`` requests overlap on the
+  GPU;
+* a request is admitted as soon as a slot is free and its estimated device
+  footprint fits in what the in-flight requests leave of the HBM budget;
+  requests that arrive while others run are admitted the moment a slot and
+  memory free up, in arrival order (a request that cannot fit even an empty
+  budget fails with ``MemoryError``);
+* each context keeps the bases it has served resident (basis upload,
+  primitive-pair records for the last field), so repeated molecules skip the
+  upload, and Cholesky factors stay on the device for the whole pivot loop.
+
+Every request computes exactly what the same call computes alone: contexts
+share no device state, and every kernel's summation order depends only on the
+request itself.
+
+``Server.run(requests)`` replays a trace (``synthetic.serving_requests``:
+Poisson arrivals) in real time and reports p50 / p99 latency beside
+throughput.
+"""
+
+from __future__ import annotations
+
+import threading
+import time
+from collections import OrderedDict, deque
+from concurrent.futures import Future
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+
+__all__ = ["Completion", "Server", "footprint_bytes", "latency_summary"]
+
+_BASE_BYTES = 64 << 20  # pair records, task lists and launch metadata of one request (upper estimate)
+
+
+def _ncart(l: int) -> int:
+    return (l + 1) * (l + 2) // 2
+
+
+def footprint_bytes(request) -> int:
+    """Estimated device memory one request holds while it runs."""
+    sizes = np.array([_ncart(s.angular_momentum) * len(s.raw_coefficients) for s in request.shells], dtype=np.int64)
+    if request.kind == "eri":
+        q = np.asarray(request.quartets, dtype=np.int64).reshape(-1, 4)
+        entries = int(np.prod(sizes[q], axis=1).sum()) if len(q) else 0
+        # packed device output, its staging for the host copy and the task list
+        return _BASE_BYTES + 2 * 16 * entries + 48 * len(q)
+    n = int(sizes.sum())
+    N = n * n
+    rank_guess = min(N, max(64, 8 * n))
+    # factors, column pool (1120 columns), residual/diagonal/work vectors
+    return _BASE_BYTES + (rank_guess + 1120 + 4) * N * 16
+
+
+@dataclass
+class Completion:
+    """One served request: its result and timeline (seconds since the run started)."""
+
+    index: int
+    kind: str
+    arrival: float
+    admitted: float = 0.0
+    finished: float = 0.0
+    slot: int = -1
+    footprint: int = 0
+    result: object = None
+    entries: int = 0          # complex ERI entries (ERI requests)
+    error: BaseException | None = None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+    @property
+    def queue_wait(self) -> float:
+        return self.admitted - self.arrival
+
+
+@dataclass
+class _Pending:
+    index: int
+    request: object
+    arrival: float
+    footprint: int
+    admitted: float = 0.0
+    future: Future = dc_field(default_factory=Future)
+
+
+class Server:
+    """Continuous-batching request loop (see module docstring).
+
+    ``runner(slot, request)`` evaluates one request on a slot; the default
+    runs it on the slot's device context.  ``hbm_budget`` (bytes) defaults to
+    half of the device's free memory at start-up."""
+
+    def __init__(self, slots: int = 4, *, hbm_budget: int | None = None, precision: str = "fp64",
+                 mixed_cutoff: float = 1e-6, device: int = 0, runner=None, bases_per_slot: int = 32):
+        if slots < 1:
+            raise ValueError("slots must be a positive integer")
+        self.slots = int(slots)
+        self.precision = precision
+        self.mixed_cutoff = float(mixed_cutoff)
+        self.device = int(device)
+        self._runner = runner or self._run_on_device
+        self._contexts: list = [None] * self.slots
+        self._bases: list[OrderedDict] = [OrderedDict() for _ in range(self.slots)]
+        self._bases_per_slot = int(bases_per_slot)
+        if hbm_budget is None:
+            hbm_budget = self._default_budget() if runner is None else 1 << 40
+        self.hbm_budget = int(hbm_budget)
+        self._cv = threading.Condition()
+        self._queue: deque[_Pending] = deque()
+        self._reserved = 0
+        self._inflight = 0
+        self._closing = False
+        self._t0 = time.perf_counter()
+        self.max_inflight = 0
+        self.max_reserved = 0
+        self._workers = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(self.slots)]
+        for w in self._workers:
+            w.start()
+
+    # ---- public ---------------------------------------------------------------
+    def now(self) -> float:
+        return time.perf_counter() - self._t0
+
+    def submit(self, request, index: int = 0, arrival: float | None = None) -> Future:
+        """Queue a request; the future resolves to its ``Completion``."""
+        fp = footprint_bytes(request)
+        p = _Pending(index, request, self.now() if arrival is None else arrival, fp)
+        if fp > self.hbm_budget:
+            p.future.set_exception(MemoryError(
+                f"request needs about {fp} bytes of device memory; the serving budget is {self.hbm_budget} bytes"))
+            return p.future
+        with self._cv:
+            if self._closing:
+                raise RuntimeError("server is closed")
+            self._queue.append(p)
+            self._cv.notify_all()
+        return p.future
+
+    def run(self, requests, *, realtime: bool = True) -> list[Completion]:
+        """Replay ``requests`` (each with ``.arrival`` seconds) and wait for all."""
+        self._t0 = time.perf_counter()
+        futures = []
+        for i, r in enumerate(requests):
+            if realtime:
+                delay = r.arrival - self.now()
+                if delay > 0:
+                    time.sleep(delay)
+            futures.append(self.submit(r, i, arrival=r.arrival if realtime else self.now()))
+        out = []
+        for f in futures:
+            try:
+                out.append(f.result())
+            except BaseException as e:  # noqa: BLE001 - reported per request
+                out.append(Completion(-1, "error", 0.0, error=e))
+        return out
+
+    def close(self) -> None:
+        with self._cv:
+            self._closing = True
+            self._cv.notify_all()
+        for w in self._workers:
+            w.join()
+        # release the resident bases, then the slots' device contexts
+        self._bases = [OrderedDict() for _ in range(self.slots)]
+        for ctx in self._contexts:
+            if ctx is not None:
+                ctx.close()
+        self._contexts = [None] * self.slots
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- scheduling -----------------------------------------------------------
+    def _take(self) -> _Pending | None:
+        """Admit the oldest request once it fits (called with the lock held)."""
+        while True:
+            if self._queue and self._reserved + self._queue[0].footprint <= self.hbm_budget:
+                p = self._queue.popleft()
+                p.admitted = self.now()
+                self._reserved += p.footprint
+                self._inflight += 1
+                self.max_inflight = max(self.max_inflight, self._inflight)
+                self.max_reserved = max(self.max_reserved, self._reserved)
+                return p
+            if self._closing and not self._queue:
+                return None
+            self._cv.wait()
+
+    def _worker(self, slot: int) -> None:
+        while True:
+            with self._cv:
+                p = self._take()
+            if p is None:
+                return
+            c = Completion(p.index, p.request.kind, p.arrival, admitted=p.admitted, slot=slot, footprint=p.footprint)
+            try:
+                c.result, c.entries = self._runner(slot, p.request)
+            except BaseException as e:  # noqa: BLE001 - delivered through the future
+                c.error = e
+            c.finished = self.now()
+            with self._cv:
+                self._reserved -= p.footprint
+                self._inflight -= 1
+                self._cv.notify_all()
+            if c.error is not None:
+                p.future.set_exception(c.error)
+            else:
+                p.future.set_result(c)
+
+    # ---- device execution -----------------------------------------------------
+    def _default_budget(self) -> int:
+        try:
+            import torch
+
+            free, _total = torch.cuda.mem_get_info(self.device)
+            return int(free // 2)
+        except Exception:  # noqa: BLE001 - no torch / no device: a fixed budget
+            return 64 << 30
+
+    def _context(self, slot: int):
+        from . import _native as nat
+
+        if self._contexts[slot] is None:
+            self._contexts[slot] = nat.Context(self.device)
+        return self._contexts[slot]
+
+    def _basis(self, slot: int, shells):
+        from ._types import Basis, Shell
+
+        cache = self._bases[slot]
+        key = tuple(shells)
+        b = cache.get(key)
+        if b is None:
+            b = Basis([Shell.from_record(s) for s in shells])
+            cache[key] = b
+            while len(cache) > self._bases_per_slot:
+                cache.popitem(last=False)
+        else:
+            cache.move_to_end(key)
+        return b
+
+    def _run_on_device(self, slot: int, request):
+        from ._types import MagneticField
+        from .cholesky import _cholesky_device
+        from .eri import _eri_batch
+
+        ctx = self._context(slot)
+        basis = self._basis(slot, request.shells)
+        field = MagneticField(request.field)
+        if request.kind == "eri":
+            res = _eri_batch(basis, request.quartets, field=field, precision=self.precision,
+                             mixed_cutoff=self.mixed_cutoff, context=ctx)
+            return res, int(res[2][-1])
+        if request.kind == "cholesky":
+            return _cholesky_device(basis, field, float(request.threshold), 0.0, None, 32, context=ctx), 0
+        raise ValueError("request kind must be 'eri' or 'cholesky'")
+
+
+def latency_summary(done: list[Completion]) -> dict:
+    """p50 / p99 latency, queue wait and throughput of a served trace."""
+    ok = [c for c in done if c.error is None]
+    if not ok:
+        return {"requests": len(done), "completed": 0}
+    lat = np.array([c.latency for c in ok]) * 1e3
+    wait = np.array([c.queue_wait for c in ok]) * 1e3
+    start = min(c.arrival for c in ok)
+    end = max(c.finished for c in ok)
+    entries = sum(c.entries for c in ok)
+    out = {
+        "requests": len(done),
+        "completed": len(ok),
+        "p50_ms": float(np.percentile(lat, 50)),
+        "p99_ms": float(np.percentile(lat, 99)),
+        "mean_ms": float(lat.mean()),
+        "max_ms": float(lat.max()),
+        "queue_wait_p50_ms": float(np.percentile(wait, 50)),
+        "queue_wait_p99_ms": float(np.percentile(wait, 99)),
+        "makespan_s": float(end - start),
+        "eris": int(entries),
+        "eris_per_s": float(entries / max(end - start, 1e-9)),
+        "requests_per_s": float(len(ok) / max(end - start, 1e-9)),
+    }
+    for kind in ("eri", "cholesky"):
+        k = np.array([c.latency for c in ok if c.kind == kind]) * 1e3
+        if len(k):
+            out[f"{kind}_p50_ms"] = float(np.percentile(k, 50))
+            out[f"{kind}_p99_ms"] = float(np.percentile(k, 99))
+            out[f"{kind}_count"] = int(len(k))
+    return out

@@ -220,6 +220,36 @@ int gx_eri_plan_counts(gx_eri_plan* plan, int64_t* fp64_quartets, int64_t* fp32_
                        double* fp32_flops);
 void gx_eri_plan_destroy(gx_eri_plan* plan);
 
+/* Number of (la, lb, lc, ld) classes (one kernel launch each). */
+int gx_eri_plan_class_count(const gx_eri_plan* plan);
+/* Executions served by replaying the plan's CUDA graph so far (a plan is
+ * captured on its second execution with the same stream, output, precision
+ * and cutoff, and replayed from then on). */
+int gx_eri_plan_graph_replays(const gx_eri_plan* plan);
+
+/* Per-class timing of one execution (synchronous). */
+typedef struct gx_class_profile {
+    int la, lb, lc, ld;
+    int64_t tasks;                 /* segmented shell quartets */
+    int64_t primitive_quartets;    /* before screening */
+    int64_t fp64_quartets;         /* evaluated in FP64 */
+    int64_t fp32_quartets;         /* evaluated in FP32 (mixed precision) */
+    double model_flops_per_quartet;
+    float ms;                      /* event-timed kernel duration */
+    int per_group;                 /* launch configuration: primitive quartets per warp unit (0 = default) */
+    int warps_per_block, batch;    /* generic kernel: warps per block, phase-1 batch */
+    int64_t groups;                /* warp work units */
+} gx_class_profile;
+int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                        void* out_device, gx_class_profile* out);
+/* Autotune the launch configuration of every class for one precision mode:
+ * each class is timed (best of `repeats`) over its candidate work-unit sizes,
+ * warps per block and phase-1 batch sizes, and the fastest is kept for later
+ * executions in that mode.  Writes out_device.  default_ms / tuned_ms: summed
+ * class times before and after. */
+int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
+                         void* out_device, int repeats, double* default_ms, double* tuned_ms);
+
 /* Canonical shell quartets of an ns-shell basis: the lexicographic
  * minimum of each finite-field orbit {(ab|cd), (cd|ab), (ba|dc)*, (dc|ba)*}
  * (canonicalize_shell_quartet, src/eri.cpp:414-429), in the enumeration

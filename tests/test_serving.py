@@ -1,0 +1,93 @@
+"""Host logic of the serving loop (no GPU): admission by device footprint,
+arrival-order admission, overlap up to the slot count, rejection of requests
+larger than the whole budget, latency summary."""
+
+from __future__ import annotations
+
+import threading
+import time
+
+import pytest
+
+from giaoint_gb300 import synthetic as syn
+from giaoint_gb300.serving import Server, footprint_bytes, latency_summary
+
+
+def _trace(count=16):
+    return syn.serving_requests(count=count, rate=400.0, seed=5, atoms=(3, 5), max_entries=1 << 16,
+                                cholesky_fraction=0.3, cholesky_atoms=(3, 3))
+
+
+def test_admission_respects_budget_slots_and_arrival_order():
+    reqs = _trace()
+    fps = [footprint_bytes(r) for r in reqs]
+    budget = max(fps) + min(fps)  # the largest request plus one more at most
+    lock = threading.Lock()
+    live = {"n": 0, "bytes": 0, "max_n": 0, "max_bytes": 0}
+    order = []
+
+    def runner(slot, req):
+        fp = footprint_bytes(req)
+        with lock:
+            live["n"] += 1
+            live["bytes"] += fp
+            live["max_n"] = max(live["max_n"], live["n"])
+            live["max_bytes"] = max(live["max_bytes"], live["bytes"])
+            order.append(req.arrival)
+        time.sleep(0.01)
+        with lock:
+            live["n"] -= 1
+            live["bytes"] -= fp
+        return req.kind, 10
+
+    with Server(slots=3, hbm_budget=budget, runner=runner) as srv:
+        done = srv.run(reqs)
+    assert all(c.error is None for c in done)
+    assert live["max_bytes"] <= budget
+    assert 1 <= live["max_n"] <= 3
+    assert srv.max_reserved <= budget
+    by_arrival = sorted(done, key=lambda c: c.arrival)
+    admitted = [c.admitted for c in by_arrival]
+    assert admitted == sorted(admitted)  # admitted in arrival order
+    assert sorted(order) == [c.arrival for c in by_arrival]
+    s = latency_summary(done)
+    assert s["completed"] == len(reqs)
+    assert s["p99_ms"] >= s["p50_ms"] > 0.0
+    assert s["eris"] == 10 * len(reqs)
+
+
+def test_requests_overlap_when_they_fit():
+    reqs = _trace(8)
+    started = []
+    gate = threading.Barrier(2, timeout=5)
+
+    def runner(slot, req):
+        started.append(slot)
+        if len(started) <= 2:
+            gate.wait()  # the first two requests must run at the same time
+        return None, 0
+
+    with Server(slots=2, hbm_budget=1 << 50, runner=runner) as srv:
+        done = srv.run(reqs, realtime=False)
+    assert all(c.error is None for c in done)
+    assert srv.max_inflight == 2
+
+
+def test_oversize_request_is_rejected():
+    reqs = _trace(4)
+    with Server(slots=1, hbm_budget=1024, runner=lambda s, r: (None, 0)) as srv:
+        fut = srv.submit(reqs[0])
+        with pytest.raises(MemoryError, match="serving budget"):
+            fut.result(timeout=5)
+
+
+def test_runner_errors_reach_the_caller():
+    reqs = _trace(3)
+
+    def runner(slot, req):
+        raise ValueError("bad request")
+
+    with Server(slots=2, hbm_budget=1 << 50, runner=runner) as srv:
+        fut = srv.submit(reqs[0])
+        with pytest.raises(ValueError, match="bad request"):
+            fut.result(timeout=5)
