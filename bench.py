@@ -65,18 +65,19 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from giaoint_gb300.replicas import dist_env as env
+
+    return env()
 
 
 def workload(natoms: int, rank: int):
+    """The 12-atom molecule (seed 2026) and this rank's field (replicas: one
+    field per rank, no data-path collective)."""
     from giaoint_gb300 import synthetic as syn
+    from giaoint_gb300.replicas import field_for_rank
 
     recs = syn.random_molecule(2026, natoms=natoms)
-    B = syn.random_field(2026) if rank == 0 else syn.field_grid(64, 0.2)[rank % 64]
-    return recs, B
+    return recs, field_for_rank(rank)
 
 
 class ClockSampler:
@@ -185,6 +186,40 @@ def cholesky_leg(gi, nat, ctx, run_cpu: bool):
             k += 1
         out["pivots_equal_prefix"] = k
         out["speedup_vs_cpu_port"] = cpu_s / gpu_s
+    return out
+
+
+def full_tensor_leg(ctx, run_cpu: bool):
+    """Plain FP64 full unscreened tensor of the 19-AO atom (4s 3p 1d, B = (0,
+    0, 0.1)): latency of one gi.eri(storage="full") call through the C ABI
+    (gx_eri_full, host output, every primitive quartet evaluated), with the
+    oracle port's time beside it."""
+    import giaoint_gb300 as gi
+    from giaoint_gb300 import synthetic as syn
+    from giaoint_gb300.eri import _eri_full
+
+    recs = syn.full_tensor_atom()
+    basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
+    field = gi.MagneticField((0.0, 0.0, 0.1))
+    for _ in range(3):
+        full = _eri_full(basis, field=field, context=ctx, precision="fp64_exact")
+    times = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        full = _eri_full(basis, field=field, context=ctx, precision="fp64_exact")
+        times.append(time.perf_counter() - t0)
+    out = {"workload": "19-AO atom 4s3p1d, B=(0,0,0.1), full complex128 tensor 19^4",
+           "ms_per_call_p50": 1e3 * statistics.median(times), "ms_per_call_min": 1e3 * min(times)}
+    if run_cpu:
+        from oracle import oracle as O
+
+        orc = O.Oracle()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = orc.eri_full(recs, (0.0, 0.0, 0.1), None, threads)
+        out["cpu_port_ms"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_port_threads"] = threads
+        out["max_abs_diff_vs_cpu_port"] = float(np.max(np.abs(full - ref)))
     return out
 
 
@@ -419,6 +454,8 @@ def run_gpu(args):
             dt = time.perf_counter() - t0
             if i > 0:
                 times.append(dt)
+            else:
+                cold_s = dt  # builds and caches the class-sorted plan on the host
         e2e_s = float(statistics.mean(times))
         if world > 1:
             t = torch.tensor([e2e_s], device=f"cuda:{local}")
@@ -429,8 +466,18 @@ def run_gpu(args):
         dev_sample = out[: 2 * min(total, 1 << 20)].cpu().numpy()
         e2e_diff = float(np.max(np.abs(dev_sample - host[: len(dev_sample)].numpy()), initial=0.0))
         assert e2e_diff <= 1e-11, f"e2e and device results differ by {e2e_diff}"
-        e2e = {"value": world * total / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(nq * 16 + ntask.value * 40),
-               "d2h_bytes_per_step": int(total * 16), "seconds_per_step": e2e_s,
+        # the device-to-host leg alone, for the breakdown: one pinned copy
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host.copy_(out.view(-1)[: 2 * total])
+        torch.cuda.synchronize()
+        d2h_s = time.perf_counter() - t0
+        e2e = {"value": world * total / e2e_s, "unit": UNIT,
+               # per warm call: the field (B, O); the quartet list is read and
+               # hashed on the host, its plan is cached on the device
+               "h2d_bytes_per_step": 48, "d2h_bytes_per_step": int(total * 16), "seconds_per_step": e2e_s,
+               "cold_call_seconds": cold_s, "cold_h2d_bytes": int(ntask.value * 40 + 48),
+               "d2h_copy_seconds": d2h_s, "d2h_gb_per_s": total * 16 / d2h_s / 1e9,
                "api": "gx_eri_batch (C ABI, pinned host buffers)", "max_abs_diff_vs_device_path": e2e_diff}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -442,6 +489,10 @@ def run_gpu(args):
     if rank == 0 and not args.no_cholesky:
         nat.check(lib.gx_context_set_stream(ctx.handle, None))
         chol = cholesky_leg(gi, nat, ctx, run_cpu=(world == 1 and not args.no_cpu))
+    full_tensor = None
+    if rank == 0:
+        nat.check(lib.gx_context_set_stream(ctx.handle, None))
+        full_tensor = full_tensor_leg(ctx, run_cpu=(world == 1 and not args.no_cpu))
     serving = None
     if rank == 0 and not args.no_serving:
         serving = serving_leg(args)
@@ -484,6 +535,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "cholesky": chol,
             "field_sweep": sweep,
+            "full_tensor": full_tensor,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

@@ -60,6 +60,9 @@ class GxClassProfile(ctypes.Structure):
         ("warps_per_block", ctypes.c_int),
         ("batch", ctypes.c_int),
         ("groups", ctypes.c_int64),
+        ("kt", ctypes.c_int),
+        ("ct", ctypes.c_int),
+        ("min_blocks", ctypes.c_int),
     ]
 
 

@@ -40,7 +40,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     sources = sorted(CSRC.glob("*.cu"))
     newest_header = max(p.stat().st_mtime for p in _headers())
-    flags = ["-std=c++20", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC", "-I", str(ROOT / "include")]
+    flags = ["-std=c++20", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp", "-I", str(ROOT / "include")]
     if verbose:
         flags += ["-Xptxas", "-v"]
     compiler = nvcc()
@@ -59,7 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs = list(pool.map(compile_one, sources))
     if force or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(f".{os.getpid()}.so")
-        subprocess.run([compiler, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart"], check=True)
+        subprocess.run([compiler, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-lcudart", "-lgomp"], check=True)
         os.replace(tmp, LIB)
     return LIB
 

@@ -465,6 +465,9 @@ struct ClassConf {
     int per_group = 0;  // primitive quartets per warp work unit (small: 1024, generic: 32)
     int wpb = 0;        // generic kernel: warps per block cap (4)
     int b1 = 0;         // generic kernel: phase-1 batch cap (32)
+    int kt = 0;         // generic kernel: Hermite rows per lane in the ket transform (1, 2, 4; 0 = by lane use)
+    int ct = 0;         // generic kernel: ket components per lane in the bra transform (1-4; 0 = by lane use)
+    int minb = 0;       // generic kernel: register-budget variant (2 or 4 resident blocks; 0 = 2)
 };
 
 // Warp work units of every class: (first task within the class, task count).
@@ -504,6 +507,57 @@ double model_flops(int la, int lb, int lc, int ld) {
     return 8 * R + ere + 8 * nab * ncd + 8 * (L + 1);
 }
 
+// Plans of recent gx_eri_batch calls, per context: a repeated quartet list
+// (same basis, same kept quartets after screening) reuses its class-sorted
+// task list and work units instead of rebuilding them on the host.  Keyed by
+// two independent 64-bit hashes of the kept quartets plus their count and
+// output size; at most 4 plans and 2 GiB of task lists per context, least
+// recently used first out.  Entries are used with the context's mutex held.
+struct CachedPlan {
+    const gx_basis* basis;
+    uint64_t h1, h2;
+    int64_t count, entries;
+    std::unique_ptr<PlanData> plan;
+};
+std::mutex g_plan_cache_mu;
+std::map<const gx_context*, std::list<CachedPlan>> g_plan_cache;
+
+std::list<CachedPlan>& plan_cache(const gx_context* ctx) {
+    std::lock_guard<std::mutex> lock(g_plan_cache_mu);
+    return g_plan_cache[ctx];
+}
+
+// Autotuned launch configurations per (context, basis, precision mode) and
+// class, recorded by gx_eri_plan_autotune and applied to the plans that
+// gx_eri_batch builds for the same basis.
+using TuneKey = std::tuple<const gx_context*, const gx_basis*, int>;
+std::map<TuneKey, std::map<std::array<int, 4>, ClassConf>> g_tune_db;
+
+// Forget the cached plans and tunings of a basis (null: of the whole context).
+void drop_cached_plans(const gx_context* ctx, const gx_basis* b) {
+    std::lock_guard<std::mutex> lock(g_plan_cache_mu);
+    for (auto it = g_tune_db.begin(); it != g_tune_db.end();) {
+        if (std::get<0>(it->first) == ctx && (!b || std::get<1>(it->first) == b))
+            it = g_tune_db.erase(it);
+        else
+            ++it;
+    }
+    auto it = g_plan_cache.find(ctx);
+    if (it == g_plan_cache.end()) return;
+    if (!b) {
+        g_plan_cache.erase(it);
+        return;
+    }
+    it->second.remove_if([&](const CachedPlan& c) { return c.basis == b; });
+}
+
+void record_tuning(const gx_context* ctx, const gx_basis* b, int precision, const PlanData& plan,
+                   const std::vector<ClassConf>& conf) {
+    std::lock_guard<std::mutex> lock(g_plan_cache_mu);
+    auto& db = g_tune_db[TuneKey{ctx, b, precision}];
+    for (size_t ci = 0; ci < plan.classes.size(); ++ci) db[plan.classes[ci].key] = conf[ci];
+}
+
 // Warp work units of class ci: runs of tasks with equal primitive counts
 // (Kab, Kcd).  Small classes (one lane per primitive quartet) take up to
 // `per_group` (default 1024) primitive quartets and 128 tasks per unit; the
@@ -540,6 +594,24 @@ void make_group_set(gx_context* ctx, const PlanData& plan, const std::vector<Cla
         all.insert(all.end(), g.begin(), g.end());
     }
     upload(out.dev, all, ctx->stream);
+}
+
+// Give `plan` the recorded tuning of (basis, precision), when there is one.
+void apply_recorded_tuning(gx_context* ctx, const gx_basis* b, int precision, PlanData& plan) {
+    if (plan.tuned[precision].valid) return;
+    std::vector<ClassConf> conf(plan.classes.size());
+    {
+        std::lock_guard<std::mutex> lock(g_plan_cache_mu);
+        auto it = g_tune_db.find(TuneKey{ctx, b, precision});
+        if (it == g_tune_db.end()) return;
+        for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
+            auto c = it->second.find(plan.classes[ci].key);
+            if (c != it->second.end()) conf[ci] = c->second;
+        }
+    }
+    make_group_set(ctx, plan, conf, plan.tuned[precision].groups);
+    plan.tuned[precision].conf = conf;
+    plan.tuned[precision].valid = true;
 }
 
 void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
@@ -636,7 +708,7 @@ gx::EriDev make_dev(gx_context* ctx, gx_basis* b, FieldPairs& fp, double2* out, 
 // optional pointers.
 void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t ci, const ClassConf& conf,
                   const int2* groups, int ngroup, unsigned long long* counters, cudaStream_t s, int* used_b1 = nullptr,
-                  int* used_wpb = nullptr) {
+                  int* used_wpb = nullptr, int* used_tiles = nullptr) {
     const auto& pc = plan.classes[ci];
     const auto& k = pc.key;
     dev.counters = counters ? counters + 2 * ci : nullptr;
@@ -673,7 +745,9 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     // Tiles: rows per lane KT of the ket transform and ket components per lane
     // CT of the bra transform, chosen for the best lane utilisation (padding
     // of Nab to a multiple of KT counts as waste), the wider tile on ties.
-    {
+    if (conf.kt == 1 || conf.kt == 2 || conf.kt == 4) {
+        qc.KT = conf.kt;
+    } else {
         double best = -1.0;
         for (int kt : {4, 2, 1}) {
             const int nkb = (qc.Nab + kt - 1) / kt;
@@ -684,7 +758,9 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
             }
         }
     }
-    {
+    if (conf.ct >= 1 && conf.ct <= 4 && ncd % conf.ct == 0) {
+        qc.CT = conf.ct;
+    } else {
         double best = -1.0;
         qc.CT = 1;
         for (int ct : {4, 3, 2, 1}) {
@@ -696,8 +772,8 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
                 qc.CT = ct;
             }
         }
-        if (qc.CH < ncd) qc.CH = std::max(qc.CT, qc.CH / qc.CT * qc.CT);  // chunks hold whole CT tiles
     }
+    if (qc.CH < ncd) qc.CH = std::max(qc.CT, qc.CH / qc.CT * qc.CT);  // chunks hold whole CT tiles
     qc.nchunk = (ncd + qc.CH - 1) / qc.CH;
     int B1 = conf.b1 > 0 ? std::min(32, conf.b1) : 32;
     while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
@@ -717,6 +793,7 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     qc.tasks = plan.tasks.as<gx::Task>() + pc.first;
     qc.ngroup = ngroup;
     qc.groups = groups;
+    qc.minb = conf.minb == 4 ? 4 : 2;
     const size_t per_warp = gx::quartet_smem_bytes(qc, 1, dev.fp32_cut > 0.0f);
     const int cap = conf.wpb > 0 ? std::min(4, conf.wpb) : 4;
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(cap, (200 * 1024) / per_warp));
@@ -724,6 +801,11 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
     if (used_b1) *used_b1 = B1;
     if (used_wpb) *used_wpb = wpb;
+    if (used_tiles) {
+        used_tiles[0] = qc.KT;
+        used_tiles[1] = qc.CT;
+        used_tiles[2] = qc.minb;
+    }
 }
 
 // Enqueue the pair records for (B, O) and every class launch; no host sync
@@ -749,13 +831,22 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
 
 // Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
 // index = contraction * ncart + component) and wait for them.
+void run_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, PlanData& plan, double2* out,
+              float* kernel_ms, int64_t* primitive_quartets, int precision, double mixed_cutoff, int64_t* evaluated);
+
 void run_quartets(gx_context* ctx, gx_basis* b, const double* B, const double* O,
                   const std::vector<QuartetRequest>& req, double2* out, float* kernel_ms,
                   int64_t* primitive_quartets = nullptr, int precision = GX_PRECISION_FP64,
                   double mixed_cutoff = 0.0, int64_t* evaluated = nullptr) {
-    cudaStream_t s = ctx->stream;
     PlanData plan;
     build_plan(ctx, b, req, plan);
+    run_plan(ctx, b, B, O, plan, out, kernel_ms, primitive_quartets, precision, mixed_cutoff, evaluated);
+}
+
+// Evaluate a built plan into `out` and wait for it.
+void run_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, PlanData& plan, double2* out,
+              float* kernel_ms, int64_t* primitive_quartets, int precision, double mixed_cutoff, int64_t* evaluated) {
+    cudaStream_t s = ctx->stream;
     if (primitive_quartets) *primitive_quartets = plan.primitive_quartets;
     unsigned long long* counters = nullptr;
     if (evaluated) {
@@ -790,8 +881,11 @@ void run_quartets(gx_context* ctx, gx_basis* b, const double* B, const double* O
 }
 
 void validate_quartets(const gx_basis* b, const uint32_t* q, int64_t nq) {
-    for (int64_t i = 0; i < 4 * nq; ++i)
-        if (q[i] >= (uint32_t)b->ns) raise(GX_ERANGE, "ERI shell-quartet index is out of range");
+    const uint32_t ns = (uint32_t)b->ns;
+    int bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+    for (int64_t i = 0; i < 4 * nq; ++i) bad |= q[i] >= ns;
+    if (bad) raise(GX_ERANGE, "ERI shell-quartet index is out of range");
 }
 
 std::vector<double> schwarz_values(gx_context* ctx, gx_basis* b, const double* B, const double* O) {
@@ -841,22 +935,61 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         GX_CUDA(cudaSetDevice(ctx->device));
         std::vector<double> q;
         if (screening > 0.0) q = schwarz_values(ctx, b, B, O);
-        std::vector<QuartetRequest> req;
-        req.reserve((size_t)nq);
-        int64_t off = 0, screened = 0;
-        for (int64_t i = 0; i < nq; ++i) {
-            const uint32_t* x = quartets + 4 * i;
-            if (screening > 0.0 &&
-                q[(size_t)x[0] * b->ns + x[1]] * q[(size_t)x[2] * b->ns + x[3]] < screening) {
-                ++screened;
-                continue;
+        auto keep = [&](const uint32_t* x) {
+            return !(screening > 0.0 && q[(size_t)x[0] * b->ns + x[1]] * q[(size_t)x[2] * b->ns + x[3]] < screening);
+        };
+        // pass 1 (parallel over chunks): kept quartets, offsets and the
+        // plan-cache key (per-chunk hashes combined in chunk order)
+        std::vector<int64_t> nao(b->ns);
+        for (int k = 0; k < b->ns; ++k) nao[k] = b->nao_of(k);
+        constexpr int64_t kChunk = 1 << 16;
+        const int64_t nchunk = (nq + kChunk - 1) / kChunk;
+        std::vector<int64_t> ccount(nchunk + 1, 0), centries(nchunk + 1, 0);
+        std::vector<uint64_t> ch1(nchunk), ch2(nchunk);
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < nchunk; ++c) {
+            int64_t n = 0, e = 0;
+            uint64_t a = 0x243F6A8885A308D3ull, z = 0x13198A2E03707344ull;
+            for (int64_t i = c * kChunk; i < std::min(nq, (c + 1) * kChunk); ++i) {
+                const uint32_t* x = quartets + 4 * i;
+                if (!keep(x)) continue;
+                uint64_t v0, v1;
+                std::memcpy(&v0, x, 8);
+                std::memcpy(&v1, x + 2, 8);
+                a = (((a ^ v0) * 0x9E3779B97F4A7C15ull) ^ v1) * 0xBF58476D1CE4E5B9ull;
+                a ^= a >> 31;
+                z = (z + v0 * 0xC2B2AE3D27D4EB4Full + (v1 ^ (uint64_t)n)) * 0x94D049BB133111EBull;
+                z ^= z >> 29;
+                e += nao[x[0]] * nao[x[1]] * nao[x[2]] * nao[x[3]];
+                ++n;
             }
-            if (kept) std::memcpy(kept + 4 * req.size(), x, 4 * sizeof(uint32_t));
-            offsets[req.size()] = off;
-            req.push_back({x[0], x[1], x[2], x[3], off});
-            off += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+            ccount[c + 1] = n;
+            centries[c + 1] = e;
+            ch1[c] = a;
+            ch2[c] = z;
         }
-        offsets[req.size()] = off;
+        uint64_t h1 = 0x452821E638D01377ull, h2 = 0xBE5466CF34E90C6Cull;
+        for (int64_t c = 0; c < nchunk; ++c) {
+            h1 = ((h1 ^ ch1[c]) * 0x9E3779B97F4A7C15ull) ^ (uint64_t)ccount[c + 1];
+            h2 = (h2 + ch2[c] * 0xC2B2AE3D27D4EB4Full) ^ (h2 >> 29);
+            ccount[c + 1] += ccount[c];
+            centries[c + 1] += centries[c];
+        }
+        const int64_t count = ccount[nchunk], off = centries[nchunk];
+#pragma omp parallel for schedule(static)
+        for (int64_t c = 0; c < nchunk; ++c) {
+            int64_t k = ccount[c], o = centries[c];
+            for (int64_t i = c * kChunk; i < std::min(nq, (c + 1) * kChunk); ++i) {
+                const uint32_t* x = quartets + 4 * i;
+                if (!keep(x)) continue;
+                if (kept) std::memcpy(kept + 4 * k, x, 4 * sizeof(uint32_t));
+                offsets[k] = o;
+                o += nao[x[0]] * nao[x[1]] * nao[x[2]] * nao[x[3]];
+                ++k;
+            }
+        }
+        offsets[count] = off;
+        const int64_t screened = nq - count;
         if (off > capacity) raise(GX_ELENGTH, "ERI output buffer is too small");
         double2* dout;
         if (out_is_device) {
@@ -867,14 +1000,46 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         }
         float ms = 0.f;
         int64_t nprim = 0, evaluated[2] = {0, 0};
-        if (!req.empty())
-            run_quartets(ctx, b, B, O, req, dout, &ms, &nprim, precision, mixed_cutoff, stats ? evaluated : nullptr);
+        if (count) {
+            auto& cache = plan_cache(ctx);
+            auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
+                return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == off;
+            });
+            if (hit == cache.end()) {
+                std::vector<QuartetRequest> req;
+                req.reserve((size_t)count);
+                int64_t o = 0;
+                for (int64_t i = 0; i < nq; ++i) {
+                    const uint32_t* x = quartets + 4 * i;
+                    if (!keep(x)) continue;
+                    req.push_back({x[0], x[1], x[2], x[3], o});
+                    o += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+                }
+                auto plan = std::make_unique<PlanData>();
+                build_plan(ctx, b, req, *plan);
+                cache.push_front({b, h1, h2, count, off, std::move(plan)});
+                size_t bytes = 0;
+                int kept_plans = 0;
+                for (auto it = cache.begin(); it != cache.end();) {
+                    bytes += it->plan->tasks.bytes;
+                    if (++kept_plans > 4 || (kept_plans > 1 && bytes > (size_t(2) << 30)))
+                        it = cache.erase(it);
+                    else
+                        ++it;
+                }
+            } else {
+                cache.splice(cache.begin(), cache, hit);  // most recently used first
+            }
+            apply_recorded_tuning(ctx, b, precision, *cache.front().plan);
+            run_plan(ctx, b, B, O, *cache.front().plan, dout, &ms, &nprim, precision, mixed_cutoff,
+                     stats ? evaluated : nullptr);
+        }
         if (!out_is_device && off)
             GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(cudaStreamSynchronize(ctx->stream));
         if (stats) {
             stats->requested = nq;
-            stats->computed = (int64_t)req.size();
+            stats->computed = count;
             stats->screened = screened;
             stats->primitive_quartets = evaluated[0] + evaluated[1];
             stats->fp32_primitive_quartets = evaluated[1];
@@ -975,6 +1140,7 @@ void gx_context_destroy(gx_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    drop_cached_plans(ctx, nullptr);
     ctx->pair_classes.clear();
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
@@ -1023,6 +1189,7 @@ void gx_basis_destroy(gx_basis* b) {
     std::lock_guard<std::mutex> lock(b->ctx->mu);
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
+    drop_cached_plans(b->ctx, b);
     delete b;
 }
 
@@ -1452,6 +1619,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         std::list<std::pair<int64_t, int>> lru;   // raw-column cache, oldest first
         std::map<int64_t, std::list<std::pair<int64_t, int>>::iterator> lru_pos;
         std::vector<double> hostblk;
+        std::map<std::pair<int, int>, std::unique_ptr<PlanData>> column_plans;
         int64_t rank = 0;
         auto residual_at = [&](const std::vector<int64_t>& idx, std::vector<double>& vals) {
             vals.resize(idx.size());
@@ -1543,7 +1711,15 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                         off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
                     }
                 ctx->scratch_a.reserve(off * sizeof(double2));
-                run_quartets(ctx, b, iB, iO, req, ctx->scratch_a.as<double2>(), nullptr);
+                // the column quartet list depends only on the pivot shell pair:
+                // build its plan once per factorisation
+                auto& cplan = column_plans[{sa, sb}];
+                if (!cplan) {
+                    cplan = std::make_unique<PlanData>();
+                    build_plan(ctx, b, req, *cplan);
+                }
+                run_plan(ctx, b, iB, iO, *cplan, ctx->scratch_a.as<double2>(), nullptr, nullptr, GX_PRECISION_FP64,
+                         0.0, nullptr);
                 std::vector<int> cl;
                 std::vector<void*> dst;
                 for (int64_t f : cands) {
@@ -1833,12 +2009,12 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
         const GroupSet& gs = tuned.valid ? tuned.groups : pd.base;
         std::vector<cudaEvent_t> ev(nc + 1);
         for (auto& e : ev) GX_CUDA(cudaEventCreate(&e));
-        std::vector<int> b1(nc), wpb(nc);
+        std::vector<int> b1(nc), wpb(nc), tiles(3 * nc, 0);
         GX_CUDA(cudaEventRecord(ev[0], s));
         for (size_t ci = 0; ci < nc; ++ci) {
             launch_class(ctx, dev, pd, ci, tuned.valid ? tuned.conf[ci] : ClassConf{},
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, &b1[ci],
-                         &wpb[ci]);
+                         &wpb[ci], &tiles[3 * ci]);
             GX_CUDA(cudaEventRecord(ev[ci + 1], s));
         }
         GX_CUDA(cudaEventSynchronize(ev[nc]));
@@ -1863,6 +2039,9 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
             o.warps_per_block = wpb[ci];
             o.batch = b1[ci];
             o.groups = (int64_t)gs.range[ci].second;
+            o.kt = tiles[3 * ci];
+            o.ct = tiles[3 * ci + 1];
+            o.min_blocks = tiles[3 * ci + 2];
         }
         for (auto& e : ev) cudaEventDestroy(e);
         check_status(ctx);
@@ -1905,25 +2084,60 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
                             if (!(per == 32 && w == 4 && b1 == 32)) cands.push_back(ClassConf{per, w, b1});
             }
             double best_ms = 0.0, def_ms = 0.0;
-            for (size_t c = 0; c < cands.size(); ++c) {
-                const auto groups = make_groups(ctx, pd, ci, cands[c]);
+            auto time_conf = [&](const ClassConf& cf) {
+                const auto groups = make_groups(ctx, pd, ci, cf);
                 upload(tmp, groups, s);
                 double t = 1e30;
                 for (int r = 0; r <= repeats; ++r) {  // first launch warms caches
                     GX_CUDA(cudaEventRecord(e0, s));
-                    launch_class(ctx, dev, pd, ci, cands[c], tmp.as<int2>(), (int)groups.size(), nullptr, s);
+                    launch_class(ctx, dev, pd, ci, cf, tmp.as<int2>(), (int)groups.size(), nullptr, s);
                     GX_CUDA(cudaEventRecord(e1, s));
                     GX_CUDA(cudaEventSynchronize(e1));
                     float ms = 0.0f;
                     GX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
                     if (r > 0) t = std::min(t, (double)ms);
                 }
+                return t;
+            };
+            for (size_t c = 0; c < cands.size(); ++c) {
+                const double t = time_conf(cands[c]);
                 if (c == 0) {
                     def_ms = best_ms = t;
                 } else if (t < 0.97 * best_ms) {  // keep the default unless clearly faster
                     best_ms = t;
                     best[ci] = cands[c];
                 }
+            }
+            if (!gx::small_class(k[0], k[1], k[2], k[3])) {
+                // second stage: transform tiles under the chosen work split
+                const int ncd = ctx->pair_class(k[2], k[3]).nab;
+                for (int kt : {1, 2, 4})
+                    for (int ct : {1, 2, 3, 4}) {
+                        if (ncd % ct) continue;
+                        ClassConf cf = best[ci];
+                        cf.kt = kt;
+                        cf.ct = ct;
+                        const double t = time_conf(cf);
+                        if (t < 0.97 * best_ms) {
+                            best_ms = t;
+                            best[ci] = cf;
+                        }
+                    }
+                // third stage: the kernel variant with half the registers and
+                // twice the resident warps, with and without smaller units
+                const ClassConf base = best[ci];
+                for (int per : {0, 16, 32, 64})
+                    for (int b1 : {0, 16}) {
+                        ClassConf cf = base;
+                        cf.minb = 4;
+                        if (per) cf.per_group = per;
+                        if (b1) cf.b1 = b1;
+                        const double t = time_conf(cf);
+                        if (t < 0.97 * best_ms) {
+                            best_ms = t;
+                            best[ci] = cf;
+                        }
+                    }
             }
             tot_default += def_ms;
             tot_best += best_ms;
@@ -1935,6 +2149,7 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
         make_group_set(ctx, pd, best, tuned.groups);
         tuned.conf = best;
         tuned.valid = true;
+        record_tuning(ctx, plan->basis, precision, pd, best);
         GX_CUDA(cudaStreamSynchronize(s));
         ++plan->generation;
         plan->graph.reset();

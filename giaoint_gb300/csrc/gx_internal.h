@@ -78,6 +78,7 @@ struct QuartetClass {
     int B1, CH;            // phase-1 batch (primitive quartets), ket-component chunk
     int nchunk;            // ket chunks per task group, run by separate warps
     int coop;              // batches of at most this many entries use the warp-cooperative recurrence
+    int minb;              // register budget variant of the kernel: 2 or 4 resident blocks
     int KT, CT;            // Hermite rows per lane in the ket transform, ket components per lane in the bra transform
     int ntask;
     const Task* tasks;

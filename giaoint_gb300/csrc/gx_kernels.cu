@@ -509,6 +509,9 @@ __device__ __forceinline__ void hermite_rec(int L, const T* seed, const T* X, T*
 // Per-warp shared layout of quartet_kernel (all offsets in bytes).  R holds
 // B1 + 1 columns (the last one is the cooperative recurrence's second
 // buffer); `seed` holds one entry's seeds and X' for the cooperative path.
+// The FP32 table R32 of the mixed-precision pass shares R's memory: a batch
+// of that pass is either FP32 (R32) or, for its deferred FP64 fallbacks,
+// FP64 (R) after the FP32 part is consumed.
 struct WarpSmem {
     size_t R, W, R32, W32, queue, flag, eoff, seed, total;
 };
@@ -517,8 +520,8 @@ __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, b
     const size_t B1p = B1 + 1;
     w.R = 0;
     w.W = w.R + (size_t)NL * B1p * 16;
-    w.R32 = w.W + (size_t)Nab * CH * 16;
-    w.W32 = w.R32 + (mixed ? (((size_t)NL * B1p * 8 + 15) / 16) * 16 : 0);
+    w.R32 = w.R;
+    w.W32 = w.W + (size_t)Nab * CH * 16;
     w.queue = w.W32 + (mixed ? (((size_t)Nab * CH * 8 + 15) / 16) * 16 : 0);
     w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
     w.eoff = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
@@ -649,6 +652,7 @@ __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const uint32_
                 const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
                 const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
                 const bool neg = (k2 + l2 + m2) & 1;
+                if (flag[jj] == 2) continue;  // deferred: evaluated in FP64 after the batch
                 if (flag[jj]) {
                     double2 ev = __ldg(&pp.Epool[eoff[jj] + bo + e]);
                     if (neg) ev = c2(-ev.x, -ev.y);
@@ -787,10 +791,11 @@ __device__ __forceinline__ void step_b_any(const EriDev& d, const QuartetClass& 
 }
 
 // Seeds of primitive quartet (ip, iq) for pass `pass`: returns 1 (FP64 seeds
-// in Sh), 0 (FP32 seeds in S32) or 2 (FP32 pass falling back to FP64, seeds
-// in Sh).  Pass 0 is FP64; in pass 1 (FP32 quartets) the Boys function runs
-// in FP32 in its asymptotic sector and in FP64 elsewhere, and the seeds go to
-// the FP32 recurrence when they fit its range.
+// in Sh), 0 (FP32 seeds in S32) or 2 (FP32 pass, seeds outside the FP32
+// range: the quartet is deferred to FP64 after the batch).  Pass 0 is FP64;
+// in pass 1 (FP32 quartets) the Boys function runs in FP32 in its asymptotic
+// sector and in FP64 elsewhere, and the seeds go to the FP32 recurrence when
+// they fit its range.
 __device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int pass, const QuartetArgs& qa, double2* Sh,
                                            float2* S32, long long item) {
     if (pass == 0) {
@@ -807,7 +812,11 @@ __device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int pass, con
     return ok ? 0 : 2;
 }
 
-__global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass qc) {
+// MINB: blocks of 128 threads the register budget must leave room for (2:
+// up to 255 registers per thread, no spills; 4: 128 registers, a few spills,
+// twice the resident warps); the autotuner picks per class.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetClass qc) {
     extern __shared__ double2 sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
@@ -845,6 +854,7 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
     for (int unit = blockIdx.x * wpb + wib; unit < nunit; unit += gridDim.x * wpb) {
         const int grp = unit / qc.nchunk;
         const int c0 = (unit - grp * qc.nchunk) * qc.CH;
+        const unsigned first_chunk = c0 == 0;
         const int chn = min(qc.CH, ncd - c0);
         const int2 gi = qc.groups[grp];
         const Task t0 = qc.tasks[gi.x];
@@ -916,24 +926,24 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
                             double2 Sh[BOYS_MAX_ORDER + 1];
                             float2 S32[BOYS_MAX_ORDER + 1];
                             const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
-                            if (f) {
+                            if (f == 1) {
                                 for (int n = 0; n <= qc.L; ++n) sseed[n] = Sh[n];
                                 for (int x = 0; x < 3; ++x) sseed[qc.L + 1 + x] = qa.X[x];
-                                ++cnt64;
-                            } else {
+                                cnt64 += first_chunk;
+                            } else if (f == 0) {
                                 float2* s32 = reinterpret_cast<float2*>(sseed);
                                 for (int n = 0; n <= qc.L; ++n) s32[n] = S32[n];
                                 for (int x = 0; x < 3; ++x)
                                     s32[qc.L + 1 + x] = make_float2((float)qa.X[x].x, (float)qa.X[x].y);
-                                ++cnt32;
+                                cnt32 += first_chunk;
                             }
                             flag[j] = f;
                             eoff[j] = pp.Eoff[iq];
                         }
                         __syncwarp();
-                        if (flag[j]) {
+                        if (flag[j] == 1) {
                             coop_rec<double2>(qc.L, sseed, sseed + qc.L + 1, R, B1p, j, qc.B1, d.herm_xyz, lane);
-                        } else {
+                        } else if (flag[j] == 0) {
                             const float2* s32 = reinterpret_cast<const float2*>(sseed);
                             coop_rec<float2>(qc.L, s32, s32 + qc.L + 1, R32, B1p, j, qc.B1, d.herm_xyz, lane);
                         }
@@ -949,15 +959,15 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
                     double2 Sh[BOYS_MAX_ORDER + 1];
                     float2 S32[BOYS_MAX_ORDER + 1];
                     const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
-                    if (f) {
+                    if (f == 1) {
                         hermite_rec<double2>(qc.L, Sh, qa.X, R + lane, B1p);
-                        ++cnt64;
-                    } else {
+                        cnt64 += first_chunk;
+                    } else if (f == 0) {
                         const float2 X32[3] = {make_float2((float)qa.X[0].x, (float)qa.X[0].y),
                                                make_float2((float)qa.X[1].x, (float)qa.X[1].y),
                                                make_float2((float)qa.X[2].x, (float)qa.X[2].y)};
                         hermite_rec<float2>(qc.L, S32, X32, R32 + lane, B1p);
-                        ++cnt32;
+                        cnt32 += first_chunk;
                     }
                     flag[lane] = f;
                     eoff[lane] = pp.Eoff[iq];
@@ -987,7 +997,7 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
                     }
                     bool has64 = false, has32 = false;
                     for (int jj = j0; jj < j1; ++jj) {
-                        has64 = has64 || flag[jj] != 0;
+                        has64 = has64 || flag[jj] == 1;
                         has32 = has32 || flag[jj] == 0;
                     }
                     step_k_any(qc, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn,
@@ -995,6 +1005,47 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
                     any64 = any64 || has64;
                     any32 = any32 || has32;
                     j0 = j1;
+                }
+                // Deferred FP64 fallbacks of the FP32 pass: the batch's FP32
+                // columns are consumed, so R (sharing their memory) takes the
+                // fallbacks' FP64 tables; each is contracted and added to the
+                // output on its own, through W, which the FP32 pass leaves
+                // unused.
+                if (__any_sync(0xffffffffu, lane < nb && flag[lane] == 2)) {
+                    __syncwarp();
+                    if (lane < nb && flag[lane] == 2) {
+                        const int idx = queue[lane];
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                        const QuartetArgs qa = quartet_args(pp, ip, iq);
+                        double2 Sh[BOYS_MAX_ORDER + 1];
+                        quartet_seeds_rt(d, qc.L, qa, Sh, gi.x + g);
+                        hermite_rec<double2>(qc.L, Sh, qa.X, R + lane, B1p);
+                        flag[lane] = 1;
+                        cnt64 += first_chunk;
+                    } else if (lane < nb) {
+                        flag[lane] = 3;  // consumed FP32 entry
+                    }
+                    __syncwarp();
+                    for (int j = 0; j < nb; ++j) {
+                        if (flag[j] != 1) continue;
+                        for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
+                        __syncwarp();
+                        step_k_any(qc, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j, j + 1, true, false, W, W32, c0,
+                                   chn, lane);
+                        __syncwarp();
+                        const int key = queue[j] / Kcd;
+                        const int cg = key / Kab, cP = key - cg * Kab;
+                        const Task tc = qc.tasks[gi.x + cg];
+                        step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, true, false,
+                                   c0, chn, lane);
+                        __syncwarp();
+                    }
+                    for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
+                    __syncwarp();
                 }
             }
             if (cur >= 0) {
@@ -1008,6 +1059,7 @@ __global__ void __launch_bounds__(128, 2) quartet_kernel(EriDev d, QuartetClass 
         }
     }
     if (d.counters) {
+        // each primitive quartet is counted once, by the warps of chunk 0
         const unsigned long long a64 = __reduce_add_sync(0xffffffffu, (unsigned)cnt64);
         const unsigned long long a32 = __reduce_add_sync(0xffffffffu, (unsigned)cnt32);
         if (lane == 0) {
@@ -1034,13 +1086,20 @@ cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps
         g_const_ready = true;
     }
     const size_t smem = quartet_smem_bytes(qc, warps_per_block, dev.fp32_cut > 0.0f);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(quartet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static size_t configured[2] = {0, 0};
+    const int v = qc.minb == 4 ? 1 : 0;
+    if (smem > 48 * 1024 && smem > configured[v]) {
+        cudaError_t e = v ? cudaFuncSetAttribute(quartet_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem)
+                          : cudaFuncSetAttribute(quartet_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)smem);
         if (e != cudaSuccess) return e;
-        configured = smem;
+        configured[v] = smem;
     }
-    quartet_kernel<<<grid, warps_per_block * 32, smem, s>>>(dev, qc);
+    if (v)
+        quartet_kernel<4><<<grid, warps_per_block * 32, smem, s>>>(dev, qc);
+    else
+        quartet_kernel<2><<<grid, warps_per_block * 32, smem, s>>>(dev, qc);
     return cudaGetLastError();
 }
 

@@ -134,3 +134,42 @@ class EriPlan:
             self.close()
         except Exception:
             pass
+
+
+def _main(argv=None) -> None:
+    """Evaluate one (la, lb, lc, ld) class of the seeded synthetic molecule
+    through a plan, once per precision mode, and print the counts: a small,
+    self-contained workload for profiling one kernel launch per mode.
+
+        python -m giaoint_gb300.plan --atoms 12 --class 1111 --precision fp64,mixed
+    """
+    import argparse
+
+    import torch
+
+    from . import synthetic as syn
+    from ._types import Shell
+
+    p = argparse.ArgumentParser(prog="python -m giaoint_gb300.plan")
+    p.add_argument("--atoms", type=int, default=12)
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--class", dest="cls", default="1111", help="four digits la lb lc ld")
+    p.add_argument("--precision", default="fp64,mixed")
+    a = p.parse_args(argv)
+    key = tuple(int(c) for c in a.cls)
+    recs = syn.random_molecule(a.seed, natoms=a.atoms)
+    basis = Basis([Shell.from_record(r) for r in recs])
+    ls = np.array([r.angular_momentum for r in recs])
+    q = canonical_quartets(len(recs))
+    sel = q[np.all(ls[q.astype(np.int64)] == np.array(key), axis=1)]
+    plan = EriPlan(basis, sel)
+    out = torch.empty(max(plan.total, 1), dtype=torch.complex128, device="cuda:0")
+    field = MagneticField(syn.random_field(a.seed))
+    for prec in a.precision.split(","):
+        plan.execute(out, field, precision=prec)
+        plan.synchronize()
+        print(prec, {"class": key, "quartets": len(sel), **plan.counts()}, flush=True)
+
+
+if __name__ == "__main__":
+    _main()

@@ -239,6 +239,8 @@ typedef struct gx_class_profile {
     int per_group;                 /* launch configuration: primitive quartets per warp unit (0 = default) */
     int warps_per_block, batch;    /* generic kernel: warps per block, phase-1 batch */
     int64_t groups;                /* warp work units */
+    int kt, ct;                    /* generic kernel: ket-transform rows and bra-transform components per lane */
+    int min_blocks;                /* generic kernel: register-budget variant (resident blocks) */
 } gx_class_profile;
 int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                         void* out_device, gx_class_profile* out);
