@@ -178,7 +178,7 @@ struct gx_context {
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     double boys_table_agreement = 0.0;
-    DeviceBuffer boys_S, boys_E0, gl, herm, status;
+    DeviceBuffer boys_S, boys_E0, gl, herm, rec_plan, rec_plan_off, status;
     std::mutex mu;
     std::map<std::pair<int, int>, std::unique_ptr<PairClassHost>> pair_classes;
     // scratch
@@ -409,6 +409,8 @@ FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
     dev.boys = b->ctx->boys();
     dev.gl = b->ctx->gl.as<gx::GLRules>();
     dev.herm_xyz = b->ctx->herm.as<uint32_t>();
+    dev.rec_plan = b->ctx->rec_plan.as<int2>();
+    dev.rec_plan_off = b->ctx->rec_plan_off.as<int>();
     GX_CUDA(gx::launch_pair_precompute(b->dev(), B, O, b->npp, b->d_pp_a.as<int>(), b->d_pp_b.as<int>(),
                                        b->d_pp_pa.as<int>(), b->d_pp_pb.as<int>(), b->d_pp_class.as<int>(),
                                        b->d_classes.as<gx::PairClassDev>(), fp.p.as<double>(), fp.Pr.as<double>(),
@@ -562,7 +564,7 @@ void record_tuning(const gx_context* ctx, const gx_basis* b, int precision, cons
 // (Kab, Kcd).  Small classes (one lane per primitive quartet) take up to
 // `per_group` (default 1024) primitive quartets and 128 tasks per unit; the
 // generic kernel about `per_group` (default 32) primitive quartets and at
-// most 128 tasks per unit, fewer tasks when the class is too small to give
+// most 1024 tasks per unit, fewer tasks when the class is too small to give
 // every SM eight warps.
 std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_t ci, const ClassConf& conf) {
     const PlanClass& pc = plan.classes[ci];
@@ -576,7 +578,7 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
         const int kk_code = plan.task_kk[i];
         const int kk = (kk_code >> 16) * (kk_code & 0xffff);
         const int want = small ? std::max(1, std::min(128, per / kk))
-                               : std::max(1, std::min({128, (per + kk - 1) / kk, spread}));
+                               : std::max(1, std::min({1024, (per + kk - 1) / kk, spread}));
         size_t j = i + 1;
         while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
         groups.push_back(make_int2((int)(i - pc.first), (int)(j - i)));
@@ -698,6 +700,8 @@ gx::EriDev make_dev(gx_context* ctx, gx_basis* b, FieldPairs& fp, double2* out, 
     dev.boys = ctx->boys();
     dev.gl = ctx->gl.as<gx::GLRules>();
     dev.herm_xyz = ctx->herm.as<uint32_t>();
+    dev.rec_plan = ctx->rec_plan.as<int2>();
+    dev.rec_plan_off = ctx->rec_plan_off.as<int>();
     dev.out = out;
     dev.status = ctx->status.as<gx::DevStatus>();
     return dev;
@@ -1116,6 +1120,36 @@ int gx_context_create(int device, gx_context** out) {
                     herm[gx::herm_index(k, l, m)] = (uint32_t)(k | (l << 8) | (m << 16));
                 }
         upload(ctx->herm, herm, ctx->stream);
+        {
+            std::vector<int2> plan;
+            std::vector<int> off{0, 0};  // L = 0 has no steps
+            for (int L = 1; L <= gx::REC_PLAN_MAX; ++L) {
+                for (int n = L - 1; n >= 0; --n) {
+                    for (int dg = L - n; dg >= 1; --dg)
+                        for (int k = dg; k >= 0; --k)
+                            for (int l = dg - k; l >= 0; --l) {
+                                const int m = dg - k - l;
+                                int axis, pw, i1, i2;
+                                if (k > 0) {
+                                    axis = 0, pw = k, i1 = gx::herm_index(k - 1, l, m);
+                                    i2 = k > 1 ? gx::herm_index(k - 2, l, m) : 0;
+                                } else if (l > 0) {
+                                    axis = 1, pw = l, i1 = gx::herm_index(0, l - 1, m);
+                                    i2 = l > 1 ? gx::herm_index(0, l - 2, m) : 0;
+                                } else {
+                                    axis = 2, pw = m, i1 = gx::herm_index(0, 0, m - 1);
+                                    i2 = m > 1 ? gx::herm_index(0, 0, m - 2) : 0;
+                                }
+                                plan.push_back(make_int2(gx::herm_index(k, l, m) | (i1 << 16),
+                                                         i2 | (axis << 14) | ((pw - 1) << 16)));
+                            }
+                    plan.push_back(make_int2(0, (1 << 22) | (n << 23)));
+                }
+                off.push_back((int)plan.size());
+            }
+            upload(ctx->rec_plan, plan, ctx->stream);
+            upload(ctx->rec_plan_off, off, ctx->stream);
+        }
         ctx->status.reserve(sizeof(gx::DevStatus));
         const size_t npts = (size_t)gx::BOYS_NX * gx::BOYS_NY;
         ctx->boys_S.reserve(npts * gx::BOYS_TABLE_ORDERS * sizeof(double2));
@@ -2078,7 +2112,7 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
             if (gx::small_class(k[0], k[1], k[2], k[3])) {
                 for (int per : {256, 4096}) cands.push_back(ClassConf{per, 0, 0});
             } else {
-                for (int per : {16, 32, 64, 128, 256})
+                for (int per : {16, 32, 64, 128, 256, 512, 1024})
                     for (int w : {2, 4})
                         for (int b1 : {16, 32})
                             if (!(per == 32 && w == 4 && b1 == 32)) cands.push_back(ClassConf{per, w, b1});

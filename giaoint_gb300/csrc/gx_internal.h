@@ -92,6 +92,8 @@ struct EriDev {
     BoysTable boys;
     const GLRules* gl;
     const uint32_t* herm_xyz;  // packed (k, l, m) of herm index, L <= 32
+    const int2* rec_plan;      // Hermite recurrence steps of every L <= REC_PLAN_MAX (see rec_plan_entry)
+    const int* rec_plan_off;   // [REC_PLAN_MAX + 2] first step of each L
     double2* out;
     DevStatus* status;
     float skip_cut;   // primitive quartets with bound product below this are skipped
@@ -100,6 +102,15 @@ struct EriDev {
                       // sector and FP64 ones elsewhere, then the FP32 recurrence.
     unsigned long long* counters;  // [0] FP64, [1] FP32 primitive quartets evaluated (may be null)
 };
+
+// In-place descending-level Hermite recurrence as a step list per total order
+// L (the order of hermite_rec): for n = L-1 .. 0, every multi-index of total
+// degree d = L-n .. 1 (x-major), then the seed of level n.  A step is
+//   x = dst | s1 << 16,
+//   y = s2 | axis << 14 | coef << 16 | seed << 22 | n << 23,
+// meaning col[dst] = X[axis] col[s1] + coef col[s2] (coef = power - 1, 0: no
+// second term), or col[0] = seed[n] when the seed bit is set.
+constexpr int REC_PLAN_MAX = 16;
 
 // ---- launch wrappers (gx_kernels.cu) -------------------------------------
 

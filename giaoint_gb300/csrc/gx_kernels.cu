@@ -506,6 +506,38 @@ __device__ __forceinline__ void hermite_rec(int L, const T* seed, const T* X, T*
     }
 }
 
+// The same recurrence driven by the precomputed step list of order L (every
+// lane reads the same step: one broadcast load instead of the index
+// arithmetic of the nested loops).
+template <typename T>
+__device__ __forceinline__ void hermite_rec_plan(const int2* plan, int nsteps, int L, const T* seed, const T* X, T* col,
+                                                 int stride) {
+    col[0] = seed[L];
+    for (int i = 0; i < nsteps; ++i) {
+        const int2 st = __ldg(&plan[i]);
+        if (st.y & (1 << 22)) {
+            col[0] = seed[(st.y >> 23) & 63];
+            continue;
+        }
+        const int dst = st.x & 0xffff, s1 = (st.x >> 16) & 0xffff;
+        const int s2 = st.y & 0x3fff, axis = (st.y >> 14) & 3, coef = (st.y >> 16) & 63;
+        const T xa = axis == 0 ? X[0] : (axis == 1 ? X[1] : X[2]);
+        T v = tmul(xa, col[s1 * stride]);
+        if (coef > 0) v = tmacr(v, coef, col[s2 * stride]);
+        col[dst * stride] = v;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void hermite_rec_any(const EriDev& d, int L, const T* seed, const T* X, T* col, int stride) {
+    if (L >= 1 && L <= REC_PLAN_MAX) {
+        const int o = d.rec_plan_off[L];
+        hermite_rec_plan<T>(d.rec_plan + o, d.rec_plan_off[L + 1] - o, L, seed, X, col, stride);
+    } else {
+        hermite_rec<T>(L, seed, X, col, stride);
+    }
+}
+
 // Per-warp shared layout of quartet_kernel (all offsets in bytes).  R holds
 // B1 + 1 columns (the last one is the cooperative recurrence's second
 // buffer); `seed` holds one entry's seeds and X' for the cooperative path.
@@ -604,9 +636,11 @@ __device__ __forceinline__ float2 group_sum(float2 v, int J) {
 // pair) into W (FP64 entries) and W32 (FP32 entries):
 //   W[K][cd] += sum_j sum_{K' in box(cd)} (-1)^{|K'|} E~cd_j[K'] Rh_j[K + K'].
 // A work item is KT consecutive Hermite rows K of one ket component cd (KT
-// independent accumulators); its (entry, box entry) terms are split over the
-// item's J lanes and summed by a butterfly.  eoff[j]: E~ record of the
-// entry's ket pair; flag[j]: 0 FP32, else FP64.
+// independent accumulators).  The item's box entries are split over its J
+// lanes; for each box entry the R row indices are formed once and reused for
+// every entry of the run, so the per-term work is one coefficient load, KT
+// table loads and KT complex FMAs.  eoff[j]: E~ record of the entry's ket
+// pair; flag[j]: 0 FP32, 1 FP64, 2 deferred (skipped here).
 template <int KT>
 __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const uint32_t* herm_xyz, const PairData& pp,
                                            const double2* R, const float2* R32, int B1p, const int* flag,
@@ -644,27 +678,30 @@ __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const uint32_
             const int bo = qc.ket.boxoff[cd];
             const int bd = qc.ket.boxdim[cd];
             const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-            const int tot = (j1 - j0) * nbox;
-            for (int t = sub; t < tot; t += J) {
-                const int jr = t / nbox;
-                const int e = t - jr * nbox;
-                const int jj = j0 + jr;
+            for (int e = sub; e < nbox; e += J) {
                 const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
                 const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
                 const bool neg = (k2 + l2 + m2) & 1;
-                if (flag[jj] == 2) continue;  // deferred: evaluated in FP64 after the batch
-                if (flag[jj]) {
-                    double2 ev = __ldg(&pp.Epool[eoff[jj] + bo + e]);
-                    if (neg) ev = c2(-ev.x, -ev.y);
+                int ridx[KT];
 #pragma unroll
-                    for (int u = 0; u < KT; ++u)
-                        a64[u] = cmac(a64[u], ev, R[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
-                } else {
-                    float2 ev = __ldg(&pp.Epool32[eoff[jj] + bo + e]);
-                    if (neg) ev = make_float2(-ev.x, -ev.y);
+                for (int u = 0; u < KT; ++u) ridx[u] = herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p;
+                if (has64) {
+                    for (int jj = j0; jj < j1; ++jj) {
+                        if (flag[jj] != 1) continue;
+                        double2 ev = __ldg(&pp.Epool[eoff[jj] + bo + e]);
+                        if (neg) ev = c2(-ev.x, -ev.y);
 #pragma unroll
-                    for (int u = 0; u < KT; ++u)
-                        a32[u] = tmac(a32[u], ev, R32[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                        for (int u = 0; u < KT; ++u) a64[u] = cmac(a64[u], ev, R[ridx[u] + jj]);
+                    }
+                }
+                if (has32) {
+                    for (int jj = j0; jj < j1; ++jj) {
+                        if (flag[jj] != 0) continue;
+                        float2 ev = __ldg(&pp.Epool32[eoff[jj] + bo + e]);
+                        if (neg) ev = make_float2(-ev.x, -ev.y);
+#pragma unroll
+                        for (int u = 0; u < KT; ++u) a32[u] = tmac(a32[u], ev, R32[ridx[u] + jj]);
+                    }
                 }
             }
         }
@@ -960,13 +997,13 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                     float2 S32[BOYS_MAX_ORDER + 1];
                     const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
                     if (f == 1) {
-                        hermite_rec<double2>(qc.L, Sh, qa.X, R + lane, B1p);
+                        hermite_rec_any<double2>(d, qc.L, Sh, qa.X, R + lane, B1p);
                         cnt64 += first_chunk;
                     } else if (f == 0) {
                         const float2 X32[3] = {make_float2((float)qa.X[0].x, (float)qa.X[0].y),
                                                make_float2((float)qa.X[1].x, (float)qa.X[1].y),
                                                make_float2((float)qa.X[2].x, (float)qa.X[2].y)};
-                        hermite_rec<float2>(qc.L, S32, X32, R32 + lane, B1p);
+                        hermite_rec_any<float2>(d, qc.L, S32, X32, R32 + lane, B1p);
                         cnt32 += first_chunk;
                     }
                     flag[lane] = f;
@@ -1023,7 +1060,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         const QuartetArgs qa = quartet_args(pp, ip, iq);
                         double2 Sh[BOYS_MAX_ORDER + 1];
                         quartet_seeds_rt(d, qc.L, qa, Sh, gi.x + g);
-                        hermite_rec<double2>(qc.L, Sh, qa.X, R + lane, B1p);
+                        hermite_rec_any<double2>(d, qc.L, Sh, qa.X, R + lane, B1p);
                         flag[lane] = 1;
                         cnt64 += first_chunk;
                     } else if (lane < nb) {
