@@ -470,6 +470,7 @@ struct ClassConf {
     int kt = 0;         // generic kernel: Hermite rows per lane in the ket transform (1, 2, 4; 0 = by lane use)
     int ct = 0;         // generic kernel: ket components per lane in the bra transform (1-4; 0 = by lane use)
     int minb = 0;       // generic kernel: register-budget variant (2 or 4 resident blocks; 0 = 2)
+    int nostage = 0;    // generic kernel: 1 = read E~ records and class tables from global memory
 };
 
 // Warp work units of every class: (first task within the class, task count).
@@ -798,6 +799,14 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     qc.ngroup = ngroup;
     qc.groups = groups;
     qc.minb = conf.minb == 4 ? 4 : 2;
+    // stage E~ records per warp and the class tables per block when small
+    {
+        const int emax = std::max(qc.ket.Etot, qc.bra.Etot);
+        qc.stage_e = emax <= 384 && !conf.nostage ? emax : 0;
+        const int words = 2 * qc.ket.nab + qc.ket.Etot + 2 * qc.bra.nab + qc.bra.Etot +
+                          qc.Nab * gx::herm_count(k[2] + k[3]);
+        qc.tab_words = words <= 4096 && !conf.nostage ? words : 0;
+    }
     const size_t per_warp = gx::quartet_smem_bytes(qc, 1, dev.fp32_cut > 0.0f);
     const int cap = conf.wpb > 0 ? std::min(4, conf.wpb) : 4;
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(cap, (200 * 1024) / per_warp));
@@ -2159,6 +2168,15 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
                     }
                 // third stage: the kernel variant with half the registers and
                 // twice the resident warps, with and without smaller units
+                {
+                    ClassConf cf = best[ci];
+                    cf.nostage = 1;
+                    const double t = time_conf(cf);
+                    if (t < 0.97 * best_ms) {
+                        best_ms = t;
+                        best[ci] = cf;
+                    }
+                }
                 const ClassConf base = best[ci];
                 for (int per : {0, 16, 32, 64})
                     for (int b1 : {0, 16}) {

@@ -79,6 +79,8 @@ struct QuartetClass {
     int nchunk;            // ket chunks per task group, run by separate warps
     int coop;              // batches of at most this many entries use the warp-cooperative recurrence
     int minb;              // register budget variant of the kernel: 2 or 4 resident blocks
+    int stage_e;           // words (complex) of the per-warp E~ staging buffer (0: read E~ from global memory)
+    int tab_words;         // 32-bit words of the block-shared class tables (0: read them from global memory)
     int KT, CT;            // Hermite rows per lane in the ket transform, ket components per lane in the bra transform
     int ntask;
     const Task* tasks;

@@ -545,9 +545,9 @@ __device__ __forceinline__ void hermite_rec_any(const EriDev& d, int L, const T*
 // of that pass is either FP32 (R32) or, for its deferred FP64 fallbacks,
 // FP64 (R) after the FP32 part is consumed.
 struct WarpSmem {
-    size_t R, W, R32, W32, queue, flag, eoff, seed, total;
+    size_t R, W, R32, W32, queue, flag, eoff, seed, stage, total;
 };
-__host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed) {
+__host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed, int stage_e) {
     WarpSmem w;
     const size_t B1p = B1 + 1;
     w.R = 0;
@@ -558,9 +558,30 @@ __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, b
     w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
     w.eoff = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
     w.seed = w.eoff + (((size_t)B1 * 8 + 15) / 16) * 16;
-    w.total = w.seed + (size_t)(BOYS_MAX_ORDER + 1 + 3) * 16;
+    w.stage = w.seed + (size_t)(BOYS_MAX_ORDER + 1 + 3) * 16;
+    // FP64 record (16 B per word) followed by its FP32 copy (8 B per word)
+    w.total = w.stage + (((size_t)stage_e * 24 + 15) / 16) * 16;
     return w;
 }
+
+// Block-shared class tables (32-bit words): ket boxoff[ncd], ket
+// boxdim[ncd], ket box entries as Hermite indices with the (-1)^{|K'|} sign in
+// bit 16 [Etot_ket], bra boxoff[nab], bra boxdim[nab], bra box entries as
+// Hermite indices [Etot_bra], and hsum[K][K'] = index of K + K' for every bra
+// row K < Nab and ket row K' < herm_count(Lcd).
+__host__ __device__ inline int class_tab_words(const QuartetClass& qc) {
+    return 2 * qc.ket.nab + qc.ket.Etot + 2 * qc.bra.nab + qc.bra.Etot + qc.Nab * herm_count(qc.ket.Lab);
+}
+struct ClassTabs {
+    const int* kbo;
+    const int* kbd;
+    const uint32_t* kh;
+    const int* bbo;
+    const int* bbd;
+    const uint32_t* bh;
+    const int* hsum;
+    int ncdh;
+};
 
 // Warp-cooperative Hermite recurrence of one primitive quartet: level n
 // (entries of total degree <= L - n) from level n + 1, all entries of a
@@ -635,124 +656,180 @@ __device__ __forceinline__ float2 group_sum(float2 v, int J) {
 // Ket transform of the batch entries j0..j1-1 (one run with the same bra
 // pair) into W (FP64 entries) and W32 (FP32 entries):
 //   W[K][cd] += sum_j sum_{K' in box(cd)} (-1)^{|K'|} E~cd_j[K'] Rh_j[K + K'].
-// A work item is KT consecutive Hermite rows K of one ket component cd (KT
-// independent accumulators).  The item's box entries are split over its J
-// lanes; for each box entry the R row indices are formed once and reused for
-// every entry of the run, so the per-term work is one coefficient load, KT
-// table loads and KT complex FMAs.  eoff[j]: E~ record of the entry's ket
+// Entry by entry, the warp first copies the entry's ket E~ record into its
+// staging buffer with one coalesced load (stg; null: read it from global
+// memory), then every work item -- KT consecutive Hermite rows K of one ket
+// component cd, its box entries split over the item's J lanes -- contracts
+// it against the entry's R column.  eoff[j]: E~ record of the entry's ket
 // pair; flag[j]: 0 FP32, 1 FP64, 2 deferred (skipped here).
 template <int KT>
-__device__ __forceinline__ void step_k_run(const QuartetClass& qc, const uint32_t* herm_xyz, const PairData& pp,
-                                           const double2* R, const float2* R32, int B1p, const int* flag,
-                                           const long long* eoff, int j0, int j1, bool has64, bool has32,
-                                           double2* W, float2* W32, int c0, int chn, int lane) {
+__device__ __forceinline__ void step_k_run(const QuartetClass& qc, const ClassTabs& tb, const uint32_t* herm_xyz,
+                                           const PairData& pp, const double2* R, const float2* R32, int B1p,
+                                           const int* flag, const long long* eoff, int j0, int j1, double2* W,
+                                           float2* W32, double2* stg, int c0, int chn, int lane) {
     const int nkb = (qc.Nab + KT - 1) / KT;
     const int I = nkb * chn;
     const int J = lanes_per_item(I);
     const int rounds = (I * J + 31) / 32;
-    for (int rd = 0; rd < rounds; ++rd) {
-        const int slot = rd * 32 + lane;
-        const int it = slot / J, sub = slot - it * J;
-        const bool act = it < I;
-        double2 a64[KT];
-        float2 a32[KT];
-#pragma unroll
-        for (int u = 0; u < KT; ++u) {
-            a64[u] = c2(0.0, 0.0);
-            a32[u] = make_float2(0.0f, 0.0f);
+    float2* stg32 = reinterpret_cast<float2*>(stg + qc.stage_e);
+    for (int jj = j0; jj < j1; ++jj) {
+        const int f = flag[jj];
+        if (f == 2) continue;  // deferred: evaluated in FP64 after the batch
+        const bool is64 = f == 1;
+        const double2* E64 = pp.Epool + eoff[jj];
+        const float2* E32 = pp.Epool32 + eoff[jj];
+        if (stg) {
+            if (is64)
+                for (int i = lane; i < qc.ket.Etot; i += 32) stg[i] = __ldg(&E64[i]);
+            else
+                for (int i = lane; i < qc.ket.Etot; i += 32) stg32[i] = __ldg(&E32[i]);
+            __syncwarp();
+            E64 = stg;
+            E32 = stg32;
         }
-        int kb = 0, cdl = 0;
-        if (act) {
-            kb = it / chn;
-            cdl = it - kb * chn;
-            const int cd = c0 + cdl;
-            int bk[KT], bl[KT], bm[KT];
+        for (int rd = 0; rd < rounds; ++rd) {
+            const int slot = rd * 32 + lane;
+            const int it = slot / J, sub = slot - it * J;
+            const bool act = it < I;
+            double2 a64[KT];
+            float2 a32[KT];
 #pragma unroll
             for (int u = 0; u < KT; ++u) {
-                const int K = kb * KT + u;
-                const uint32_t kx = __ldg(&herm_xyz[K < qc.Nab ? K : 0]);
-                bk[u] = kx & 255;
-                bl[u] = (kx >> 8) & 255;
-                bm[u] = (kx >> 16) & 255;
+                a64[u] = c2(0.0, 0.0);
+                a32[u] = make_float2(0.0f, 0.0f);
             }
-            const int bo = qc.ket.boxoff[cd];
-            const int bd = qc.ket.boxdim[cd];
-            const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
-            for (int e = sub; e < nbox; e += J) {
-                const uint32_t ke = __ldg(&qc.ket.ent[bo + e]);
-                const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
-                const bool neg = (k2 + l2 + m2) & 1;
-                int ridx[KT];
+            int kb = 0, cdl = 0;
+            if (act && tb.hsum) {
+                // table path: R row of (K, K') = hsum[K][K']
+                kb = it / chn;
+                cdl = it - kb * chn;
+                const int cd = c0 + cdl;
+                int hb[KT];
 #pragma unroll
-                for (int u = 0; u < KT; ++u) ridx[u] = herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p;
-                if (has64) {
-                    for (int jj = j0; jj < j1; ++jj) {
-                        if (flag[jj] != 1) continue;
-                        double2 ev = __ldg(&pp.Epool[eoff[jj] + bo + e]);
+                for (int u = 0; u < KT; ++u) {
+                    const int K = kb * KT + u;
+                    hb[u] = (K < qc.Nab ? K : 0) * tb.ncdh;
+                }
+                const int bo = tb.kbo[cd];
+                const int bd = tb.kbd[cd];
+                const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+                for (int e = sub; e < nbox; e += J) {
+                    const uint32_t kk = tb.kh[bo + e];
+                    const int Kp = kk & 0xffff;
+                    const bool neg = kk >> 16;
+                    if (is64) {
+                        double2 ev = E64[bo + e];
                         if (neg) ev = c2(-ev.x, -ev.y);
 #pragma unroll
-                        for (int u = 0; u < KT; ++u) a64[u] = cmac(a64[u], ev, R[ridx[u] + jj]);
-                    }
-                }
-                if (has32) {
-                    for (int jj = j0; jj < j1; ++jj) {
-                        if (flag[jj] != 0) continue;
-                        float2 ev = __ldg(&pp.Epool32[eoff[jj] + bo + e]);
+                        for (int u = 0; u < KT; ++u) a64[u] = cmac(a64[u], ev, R[tb.hsum[hb[u] + Kp] * B1p + jj]);
+                    } else {
+                        float2 ev = E32[bo + e];
                         if (neg) ev = make_float2(-ev.x, -ev.y);
 #pragma unroll
-                        for (int u = 0; u < KT; ++u) a32[u] = tmac(a32[u], ev, R32[ridx[u] + jj]);
+                        for (int u = 0; u < KT; ++u) a32[u] = tmac(a32[u], ev, R32[tb.hsum[hb[u] + Kp] * B1p + jj]);
+                    }
+                }
+            } else if (act) {
+                kb = it / chn;
+                cdl = it - kb * chn;
+                const int cd = c0 + cdl;
+                int bk[KT], bl[KT], bm[KT];
+#pragma unroll
+                for (int u = 0; u < KT; ++u) {
+                    const int K = kb * KT + u;
+                    const uint32_t kx = herm_xyz[K < qc.Nab ? K : 0];
+                    bk[u] = kx & 255;
+                    bl[u] = (kx >> 8) & 255;
+                    bm[u] = (kx >> 16) & 255;
+                }
+                const int bo = qc.ket.boxoff[cd];
+                const int bd = qc.ket.boxdim[cd];
+                const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+                for (int e = sub; e < nbox; e += J) {
+                    const uint32_t ke = qc.ket.ent[bo + e];
+                    const int k2 = ke & 255, l2 = (ke >> 8) & 255, m2 = (ke >> 16) & 255;
+                    const bool neg = (k2 + l2 + m2) & 1;
+                    if (is64) {
+                        double2 ev = E64[bo + e];
+                        if (neg) ev = c2(-ev.x, -ev.y);
+#pragma unroll
+                        for (int u = 0; u < KT; ++u)
+                            a64[u] = cmac(a64[u], ev, R[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                    } else {
+                        float2 ev = E32[bo + e];
+                        if (neg) ev = make_float2(-ev.x, -ev.y);
+#pragma unroll
+                        for (int u = 0; u < KT; ++u)
+                            a32[u] = tmac(a32[u], ev, R32[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                    }
+                }
+            }
+            if (J > 1) {
+#pragma unroll
+                for (int u = 0; u < KT; ++u) {
+                    if (is64)
+                        a64[u] = group_sum(a64[u], J);
+                    else
+                        a32[u] = group_sum(a32[u], J);
+                }
+            }
+            if (act && sub == 0) {
+#pragma unroll
+                for (int u = 0; u < KT; ++u) {
+                    const int K = kb * KT + u;
+                    if (K < qc.Nab) {
+                        if (is64) {
+                            W[K * qc.CH + cdl] = cadd(W[K * qc.CH + cdl], a64[u]);
+                        } else {
+                            float2& w = W32[K * qc.CH + cdl];
+                            w.x += a32[u].x;
+                            w.y += a32[u].y;
+                        }
                     }
                 }
             }
         }
-        if (J > 1) {
-#pragma unroll
-            for (int u = 0; u < KT; ++u) {
-                if (has64) a64[u] = group_sum(a64[u], J);
-                if (has32) a32[u] = group_sum(a32[u], J);
-            }
-        }
-        if (act && sub == 0) {
-#pragma unroll
-            for (int u = 0; u < KT; ++u) {
-                const int K = kb * KT + u;
-                if (K < qc.Nab) {
-                    if (has64) W[K * qc.CH + cdl] = cadd(W[K * qc.CH + cdl], a64[u]);
-                    if (has32) {
-                        float2& w = W32[K * qc.CH + cdl];
-                        w.x += a32[u].x;
-                        w.y += a32[u].y;
-                    }
-                }
-            }
-        }
+        if (stg) __syncwarp();  // the next entry overwrites the staging buffer
     }
 }
 
-__device__ __forceinline__ void step_k_any(const QuartetClass& qc, const uint32_t* herm_xyz, const PairData& pp,
-                                           const double2* R, const float2* R32, int B1p, const int* flag,
-                                           const long long* eoff, int j0, int j1, bool has64, bool has32,
-                                           double2* W, float2* W32, int c0, int chn, int lane) {
+__device__ __forceinline__ void step_k_any(const QuartetClass& qc, const ClassTabs& tb, const uint32_t* herm_xyz,
+                                           const PairData& pp, const double2* R, const float2* R32, int B1p,
+                                           const int* flag, const long long* eoff, int j0, int j1, double2* W,
+                                           float2* W32, double2* stg, int c0, int chn, int lane) {
     if (qc.KT == 4)
-        step_k_run<4>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+        step_k_run<4>(qc, tb, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
     else if (qc.KT == 2)
-        step_k_run<2>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+        step_k_run<2>(qc, tb, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
     else
-        step_k_run<1>(qc, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn, lane);
+        step_k_run<1>(qc, tb, herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
 }
 
 // Bra transform of W (FP64) and W32 (FP32) into the task's output block:
 //   out[ab][cd] += sum_{K in box(ab)} E~ab[K] W[K][cd].
-// A work item is CT consecutive ket components of one bra component ab (the
-// chunk length is a multiple of CT); its box entries are split over the
-// item's J lanes.  FP32 partial sums are added in FP64.
+// The bra E~ record (FP64 and/or FP32) is first copied into the warp's
+// staging buffer (stg; null: read from global memory).  A work item is CT
+// consecutive ket components of one bra component ab (the chunk length is a
+// multiple of CT); its box entries are split over the item's J lanes.  FP32
+// partial sums are added in FP64.
 template <int CT>
-__device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, const Task& tg, int ip, double2* W,
-                                       float2* W32, bool use64, bool use32, int c0, int chn, int lane) {
+__device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, const ClassTabs& tb, const Task& tg,
+                                       int ip, double2* W, float2* W32, bool use64, bool use32, double2* stg, int c0,
+                                       int chn, int lane) {
     const int nab = qc.bra.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const double2* Ea = d.pairs.Epool + d.pairs.Eoff[ip];
     const float2* Ea32 = d.pairs.Epool32 + d.pairs.Eoff[ip];
+    if (stg) {
+        float2* stg32 = reinterpret_cast<float2*>(stg + qc.stage_e);
+        if (use64)
+            for (int i = lane; i < qc.bra.Etot; i += 32) stg[i] = __ldg(&Ea[i]);
+        if (use32)
+            for (int i = lane; i < qc.bra.Etot; i += 32) stg32[i] = __ldg(&Ea32[i]);
+        __syncwarp();
+        Ea = stg;
+        Ea32 = stg32;
+    }
     const int nct = chn / CT;
     const int I = nab * nct;
     const int J = lanes_per_item(I);
@@ -772,23 +849,26 @@ __device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, 
         if (act) {
             ab = it / nct;
             cdl0 = (it - ab * nct) * CT;
-            const int bo = qc.bra.boxoff[ab];
-            const int bd = qc.bra.boxdim[ab];
+            const int bo = tb.hsum ? tb.bbo[ab] : qc.bra.boxoff[ab];
+            const int bd = tb.hsum ? tb.bbd[ab] : qc.bra.boxdim[ab];
             const int nbox = (bd & 255) * ((bd >> 8) & 255) * ((bd >> 16) & 255);
+            auto row = [&](int e) -> int {
+                if (tb.hsum) return (int)tb.bh[bo + e];
+                const uint32_t ke = qc.bra.ent[bo + e];
+                return herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+            };
             if (use32) {
                 for (int e = sub; e < nbox; e += J) {
-                    const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
-                    const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
-                    const float2 ea32 = __ldg(&Ea32[bo + e]);
+                    const int K = row(e);
+                    const float2 ea32 = Ea32[bo + e];
 #pragma unroll
                     for (int u = 0; u < CT; ++u) acc32[u] = tmac(acc32[u], ea32, W32[K * qc.CH + cdl0 + u]);
                 }
             }
             if (use64) {
                 for (int e = sub; e < nbox; e += J) {
-                    const uint32_t ke = __ldg(&qc.bra.ent[bo + e]);
-                    const int K = herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
-                    const double2 ea = __ldg(&Ea[bo + e]);
+                    const int K = row(e);
+                    const double2 ea = Ea[bo + e];
 #pragma unroll
                     for (int u = 0; u < CT; ++u) acc[u] = cmac(acc[u], ea, W[K * qc.CH + cdl0 + u]);
                 }
@@ -814,16 +894,17 @@ __device__ __forceinline__ void step_b(const EriDev& d, const QuartetClass& qc, 
             }
         }
     }
+    if (stg) __syncwarp();  // the staging buffer is reused by the next transform
 }
 
-__device__ __forceinline__ void step_b_any(const EriDev& d, const QuartetClass& qc, const Task& tg, int ip,
-                                           double2* W, float2* W32, bool use64, bool use32, int c0, int chn,
-                                           int lane) {
+__device__ __forceinline__ void step_b_any(const EriDev& d, const QuartetClass& qc, const ClassTabs& tb,
+                                           const Task& tg, int ip, double2* W, float2* W32, bool use64, bool use32,
+                                           double2* stg, int c0, int chn, int lane) {
     switch (qc.CT) {
-        case 4: step_b<4>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
-        case 3: step_b<3>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
-        case 2: step_b<2>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
-        default: step_b<1>(d, qc, tg, ip, W, W32, use64, use32, c0, chn, lane); break;
+        case 4: step_b<4>(d, qc, tb, tg, ip, W, W32, use64, use32, stg, c0, chn, lane); break;
+        case 3: step_b<3>(d, qc, tb, tg, ip, W, W32, use64, use32, stg, c0, chn, lane); break;
+        case 2: step_b<2>(d, qc, tb, tg, ip, W, W32, use64, use32, stg, c0, chn, lane); break;
+        default: step_b<1>(d, qc, tb, tg, ip, W, W32, use64, use32, stg, c0, chn, lane); break;
     }
 }
 
@@ -855,13 +936,52 @@ __device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int pass, con
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetClass qc) {
     extern __shared__ double2 sm[];
+    // class tables into block-shared memory, read by every warp of the block
+    ClassTabs tabs{};
+    if (qc.tab_words > 0) {
+        int* t = reinterpret_cast<int*>(sm);
+        const int ncdh = herm_count(qc.ket.Lab);
+        int* kbo = t;
+        int* kbd = kbo + qc.ket.nab;
+        uint32_t* kh = reinterpret_cast<uint32_t*>(kbd + qc.ket.nab);
+        int* bbo = reinterpret_cast<int*>(kh + qc.ket.Etot);
+        int* bbd = bbo + qc.bra.nab;
+        uint32_t* bh = reinterpret_cast<uint32_t*>(bbd + qc.bra.nab);
+        int* hsum = reinterpret_cast<int*>(bh + qc.bra.Etot);
+        for (int i = threadIdx.x; i < qc.ket.nab; i += blockDim.x) {
+            kbo[i] = qc.ket.boxoff[i];
+            kbd[i] = qc.ket.boxdim[i];
+        }
+        for (int i = threadIdx.x; i < qc.ket.Etot; i += blockDim.x) {
+            const uint32_t ke = qc.ket.ent[i];
+            const int k = ke & 255, l = (ke >> 8) & 255, m = (ke >> 16) & 255;
+            kh[i] = (uint32_t)herm_index(k, l, m) | ((uint32_t)((k + l + m) & 1) << 16);
+        }
+        for (int i = threadIdx.x; i < qc.bra.nab; i += blockDim.x) {
+            bbo[i] = qc.bra.boxoff[i];
+            bbd[i] = qc.bra.boxdim[i];
+        }
+        for (int i = threadIdx.x; i < qc.bra.Etot; i += blockDim.x) {
+            const uint32_t ke = qc.bra.ent[i];
+            bh[i] = (uint32_t)herm_index(ke & 255, (ke >> 8) & 255, (ke >> 16) & 255);
+        }
+        for (int i = threadIdx.x; i < qc.Nab * ncdh; i += blockDim.x) {
+            const int K = i / ncdh, Kp = i - K * ncdh;
+            const uint32_t a = d.herm_xyz[K], b = d.herm_xyz[Kp];
+            hsum[i] = herm_index((a & 255) + (b & 255), ((a >> 8) & 255) + ((b >> 8) & 255),
+                                 ((a >> 16) & 255) + ((b >> 16) & 255));
+        }
+        __syncthreads();
+        tabs = ClassTabs{kbo, kbd, kh, bbo, bbd, bh, hsum, ncdh};
+    }
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
     const int B1p = qc.B1 + 1;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
-    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f);
-    char* base = reinterpret_cast<char*>(sm) + (size_t)wib * lay.total;
+    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e);
+    const size_t tab_bytes = (((size_t)qc.tab_words * 4 + 15) / 16) * 16;
+    char* base = reinterpret_cast<char*>(sm) + tab_bytes + (size_t)wib * lay.total;
     double2* R = reinterpret_cast<double2*>(base + lay.R);
     double2* W = reinterpret_cast<double2*>(base + lay.W);
     float2* R32 = reinterpret_cast<float2*>(base + lay.R32);
@@ -870,6 +990,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     int* flag = reinterpret_cast<int*>(base + lay.flag);
     long long* eoff = reinterpret_cast<long long*>(base + lay.eoff);  // E~ record of each entry's ket pair
     double2* sseed = reinterpret_cast<double2*>(base + lay.seed);  // [L+1] seeds, then X'[3]
+    double2* stg = qc.stage_e > 0 ? reinterpret_cast<double2*>(base + lay.stage) : nullptr;  // E~ staging
     const int nab = qc.bra.nab, ncd = qc.ket.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const int ns = d.basis.ns;
@@ -1020,8 +1141,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                             __syncwarp();
                             const int cg = cur / Kab, cP = cur - cg * Kab;
                             const Task tc = qc.tasks[gi.x + cg];
-                            step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64,
-                                       any32, c0, chn, lane);
+                            step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64,
+                                       any32, stg, c0, chn, lane);
                             __syncwarp();
                             for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
                                 if (any64) W[it] = c2(0.0, 0.0);
@@ -1037,8 +1158,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         has64 = has64 || flag[jj] == 1;
                         has32 = has32 || flag[jj] == 0;
                     }
-                    step_k_any(qc, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, has64, has32, W, W32, c0, chn,
-                               lane);
+                    step_k_any(qc, tabs, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
                     any64 = any64 || has64;
                     any32 = any32 || has32;
                     j0 = j1;
@@ -1071,14 +1191,13 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         if (flag[j] != 1) continue;
                         for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
                         __syncwarp();
-                        step_k_any(qc, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j, j + 1, true, false, W, W32, c0,
-                                   chn, lane);
+                        step_k_any(qc, tabs, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j, j + 1, W, W32, stg, c0, chn, lane);
                         __syncwarp();
                         const int key = queue[j] / Kcd;
                         const int cg = key / Kab, cP = key - cg * Kab;
                         const Task tc = qc.tasks[gi.x + cg];
-                        step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, true, false,
-                                   c0, chn, lane);
+                        step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, true, false,
+                                   stg, c0, chn, lane);
                         __syncwarp();
                     }
                     for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
@@ -1089,8 +1208,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                 __syncwarp();
                 const int cg = cur / Kab, cP = cur - cg * Kab;
                 const Task tc = qc.tasks[gi.x + cg];
-                step_b_any(d, qc, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64, any32, c0,
-                           chn, lane);
+                step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64, any32, stg,
+                           c0, chn, lane);
             }
             __syncwarp();
         }
@@ -1107,7 +1226,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
 }
 
 size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed) {
-    return (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed).total;
+    return (((size_t)qc.tab_words * 4 + 15) / 16) * 16 +
+           (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed, qc.stage_e).total;
 }
 
 static bool g_const_ready = false;
