@@ -541,18 +541,16 @@ __device__ __forceinline__ void hermite_rec_any(const EriDev& d, int L, const T*
 // Per-warp shared layout of quartet_kernel (all offsets in bytes).  R holds
 // B1 + 1 columns (the last one is the cooperative recurrence's second
 // buffer); `seed` holds one entry's seeds and X' for the cooperative path.
-// The FP32 table R32 of the mixed-precision pass shares R's memory: a batch
-// of that pass is either FP32 (R32) or, for its deferred FP64 fallbacks,
-// FP64 (R) after the FP32 part is consumed.
+// FP32 entries of a mixed-precision batch keep their table in R too: the
+// float2 of row r sits in the first half of the 16-byte slot of column j.
 struct WarpSmem {
-    size_t R, W, R32, W32, queue, flag, eoff, seed, stage, total;
+    size_t R, W, W32, queue, flag, eoff, seed, stage, total;
 };
 __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed, int stage_e) {
     WarpSmem w;
     const size_t B1p = B1 + 1;
     w.R = 0;
     w.W = w.R + (size_t)NL * B1p * 16;
-    w.R32 = w.R;
     w.W32 = w.W + (size_t)Nab * CH * 16;
     w.queue = w.W32 + (mixed ? (((size_t)Nab * CH * 8 + 15) / 16) * 16 : 0);
     w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
@@ -660,8 +658,9 @@ __device__ __forceinline__ float2 group_sum(float2 v, int J) {
 // staging buffer with one coalesced load (stg; null: read it from global
 // memory), then every work item -- KT consecutive Hermite rows K of one ket
 // component cd, its box entries split over the item's J lanes -- contracts
-// it against the entry's R column.  eoff[j]: E~ record of the entry's ket
-// pair; flag[j]: 0 FP32, 1 FP64, 2 deferred (skipped here).
+// it against the entry's R column (FP32 entries: the float2 in the first half
+// of each 16-byte slot of R, R32[(row B1p + j) 2]).  eoff[j]: E~ record of the
+// entry's ket pair; flag[j]: 0 FP32, 1 FP64.
 template <int KT>
 __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const ClassTabs& tb, const uint32_t* herm_xyz,
                                            const PairData& pp, const double2* R, const float2* R32, int B1p,
@@ -674,7 +673,6 @@ __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const ClassTa
     float2* stg32 = reinterpret_cast<float2*>(stg + qc.stage_e);
     for (int jj = j0; jj < j1; ++jj) {
         const int f = flag[jj];
-        if (f == 2) continue;  // deferred: evaluated in FP64 after the batch
         const bool is64 = f == 1;
         const double2* E64 = pp.Epool + eoff[jj];
         const float2* E32 = pp.Epool32 + eoff[jj];
@@ -726,7 +724,7 @@ __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const ClassTa
                         float2 ev = E32[bo + e];
                         if (neg) ev = make_float2(-ev.x, -ev.y);
 #pragma unroll
-                        for (int u = 0; u < KT; ++u) a32[u] = tmac(a32[u], ev, R32[tb.hsum[hb[u] + Kp] * B1p + jj]);
+                        for (int u = 0; u < KT; ++u) a32[u] = tmac(a32[u], ev, R32[(tb.hsum[hb[u] + Kp] * B1p + jj) * 2]);
                     }
                 }
             } else if (act) {
@@ -760,7 +758,7 @@ __device__ __forceinline__ void step_k_run(const QuartetClass& qc, const ClassTa
                         if (neg) ev = make_float2(-ev.x, -ev.y);
 #pragma unroll
                         for (int u = 0; u < KT; ++u)
-                            a32[u] = tmac(a32[u], ev, R32[herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj]);
+                            a32[u] = tmac(a32[u], ev, R32[(herm_index(bk[u] + k2, bl[u] + l2, bm[u] + m2) * B1p + jj) * 2]);
                     }
                 }
             }
@@ -908,19 +906,17 @@ __device__ __forceinline__ void step_b_any(const EriDev& d, const QuartetClass& 
     }
 }
 
-// Seeds of primitive quartet (ip, iq) for pass `pass`: returns 1 (FP64 seeds
-// in Sh), 0 (FP32 seeds in S32) or 2 (FP32 pass, seeds outside the FP32
-// range: the quartet is deferred to FP64 after the batch).  Pass 0 is FP64;
-// in pass 1 (FP32 quartets) the Boys function runs in FP32 in its asymptotic
-// sector and in FP64 elsewhere, and the seeds go to the FP32 recurrence when
-// they fit its range.
-__device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int pass, const QuartetArgs& qa, double2* Sh,
+// Seeds of one primitive quartet: returns 1 (FP64 seeds in Sh), 0 (FP32
+// seeds in S32) or 2 (FP32 wanted but the seeds leave the FP32 range: FP64
+// seeds in Sh).  For an FP32 quartet (want32) the Boys function runs in FP32
+// in its asymptotic sector and in FP64 elsewhere.
+__device__ __forceinline__ int entry_seeds(const EriDev& d, int L, int want32, const QuartetArgs& qa, double2* Sh,
                                            float2* S32, long long item) {
-    if (pass == 0) {
+    if (!want32) {
         quartet_seeds_rt(d, L, qa, Sh, item);
         return 1;
     }
-    if (pass == 1 && seeds32(qa.C, qa.rho, qa.tre, qa.tim, L, S32)) return 0;
+    if (seeds32(qa.C, qa.rho, qa.tre, qa.tim, L, S32)) return 0;
     quartet_seeds_rt(d, L, qa, Sh, item);
     bool ok = true;
     for (int n = 0; n <= L; ++n) {
@@ -984,7 +980,6 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     char* base = reinterpret_cast<char*>(sm) + tab_bytes + (size_t)wib * lay.total;
     double2* R = reinterpret_cast<double2*>(base + lay.R);
     double2* W = reinterpret_cast<double2*>(base + lay.W);
-    float2* R32 = reinterpret_cast<float2*>(base + lay.R32);
     float2* W32 = reinterpret_cast<float2*>(base + lay.W32);
     int* queue = reinterpret_cast<int*>(base + lay.queue);
     int* flag = reinterpret_cast<int*>(base + lay.flag);
@@ -995,11 +990,12 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
     const int ns = d.basis.ns;
     const PairData& pp = d.pairs;
-    const float cut64 = fmaxf(cut32, skip);
-    // Mixed precision: pass 0 evaluates the FP64 quartets, pass 1 the FP32
-    // ones (FP32 Boys in the asymptotic sector, FP64 Boys elsewhere), so that
-    // both passes fill their batches densely.
-    const int npass = cut32 > 0.0f ? 2 : 1;
+    // Mixed precision runs in the same batches as FP64: every entry carries its
+    // own precision (FP32 below cut32), FP32 R columns share the slots of the
+    // FP64 ones (a float2 in each 16-byte slot), and W / W32 accumulate side by
+    // side, so batches stay dense and each bra pair is contracted once.
+    const bool mixed = cut32 > 0.0f;
+    float2* const R32s = reinterpret_cast<float2*>(R);  // FP32 column j: R32s + 2 j, stride 2 B1p
     unsigned long long cnt64 = 0, cnt32 = 0;
     // A warp takes one work unit: a group of tasks with equal primitive
     // counts and one chunk of ket components (chunks of a group run on
@@ -1030,10 +1026,10 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
             }
         }
         __syncwarp();
-        for (int pass = 0; pass < npass; ++pass) {
+        {
             for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
                 W[it] = c2(0.0, 0.0);
-                if (npass > 1) W32[it] = make_float2(0.0f, 0.0f);
+                if (mixed) W32[it] = make_float2(0.0f, 0.0f);
             }
             int cur = -1;  // g * Kab + P of the accumulating bra pair
             bool any64 = false, any32 = false;  // precisions accumulated into W / W32 for `cur`
@@ -1052,7 +1048,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
                         const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
                         const float b = pp.sbound[op] * pp.sbound[oq];
-                        valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
+                        valid = b >= skip;
                     }
                     const unsigned mask = __ballot_sync(0xffffffffu, valid);
                     const int cnt = __popc(mask);
@@ -1083,7 +1079,11 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                             const QuartetArgs qa = quartet_args(pp, ip, iq);
                             double2 Sh[BOYS_MAX_ORDER + 1];
                             float2 S32[BOYS_MAX_ORDER + 1];
-                            const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
+                            const bool want32 =
+                                mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
+                                                 pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] < cut32;
+                            int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
+                            if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
                             if (f == 1) {
                                 for (int n = 0; n <= qc.L; ++n) sseed[n] = Sh[n];
                                 for (int x = 0; x < 3; ++x) sseed[qc.L + 1 + x] = qa.X[x];
@@ -1103,7 +1103,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                             coop_rec<double2>(qc.L, sseed, sseed + qc.L + 1, R, B1p, j, qc.B1, d.herm_xyz, lane);
                         } else if (flag[j] == 0) {
                             const float2* s32 = reinterpret_cast<const float2*>(sseed);
-                            coop_rec<float2>(qc.L, s32, s32 + qc.L + 1, R32, B1p, j, qc.B1, d.herm_xyz, lane);
+                            coop_rec<float2>(qc.L, s32, s32 + qc.L + 1, R32s, 2 * B1p, 2 * j, 2 * qc.B1, d.herm_xyz,
+                                             lane);
                         }
                     }
                 } else if (lane < nb) {
@@ -1116,15 +1117,19 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                     const QuartetArgs qa = quartet_args(pp, ip, iq);
                     double2 Sh[BOYS_MAX_ORDER + 1];
                     float2 S32[BOYS_MAX_ORDER + 1];
-                    const int f = entry_seeds(d, qc.L, pass, qa, Sh, S32, gi.x + g);
+                    const bool want32 = mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
+                                                         pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] <
+                                                     cut32;
+                    int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
+                    if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
                     if (f == 1) {
                         hermite_rec_any<double2>(d, qc.L, Sh, qa.X, R + lane, B1p);
                         cnt64 += first_chunk;
-                    } else if (f == 0) {
+                    } else {
                         const float2 X32[3] = {make_float2((float)qa.X[0].x, (float)qa.X[0].y),
                                                make_float2((float)qa.X[1].x, (float)qa.X[1].y),
                                                make_float2((float)qa.X[2].x, (float)qa.X[2].y)};
-                        hermite_rec_any<float2>(d, qc.L, S32, X32, R32 + lane, B1p);
+                        hermite_rec_any<float2>(d, qc.L, S32, X32, R32s + 2 * lane, 2 * B1p);
                         cnt32 += first_chunk;
                     }
                     flag[lane] = f;
@@ -1158,50 +1163,10 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         has64 = has64 || flag[jj] == 1;
                         has32 = has32 || flag[jj] == 0;
                     }
-                    step_k_any(qc, tabs, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
+                    step_k_any(qc, tabs, d.herm_xyz, pp, R, R32s, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
                     any64 = any64 || has64;
                     any32 = any32 || has32;
                     j0 = j1;
-                }
-                // Deferred FP64 fallbacks of the FP32 pass: the batch's FP32
-                // columns are consumed, so R (sharing their memory) takes the
-                // fallbacks' FP64 tables; each is contracted and added to the
-                // output on its own, through W, which the FP32 pass leaves
-                // unused.
-                if (__any_sync(0xffffffffu, lane < nb && flag[lane] == 2)) {
-                    __syncwarp();
-                    if (lane < nb && flag[lane] == 2) {
-                        const int idx = queue[lane];
-                        const int g = idx / KK, r = idx - g * KK;
-                        const int P = r / Kcd, Q = r - P * Kcd;
-                        const Task tg = qc.tasks[gi.x + g];
-                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
-                        const QuartetArgs qa = quartet_args(pp, ip, iq);
-                        double2 Sh[BOYS_MAX_ORDER + 1];
-                        quartet_seeds_rt(d, qc.L, qa, Sh, gi.x + g);
-                        hermite_rec_any<double2>(d, qc.L, Sh, qa.X, R + lane, B1p);
-                        flag[lane] = 1;
-                        cnt64 += first_chunk;
-                    } else if (lane < nb) {
-                        flag[lane] = 3;  // consumed FP32 entry
-                    }
-                    __syncwarp();
-                    for (int j = 0; j < nb; ++j) {
-                        if (flag[j] != 1) continue;
-                        for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
-                        __syncwarp();
-                        step_k_any(qc, tabs, d.herm_xyz, pp, R, R32, B1p, flag, eoff, j, j + 1, W, W32, stg, c0, chn, lane);
-                        __syncwarp();
-                        const int key = queue[j] / Kcd;
-                        const int cg = key / Kab, cP = key - cg * Kab;
-                        const Task tc = qc.tasks[gi.x + cg];
-                        step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, true, false,
-                                   stg, c0, chn, lane);
-                        __syncwarp();
-                    }
-                    for (int it = lane; it < qc.Nab * qc.CH; it += 32) W[it] = c2(0.0, 0.0);
-                    __syncwarp();
                 }
             }
             if (cur >= 0) {
