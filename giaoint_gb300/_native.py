@@ -87,6 +87,7 @@ SIGNATURES = {
     "gx_eri_shell": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d]),
     "gx_eri_full": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]),
     "gx_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d]),
+    "gx_nuclear_attraction": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.c_int, _d, _d, _d]),
     "gx_cholesky_diagonal": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
     "gx_cholesky_columns": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
     "gx_cholesky": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.POINTER(GxCholeskyOptions), _d, _i64, _i64, _d]),

@@ -1405,6 +1405,56 @@ int gx_primitive_eri(gx_context* ctx, const double* exps, const double* centers,
     });
 }
 
+int gx_nuclear_attraction(gx_context* ctx, gx_basis* b, const double* B, const double* O, int nnuc,
+                          const double* charges, const double* centers, double* out) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        if (nnuc < 0) raise(GX_EINVAL, "nucleus count must be non-negative");
+        for (int c = 0; c < nnuc; ++c) {
+            if (!std::isfinite(charges[c]) || charges[c] <= 0.0)
+                raise(GX_EINVAL, "nuclear charge must be finite and positive");
+            for (int x = 0; x < 3; ++x)
+                if (!std::isfinite(centers[3 * c + x])) raise(GX_EINVAL, "nuclear center values must be finite");
+        }
+        int lmax = 0;
+        for (int s = 0; s < b->ns; ++s) lmax = std::max(lmax, b->l[s]);
+        if (2 * lmax > 32) raise(GX_EINVAL, "nuclear attraction supports combined angular order through 32");
+        const int nab_max = gx::ncart(lmax) * gx::ncart(lmax);
+        const size_t smem = (size_t)(2 * gx::herm_count(2 * lmax) + 2 * lmax + 4 + nab_max) * sizeof(double2);
+        if (smem > 200 * 1024)
+            raise(GX_EINVAL, "nuclear attraction on the GPU supports shells through angular momentum 11");
+        const int64_t n = b->nao;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        if (n == 0) return;
+        FieldPairs& fp = field_pairs(b, B, O);
+        std::vector<long long> seg_ao(std::max(b->nseg, 1));
+        for (int s = 0; s < b->ns; ++s)
+            for (int x = 0; x < b->ncontr[s]; ++x)
+                seg_ao[b->seg_first[s] + x] = b->ao_off[s] + (long long)x * b->ncart_of(s);
+        std::vector<double> nuc(std::max(4 * nnuc, 1));
+        for (int c = 0; c < nnuc; ++c) {
+            nuc[c] = charges[c];
+            for (int x = 0; x < 3; ++x) nuc[nnuc + 3 * c + x] = centers[3 * c + x];
+        }
+        upload(ctx->scratch_c, nuc, st);
+        DeviceBuffer d_seg;
+        upload(d_seg, seg_ao, st);
+        ctx->scratch_b.reserve((size_t)n * n * sizeof(double2));
+        ctx->reset_status();
+        GX_CUDA(gx::launch_nuclear(b->dev(), pair_view(b, fp), ctx->boys(), ctx->gl.as<gx::GLRules>(),
+                                   ctx->herm.as<uint32_t>(), b->d_classes.as<gx::PairClassDev>(),
+                                   b->d_pp_class.as<int>(), nnuc, ctx->scratch_c.as<double>(),
+                                   ctx->scratch_c.as<double>() + nnuc, d_seg.as<long long>(), n, 2 * lmax, nab_max,
+                                   ctx->scratch_b.as<double2>(), ctx->status.as<gx::DevStatus>(), st));
+        GX_CUDA(cudaMemcpyAsync(out, ctx->scratch_b.ptr, (size_t)n * n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        check_status(ctx);
+    });
+}
+
 int gx_cholesky_diagonal(gx_context* ctx, gx_basis* b, const int64_t* pairs, int64_t npairs, const double* B,
                          const double* O, double* out) {
     return guarded([&] {

@@ -130,6 +130,12 @@ cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
                                 long long n, double2* full, cudaStream_t s);
 
+// nuclear attraction (gx_nuclear.cu)
+cudaError_t launch_nuclear(const BasisDev& bs, const PairData& pp, const BoysTable& boys, const GLRules* gl,
+                           const uint32_t* herm_xyz, const PairClassDev* classes, const int* pp_class, int nnuc,
+                           const double* charge, const double* center, const long long* seg_ao, long long n,
+                           int max_pair_L, int max_nab, double2* out, DevStatus* status, cudaStream_t s);
+
 // register-resident small classes (gx_small.cu)
 bool small_class(int la, int lb, int lc, int ld);
 cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s);

@@ -187,6 +187,14 @@ int gx_cholesky(gx_context* ctx, gx_basis* basis, const double* B, const double*
                 double* max_residual);
 
 
+/* GIAO nuclear-attraction matrix out[mu][nu] (complex128, n x n, AO order
+ * of the basis) = sum_C -Z_C <mu|1/|r - C||nu> over nnuc point charges
+ * (charges[nnuc] > 0, centers[3*nnuc]).  Replaces
+ * compute_nuclear_attraction_matrix (src/nuclear.cpp:304-330; bindings.cpp:
+ * 578-600).  Shells through l = 11. */
+int gx_nuclear_attraction(gx_context* ctx, gx_basis* basis, const double* B, const double* O, int nnuc,
+                          const double* charges, const double* centers, double* out);
+
 /* ---------------------------------------------------------------------- */
 /* streams, plans and device-resident execution                            */
 /* ---------------------------------------------------------------------- */
