@@ -22,6 +22,7 @@ from ._types import (
 from .boys import BoysRegion, boys, boys_with_diagnostics
 from .cholesky import CholeskyERI, cholesky_eri
 from .eri import EriBatch, canonical_quartets, eri, eri_batches, eri_schwarz_bounds, eri_shell, primitive_eri
+from .nuclear import nuclear_attraction, nuclear_attraction_shell, primitive_nuclear_attraction
 
 __version__ = "0.1.0"
 
@@ -46,7 +47,10 @@ __all__ = [
     "eri_batches",
     "eri_schwarz_bounds",
     "eri_shell",
+    "nuclear_attraction",
+    "nuclear_attraction_shell",
     "primitive_eri",
+    "primitive_nuclear_attraction",
     "primitive_normalization",
     "resolve_num_threads",
     "set_num_threads",

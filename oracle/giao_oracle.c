@@ -1087,3 +1087,131 @@ int or_cholesky_columns(BASIS_ARGS, const long* pivots, long npiv, const double*
     basis_free(&bs);
     return failed;
 }
+
+
+/* ------------------------------------------------------------------ */
+/* nuclear attraction (src/nuclear.cpp:27-170, 207-330)                 */
+/* ------------------------------------------------------------------ */
+
+/* One primitive pair and one point charge, unit coefficients and no
+ * primitive normalisation (the reference's NuclearKernel::compute): the
+ * four-index table R^n_{tuv} of the complex displacement P' - C with the
+ * -i q terms of the London phase, filled by increasing degree t+u+v. */
+static int nuclear_kernel(const prim_t* a, const prim_t* b, double Z, const double* C, const field_t* f, cplx* out) {
+    pair_t pr;
+    gaussian_product(a->alpha, a->center, b->alpha, b->center, f, &pr);
+    const int mx = a->ang[0] + b->ang[0], my = a->ang[1] + b->ang[1], mz = a->ang[2] + b->ang[2];
+    const int L = mx + my + mz;
+    if (L > 32) return set_err(-1, "nuclear attraction supports combined angular order through 32");
+    double herm[3][34];
+    for (int ax = 0; ax < 3; ++ax)
+        hermite_1d(a->ang[ax], b->ang[ax], a->center[ax], b->center[ax], pr.P[ax], pr.p, herm[ax]);
+    cplx d[3];
+    for (int i = 0; i < 3; ++i) d[i] = pr.Pc[i] - C[i];
+    const cplx arg = pr.p * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const int scaled = creal(arg) < 0.0;
+    cplx boys[33];
+    int region;
+    double e;
+    long segs;
+    int rc = or_boys(creal(arg), cimag(arg), L, scaled, (double*)boys, &region, &e, &segs);
+    if (rc) return rc;
+    cplx common = pr.london;
+    if (scaled) {
+        const double dx = pr.P[0] - C[0], dy = pr.P[1] - C[1], dz = pr.P[2] - C[2];
+        const double qc = pr.q[0] * C[0] + pr.q[1] * C[1] + pr.q[2] * C[2];
+        common = cexp(CMPLX(-pr.p * (dx * dx + dy * dy + dz * dz), -qc));
+    }
+    const size_t sx = (size_t)(my + 1) * (mz + 1), sy = (size_t)(mz + 1), per_n = (size_t)(mx + 1) * sx;
+    cplx* R = (cplx*)calloc((size_t)(L + 1) * per_n, sizeof(cplx));
+    if (!R) return set_err(-3, "out of memory");
+#define RN(n, t, u, v) R[(size_t)(n) * per_n + (size_t)(t) * sx + (size_t)(u) * sy + (size_t)(v)]
+    double radial = 1.0;
+    for (int n = 0; n <= L; ++n) {
+        RN(n, 0, 0, 0) = common * radial * boys[n];
+        radial *= -2.0 * pr.p;
+    }
+    for (int deg = 1; deg <= L; ++deg)
+        for (int t = 0; t <= mx && t <= deg; ++t)
+            for (int u = 0; u <= my && t + u <= deg; ++u) {
+                const int v = deg - t - u;
+                if (v > mz) continue;
+                for (int n = 0; n + deg <= L; ++n) {
+                    cplx val;
+                    if (t > 0) {
+                        val = CMPLX(0.0, -pr.q[0]) * RN(n, t - 1, u, v) + d[0] * RN(n + 1, t - 1, u, v);
+                        if (t > 1) val += (double)(t - 1) * RN(n + 1, t - 2, u, v);
+                    } else if (u > 0) {
+                        val = CMPLX(0.0, -pr.q[1]) * RN(n, t, u - 1, v) + d[1] * RN(n + 1, t, u - 1, v);
+                        if (u > 1) val += (double)(u - 1) * RN(n + 1, t, u - 2, v);
+                    } else {
+                        val = CMPLX(0.0, -pr.q[2]) * RN(n, t, u, v - 1) + d[2] * RN(n + 1, t, u, v - 1);
+                        if (v > 1) val += (double)(v - 1) * RN(n + 1, t, u, v - 2);
+                    }
+                    RN(n, t, u, v) = val;
+                }
+            }
+    cplx acc = 0.0;
+    for (int t = 0; t <= mx; ++t)
+        for (int u = 0; u <= my; ++u)
+            for (int v = 0; v <= mz; ++v) acc += herm[0][t] * herm[1][u] * herm[2][v] * RN(0, t, u, v);
+#undef RN
+    free(R);
+    *out = -Z * (2.0 * M_PI / pr.p) * pr.K * acc;
+    return 0;
+}
+
+/* Full AO matrix out[mu][nu] (complex, row-major n x n): every ordered shell
+ * pair, primitive pairs and Cartesian components in the reference's loop
+ * order (src/nuclear.cpp:207-302), coefficients (contraction-normalised) and
+ * primitive normalisations applied per component. */
+int or_nuclear_matrix(BASIS_ARGS, int nnuc, const double* charges, const double* ncenters, const double* B,
+                      const double* O, double* out_) {
+    basis_t bs;
+    int rc = basis_init(&bs, ns, centers, ls, nprims, ncontrs, exps, coefs);
+    cplx* out = (cplx*)out_;
+    if (!rc) {
+        field_t f;
+        memcpy(f.B, B, sizeof f.B);
+        memcpy(f.O, O, sizeof f.O);
+        const size_t n = bs.nao;
+        for (size_t i = 0; i < n * n; ++i) out[i] = 0.0;
+        int ca[153][3], cb[153][3];
+        for (int sa = 0; sa < ns && !rc; ++sa)
+            for (int sb = 0; sb < ns && !rc; ++sb) {
+                const int na = cart_components(ls[sa], ca), nb = cart_components(ls[sb], cb);
+                for (int pa = 0; pa < nprims[sa] && !rc; ++pa)
+                    for (int pb = 0; pb < nprims[sb] && !rc; ++pb)
+                        for (int ia = 0; ia < na && !rc; ++ia)
+                            for (int ib = 0; ib < nb && !rc; ++ib) {
+                                prim_t a, b;
+                                a.alpha = exps[bs.eoff[sa] + pa];
+                                b.alpha = exps[bs.eoff[sb] + pb];
+                                for (int x = 0; x < 3; ++x) {
+                                    a.center[x] = centers[3 * sa + x];
+                                    b.center[x] = centers[3 * sb + x];
+                                    a.ang[x] = ca[ia][x];
+                                    b.ang[x] = cb[ib][x];
+                                }
+                                cplx v = 0.0;
+                                for (int c = 0; c < nnuc && !rc; ++c) {
+                                    cplx term;
+                                    rc = nuclear_kernel(&a, &b, charges[c], ncenters + 3 * c, &f, &term);
+                                    v += term;
+                                }
+                                if (rc) break;
+                                v *= or_primitive_normalization(a.alpha, a.ang[0], a.ang[1], a.ang[2]) *
+                                     or_primitive_normalization(b.alpha, b.ang[0], b.ang[1], b.ang[2]);
+                                for (int xa = 0; xa < ncontrs[sa]; ++xa)
+                                    for (int xb = 0; xb < ncontrs[sb]; ++xb) {
+                                        const size_t mu = bs.aooff[sa] + (size_t)xa * na + ia;
+                                        const size_t nu = bs.aooff[sb] + (size_t)xb * nb + ib;
+                                        out[mu * n + nu] += coefs[bs.coff[sa] + (size_t)xa * nprims[sa] + pa] *
+                                                            coefs[bs.coff[sb] + (size_t)xb * nprims[sb] + pb] * v;
+                                    }
+                            }
+            }
+    }
+    basis_free(&bs);
+    return rc;
+}

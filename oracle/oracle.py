@@ -151,6 +151,12 @@ def _arrays(specs: list[ShellSpec]) -> _Arrays:
                    normalize, total, offsets)
 
 
+def _nuclei(nuclei):
+    ch = np.ascontiguousarray([float(z) for z, _ in nuclei] or [0.0], dtype=np.float64)
+    cc = np.ascontiguousarray([float(x) for _, c in nuclei for x in c] or [0.0, 0.0, 0.0], dtype=np.float64)
+    return ch, cc
+
+
 def _vec3(v) -> np.ndarray:
     return np.ascontiguousarray([0.0, 0.0, 0.0] if v is None else v, dtype=np.float64)
 
@@ -261,6 +267,17 @@ class Oracle(_Backend):
                                          ctypes.c_int(threads), out.ctypes.data_as(_d)))
         return out[: n**4].reshape(n, n, n, n)
 
+    def nuclear(self, shells, nuclei, B=None, O=None) -> np.ndarray:
+        """Nuclear-attraction matrix; nuclei = [(charge, (x, y, z)), ...]."""
+        a = self._basis(shells)
+        n = a.nao
+        ch, cc = _nuclei(nuclei)
+        out = np.zeros(max(n * n, 1), dtype=np.complex128)
+        self._check(self.lib.or_nuclear_matrix(*a.args(), ctypes.c_int(len(nuclei)), ch.ctypes.data_as(_d),
+                                               cc.ctypes.data_as(_d), _vec3(B).ctypes.data_as(_d),
+                                               _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[: n * n].reshape(n, n)
+
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)
         out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
@@ -341,6 +358,16 @@ class Reference(_Backend):
                                           _vec3(O).ctypes.data_as(_d), ctypes.c_int(threads),
                                           out.ctypes.data_as(_d)))
         return out[: n**4].reshape(n, n, n, n)
+
+    def nuclear(self, shells, nuclei, B=None, O=None) -> np.ndarray:
+        a = self._basis(shells)
+        n = a.nao
+        ch, cc = _nuclei(nuclei)
+        out = np.zeros(max(n * n, 1), dtype=np.complex128)
+        self._check(self.lib.ref_nuclear_matrix(*self._bargs(a), ctypes.c_int(len(nuclei)), ch.ctypes.data_as(_d),
+                                                cc.ctypes.data_as(_d), _vec3(B).ctypes.data_as(_d),
+                                                _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[: n * n].reshape(n, n)
 
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)

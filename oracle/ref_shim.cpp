@@ -15,6 +15,7 @@
 //   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
 #include "giao_integrals/boys.hpp"
 #include "giao_integrals/eri.hpp"
+#include "giao_integrals/nuclear.hpp"
 #include "giao_integrals/types.hpp"
 #include "cholesky.hpp"
 
@@ -171,6 +172,21 @@ int ref_eri_full(int ns, const double* centers, const int* ls, const int* nprims
         auto span = std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out), n * n * n * n);
         [[maybe_unused]] auto st =
             giao::compute_eri_tensor(basis, make_field(B, O), {0.0, (std::size_t)threads}, nullptr, span);
+    });
+}
+
+int ref_nuclear_matrix(int ns, const double* centers, const int* ls, const int* nprims,
+                       const int* ncontrs, const double* exps, const double* coefs,
+                       const int* normalize, int nnuc, const double* charges, const double* ncenters,
+                       const double* B, const double* O, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        std::vector<giao::Nucleus> nuclei;
+        for (int c = 0; c < nnuc; ++c)
+            nuclei.emplace_back(charges[c], giao::Vec3{ncenters[3 * c], ncenters[3 * c + 1], ncenters[3 * c + 2]});
+        const std::size_t n = basis.ao_count();
+        giao::compute_nuclear_attraction_matrix(
+            basis, nuclei, make_field(B, O), std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out), n * n));
     });
 }
 

@@ -21,6 +21,7 @@ def golden():
         m8 = json.loads((GOLDEN / "primitive_eri_m8.json").read_text())
         cholesky = json.loads((GOLDEN / "cholesky.json").read_text())
         blocks = dict(np.load(GOLDEN / "eri_blocks.npz"))
+        nuclear = dict(np.load(GOLDEN / "nuclear.npz"))
 
     return G
 

@@ -3,7 +3,8 @@
 Run where the reference checkout exists (GIAO_REFERENCE_ROOT, default the
 read-only reference path used to build oracle/_ref):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py nuclear    # one fixture
 
 Inputs and outputs:
 
@@ -17,6 +18,10 @@ Inputs and outputs:
 * ``eri_blocks.npz`` -- reference ``evaluate_eri_shell_quartets`` output for
   the 19-AO atom (all canonical quartets, B=(0,0,0.1)) and a seeded subset of
   the 12-atom molecule's canonical quartets;
+* ``nuclear.npz`` -- reference ``compute_nuclear_attraction_matrix`` for a
+  seeded three-atom molecule (nuclei at the atoms, charges 1, 2, 3; finite
+  field with a shifted gauge origin, and zero field) and for the 19-AO atom
+  (Z = 10 at the origin, B = (0, 0, 0.1));
 * ``cholesky.json`` -- the reference's own NumPy Cholesky driver
   (python/giao_integrals/cholesky.py, executed unmodified over the reference
   library's native diagonal/column generators) on the two-shell d/f system of
@@ -218,15 +223,46 @@ def cholesky_fixture(ref):
     return {"shells": shells, "cases": cases}
 
 
+NUCLEAR_FIELD = (0.05, -0.1, 0.12)
+NUCLEAR_ORIGIN = (0.3, 0.1, -0.2)
+
+
+def nuclear_molecule():
+    recs = syn.random_molecule(7, natoms=3)
+    atoms = []
+    for r in recs:
+        if r.center not in atoms:
+            atoms.append(r.center)
+    return recs, [(1.0 + i, c) for i, c in enumerate(atoms)]
+
+
+def nuclear_fixture(ref):
+    recs, nuclei = nuclear_molecule()
+    v1 = ref.nuclear(recs, nuclei, NUCLEAR_FIELD, NUCLEAR_ORIGIN)
+    v0 = ref.nuclear(recs, nuclei, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    atom = syn.full_tensor_atom()
+    va = ref.nuclear(atom, [(10.0, (0.0, 0.0, 0.0))], (0.0, 0.0, 0.1), (0.0, 0.0, 0.0))
+    np.savez_compressed(HERE / "nuclear.npz", mol_field=v1, mol_zero=v0, atom=va,
+                        charges=np.asarray([z for z, _ in nuclei]),
+                        centers=np.asarray([c for _, c in nuclei]))
+
+
 def main():
     if build_ref.build() is None:
         raise SystemExit("the reference checkout is required to generate fixtures")
     ref = O.Reference()
     orc = O.Oracle()
-    (HERE / "boys.json").write_text(json.dumps(boys_fixture(ref)))
-    (HERE / "primitive_eri_m8.json").write_text(json.dumps(m8_fixture(ref)))
-    blocks_fixture(ref, orc)
-    (HERE / "cholesky.json").write_text(json.dumps(cholesky_fixture(ref)))
+    only = set(sys.argv[1:])
+    if not only or "boys" in only:
+        (HERE / "boys.json").write_text(json.dumps(boys_fixture(ref)))
+    if not only or "m8" in only:
+        (HERE / "primitive_eri_m8.json").write_text(json.dumps(m8_fixture(ref)))
+    if not only or "blocks" in only:
+        blocks_fixture(ref, orc)
+    if not only or "nuclear" in only:
+        nuclear_fixture(ref)
+    if not only or "cholesky" in only:
+        (HERE / "cholesky.json").write_text(json.dumps(cholesky_fixture(ref)))
     for p in sorted(HERE.iterdir()):
         print(p.name, p.stat().st_size)
 

@@ -75,3 +75,23 @@ def test_canonical_quartet_enumeration(oracle):
     for ns in (1, 2, 3, 5):
         np.testing.assert_array_equal(gi.canonical_quartets(ns), oracle.canonical_quartets(ns))
     assert len(oracle.canonical_quartets(72)) == 6722352
+
+
+def test_nuclear_attraction_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of src/nuclear.cpp against the reference library's
+    compute_nuclear_attraction_matrix (golden nuclear.npz)."""
+    from giaoint_gb300 import synthetic as syn
+
+    g = golden.nuclear
+    recs = syn.random_molecule(7, natoms=3)
+    nuclei = [(float(z), tuple(c)) for z, c in zip(g["charges"], g["centers"])]
+    v1 = oracle.nuclear(recs, nuclei, (0.05, -0.1, 0.12), (0.3, 0.1, -0.2))
+    v0 = oracle.nuclear(recs, nuclei, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+    va = oracle.nuclear(syn.full_tensor_atom(), [(10.0, (0.0, 0.0, 0.0))], (0.0, 0.0, 0.1), (0.0, 0.0, 0.0))
+    np.testing.assert_allclose(v1, g["mol_field"], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(v0, g["mol_zero"], rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(va, g["atom"], rtol=1e-13, atol=1e-13)
+    # Hermitian, and the field changes it
+    assert np.abs(v1 - v1.conj().T).max() < 1e-12
+    assert np.abs(v1 - v0).max() > 1e-6
+
