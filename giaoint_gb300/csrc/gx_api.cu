@@ -177,6 +177,11 @@ struct gx_context {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    // auxiliary streams on which the class launches of one plan execution run
+    // concurrently (fork/join with events on `stream`)
+    std::vector<cudaStream_t> aux;
+    std::vector<cudaEvent_t> aux_done;
+    cudaEvent_t fork = nullptr;
     double boys_table_agreement = 0.0;
     DeviceBuffer boys_S, boys_E0, gl, herm, rec_plan, rec_plan_off, status;
     std::mutex mu;
@@ -836,10 +841,39 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
     const auto& tuned = plan.tuned[precision];
     const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
     static const ClassConf kDefault{};
-    for (size_t ci = 0; ci < plan.classes.size(); ++ci)
-        launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
-                     gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s);
-    return 1 + (int)plan.classes.size();
+    const size_t nc = plan.classes.size();
+    // The classes write disjoint output blocks, so they run concurrently on
+    // the auxiliary streams: a plan of many small classes (a Cholesky column
+    // batch) costs about its longest class instead of the sum, and the tails
+    // of large classes overlap.  Under stream capture this becomes parallel
+    // graph branches.
+    const int K = (int)std::min<size_t>(nc, 8);
+    if (K > 1) {
+        if (ctx->aux.empty()) {
+            ctx->aux.resize(8);
+            ctx->aux_done.resize(8);
+            for (int k = 0; k < 8; ++k) {
+                GX_CUDA(cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking));
+                GX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done[k], cudaEventDisableTiming));
+            }
+            GX_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+        }
+        GX_CUDA(cudaEventRecord(ctx->fork, s));
+        for (int k = 0; k < K; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
+        for (size_t ci = 0; ci < nc; ++ci)
+            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters,
+                         ctx->aux[ci % K]);
+        for (int k = 0; k < K; ++k) {
+            GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
+            GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
+        }
+    } else {
+        for (size_t ci = 0; ci < nc; ++ci)
+            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s);
+    }
+    return 1 + (int)nc;
 }
 
 // Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
@@ -1185,6 +1219,9 @@ void gx_context_destroy(gx_context* ctx) {
     cudaStreamSynchronize(ctx->stream);
     drop_cached_plans(ctx, nullptr);
     ctx->pair_classes.clear();
+    for (auto st : ctx->aux) cudaStreamDestroy(st);
+    for (auto ev : ctx->aux_done) cudaEventDestroy(ev);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

@@ -169,11 +169,14 @@ __global__ void chol_gemv_kernel(const T* L, long long ld, int rank, long long p
     for (int r0 = 0; r0 < rank; r0 += 256) {
         const int nr = min(256, rank - r0);
         __syncthreads();
-        if ((int)threadIdx.x < nr) coef[threadIdx.x] = L[(long long)(r0 + threadIdx.x) * ld + piv];
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) coef[i] = L[(long long)(r0 + i) * ld + piv];
         __syncthreads();
         if (j < N) {
+            // eight independent row loads in flight per thread: the GEMV is
+            // bound by HBM bandwidth, not by load latency
+#pragma unroll 8
             for (int r = 0; r < nr; ++r) {
-                const T lv = L[(long long)(r0 + r) * ld + j];
+                const T lv = __ldg(&L[(long long)(r0 + r) * ld + j]);
                 if constexpr (sizeof(T) == 8) {
                     acc -= coef[r] * lv;
                 } else {
@@ -219,13 +222,13 @@ cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, l
                              void* work, int n, double* res, double* scale, void* Lrow, void* partial, void* out,
                              cudaStream_t s) {
     const long long N = (long long)n * n;
-    const int blocks = (int)((N + 255) / 256);
+    const int blocks = (int)((N + 127) / 128);
     if (real) {
-        chol_gemv_kernel<double><<<blocks, 256, 0, s>>>(static_cast<const double*>(L), ld, rank, piv,
+        chol_gemv_kernel<double><<<blocks, 128, 0, s>>>(static_cast<const double*>(L), ld, rank, piv,
                                                         static_cast<const double*>(column),
                                                         static_cast<double*>(work), N);
     } else {
-        chol_gemv_kernel<double2><<<blocks, 256, 0, s>>>(static_cast<const double2*>(L), ld, rank, piv,
+        chol_gemv_kernel<double2><<<blocks, 128, 0, s>>>(static_cast<const double2*>(L), ld, rank, piv,
                                                          static_cast<const double2*>(column),
                                                          static_cast<double2*>(work), N);
     }
