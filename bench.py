@@ -185,6 +185,19 @@ def cholesky_leg(gi, nat, ctx, run_cpu: bool):
         while k < min(len(ref.pivots), len(res.pivots)) and tuple(ref.pivots[k]) == tuple(res.pivots[k]):
             k += 1
         out["pivots_equal_prefix"] = k
+        if k < min(len(ref.pivots), len(res.pivots)):
+            # residual gap of the two choices at the first divergence, from the
+            # port's own factors: parity requires equal pivots only where it
+            # exceeds 1e-10 (a near tie otherwise)
+            n = res.vectors.shape[1]
+            L = ref.vectors[:k].reshape(k, n * n)
+            orc = O.Oracle()
+            pairs = [(a_, b_) for a_ in range(len(recs)) for b_ in range(a_, len(recs))]
+            diag = orc.cholesky_diagonal(recs, pairs, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), threads).ravel()
+            rk = diag - (np.abs(L) ** 2).sum(axis=0)  # the residual diagonal before pivot k
+            a = int(ref.pivots[k][0]) * n + int(ref.pivots[k][1])
+            b = int(res.pivots[k][0]) * n + int(res.pivots[k][1])
+            out["first_divergence_residual_gap"] = float(abs(rk[a] - rk[b]))
         out["speedup_vs_cpu_port"] = cpu_s / gpu_s
     return out
 

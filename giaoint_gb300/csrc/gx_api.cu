@@ -847,12 +847,13 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
     // batch) costs about its longest class instead of the sum, and the tails
     // of large classes overlap.  Under stream capture this becomes parallel
     // graph branches.
-    const int K = (int)std::min<size_t>(nc, 8);
+    constexpr int kAux = 32;
+    const int K = (int)std::min<size_t>(nc, kAux);
     if (K > 1) {
         if (ctx->aux.empty()) {
-            ctx->aux.resize(8);
-            ctx->aux_done.resize(8);
-            for (int k = 0; k < 8; ++k) {
+            ctx->aux.resize(kAux);
+            ctx->aux_done.resize(kAux);
+            for (int k = 0; k < kAux; ++k) {
                 GX_CUDA(cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking));
                 GX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done[k], cudaEventDisableTiming));
             }
@@ -1725,9 +1726,14 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         }
         GX_CUDA(cudaMemcpyAsync(d_res.ptr, d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
         CholRed red;
+        int status_code = 0;
         auto fetch_red = [&] {
+            // the reduction result and the kernels' status word in one wait (a
+            // failure in a column batch is reported before the next pivot)
             GX_CUDA(cudaMemcpyAsync(&red, d_red.ptr, sizeof red, cudaMemcpyDeviceToHost, st));
+            GX_CUDA(cudaMemcpyAsync(&status_code, ctx->status.ptr, sizeof status_code, cudaMemcpyDeviceToHost, st));
             GX_CUDA(cudaStreamSynchronize(st));
+            if (status_code) check_status(ctx);
         };
         GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
         fetch_red();
@@ -1749,7 +1755,24 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         std::list<std::pair<int64_t, int>> lru;   // raw-column cache, oldest first
         std::map<int64_t, std::list<std::pair<int64_t, int>>::iterator> lru_pos;
         std::vector<double> hostblk;
-        std::map<std::pair<int, int>, std::unique_ptr<PlanData>> column_plans;
+        // Column evaluation of one pivot shell pair: its plan and block offsets.
+        struct ColumnPlan {
+            PlanData plan;
+            DeviceBuffer boff;
+            int nblocks = 0;
+            int64_t entries = 0;
+        };
+        std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
+        DeviceBuffer column_info;
+        {
+            // largest column batch: all (x, y) blocks against the largest pivot pair
+            int64_t sum_xy = 0, max_ao = 0;
+            for (int x = 0; x < ns; ++x) {
+                max_ao = std::max<int64_t>(max_ao, b->nao_of(x));
+                for (int y = real ? x : 0; y < ns; ++y) sum_xy += b->nao_of(x) * b->nao_of(y);
+            }
+            ctx->scratch_a.reserve(std::max<int64_t>(sum_xy * max_ao * max_ao, 1) * sizeof(double2));
+        }
         int64_t rank = 0;
         auto residual_at = [&](const std::vector<int64_t>& idx, std::vector<double>& vals) {
             vals.resize(idx.size());
@@ -1826,30 +1849,36 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                                                                                  std::min(32, opt->pivot_batch_size)));
                 drop_batch();
                 cands = keep;
-                // columns (mu nu | p1 p0) for all shell pairs (real: b >= a)
+                // columns (mu nu | p1 p0) for all shell pairs (real: b >= a).  The
+                // quartet list, its plan and block offsets depend only on the
+                // pivot shell pair: built once per factorisation and reused.
                 const int sa = a, sb = c;
-                std::vector<QuartetRequest> req;
-                std::vector<long long> boff;
-                std::vector<int> info;
-                int64_t off = 0;
-                for (int x = 0; x < ns; ++x)
-                    for (int y = real ? x : 0; y < ns; ++y) {
-                        req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
-                        boff.push_back(off);
-                        info.insert(info.end(), {(int)b->ao_off[x], (int)b->ao_off[y], (int)b->nao_of(x),
-                                                 (int)b->nao_of(y), x == y ? 1 : 0});
-                        off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
-                    }
-                ctx->scratch_a.reserve(off * sizeof(double2));
-                // the column quartet list depends only on the pivot shell pair:
-                // build its plan once per factorisation
-                auto& cplan = column_plans[{sa, sb}];
-                if (!cplan) {
-                    cplan = std::make_unique<PlanData>();
-                    build_plan(ctx, b, req, *cplan);
+                auto& cp = column_plans[{sa, sb}];
+                if (!cp) {
+                    cp = std::make_unique<ColumnPlan>();
+                    std::vector<QuartetRequest> req;
+                    std::vector<long long> boff;
+                    int64_t off = 0;
+                    for (int x = 0; x < ns; ++x)
+                        for (int y = real ? x : 0; y < ns; ++y) {
+                            req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
+                            boff.push_back(off);
+                            off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
+                        }
+                    build_plan(ctx, b, req, cp->plan);
+                    upload(cp->boff, boff, st);
+                    cp->nblocks = (int)req.size();
+                    cp->entries = off;
                 }
-                run_plan(ctx, b, iB, iO, *cplan, ctx->scratch_a.as<double2>(), nullptr, nullptr, GX_PRECISION_FP64,
-                         0.0, nullptr);
+                if (column_info.ptr == nullptr) {
+                    std::vector<int> info;
+                    for (int x = 0; x < ns; ++x)
+                        for (int y = real ? x : 0; y < ns; ++y)
+                            info.insert(info.end(), {(int)b->ao_off[x], (int)b->ao_off[y], (int)b->nao_of(x),
+                                                     (int)b->nao_of(y), x == y ? 1 : 0});
+                    upload(column_info, info, st);
+                }
+                execute_plan(ctx, b, iB, iO, cp->plan, ctx->scratch_a.as<double2>(), GX_PRECISION_FP64, 0.0, nullptr);
                 std::vector<int> cl;
                 std::vector<void*> dst;
                 for (int64_t f : cands) {
@@ -1859,12 +1888,10 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                     cand_slot.push_back(slot);
                     dst.push_back(pool.ptr(slot));
                 }
-                upload(d_boff, boff, st);
-                upload(d_info, info, st);
                 upload(d_cand, cl, st);
                 upload(d_dst, dst, st);
-                GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), d_boff.as<long long>(),
-                                             d_info.as<int>(), (int)req.size(), d_cand.as<int>(), (int)cands.size(),
+                GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), cp->boff.as<long long>(),
+                                             column_info.as<int>(), cp->nblocks, d_cand.as<int>(), (int)cands.size(),
                                              (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
                 if (reuse) {
                     for (size_t k = 0; k < cands.size(); ++k) {
