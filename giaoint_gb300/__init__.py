@@ -21,7 +21,19 @@ from ._types import (
 )
 from .boys import BoysRegion, boys, boys_with_diagnostics
 from .cholesky import CholeskyERI, cholesky_eri
-from .eri import EriBatch, canonical_quartets, eri, eri_batches, eri_schwarz_bounds, eri_shell, primitive_eri
+from .eri import (
+    EriBatch,
+    EriDerivativeBatch,
+    canonical_quartets,
+    eri,
+    eri_batches,
+    eri_center_derivatives_shell,
+    eri_derivative_batches,
+    eri_schwarz_bounds,
+    eri_shell,
+    primitive_eri,
+    primitive_eri_center_derivatives,
+)
 from .nuclear import nuclear_attraction, nuclear_attraction_shell, primitive_nuclear_attraction
 
 __version__ = "0.1.0"
@@ -33,6 +45,7 @@ __all__ = [
     "CartesianExponent",
     "CholeskyERI",
     "EriBatch",
+    "EriDerivativeBatch",
     "MagneticField",
     "Nucleus",
     "PrimitiveGaussian",
@@ -45,11 +58,14 @@ __all__ = [
     "cholesky_eri",
     "eri",
     "eri_batches",
+    "eri_center_derivatives_shell",
+    "eri_derivative_batches",
     "eri_schwarz_bounds",
     "eri_shell",
     "nuclear_attraction",
     "nuclear_attraction_shell",
     "primitive_eri",
+    "primitive_eri_center_derivatives",
     "primitive_nuclear_attraction",
     "primitive_normalization",
     "resolve_num_threads",

@@ -188,6 +188,7 @@ struct gx_context {
     std::map<std::pair<int, int>, std::unique_ptr<PairClassHost>> pair_classes;
     // scratch
     DeviceBuffer out, tasks, scratch_a, scratch_b, scratch_c;
+    DeviceBuffer deriv_vals, deriv_meta;
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -285,6 +286,11 @@ struct gx_basis {
     DeviceBuffer d_pp_a, d_pp_b, d_pp_pa, d_pp_pb, d_pp_class, d_Eoff, d_classes;
     std::vector<std::pair<int, int>> class_keys;
     std::unique_ptr<FieldPairs> pairs;
+    // centre-derivative basis (built on first use): the shells of this basis
+    // followed by their Z, U and D shells, and per-shell arrays for the
+    // combine kernel
+    std::unique_ptr<gx_basis> deriv;
+    DeviceBuffer d_shell_l, d_shell_ncontr, d_shell_raw, d_shell_center;
 
     gx::BasisDev dev() const {
         return gx::BasisDev{nseg, d_center.as<double>(), d_l.as<int>(), d_nprim.as<int>(), d_primoff.as<int>(),
@@ -966,6 +972,69 @@ std::vector<double> schwarz_values(gx_context* ctx, gx_basis* b, const double* B
     return q;
 }
 
+// Upload a basis (caller holds ctx->mu).
+std::unique_ptr<gx_basis> new_basis(gx_context* ctx, int nshell, const double* centers, const int* l,
+                                    const int* nprim, const int* ncontr, const double* exponents,
+                                    const double* coefs, const int* raw) {
+    auto b = std::make_unique<gx_basis>();
+    b->ctx = ctx;
+    b->ns = nshell;
+    b->center.assign(centers, centers + 3 * (size_t)nshell);
+    b->l.assign(l, l + nshell);
+    b->nprim.assign(nprim, nprim + nshell);
+    b->ncontr.assign(ncontr, ncontr + nshell);
+    size_t ne = 0, nc = 0;
+    for (int s = 0; s < nshell; ++s) {
+        if (l[s] < 0 || l[s] > 16) raise(GX_EINVAL, "shell angular momentum above 16 is not supported");
+        if (nprim[s] <= 0 || ncontr[s] <= 0) raise(GX_EINVAL, "a shell requires primitives and contractions");
+        ne += nprim[s];
+        nc += (size_t)nprim[s] * ncontr[s];
+    }
+    b->exps.assign(exponents, exponents + ne);
+    b->coefs.assign(coefs, coefs + nc);
+    b->raw.assign(nshell, 0);
+    if (raw)
+        for (int s = 0; s < nshell; ++s) b->raw[s] = raw[s] ? 1 : 0;
+    int64_t a = 0;
+    for (int s = 0; s < nshell; ++s) {
+        b->ao_off.push_back(a);
+        a += b->nao_of(s);
+    }
+    b->nao = a;
+    build_segments(b.get());
+    GX_CUDA(cudaStreamSynchronize(ctx->stream));
+    return b;
+}
+
+// Most recently used cached plan of basis `b` for a request list identified
+// by (h1, h2, count, entries); `make()` returns the request list on a miss.
+template <class Make>
+PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
+                      Make&& make) {
+    auto& cache = plan_cache(ctx);
+    auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
+        return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == entries;
+    });
+    if (hit == cache.end()) {
+        const std::vector<QuartetRequest> req = make();
+        auto plan = std::make_unique<PlanData>();
+        build_plan(ctx, b, req, *plan);
+        cache.push_front({b, h1, h2, count, entries, std::move(plan)});
+        size_t bytes = 0;
+        int kept_plans = 0;
+        for (auto it = cache.begin(); it != cache.end();) {
+            bytes += it->plan->tasks.bytes;
+            if (++kept_plans > 4 || (kept_plans > 1 && bytes > (size_t(2) << 30)))
+                it = cache.erase(it);
+            else
+                ++it;
+        }
+    } else {
+        cache.splice(cache.begin(), cache, hit);  // most recently used first
+    }
+    return *cache.front().plan;
+}
+
 int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
                    int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
                    int64_t* offsets, void* out, bool out_is_device, int64_t capacity, gx_eri_stats* stats) {
@@ -1049,11 +1118,7 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         float ms = 0.f;
         int64_t nprim = 0, evaluated[2] = {0, 0};
         if (count) {
-            auto& cache = plan_cache(ctx);
-            auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
-                return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == off;
-            });
-            if (hit == cache.end()) {
+            PlanData& plan = lookup_plan(ctx, b, h1, h2, count, off, [&] {
                 std::vector<QuartetRequest> req;
                 req.reserve((size_t)count);
                 int64_t o = 0;
@@ -1063,24 +1128,10 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                     req.push_back({x[0], x[1], x[2], x[3], o});
                     o += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
                 }
-                auto plan = std::make_unique<PlanData>();
-                build_plan(ctx, b, req, *plan);
-                cache.push_front({b, h1, h2, count, off, std::move(plan)});
-                size_t bytes = 0;
-                int kept_plans = 0;
-                for (auto it = cache.begin(); it != cache.end();) {
-                    bytes += it->plan->tasks.bytes;
-                    if (++kept_plans > 4 || (kept_plans > 1 && bytes > (size_t(2) << 30)))
-                        it = cache.erase(it);
-                    else
-                        ++it;
-                }
-            } else {
-                cache.splice(cache.begin(), cache, hit);  // most recently used first
-            }
-            apply_recorded_tuning(ctx, b, precision, *cache.front().plan);
-            run_plan(ctx, b, B, O, *cache.front().plan, dout, &ms, &nprim, precision, mixed_cutoff,
-                     stats ? evaluated : nullptr);
+                return req;
+            });
+            apply_recorded_tuning(ctx, b, precision, plan);
+            run_plan(ctx, b, B, O, plan, dout, &ms, &nprim, precision, mixed_cutoff, stats ? evaluated : nullptr);
         }
         if (!out_is_device && off)
             GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1094,6 +1145,200 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             stats->skipped_primitive_quartets = nprim - evaluated[0] - evaluated[1];
             stats->kernel_ms = ms;
         }
+    });
+}
+
+// ---------------------------------------------------------------------------
+// ERI centre derivatives
+// ---------------------------------------------------------------------------
+
+// Exponent-dependent factor of the primitive normalisation,
+// g(alpha, l) = (2 alpha / pi)^{3/4} (4 alpha)^{l/2}; the component factor
+// prod_x ((2 l_x - 1)!!)^{-1/2} is applied by the combine kernel.
+double norm_radial(double alpha, int l) {
+    return std::exp(0.75 * std::log(2.0 * alpha / M_PI) + 0.5 * l * std::log(4.0 * alpha));
+}
+
+// Derived-shell groups of the centre-derivative basis.
+enum { kDerivZ = 0, kDerivU = 1, kDerivD = 2 };
+
+// The centre-derivative basis of `b`: shells 0..ns-1 are the shells of b;
+// then, for every shell s with l <= 15, Z_s (l + 1, coefficients
+// w g(alpha, l) 2 alpha) and U_s (l + 1, coefficients w g(alpha, l)), and for
+// l >= 1 D_s (l - 1, coefficients w g(alpha, l)), all with raw primitives
+// (no Cartesian normalisation).  A raw shell of b keeps g = 1.  Built on first
+// use and kept with b; deriv_index[3 ns] maps (group, s) to the derived shell.
+gx_basis* derivative_basis(gx_context* ctx, gx_basis* b, std::vector<int>& index) {
+    const int ns = b->ns;
+    std::vector<double> centers(b->center);
+    std::vector<int> l(b->l), np(b->nprim), nc(b->ncontr), raw(b->raw);
+    std::vector<double> exps(b->exps), coefs(b->coefs);
+    index.assign(3 * (size_t)ns, -1);
+    int next = ns;
+    for (int g = 0; g < 3; ++g) {
+        size_t eo = 0, co = 0;
+        for (int s = 0; s < ns; ++s) {
+            const int ls = b->l[s];
+            const bool present = g == kDerivD ? ls >= 1 : ls <= 15;
+            if (present) {
+                index[(size_t)g * ns + s] = next++;
+                for (int k = 0; k < 3; ++k) centers.push_back(b->center[3 * s + k]);
+                l.push_back(g == kDerivD ? ls - 1 : ls + 1);
+                np.push_back(b->nprim[s]);
+                nc.push_back(b->ncontr[s]);
+                raw.push_back(1);
+                for (int p = 0; p < b->nprim[s]; ++p) exps.push_back(b->exps[eo + p]);
+                for (int x = 0; x < b->ncontr[s]; ++x)
+                    for (int p = 0; p < b->nprim[s]; ++p) {
+                        const double alpha = b->exps[eo + p];
+                        double c = b->coefs[co + (size_t)x * b->nprim[s] + p];
+                        if (!b->raw[s]) c *= norm_radial(alpha, ls);
+                        if (g == kDerivZ) c *= 2.0 * alpha;
+                        coefs.push_back(c);
+                    }
+            }
+            eo += b->nprim[s];
+            co += (size_t)b->nprim[s] * b->ncontr[s];
+        }
+    }
+    if (!b->deriv) {
+        b->deriv = new_basis(ctx, next, centers.data(), l.data(), np.data(), nc.data(), exps.data(), coefs.data(),
+                             raw.data());
+        std::vector<int> sl(b->l), sn(b->ncontr), sr(b->raw);
+        upload(b->d_shell_l, sl, ctx->stream);
+        upload(b->d_shell_ncontr, sn, ctx->stream);
+        upload(b->d_shell_raw, sr, ctx->stream);
+        upload(b->d_shell_center, b->center, ctx->stream);
+    }
+    return b->deriv.get();
+}
+
+// Centre derivatives of nq shell quartets: blocks (4, 3, na, nb, nc, nd) at
+// offsets[i] (complex elements), in input order.
+int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
+                        int64_t nq, int64_t* offsets, void* out, bool out_is_device, int64_t capacity,
+                        float* kernel_ms) {
+    return guarded([&] {
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        if (nq < 0) raise(GX_EINVAL, "negative quartet count");
+        if (nq > (int64_t)INT32_MAX) raise(GX_ELENGTH, "derivative batch size overflow");
+        check_field(B, O);
+        const uint32_t ns = (uint32_t)b->ns;
+        int64_t off = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* x = quartets + 4 * i;
+            int L = 0;
+            int64_t size = 1;
+            for (int k = 0; k < 4; ++k) {
+                if (x[k] >= ns) raise(GX_ERANGE, "derivative shell quartet index is out of range");
+                if (b->l[x[k]] > 15) raise(GX_EINVAL, "ERI centre derivatives support shells through l = 15");
+                L += b->l[x[k]];
+                size *= b->nao_of(x[k]);
+            }
+            if (L + 1 > 32) raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
+            offsets[i] = off;
+            off += 12 * size;
+        }
+        offsets[nq] = off;
+        if (off > capacity) raise(GX_ELENGTH, "derivative output buffer is too small");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        float ms = 0.f;
+        if (nq == 0) {
+            if (kernel_ms) *kernel_ms = 0.f;
+            return;
+        }
+        std::vector<int> dix;
+        gx_basis* db = derivative_basis(ctx, b, dix);
+        const bool field = B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0;
+        // derived blocks per quartet: for each slot Z, [D], [U]; then [plain]
+        std::vector<uint32_t> dq;
+        dq.reserve((size_t)nq * 4 * (field ? 13 : 8));
+        std::vector<long long> doff((size_t)nq);
+        int64_t dtotal = 0;
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* x = quartets + 4 * i;
+            doff[i] = dtotal;
+            auto add = [&](int k, int g) {
+                uint32_t y[4] = {x[0], x[1], x[2], x[3]};
+                int64_t size = 1;
+                if (g >= 0) y[k] = (uint32_t)dix[(size_t)g * ns + x[k]];
+                for (int j = 0; j < 4; ++j) size *= db->nao_of(y[j]);
+                dq.insert(dq.end(), y, y + 4);
+                dtotal += size;
+            };
+            for (int k = 0; k < 4; ++k) {
+                add(k, kDerivZ);
+                if (b->l[x[k]] > 0) add(k, kDerivD);
+                if (field) add(k, kDerivU);
+            }
+            if (field) add(0, -1);
+        }
+        const int64_t dcount = (int64_t)dq.size() / 4;
+        uint64_t h1 = 0x452821E638D01377ull ^ (uint64_t)dcount, h2 = 0xBE5466CF34E90C6Cull;
+        for (int64_t i = 0; i < dcount; ++i) {
+            uint64_t v0, v1;
+            std::memcpy(&v0, &dq[4 * i], 8);
+            std::memcpy(&v1, &dq[4 * i + 2], 8);
+            h1 = (((h1 ^ v0) * 0x9E3779B97F4A7C15ull) ^ v1) * 0xBF58476D1CE4E5B9ull;
+            h1 ^= h1 >> 31;
+            h2 = (h2 + v0 * 0xC2B2AE3D27D4EB4Full + (v1 ^ (uint64_t)i)) * 0x94D049BB133111EBull;
+            h2 ^= h2 >> 29;
+        }
+        PlanData& plan = lookup_plan(ctx, db, h1, h2, dcount, dtotal, [&] {
+            std::vector<QuartetRequest> req;
+            req.reserve((size_t)dcount);
+            int64_t o = 0;
+            for (int64_t i = 0; i < dcount; ++i) {
+                const uint32_t* y = &dq[4 * i];
+                req.push_back({y[0], y[1], y[2], y[3], o});
+                o += db->nao_of(y[0]) * db->nao_of(y[1]) * db->nao_of(y[2]) * db->nao_of(y[3]);
+            }
+            return req;
+        });
+        apply_recorded_tuning(ctx, db, GX_PRECISION_FP64, plan);
+        ctx->deriv_vals.reserve(std::max<int64_t>(dtotal, 1) * sizeof(double2));
+        run_plan(ctx, db, B, O, plan, ctx->deriv_vals.as<double2>(), kernel_ms ? &ms : nullptr, nullptr,
+                 GX_PRECISION_FP64, 0.0, nullptr);
+        // metadata: quartets | offsets | derived offsets
+        const size_t qbytes = ((size_t)nq * 16 + 15) / 16 * 16;
+        const size_t obytes = (size_t)(nq + 1) * 8;
+        ctx->deriv_meta.reserve(qbytes + obytes + (size_t)nq * 8);
+        char* meta = ctx->deriv_meta.as<char>();
+        GX_CUDA(cudaMemcpyAsync(meta, quartets, (size_t)nq * 16, cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(cudaMemcpyAsync(meta + qbytes, offsets, obytes, cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(cudaMemcpyAsync(meta + qbytes + obytes, doff.data(), (size_t)nq * 8, cudaMemcpyHostToDevice,
+                                ctx->stream));
+        double2* dout;
+        if (out_is_device) {
+            dout = static_cast<double2*>(out);
+        } else {
+            ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
+            dout = ctx->out.as<double2>();
+        }
+        gx::DerivCombineArgs a{};
+        a.nq = (int)nq;
+        a.field = field ? 1 : 0;
+        a.quartets = reinterpret_cast<const uint32_t*>(meta);
+        a.offsets = reinterpret_cast<const long long*>(meta + qbytes);
+        a.derived_offsets = reinterpret_cast<const long long*>(meta + qbytes + obytes);
+        a.shell_l = b->d_shell_l.as<int>();
+        a.shell_ncontr = b->d_shell_ncontr.as<int>();
+        a.shell_raw = b->d_shell_raw.as<int>();
+        a.shell_center = b->d_shell_center.as<double>();
+        a.derived = ctx->deriv_vals.as<double2>();
+        a.out = dout;
+        for (int k = 0; k < 3; ++k) a.B[k] = B[k];
+        double df = 1.0;  // (2n - 1)!!
+        for (int n = 0; n < 18; ++n) {
+            if (n > 0) df *= 2.0 * n - 1.0;
+            a.inv_sqrt_df[n] = 1.0 / std::sqrt(df);
+        }
+        GX_CUDA(gx::launch_deriv_combine(a, off, ctx->sm_count, ctx->stream));
+        if (!out_is_device)
+            GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (kernel_ms) *kernel_ms = ms;
     });
 }
 
@@ -1234,34 +1479,7 @@ int gx_basis_create(gx_context* ctx, int nshell, const double* centers, const in
         if (nshell < 0) raise(GX_EINVAL, "negative shell count");
         std::lock_guard<std::mutex> lock(ctx->mu);
         GX_CUDA(cudaSetDevice(ctx->device));
-        auto b = std::make_unique<gx_basis>();
-        b->ctx = ctx;
-        b->ns = nshell;
-        b->center.assign(centers, centers + 3 * (size_t)nshell);
-        b->l.assign(l, l + nshell);
-        b->nprim.assign(nprim, nprim + nshell);
-        b->ncontr.assign(ncontr, ncontr + nshell);
-        size_t ne = 0, nc = 0;
-        for (int s = 0; s < nshell; ++s) {
-            if (l[s] < 0 || l[s] > 16) raise(GX_EINVAL, "shell angular momentum above 16 is not supported");
-            if (nprim[s] <= 0 || ncontr[s] <= 0) raise(GX_EINVAL, "a shell requires primitives and contractions");
-            ne += nprim[s];
-            nc += (size_t)nprim[s] * ncontr[s];
-        }
-        b->exps.assign(exponents, exponents + ne);
-        b->coefs.assign(coefs, coefs + nc);
-        b->raw.assign(nshell, 0);
-        if (raw)
-            for (int s = 0; s < nshell; ++s) b->raw[s] = raw[s] ? 1 : 0;
-        int64_t a = 0;
-        for (int s = 0; s < nshell; ++s) {
-            b->ao_off.push_back(a);
-            a += b->nao_of(s);
-        }
-        b->nao = a;
-        build_segments(b.get());
-        GX_CUDA(cudaStreamSynchronize(ctx->stream));
-        *out = b.release();
+        *out = new_basis(ctx, nshell, centers, l, nprim, ncontr, exponents, coefs, raw).release();
     });
 }
 
@@ -1271,6 +1489,7 @@ void gx_basis_destroy(gx_basis* b) {
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     drop_cached_plans(b->ctx, b);
+    if (b->deriv) drop_cached_plans(b->ctx, b->deriv.get());
     delete b;
 }
 
@@ -1319,6 +1538,18 @@ int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const
                         int64_t out_capacity, gx_eri_stats* stats) {
     return eri_batch_impl(ctx, basis, B, O, quartets, nq, precision, mixed_cutoff, screening_threshold, kept, offsets,
                           out_device, true, out_capacity, stats);
+}
+
+int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                              const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
+                              int64_t out_capacity, float* kernel_ms) {
+    return eri_derivative_impl(ctx, basis, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
+}
+
+int gx_eri_center_derivatives_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                     const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out_device,
+                                     int64_t out_capacity, float* kernel_ms) {
+    return eri_derivative_impl(ctx, basis, B, O, quartets, nq, offsets, out_device, true, out_capacity, kernel_ms);
 }
 
 int gx_eri_shell(gx_context* ctx, gx_basis* basis, int a, int b, int c, int d, const double* B, const double* O,

@@ -1,0 +1,158 @@
+// ERI centre derivatives d/dR_{slot,axis} (ab|cd) of London-orbital shell
+// quartets (compute_eri_center_derivatives and EriResponses::centers,
+// src/derivatives.cpp:53-87, 215-245, 556-640, 954-959 of the reference).
+//
+// For a Cartesian primitive with normalisation N(alpha, l) = g(alpha, l) h(l),
+//   g(alpha, l) = (2 alpha / pi)^{3/4} (4 alpha)^{|l|/2},
+//   h(l)        = prod_x ((2 l_x - 1)!!)^{-1/2},
+// the derivative of slot k along axis x is
+//   h(l_k) [ Z_k(l_k + 1_x) - l_x D_k(l_k - 1_x)
+//            + i phi_k sum_c (B x e_x)_c U_k(l_k + 1_c) ]
+//   + i phi_k sum_c (B x e_x)_c R_{k,c} (ab|cd),
+// phi_k = +1/2 on the bra side of a pair (slots 0, 2), -1/2 on the ket side,
+// where Z_k, U_k and D_k are contracted integrals with slot k replaced by a
+// raw-primitive shell of angular momentum l + 1, l + 1 and l - 1 and
+// contraction coefficients w g(alpha, l) 2 alpha, w g(alpha, l) and
+// w g(alpha, l).  Those blocks are ordinary ERIs of an extended basis and run
+// through the electron-repulsion class kernels; this kernel gathers them into
+// the (4, 3, na, nb, nc, nd) blocks of the reference layout.
+#include <algorithm>
+
+#include "gx_internal.h"
+
+namespace gx {
+
+namespace {
+
+__device__ __forceinline__ int comp_index(int l, int lx, int lz) {
+    const int m = l - lx;
+    return m * (m + 1) / 2 + lz;
+}
+
+// Component c of a shell of angular momentum l in the reference order
+// (x descending, then y descending).
+__device__ __forceinline__ void comp_of(int l, int c, int& lx, int& ly, int& lz) {
+    int m = 0;
+    while ((m + 1) * (m + 2) / 2 <= c) ++m;
+    lz = c - m * (m + 1) / 2;
+    lx = l - m;
+    ly = m - lz;
+}
+
+__global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) {
+    const long long total = a.offsets[a.nq];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        // quartet of element e: last i with offsets[i] <= e
+        int lo = 0, hi = a.nq - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&a.offsets[mid]) <= e) lo = mid;
+            else hi = mid - 1;
+        }
+        const int qi = lo;
+        int sh[4], l[4], nc[4], dim[4];
+        long long size = 1;
+        for (int k = 0; k < 4; ++k) {
+            sh[k] = (int)__ldg(&a.quartets[4 * qi + k]);
+            l[k] = __ldg(&a.shell_l[sh[k]]);
+            nc[k] = __ldg(&a.shell_ncontr[sh[k]]);
+            dim[k] = nc[k] * ncart(l[k]);
+            size *= dim[k];
+        }
+        long long rel = e - __ldg(&a.offsets[qi]);
+        const int d = (int)(rel / size);
+        long long r = rel - (long long)d * size;
+        const int k = d / 3, x = d - 3 * (d / 3);
+        int idx[4];
+        for (int j = 3; j >= 0; --j) {
+            idx[j] = (int)(r % dim[j]);
+            r /= dim[j];
+        }
+        // offsets of this quartet's derived blocks: per slot Z, [D], [U]; then [base]
+        long long off = __ldg(&a.derived_offsets[qi]);
+        long long zoff = 0, doff = -1, uoff = -1, boff = -1;
+        for (int j = 0; j < 4; ++j) {
+            const long long up = size / dim[j] * (nc[j] * ncart(l[j] + 1));
+            const long long dn = l[j] > 0 ? size / dim[j] * (nc[j] * ncart(l[j] - 1)) : 0;
+            if (j == k) zoff = off;
+            off += up;
+            if (l[j] > 0) {
+                if (j == k) doff = off;
+                off += dn;
+            }
+            if (a.field) {
+                if (j == k) uoff = off;
+                off += up;
+            }
+        }
+        if (a.field) boff = off;
+
+        const int lk = l[k], nck = ncart(lk);
+        const int xk = idx[k] / nck, ck = idx[k] - xk * nck;
+        int ang[3];
+        comp_of(lk, ck, ang[0], ang[1], ang[2]);
+        const double hk = __ldg(&a.shell_raw[sh[k]]) ? 1.0 : a.inv_sqrt_df[ang[0]] * a.inv_sqrt_df[ang[1]] *
+                                                              a.inv_sqrt_df[ang[2]];
+        // linear index of the derived block whose slot k has angular momentum
+        // lp and component (px, py, pz)
+        auto derived = [&](int lp, int px, int pz) {
+            long long li = 0;
+            for (int j = 0; j < 4; ++j) {
+                const int dj = j == k ? nc[j] * ncart(lp) : dim[j];
+                const int ij = j == k ? xk * ncart(lp) + comp_index(lp, px, pz) : idx[j];
+                li = li * dj + ij;
+            }
+            return li;
+        };
+        int up[3] = {ang[0], ang[1], ang[2]};
+        ++up[x];
+        double2 v = __ldg(&a.derived[zoff + derived(lk + 1, up[0], up[2])]);
+        if (ang[x] > 0) {
+            int dn[3] = {ang[0], ang[1], ang[2]};
+            --dn[x];
+            const double2 w = __ldg(&a.derived[doff + derived(lk - 1, dn[0], dn[2])]);
+            v.x -= ang[x] * w.x;
+            v.y -= ang[x] * w.y;
+        }
+        double2 res = c2(hk * v.x, hk * v.y);
+        if (a.field) {
+            const double phi = (k % 2 == 0) ? 0.5 : -0.5;
+            // (B x e_x)_c
+            double bx[3];
+            bx[0] = x == 2 ? a.B[1] : (x == 1 ? -a.B[2] : 0.0);
+            bx[1] = x == 0 ? a.B[2] : (x == 2 ? -a.B[0] : 0.0);
+            bx[2] = x == 1 ? a.B[0] : (x == 0 ? -a.B[1] : 0.0);
+            const double2 base = __ldg(&a.derived[boff + rel - (long long)d * size]);
+            double2 t = c2(0.0, 0.0);
+            for (int c = 0; c < 3; ++c) {
+                const double coef = phi * bx[c];
+                if (coef == 0.0) continue;
+                int uc[3] = {ang[0], ang[1], ang[2]};
+                ++uc[c];
+                const double2 u = __ldg(&a.derived[uoff + derived(lk + 1, uc[0], uc[2])]);
+                const double R = __ldg(&a.shell_center[3 * sh[k] + c]);
+                // coef * (h U + R base)
+                t.x += coef * (hk * u.x + R * base.x);
+                t.y += coef * (hk * u.y + R * base.y);
+            }
+            // i t
+            res.x -= t.y;
+            res.y += t.x;
+        }
+        a.out[e] = res;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_deriv_combine(const DerivCombineArgs& args, long long total, int sms, cudaStream_t s) {
+    if (total == 0) return cudaSuccess;
+    const long long want = (total + 255) / 256;
+    const long long cap = (long long)sms * 8;
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, cap));
+    deriv_combine_kernel<<<blocks, 256, 0, s>>>(args);
+    return cudaGetLastError();
+}
+
+}  // namespace gx

@@ -291,3 +291,160 @@ def primitive_eri(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussi
     nat.check(nat.lib().gx_primitive_eri(ctx.handle, nat.dptr(exps), nat.dptr(centers), nat.iptr(ang),
                                          nat.dptr(coefs), nat.iptr(norm), nat.dptr(B), nat.dptr(O), nat.dptr(out)))
     return complex(out[0], out[1])
+
+
+# ---------------------------------------------------------------------------
+# centre derivatives (src/derivatives.cpp:53-87, 215-245, 556-640, 954-959;
+# python/giao_integrals/eri.py:210-284; src/bindings.cpp:979-992, 1308-1324,
+# 2255-2303)
+# ---------------------------------------------------------------------------
+
+
+@dataclass(frozen=True)
+class EriDerivativeBatch(EriBatch):
+    """Packed local centre derivatives, with blocks (4, 3, na, nb, nc, nd).
+
+    Centre slots follow quartet order, independent even for repeated shells.
+    ``block()`` returns a view of ``values``.  Counts include screened requests.
+    """
+
+
+def _derivative_call(ctx, basis: Basis, q: np.ndarray, field, total: int, values: np.ndarray,
+                     offsets: np.ndarray) -> float:
+    B, O = field_arrays(field)
+    ms = ctypes.c_float()
+    nat.check(nat.lib().gx_eri_center_derivatives(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                                  nat.u32ptr(q), len(q), nat.i64ptr(offsets),
+                                                  nat.dptr(values.view(np.float64)), total, ctypes.byref(ms)))
+    return float(ms.value)
+
+
+def _eri_derivative_batch(basis: Basis, quartets, *, field: MagneticField | None = None,
+                          screening_threshold: float = 0.0, threads=None, bounds=None, context=None):
+    """Native packed derivative batch (src/bindings.cpp:2255-2303): returns
+    (quartets uint32[k,4], shapes int64[k,6], offsets int64[k+1], values
+    complex128, requested, screened)."""
+    resolve_num_threads(threads)
+    threshold = float(screening_threshold)
+    if not np.isfinite(threshold) or threshold < 0.0:
+        raise ValueError("screening_threshold must be finite and non-negative")
+    if threshold > 0.0 and bounds is None:
+        raise ValueError("derivative screening requires derivative bounds")
+    if bounds is not None and not bounds.matches(basis, field):
+        raise ValueError("derivative bounds do not match basis and field")
+    ctx = context or nat.default_context()
+    requested = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+    ns = len(basis.shells)
+    if len(requested) and (requested.min() < 0 or requested.max() >= ns):
+        raise IndexError("derivative shell quartet index is out of range")
+    q = requested
+    if threshold > 0.0 and len(q):
+        keep = bounds.quartet_bounds(q) >= threshold
+        q = q[keep]
+    q = np.ascontiguousarray(q.astype(np.uint32))
+    sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+    block = np.prod(sizes[q.astype(np.int64)], axis=1) if len(q) else np.zeros(0, dtype=np.int64)
+    total = int(12 * block.sum())
+    values = np.empty(max(total, 1), dtype=np.complex128)
+    offsets = np.zeros(len(q) + 1, dtype=np.int64)
+    if len(q):
+        _derivative_call(ctx, basis, q, field, total, values, offsets)
+    shapes = np.zeros((len(q), 6), dtype=np.int64)
+    if len(q):
+        shapes[:, 0] = 4
+        shapes[:, 1] = 3
+        shapes[:, 2:] = sizes[q.astype(np.int64)]
+    return q, shapes, offsets, values[:total], len(requested), len(requested) - len(q)
+
+
+def eri_derivative_batches(basis: Basis, *, field: MagneticField | None = None,
+                           quartets: Iterable[Sequence[int]] | None = None, target_bytes: int = 64 * 1024 * 1024,
+                           screening_threshold: float = 0.0, threads: int | None = None,
+                           ) -> Iterator[EriDerivativeBatch]:
+    """Stream ERI centre derivatives without a full derivative AO tensor
+    (python/giao_integrals/eri.py:220-284).
+
+    Each block has axes (quartet centre slot, nuclear xyz, mu, nu, lambda,
+    sigma); the London-phase centre response is included at fixed B and gauge
+    origin.  ``target_bytes`` bounds the packed complex values per batch (a
+    single oversized quartet is emitted alone).  Positive
+    ``screening_threshold`` values drop quartets whose derivative Schwarz
+    bound is below it."""
+    if (isinstance(target_bytes, (bool, np.bool_)) or not isinstance(target_bytes, (int, np.integer))
+            or target_bytes <= 0):
+        raise ValueError("target_bytes must be a positive integer")
+    threshold = float(screening_threshold)
+    if not np.isfinite(threshold) or threshold < 0:
+        raise ValueError("screening_threshold must be finite and non-negative")
+    thread_count = resolve_num_threads(threads)
+    bounds = _EriDerivativeSchwarzBounds(basis, field=field, threads=thread_count) if threshold > 0 else None
+    shells = basis.shells
+    packed: list[Quartet] = []
+    packed_bytes = 0
+
+    def emit() -> EriDerivativeBatch:
+        q, shapes, offsets, values, requested, screened = _eri_derivative_batch(
+            basis, packed, field=field, screening_threshold=threshold, threads=thread_count, bounds=bounds)
+        return EriDerivativeBatch(q, shapes, offsets, values, requested, screened)
+
+    for quartet in _checked_quartets(len(shells), quartets):
+        block_bytes = 12 * prod(shells[index].ao_count for index in quartet) * 16
+        if packed and packed_bytes + block_bytes > target_bytes:
+            yield emit()
+            packed.clear()
+            packed_bytes = 0
+        packed.append(quartet)
+        packed_bytes += block_bytes
+    if packed:
+        yield emit()
+
+
+def eri_center_derivatives_shell(a: Shell, b: Shell, c: Shell, d: Shell, *, field: MagneticField | None = None,
+                                 out=None, context=None) -> npt.NDArray[np.complex128]:
+    """Centre derivatives of one shell quartet, complex (4, 3, na, nb, nc, nd)
+    (compute_eri_center_derivatives; src/bindings.cpp:1308-1324)."""
+    for s in (a, b, c, d):
+        if not isinstance(s, Shell):
+            raise TypeError("a, b, c and d must be Shell objects")
+    shape = (4, 3, a.ao_count, b.ao_count, c.ao_count, d.ao_count)
+    result = _validate_out(out, shape)
+    ctx = context or nat.default_context()
+    basis = Basis([a, b, c, d])
+    q = np.array([[0, 1, 2, 3]], dtype=np.uint32)
+    total = int(np.prod(shape))
+    values = np.empty(total, dtype=np.complex128)
+    offsets = np.zeros(2, dtype=np.int64)
+    _derivative_call(ctx, basis, q, field, total, values, offsets)
+    result[...] = values.reshape(shape)
+    return result
+
+
+def primitive_eri_center_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussian,
+                                     d: PrimitiveGaussian, *, field: MagneticField | None = None,
+                                     context=None) -> npt.NDArray[np.complex128]:
+    """Centre derivatives of one primitive quartet, complex (4, 3)
+    (primitive_eri_center_derivatives; src/derivatives.cpp:836-842,
+    src/bindings.cpp:979-992)."""
+    shells, picks = [], []
+    scale = 1.0
+    for g in (a, b, c, d):
+        if not isinstance(g, PrimitiveGaussian):
+            raise TypeError("a, b, c and d must be PrimitiveGaussian objects")
+        l = sum(g.angular)
+        # unit-coefficient shell whose components carry N(alpha, component);
+        # unnormalised primitives divide it out again
+        shells.append(Shell(g.center, l, [g.exponent], [1.0], normalize=False))
+        comps = [(x, y, l - x - y) for x in range(l, -1, -1) for y in range(l - x, -1, -1)]
+        picks.append(comps.index(tuple(g.angular)))
+        scale *= g.coefficient
+        if not g.normalized:
+            scale /= nat.lib().gx_primitive_normalization(g.exponent, *g.angular)
+    full = eri_center_derivatives_shell(*shells, field=field, context=context)
+    return full[:, :, picks[0], picks[1], picks[2], picks[3]] * scale
+
+
+class _EriDerivativeSchwarzBounds:
+    """Derivative-density Schwarz factors (src/derivatives.cpp:1307-1387)."""
+
+    def __init__(self, basis: Basis, *, field: MagneticField | None = None, threads=None, context=None):
+        raise NotImplementedError("derivative screening bounds are not available yet")

@@ -140,6 +140,25 @@ int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const
                         double screening_threshold, uint32_t* kept, int64_t* offsets, void* out_device,
                         int64_t out_capacity, gx_eri_stats* stats);
 
+/* ERI centre derivatives of nq shell quartets, replacing
+ * compute_eri_derivative_blocks behind _eri_derivative_batch
+ * (src/bindings.cpp:2255-2303, src/derivatives.cpp:556-640, 954-959):
+ * block i, at offsets[i] (complex elements; the call writes the nq + 1
+ * offsets), is the C-order complex (4, 3, na, nb, nc, nd) array
+ * d/dR_{slot,axis} (ab|cd) of quartet i, slots in quartet order, London-phase
+ * centre response included at fixed B and gauge origin.  Shells through
+ * l = 15; combined angular order + 1 through 32.  out: host memory of
+ * out_capacity complex elements.  kernel_ms (may be NULL) receives the
+ * derived-integral kernel time. */
+int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                              const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
+                              int64_t out_capacity, float* kernel_ms);
+
+/* Same, with the blocks written to device memory `out_device`. */
+int gx_eri_center_derivatives_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                     const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out_device,
+                                     int64_t out_capacity, float* kernel_ms);
+
 /* One shell quartet (compute_eri, src/eri.cpp:454-585; bindings.cpp:616-639).
  * out: complex (na, nb, nc, nd) C order, host memory. */
 int gx_eri_shell(gx_context* ctx, gx_basis* basis, int a, int b, int c, int d, const double* B, const double* O,

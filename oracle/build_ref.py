@@ -1,8 +1,8 @@
 """Compile the reference's hot-path C++ sources in place into oracle/_ref.
 
 Test infrastructure only.  The reference's electron-repulsion path builds from
-seven of its own source files (src/types.cpp, overlap.cpp, hermite.cpp, boys.cpp,
-eri.cpp, cholesky.cpp, nuclear.cpp) with no generated headers and no external libraries, so
+nine of its own source files (src/types.cpp, overlap.cpp, hermite.cpp, boys.cpp,
+eri.cpp, cholesky.cpp, nuclear.cpp, derivatives.cpp, property.cpp) with no generated headers and no external libraries, so
 this recipe runs g++ on them directly (no CMake) together with
 oracle/ref_shim.cpp, and writes only into oracle/_ref/.  It needs the
 reference checkout, which exists only where fixtures are generated; the
@@ -20,7 +20,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", "/root/reference"))
-SOURCES = ["types.cpp", "overlap.cpp", "hermite.cpp", "boys.cpp", "eri.cpp", "cholesky.cpp", "nuclear.cpp"]
+SOURCES = ["types.cpp", "overlap.cpp", "hermite.cpp", "boys.cpp", "eri.cpp", "cholesky.cpp", "nuclear.cpp",
+           "derivatives.cpp", "property.cpp"]
 FLAGS = ["-std=c++20", "-O3", "-fPIC", "-fopenmp", "-DGIAO_HAS_OPENMP"]
 
 

@@ -1215,3 +1215,149 @@ int or_nuclear_matrix(BASIS_ARGS, int nnuc, const double* charges, const double*
     basis_free(&bs);
     return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* ERI centre derivatives (src/derivatives.cpp:53-87, 215-245, 556-640,  */
+/* 954-959)                                                             */
+/* ------------------------------------------------------------------ */
+
+/* Unit-coefficient primitive ERI with the angular part of slot k replaced. */
+static int eri_shifted(const prim_t* pr, int k, const int* ang, const pair_t* ab, const pair_t* cd, int real_zero,
+                       ws_t* w, cplx* v) {
+    prim_t q[4];
+    memcpy(q, pr, sizeof q);
+    for (int x = 0; x < 3; ++x) q[k].ang[x] = ang[x];
+    return eri_kernel(q, ab, cd, real_zero, w, v);
+}
+
+/* d/dR_slot,axis of one primitive quartet (raw primitives: coefficient 1,
+ * no normalisation): -l e(l-1) + 2 alpha e(l+1) + i phi sum_c (B x e_axis)_c
+ * [e(l+1_c) + R_c e(l)], phi = +1/2 on the bra side of each pair (slots 0,
+ * 2), -1/2 on the ket side (src/derivatives.cpp:53-87). */
+static int primitive_center_derivatives(const prim_t* pr, const pair_t* ab, const pair_t* cd, const field_t* f,
+                                        int real_zero, ws_t* w, cplx* out12) {
+    cplx base;
+    int rc = eri_kernel(pr, ab, cd, real_zero, w, &base);
+    if (rc) return rc;
+    for (int k = 0; k < 4; ++k) {
+        const double phi = (k % 2 == 0) ? 0.5 : -0.5;
+        cplx up[3];
+        for (int c = 0; c < 3; ++c) {
+            int a[3] = {pr[k].ang[0], pr[k].ang[1], pr[k].ang[2]};
+            ++a[c];
+            if ((rc = eri_shifted(pr, k, a, ab, cd, real_zero, w, &up[c]))) return rc;
+        }
+        for (int axis = 0; axis < 3; ++axis) {
+            cplx r = 2.0 * pr[k].alpha * up[axis];
+            if (pr[k].ang[axis] > 0) {
+                int a[3] = {pr[k].ang[0], pr[k].ang[1], pr[k].ang[2]};
+                --a[axis];
+                cplx dn;
+                if ((rc = eri_shifted(pr, k, a, ab, cd, real_zero, w, &dn))) return rc;
+                r -= (double)pr[k].ang[axis] * dn;
+            }
+            /* (B x e_axis) */
+            double e[3] = {0.0, 0.0, 0.0};
+            e[axis] = 1.0;
+            const double bx[3] = {f->B[1] * e[2] - f->B[2] * e[1], f->B[2] * e[0] - f->B[0] * e[2],
+                                  f->B[0] * e[1] - f->B[1] * e[0]};
+            for (int c = 0; c < 3; ++c) {
+                const double coef = phi * bx[c];
+                if (coef == 0.0) continue;
+                r += CMPLX(0.0, coef) * (up[c] + pr[k].center[c] * base);
+            }
+            out12[3 * k + axis] = r;
+        }
+    }
+    return 0;
+}
+
+/* Blocks (4, 3, na, nb, nc, nd) of nq shell quartets packed in input order,
+ * primitive and component loops of compute_quartet_block
+ * (src/derivatives.cpp:556-640). */
+int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
+                              double* out_) {
+    basis_t bs;
+    int rc = basis_init(&bs, ns, centers, ls, nprims, ncontrs, exps, coefs);
+    cplx* out = (cplx*)out_;
+    field_t f;
+    memcpy(f.B, B, sizeof f.B);
+    memcpy(f.O, O, sizeof f.O);
+    const int real_zero = B[0] == 0.0 && B[1] == 0.0 && B[2] == 0.0;
+    ws_t w;
+    memset(&w, 0, sizeof w);
+    size_t off = 0;
+    static int comps[4][153][3];
+    for (long qi = 0; qi < nq && !rc; ++qi) {
+        int sh[4], nc[4];
+        size_t shape[4];
+        for (int k = 0; k < 4; ++k) {
+            sh[k] = (int)quartets[4 * qi + k];
+            if (sh[k] < 0 || sh[k] >= ns) {
+                rc = set_err(-2, "derivative shell quartet index is out of range");
+                break;
+            }
+            nc[k] = cart_components(ls[sh[k]], comps[k]);
+            shape[k] = shell_ao(&bs, sh[k]);
+        }
+        if (rc) break;
+        const size_t block = shape[0] * shape[1] * shape[2] * shape[3];
+        cplx* o = out + off;
+        for (size_t i = 0; i < 12 * block; ++i) o[i] = 0.0;
+        w.boys_valid = 0;
+        for (int pa = 0; pa < nprims[sh[0]] && !rc; ++pa)
+            for (int pb = 0; pb < nprims[sh[1]] && !rc; ++pb) {
+                pair_t ab;
+                gaussian_product(exps[bs.eoff[sh[0]] + pa], centers + 3 * sh[0], exps[bs.eoff[sh[1]] + pb],
+                                 centers + 3 * sh[1], &f, &ab);
+                for (int pc = 0; pc < nprims[sh[2]] && !rc; ++pc)
+                    for (int pd = 0; pd < nprims[sh[3]] && !rc; ++pd) {
+                        pair_t cd;
+                        gaussian_product(exps[bs.eoff[sh[2]] + pc], centers + 3 * sh[2], exps[bs.eoff[sh[3]] + pd],
+                                         centers + 3 * sh[3], &f, &cd);
+                        const int pidx[4] = {pa, pb, pc, pd};
+                        for (int ca = 0; ca < nc[0] && !rc; ++ca)
+                            for (int cb = 0; cb < nc[1] && !rc; ++cb)
+                                for (int cc = 0; cc < nc[2] && !rc; ++cc)
+                                    for (int cdd = 0; cdd < nc[3] && !rc; ++cdd) {
+                                        const int cix[4] = {ca, cb, cc, cdd};
+                                        prim_t pr[4];
+                                        double norm = 1.0;
+                                        for (int k = 0; k < 4; ++k) {
+                                            pr[k].alpha = exps[bs.eoff[sh[k]] + pidx[k]];
+                                            for (int x = 0; x < 3; ++x) {
+                                                pr[k].center[x] = centers[3 * sh[k] + x];
+                                                pr[k].ang[x] = comps[k][cix[k]][x];
+                                            }
+                                            norm *= or_primitive_normalization(pr[k].alpha, pr[k].ang[0],
+                                                                               pr[k].ang[1], pr[k].ang[2]);
+                                        }
+                                        cplx d12[12];
+                                        rc = primitive_center_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12);
+                                        if (rc) break;
+                                        for (int xa = 0; xa < ncontrs[sh[0]]; ++xa)
+                                            for (int xb = 0; xb < ncontrs[sh[1]]; ++xb)
+                                                for (int xc = 0; xc < ncontrs[sh[2]]; ++xc)
+                                                    for (int xd = 0; xd < ncontrs[sh[3]]; ++xd) {
+                                                        const double kk =
+                                                            norm *
+                                                            coefs[bs.coff[sh[0]] + (size_t)xa * nprims[sh[0]] + pa] *
+                                                            coefs[bs.coff[sh[1]] + (size_t)xb * nprims[sh[1]] + pb] *
+                                                            coefs[bs.coff[sh[2]] + (size_t)xc * nprims[sh[2]] + pc] *
+                                                            coefs[bs.coff[sh[3]] + (size_t)xd * nprims[sh[3]] + pd];
+                                                        const size_t e =
+                                                            ((((size_t)xa * nc[0] + ca) * shape[1] +
+                                                              (size_t)xb * nc[1] + cb) * shape[2] +
+                                                             (size_t)xc * nc[2] + cc) * shape[3] +
+                                                            (size_t)xd * nc[3] + cdd;
+                                                        for (int dd = 0; dd < 12; ++dd) o[dd * block + e] += kk * d12[dd];
+                                                    }
+                                    }
+                    }
+            }
+        off += 12 * block;
+    }
+    ws_free(&w);
+    basis_free(&bs);
+    return rc;
+}

@@ -157,6 +157,15 @@ def _nuclei(nuclei):
     return ch, cc
 
 
+def _derivative_layout(shells, quartets):
+    """Quartet array, offsets and total of packed (4, 3, na, nb, nc, nd) blocks."""
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.uint32).reshape(-1, 4))
+    specs = as_specs(shells)
+    sizes = [12 * int(np.prod([specs[k].nao for k in row])) for row in q]
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return q, offsets, int(offsets[-1])
+
+
 def _vec3(v) -> np.ndarray:
     return np.ascontiguousarray([0.0, 0.0, 0.0] if v is None else v, dtype=np.float64)
 
@@ -278,6 +287,17 @@ class Oracle(_Backend):
                                                _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
         return out[: n * n].reshape(n, n)
 
+    def eri_center_derivatives(self, shells, quartets, B=None, O=None):
+        """Centre-derivative blocks (4, 3, na, nb, nc, nd) of each quartet,
+        packed in input order; returns (values, offsets)."""
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.or_eri_center_derivatives(*a.args(), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
+                                                       _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
+                                                       out.ctypes.data_as(_d)))
+        return out[:total], offsets
+
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)
         out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
@@ -368,6 +388,15 @@ class Reference(_Backend):
                                                 cc.ctypes.data_as(_d), _vec3(B).ctypes.data_as(_d),
                                                 _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
         return out[: n * n].reshape(n, n)
+
+    def eri_center_derivatives(self, shells, quartets, B=None, O=None):
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.ref_eri_center_derivatives(*self._bargs(a), q.ctypes.data_as(_u32),
+                                                        ctypes.c_long(len(q)), _vec3(B).ctypes.data_as(_d),
+                                                        _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[:total], offsets
 
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)

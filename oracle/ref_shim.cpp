@@ -14,6 +14,7 @@
 //   ref_cholesky_diagonal  <- src/bindings.cpp:2306-2314
 //   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
 #include "giao_integrals/boys.hpp"
+#include "giao_integrals/derivatives.hpp"
 #include "giao_integrals/eri.hpp"
 #include "giao_integrals/nuclear.hpp"
 #include "giao_integrals/types.hpp"
@@ -187,6 +188,30 @@ int ref_nuclear_matrix(int ns, const double* centers, const int* ls, const int* 
         const std::size_t n = basis.ao_count();
         giao::compute_nuclear_attraction_matrix(
             basis, nuclei, make_field(B, O), std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out), n * n));
+    });
+}
+
+// Centre-derivative blocks (4, 3, na, nb, nc, nd) of nq quartets, packed in
+// input order (compute_eri_center_derivatives, src/derivatives.cpp:954-959).
+int ref_eri_center_derivatives(int ns, const double* centers, const int* ls, const int* nprims,
+                               const int* ncontrs, const double* exps, const double* coefs,
+                               const int* normalize, const uint32_t* quartets, long nq, const double* B,
+                               const double* O, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        const auto field = make_field(B, O);
+        std::size_t off = 0;
+        for (long i = 0; i < nq; ++i) {
+            const auto& sh = basis.shells();
+            const auto& a = sh[quartets[4 * i]];
+            const auto& b = sh[quartets[4 * i + 1]];
+            const auto& c = sh[quartets[4 * i + 2]];
+            const auto& d = sh[quartets[4 * i + 3]];
+            const std::size_t size = 12 * giao::shell_quartet_size(a, b, c, d);
+            giao::compute_eri_center_derivatives(
+                a, b, c, d, field, std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out) + off, size));
+            off += size;
+        }
     });
 }
 

@@ -22,6 +22,7 @@ def golden():
         cholesky = json.loads((GOLDEN / "cholesky.json").read_text())
         blocks = dict(np.load(GOLDEN / "eri_blocks.npz"))
         nuclear = dict(np.load(GOLDEN / "nuclear.npz"))
+        derivatives = dict(np.load(GOLDEN / "derivatives.npz"))
 
     return G
 
@@ -31,3 +32,15 @@ def oracle():
     from oracle import oracle as O
 
     return O.Oracle()
+
+
+def derivative_systems(g):
+    """(name, shell specs, quartets) of the centre-derivative fixture."""
+    from oracle import oracle as O
+
+    out = []
+    for name in ("molecule3", "hand"):
+        specs = [O.ShellSpec(tuple(d["center"]), d["l"], d["exponents"], d["coefficients"], d["normalize"])
+                 for d in json.loads(str(g[f"{name}_shells"]))]
+        out.append((name, specs, g[f"{name}_quartets"]))
+    return out

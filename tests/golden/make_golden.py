@@ -4,7 +4,8 @@ Run where the reference checkout exists (GIAO_REFERENCE_ROOT, default the
 read-only reference path used to build oracle/_ref):
 
     python tests/golden/make_golden.py            # every fixture
-    python tests/golden/make_golden.py nuclear    # one fixture
+    python tests/golden/make_golden.py nuclear    # one fixture (boys, m8, blocks, nuclear,
+                                                  # derivatives, cholesky)
 
 Inputs and outputs:
 
@@ -22,6 +23,11 @@ Inputs and outputs:
   seeded three-atom molecule (nuclei at the atoms, charges 1, 2, 3; finite
   field with a shifted gauge origin, and zero field) and for the 19-AO atom
   (Z = 10 at the origin, B = (0, 0, 0.1));
+* ``derivatives.npz`` -- reference ``compute_eri_center_derivatives``
+  blocks (4, 3, na, nb, nc, nd) for a seeded three-atom molecule (seeded
+  canonical and arbitrary quartets, repeated shells) and a hand-made f/g
+  system with a two-contraction p shell, at a finite field with a shifted
+  gauge origin and at zero field;
 * ``cholesky.json`` -- the reference's own NumPy Cholesky driver
   (python/giao_integrals/cholesky.py, executed unmodified over the reference
   library's native diagonal/column generators) on the two-shell d/f system of
@@ -247,6 +253,45 @@ def nuclear_fixture(ref):
                         centers=np.asarray([c for _, c in nuclei]))
 
 
+DERIV_FIELD = (0.07, -0.04, 0.15)
+DERIV_ORIGIN = (0.2, -0.35, 0.1)
+
+
+def derivative_cases():
+    """Systems and quartet lists of the centre-derivative fixture: a seeded
+    three-atom molecule (seeded canonical and non-canonical quartets, plus
+    every slot repeating one shell), and a hand-made f/g system with a
+    two-contraction p shell."""
+    mol = O.as_specs(syn.random_molecule(5, natoms=3, box=4.0))
+    ns = len(mol)
+    rng = random.Random(20261203)
+    canon = [tuple(int(x) for x in q) for q in O.Oracle().canonical_quartets(ns)]
+    quartets = rng.sample(canon, min(24, len(canon)))
+    quartets += [tuple(rng.randrange(ns) for _ in range(4)) for _ in range(6)]
+    quartets += [(s, s, s, s) for s in range(0, ns, max(1, ns // 3))]
+    hand = [O.ShellSpec((0.1, -0.2, 0.3), 3, [0.9, 0.35], [[0.6, 0.5]]),
+            O.ShellSpec((-0.4, 0.5, 0.0), 4, [0.7], [[1.0]]),
+            O.ShellSpec((0.6, 0.2, -0.5), 1, [1.3, 0.4], [[0.5, 0.6], [0.3, -0.8]]),
+            O.ShellSpec((0.0, 0.0, 0.9), 0, [2.0, 0.5], [[0.4, 0.7]])]
+    hq = [(1, 3, 3, 3), (0, 3, 1, 3), (2, 0, 3, 3), (3, 3, 3, 3), (2, 3, 2, 3), (3, 2, 0, 3)]
+    return {"molecule3": (mol, quartets), "hand": (hand, hq)}
+
+
+def derivative_fixture(ref):
+    out = {}
+    for name, (specs, quartets) in derivative_cases().items():
+        q = np.asarray(quartets, dtype=np.uint32)
+        out[f"{name}_quartets"] = q
+        out[f"{name}_shells"] = np.asarray(json.dumps([s.__dict__ for s in specs]))
+        for label, B, origin in (("field", DERIV_FIELD, DERIV_ORIGIN), ("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))):
+            vals, offsets = ref.eri_center_derivatives(specs, q, B, origin)
+            out[f"{name}_{label}"] = vals
+            out[f"{name}_offsets"] = offsets
+    out["field"] = np.asarray(DERIV_FIELD)
+    out["origin"] = np.asarray(DERIV_ORIGIN)
+    np.savez_compressed(HERE / "derivatives.npz", **out)
+
+
 def main():
     if build_ref.build() is None:
         raise SystemExit("the reference checkout is required to generate fixtures")
@@ -261,6 +306,8 @@ def main():
         blocks_fixture(ref, orc)
     if not only or "nuclear" in only:
         nuclear_fixture(ref)
+    if not only or "derivatives" in only:
+        derivative_fixture(ref)
     if not only or "cholesky" in only:
         (HERE / "cholesky.json").write_text(json.dumps(cholesky_fixture(ref)))
     for p in sorted(HERE.iterdir()):

@@ -95,3 +95,59 @@ def test_nuclear_attraction_oracle_matches_reference(golden, oracle):
     assert np.abs(v1 - v1.conj().T).max() < 1e-12
     assert np.abs(v1 - v0).max() > 1e-6
 
+
+
+def test_eri_center_derivatives_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of compute_eri_center_derivatives
+    (src/derivatives.cpp:53-87, 215-245, 556-640) against the reference
+    library's blocks (golden derivatives.npz), zero and finite field."""
+    from conftest import derivative_systems
+
+    g = golden.derivatives
+    B, origin = tuple(g["field"]), tuple(g["origin"])
+    for name, specs, q in derivative_systems(g):
+        for label, field, o in (("field", B, origin), ("zero", None, None)):
+            vals, offsets = oracle.eri_center_derivatives(specs, q, field, o)
+            np.testing.assert_array_equal(offsets, g[f"{name}_offsets"])
+            ref = g[f"{name}_{label}"]
+            assert np.abs(vals - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (name, label)
+        # zero and finite field differ
+        assert np.abs(g[f"{name}_field"] - g[f"{name}_zero"]).max() > 1e-6
+
+
+def derivative_sum_rule_residual(specs, q, offsets, values, eri, eri_offsets, B, origin) -> float:
+    """max over blocks of |sum_slots d/dR - i (k_a - k_b + k_c - k_d) (ab|cd)| / max(1, max |block|).
+
+    Translating all four centres by delta multiplies a London-orbital ERI
+    (orbitals exp(-i k.r) phi(r - C), k = B x (C - O) / 2, fixed gauge
+    origin) by exp(i (k_a - k_b + k_c - k_d).delta), so the four slot
+    derivatives sum to i (k_a - k_b + k_c - k_d) times the ERI block."""
+    B = np.asarray(B, dtype=float)
+    O = np.asarray(origin, dtype=float)
+
+    def k(c):
+        return 0.5 * np.cross(B, np.asarray(c, dtype=float) - O)
+
+    worst = 0.0
+    for i, x in enumerate(np.asarray(q)):
+        blk = values[offsets[i]:offsets[i + 1]].reshape(4, 3, -1)
+        e = eri[eri_offsets[i]:eri_offsets[i + 1]]
+        K = k(specs[x[0]].center) - k(specs[x[1]].center) + k(specs[x[2]].center) - k(specs[x[3]].center)
+        r = np.abs(blk.sum(axis=0) - 1j * K[:, None] * e[None, :]).max()
+        worst = max(worst, r / max(1.0, np.abs(blk).max()))
+    return worst
+
+
+def test_eri_center_derivatives_translation_sum_rule_oracle(golden, oracle):
+    """The reference's derivative blocks obey the translation sum rule with
+    the oracle's ERI blocks, at zero and finite field."""
+    from conftest import derivative_systems
+
+    g = golden.derivatives
+    B, origin = tuple(g["field"]), tuple(g["origin"])
+    for name, specs, q in derivative_systems(g):
+        for label, field, o in (("field", B, origin), ("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))):
+            eri, eoff = oracle.eri_batch(specs, q, field, o)
+            r = derivative_sum_rule_residual(specs, q, g[f"{name}_offsets"], g[f"{name}_{label}"], eri, eoff,
+                                             field, o)
+            assert r <= 1e-11, (name, label, r)
