@@ -5,6 +5,7 @@
 // reference's error semantics.
 #include <algorithm>
 #include <array>
+#include <limits>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -291,6 +292,11 @@ struct gx_basis {
     // combine kernel
     std::unique_ptr<gx_basis> deriv;
     DeviceBuffer d_shell_l, d_shell_ncontr, d_shell_raw, d_shell_center;
+    // derivative-bound basis (built on first use): one raw single-primitive
+    // shell per (primitive, variant l / l + 1 / l - 1); bound_index[3 * g + v]
+    // for the g-th primitive of the basis (-1: absent)
+    std::unique_ptr<gx_basis> bound;
+    std::vector<int> bound_index;
 
     gx::BasisDev dev() const {
         return gx::BasisDev{nseg, d_center.as<double>(), d_l.as<int>(), d_nprim.as<int>(), d_primoff.as<int>(),
@@ -1213,6 +1219,175 @@ gx_basis* derivative_basis(gx_context* ctx, gx_basis* b, std::vector<int>& index
     return b->deriv.get();
 }
 
+// Index of Cartesian component k in the reference order (x descending, then y).
+int comp_index_host(const std::array<int, 3>& k) {
+    const int m = k[1] + k[2];
+    return m * (m + 1) / 2 + k[2];
+}
+
+// Derivative-density Schwarz factors of every ordered shell pair
+// (EriDerivativeSchwarzBounds, src/derivatives.cpp:1307-1372).  For
+// primitives a, b of components l_a, l_b with coefficients N(alpha, l),
+//   n(a', b') = N_a N_b sqrt|(b' a'|a' b')|  (unit raw primitives a', b'),
+// slot s of (a, b), axis x:
+//   2 alpha n(+1_x) + l_x n(-1_x) + sum_c |(B x e_x)_c| / 2 (n(+1_c) + |R_c| n),
+// contracted with |w_a w_b| over primitive pairs and maximised over
+// components, contractions, slots and axes; padded by (1 + 128 eps) and one ulp.
+// The diagonal integrals are FP64-exact blocks of the bound basis through the
+// class kernels, gathered on the device.
+void derivative_schwarz_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, double* values) {
+    const int ns = b->ns;
+    std::vector<int> goff(ns + 1, 0);  // first global primitive of each shell
+    for (int s = 0; s < ns; ++s) goff[s + 1] = goff[s] + b->nprim[s];
+    std::vector<int> eoff(ns + 1, 0), coff(ns + 1, 0);
+    for (int s = 0; s < ns; ++s) {
+        eoff[s + 1] = eoff[s] + b->nprim[s];
+        coff[s + 1] = coff[s] + b->nprim[s] * b->ncontr[s];
+    }
+    if (!b->bound) {
+        std::vector<double> centers, exps, coefs;
+        std::vector<int> l, np, nc, raw;
+        b->bound_index.assign(3 * (size_t)goff[ns], -1);
+        for (int s = 0; s < ns; ++s)
+            for (int p = 0; p < b->nprim[s]; ++p)
+                for (int v = 0; v < 3; ++v) {
+                    const int lv = v == 0 ? b->l[s] : (v == 1 ? b->l[s] + 1 : b->l[s] - 1);
+                    if (lv < 0 || lv > 16) continue;
+                    b->bound_index[3 * (size_t)(goff[s] + p) + v] = (int)l.size();
+                    for (int k = 0; k < 3; ++k) centers.push_back(b->center[3 * s + k]);
+                    l.push_back(lv);
+                    np.push_back(1);
+                    nc.push_back(1);
+                    raw.push_back(1);
+                    exps.push_back(b->exps[eoff[s] + p]);
+                    coefs.push_back(1.0);
+                }
+        b->bound = new_basis(ctx, (int)l.size(), centers.data(), l.data(), np.data(), nc.data(), exps.data(),
+                             coefs.data(), raw.data());
+    }
+    gx_basis* bb = b->bound.get();
+    // variants (left, right) of the diagonal blocks (right left | left right)
+    static const int kVar[5][2] = {{0, 0}, {1, 0}, {2, 0}, {0, 1}, {0, 2}};
+    // per unordered shell pair a <= c, primitive pair (p, q), variant: offset of
+    // its n_right x n_left diagonal values [right comp][left comp] (-1: absent)
+    std::vector<int64_t> pair_first((size_t)ns * ns, -1);
+    std::vector<QuartetRequest> req;
+    std::vector<long long> didx;
+    std::vector<int64_t> dpos;  // per (pair, p, q, variant) in order
+    int64_t off = 0;
+    for (int a = 0; a < ns; ++a)
+        for (int c = a; c < ns; ++c) {
+            pair_first[(size_t)a * ns + c] = (int64_t)dpos.size();
+            for (int p = 0; p < b->nprim[a]; ++p)
+                for (int q = 0; q < b->nprim[c]; ++q)
+                    for (int v = 0; v < 5; ++v) {
+                        const int sl = b->bound_index[3 * (size_t)(goff[a] + p) + kVar[v][0]];
+                        const int sr = b->bound_index[3 * (size_t)(goff[c] + q) + kVar[v][1]];
+                        if (sl < 0 || sr < 0) {
+                            dpos.push_back(-1);
+                            continue;
+                        }
+                        const int64_t nl = gx::ncart(bb->l[sl]), nr = gx::ncart(bb->l[sr]);
+                        req.push_back({(uint32_t)sr, (uint32_t)sl, (uint32_t)sl, (uint32_t)sr, off});
+                        dpos.push_back((int64_t)didx.size());
+                        for (int64_t cr = 0; cr < nr; ++cr)
+                            for (int64_t cl = 0; cl < nl; ++cl)
+                                didx.push_back(off + ((cr * nl + cl) * nl + cl) * nr + cr);
+                        off += nl * nl * nr * nr;
+                    }
+        }
+    std::vector<double> diag(didx.size());
+    if (!req.empty()) {
+        ctx->scratch_a.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
+        run_quartets(ctx, bb, B, O, req, ctx->scratch_a.as<double2>(), nullptr, nullptr, GX_PRECISION_FP64_EXACT);
+        ctx->scratch_b.reserve(didx.size() * sizeof(long long));
+        ctx->scratch_c.reserve(didx.size() * sizeof(double));
+        GX_CUDA(cudaMemcpyAsync(ctx->scratch_b.ptr, didx.data(), didx.size() * sizeof(long long),
+                                cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(gx::launch_gather_abs(ctx->scratch_a.as<double2>(), ctx->scratch_b.as<long long>(),
+                                      ctx->scratch_c.as<double>(), (long long)didx.size(), ctx->sm_count,
+                                      ctx->stream));
+        GX_CUDA(cudaMemcpyAsync(diag.data(), ctx->scratch_c.ptr, didx.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    const double eps = std::numeric_limits<double>::epsilon();
+#pragma omp parallel for schedule(dynamic)
+    for (int64_t pair = 0; pair < (int64_t)ns * ns; ++pair) {
+        const int sa = (int)(pair / ns), sb = (int)(pair % ns);
+        // blocks are stored for lo <= hi; slot 0 (left) is sa
+        const int lo = std::min(sa, sb), hi = std::max(sa, sb);
+        const bool swapped = sa > sb;
+        const int la = b->l[sa], lb = b->l[sb];
+        const auto ca_list = components(la), cb_list = components(lb);
+        const int na = b->nprim[sa], nb = b->nprim[sb], xa_n = b->ncontr[sa], xb_n = b->ncontr[sb];
+        double maximum = 0.0;
+        std::vector<double> contracted(6 * (size_t)xa_n * xb_n);
+        for (size_t ca = 0; ca < ca_list.size(); ++ca)
+            for (size_t cb = 0; cb < cb_list.size(); ++cb) {
+                std::fill(contracted.begin(), contracted.end(), 0.0);
+                for (int pa = 0; pa < na; ++pa)
+                    for (int pb = 0; pb < nb; ++pb) {
+                        const double alpha_a = b->exps[eoff[sa] + pa], alpha_b = b->exps[eoff[sb] + pb];
+                        const auto& A = ca_list[ca];
+                        const auto& Bc = cb_list[cb];
+                        const double Na = b->raw[sa] ? 1.0 : primitive_norm(alpha_a, A[0], A[1], A[2]);
+                        const double Nb = b->raw[sb] ? 1.0 : primitive_norm(alpha_b, Bc[0], Bc[1], Bc[2]);
+                        // n(shifted a component, variant va; shifted b component, variant vb)
+                        auto n = [&](int va, const std::array<int, 3>& ka, int vb, const std::array<int, 3>& kb) {
+                            // stored orientation: left = lo shell, right = hi shell
+                            const int vl = swapped ? vb : va, vr = swapped ? va : vb;
+                            const auto& kl = swapped ? kb : ka;
+                            const auto& kr = swapped ? ka : kb;
+                            const int pl = swapped ? pb : pa, pr = swapped ? pa : pb;
+                            int v = 0;
+                            for (; v < 5; ++v)
+                                if (kVar[v][0] == vl && kVar[v][1] == vr) break;
+                            const int nq_hi = b->nprim[hi];
+                            const int64_t slot = pair_first[(size_t)lo * ns + hi] + ((int64_t)pl * nq_hi + pr) * 5 + v;
+                            const int64_t base = dpos[slot];
+                            const int llv = gx::ncart(kl[0] + kl[1] + kl[2]);
+                            const int il = comp_index_host(kl), ir = comp_index_host(kr);
+                            return Na * Nb * std::sqrt(diag[base + (int64_t)ir * llv + il]);
+                        };
+                        double pb6[6];
+                        for (int slot = 0; slot < 2; ++slot) {
+                            const auto& raw_ang = slot == 0 ? A : Bc;
+                            const double alpha = slot == 0 ? alpha_a : alpha_b;
+                            const double* R = &b->center[3 * (slot == 0 ? sa : sb)];
+                            auto changed = [&](int dv, int axis) {
+                                std::array<int, 3> k = raw_ang;
+                                k[axis] += dv == 1 ? 1 : -1;
+                                return slot == 0 ? n(dv, k, 0, Bc) : n(0, A, dv, k);
+                            };
+                            const double base_n = n(0, A, 0, Bc);
+                            for (int axis = 0; axis < 3; ++axis) {
+                                double bound = 2.0 * alpha * changed(1, axis);
+                                if (raw_ang[axis] != 0) bound += (double)raw_ang[axis] * changed(2, axis);
+                                double e[3] = {0.0, 0.0, 0.0};
+                                e[axis] = 1.0;
+                                const double ph[3] = {B[1] * e[2] - B[2] * e[1], B[2] * e[0] - B[0] * e[2],
+                                                      B[0] * e[1] - B[1] * e[0]};
+                                for (int c = 0; c < 3; ++c) {
+                                    const double w = 0.5 * std::abs(ph[c]);
+                                    if (w != 0.0) bound += w * (changed(1, c) + std::abs(R[c]) * base_n);
+                                }
+                                pb6[slot * 3 + axis] = bound;
+                            }
+                        }
+                        for (int xa = 0; xa < xa_n; ++xa)
+                            for (int xb = 0; xb < xb_n; ++xb) {
+                                const double w = std::abs(b->coefs[coff[sa] + (size_t)xa * na + pa] *
+                                                          b->coefs[coff[sb] + (size_t)xb * nb + pb]);
+                                for (int k = 0; k < 6; ++k) contracted[((size_t)xa * xb_n + xb) * 6 + k] += w * pb6[k];
+                            }
+                    }
+                for (double v : contracted) maximum = std::max(maximum, v);
+            }
+        values[pair] = std::nextafter(maximum * (1.0 + 128.0 * eps), INFINITY);
+    }
+}
+
 // Centre derivatives of nq shell quartets: blocks (4, 3, na, nb, nc, nd) at
 // offsets[i] (complex elements), in input order.
 int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
@@ -1490,6 +1665,7 @@ void gx_basis_destroy(gx_basis* b) {
     cudaStreamSynchronize(b->ctx->stream);
     drop_cached_plans(b->ctx, b);
     if (b->deriv) drop_cached_plans(b->ctx, b->deriv.get());
+    if (b->bound) drop_cached_plans(b->ctx, b->bound.get());
     delete b;
 }
 
@@ -1544,6 +1720,24 @@ int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B,
                               const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                               int64_t out_capacity, float* kernel_ms) {
     return eri_derivative_impl(ctx, basis, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
+}
+
+int gx_eri_derivative_schwarz(gx_context* ctx, gx_basis* basis, const double* B, const double* O, double* values,
+                              double* ordinary) {
+    return guarded([&] {
+        if (!ctx || !basis) raise(GX_EINVAL, "null context or basis");
+        check_field(B, O);
+        for (int s = 0; s < basis->ns; ++s)
+            if (basis->l[s] > 15) raise(GX_EINVAL, "ERI centre derivatives support shells through l = 15");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        if (basis->ns == 0) return;
+        derivative_schwarz_impl(ctx, basis, B, O, values);
+        if (ordinary) {
+            const std::vector<double> q = schwarz_values(ctx, basis, B, O);
+            std::copy(q.begin(), q.end(), ordinary);
+        }
+    });
 }
 
 int gx_eri_center_derivatives_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,

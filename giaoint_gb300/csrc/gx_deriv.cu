@@ -144,7 +144,25 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
     }
 }
 
+__global__ void __launch_bounds__(256) gather_abs_kernel(const double2* __restrict__ src,
+                                                         const long long* __restrict__ idx, double* __restrict__ dst,
+                                                         long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double2 v = src[__ldg(&idx[i])];
+        dst[i] = hypot(v.x, v.y);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* dst, long long n, int sms,
+                              cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const long long want = (n + 255) / 256;
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, (long long)sms * 8));
+    gather_abs_kernel<<<blocks, 256, 0, s>>>(src, idx, dst, n);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_deriv_combine(const DerivCombineArgs& args, long long total, int sms, cudaStream_t s) {
     if (total == 0) return cudaSuccess;

@@ -154,6 +154,9 @@ struct DerivCombineArgs {
     double inv_sqrt_df[18];          // 1 / sqrt((2n - 1)!!)
 };
 cudaError_t launch_deriv_combine(const DerivCombineArgs& args, long long total, int sms, cudaStream_t s);
+// dst[i] = |src[idx[i]]| (diagonal elements of the derivative-bound blocks)
+cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* dst, long long n, int sms,
+                              cudaStream_t s);
 
 // register-resident small classes (gx_small.cu)
 bool small_class(int la, int lb, int lc, int ld);

@@ -444,7 +444,45 @@ def primitive_eri_center_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussian,
 
 
 class _EriDerivativeSchwarzBounds:
-    """Derivative-density Schwarz factors (src/derivatives.cpp:1307-1387)."""
+    """Derivative-density Schwarz factors (src/derivatives.cpp:1307-1387,
+    src/bindings.cpp:2242-2253), computed on the GPU (gx_eri_derivative_schwarz).
+
+    A quartet's bound max(D_ab Q_cd, Q_ab D_cd), padded by (1 + 128 eps) and
+    one ulp, bounds every local derivative component of its block.  The
+    object is tied to the basis object and the exact field it was built for."""
 
     def __init__(self, basis: Basis, *, field: MagneticField | None = None, threads=None, context=None):
-        raise NotImplementedError("derivative screening bounds are not available yet")
+        if not isinstance(basis, Basis):
+            raise TypeError("basis must be a Basis")
+        resolve_num_threads(threads)
+        ctx = context or nat.default_context()
+        self._basis = basis
+        B, O = field_arrays(field)
+        self._field = (tuple(B.tolist()), tuple(O.tolist()))
+        ns = len(basis.shells)
+        self._n = ns
+        values = np.zeros(max(ns * ns, 1), dtype=np.float64)
+        ordinary = np.zeros(max(ns * ns, 1), dtype=np.float64)
+        nat.check(nat.lib().gx_eri_derivative_schwarz(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                                      nat.dptr(values), nat.dptr(ordinary)))
+        self.values = values[: ns * ns]
+        self.ordinary = ordinary[: ns * ns]
+
+    def matches(self, basis, field) -> bool:
+        B, O = field_arrays(field)
+        return basis is self._basis and (tuple(B.tolist()), tuple(O.tolist())) == self._field
+
+    def quartet_bounds(self, quartets) -> np.ndarray:
+        q = np.asarray(quartets, dtype=np.int64).reshape(-1, 4)
+        if len(q) and (q.min() < 0 or q.max() >= self._n):
+            raise IndexError("derivative shell quartet index is out of range")
+        n = self._n
+        ab = q[:, 0] * n + q[:, 1]
+        cd = q[:, 2] * n + q[:, 3]
+        bound = np.maximum(self.values[ab] * self.ordinary[cd], self.ordinary[ab] * self.values[cd])
+        return np.nextafter(bound * (1.0 + 128.0 * np.finfo(np.float64).eps), np.inf)
+
+    def quartet_bound(self, quartet) -> float:
+        if len(quartet) != 4:
+            raise ValueError("each shell quartet must contain four indices")
+        return float(self.quartet_bounds([quartet])[0])

@@ -154,6 +154,16 @@ int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B,
                               const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                               int64_t out_capacity, float* kernel_ms);
 
+/* Derivative-density Schwarz factors, replacing EriDerivativeSchwarzBounds
+ * (src/derivatives.cpp:1307-1372, bindings.cpp:2242-2253): values[ns*ns]
+ * receives the factor of every ordered shell pair (a, b) at a*ns + b, and
+ * ordinary[ns*ns] (may be NULL) the ordinary ERI Schwarz factors of
+ * gx_schwarz.  A quartet's derivative bound is
+ * max(values[ab] ordinary[cd], ordinary[ab] values[cd]), padded by
+ * (1 + 128 eps) and one ulp (src/derivatives.cpp:1374-1383). */
+int gx_eri_derivative_schwarz(gx_context* ctx, gx_basis* basis, const double* B, const double* O, double* values,
+                              double* ordinary);
+
 /* Same, with the blocks written to device memory `out_device`. */
 int gx_eri_center_derivatives_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
                                      const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out_device,

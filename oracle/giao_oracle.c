@@ -1361,3 +1361,100 @@ int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, con
     basis_free(&bs);
     return rc;
 }
+
+/* Derivative-density Schwarz factors of every ordered shell pair
+ * (src/derivatives.cpp:1307-1372): for primitives (a, b) with coefficients
+ * N(alpha, component), n(a', b') = sqrt|(b' a'|a' b')|; slot s, axis x:
+ * 2 alpha n(+1_x) + l_x n(-1_x) + sum_c |(B x e_x)_c| / 2 (n(+1_c) + |R_c| n),
+ * contracted with |w_a w_b|, maximised, padded by (1 + 128 eps) and one ulp. */
+static double bound_norm(const prim_t* left, const prim_t* right, double cl, double cr, const field_t* f,
+                         int real_zero, ws_t* w, int* rc) {
+    prim_t q[4] = {*right, *left, *left, *right};
+    pair_t ab, cd;
+    gaussian_product(right->alpha, right->center, left->alpha, left->center, f, &ab);
+    gaussian_product(left->alpha, left->center, right->alpha, right->center, f, &cd);
+    cplx v;
+    w->boys_valid = 0;
+    *rc = eri_kernel(q, &ab, &cd, real_zero, w, &v);
+    return sqrt(cabs(v * (cl * cr) * (cl * cr)));
+}
+
+int or_eri_derivative_bounds(BASIS_ARGS, const double* B, const double* O, double* out) {
+    basis_t bs;
+    int rc = basis_init(&bs, ns, centers, ls, nprims, ncontrs, exps, coefs);
+    field_t f;
+    memcpy(f.B, B, sizeof f.B);
+    memcpy(f.O, O, sizeof f.O);
+    const int real_zero = B[0] == 0.0 && B[1] == 0.0 && B[2] == 0.0;
+    ws_t w;
+    memset(&w, 0, sizeof w);
+    static int comps[2][153][3];
+    for (int sa = 0; sa < ns && !rc; ++sa)
+        for (int sb = 0; sb < ns && !rc; ++sb) {
+            const int na = cart_components(ls[sa], comps[0]), nb = cart_components(ls[sb], comps[1]);
+            const int xa_n = ncontrs[sa], xb_n = ncontrs[sb];
+            double* contracted = (double*)malloc(sizeof(double) * 6 * xa_n * xb_n);
+            double maximum = 0.0;
+            for (int ca = 0; ca < na && !rc; ++ca)
+                for (int cb = 0; cb < nb && !rc; ++cb) {
+                    for (int i = 0; i < 6 * xa_n * xb_n; ++i) contracted[i] = 0.0;
+                    for (int pa = 0; pa < nprims[sa] && !rc; ++pa)
+                        for (int pb = 0; pb < nprims[sb] && !rc; ++pb) {
+                            prim_t g[2];
+                            const int sh[2] = {sa, sb}, pp[2] = {pa, pb}, cc[2] = {ca, cb};
+                            double cf[2];
+                            for (int k = 0; k < 2; ++k) {
+                                g[k].alpha = exps[bs.eoff[sh[k]] + pp[k]];
+                                for (int x = 0; x < 3; ++x) {
+                                    g[k].center[x] = centers[3 * sh[k] + x];
+                                    g[k].ang[x] = comps[k][cc[k]][x];
+                                }
+                                cf[k] = or_primitive_normalization(g[k].alpha, g[k].ang[0], g[k].ang[1], g[k].ang[2]);
+                            }
+                            double pb6[6];
+                            for (int slot = 0; slot < 2 && !rc; ++slot) {
+                                const prim_t* raw = &g[slot];
+                                prim_t base_l = g[0], base_r = g[1];
+                                const double n0 = bound_norm(&base_l, &base_r, cf[0], cf[1], &f, real_zero, &w, &rc);
+                                for (int axis = 0; axis < 3 && !rc; ++axis) {
+                                    prim_t ch[2] = {g[0], g[1]};
+                                    ch[slot].ang[axis] += 1;
+                                    double bound = 2.0 * raw->alpha *
+                                                   bound_norm(&ch[0], &ch[1], cf[0], cf[1], &f, real_zero, &w, &rc);
+                                    if (raw->ang[axis] != 0) {
+                                        prim_t dn[2] = {g[0], g[1]};
+                                        dn[slot].ang[axis] -= 1;
+                                        bound += (double)raw->ang[axis] *
+                                                 bound_norm(&dn[0], &dn[1], cf[0], cf[1], &f, real_zero, &w, &rc);
+                                    }
+                                    double e[3] = {0.0, 0.0, 0.0};
+                                    e[axis] = 1.0;
+                                    const double ph[3] = {B[1] * e[2] - B[2] * e[1], B[2] * e[0] - B[0] * e[2],
+                                                          B[0] * e[1] - B[1] * e[0]};
+                                    for (int c = 0; c < 3; ++c) {
+                                        const double wgt = 0.5 * fabs(ph[c]);
+                                        if (wgt == 0.0) continue;
+                                        prim_t up[2] = {g[0], g[1]};
+                                        up[slot].ang[c] += 1;
+                                        bound += wgt * (bound_norm(&up[0], &up[1], cf[0], cf[1], &f, real_zero, &w, &rc) +
+                                                        fabs(raw->center[c]) * n0);
+                                    }
+                                    pb6[slot * 3 + axis] = bound;
+                                }
+                            }
+                            for (int xa = 0; xa < xa_n; ++xa)
+                                for (int xb = 0; xb < xb_n; ++xb) {
+                                    const double wgt = fabs(coefs[bs.coff[sa] + (size_t)xa * nprims[sa] + pa] *
+                                                            coefs[bs.coff[sb] + (size_t)xb * nprims[sb] + pb]);
+                                    for (int k = 0; k < 6; ++k) contracted[(xa * xb_n + xb) * 6 + k] += wgt * pb6[k];
+                                }
+                        }
+                    for (int i = 0; i < 6 * xa_n * xb_n; ++i) maximum = fmax(maximum, contracted[i]);
+                }
+            free(contracted);
+            out[(size_t)sa * ns + sb] = nextafter(maximum * (1.0 + 128.0 * 2.220446049250313e-16), INFINITY);
+        }
+    ws_free(&w);
+    basis_free(&bs);
+    return rc;
+}

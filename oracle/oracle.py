@@ -298,6 +298,14 @@ class Oracle(_Backend):
                                                        out.ctypes.data_as(_d)))
         return out[:total], offsets
 
+    def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:
+        """Derivative Schwarz factors of every ordered shell pair, [ns, ns]."""
+        a = self._basis(shells)
+        out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
+        self._check(self.lib.or_eri_derivative_bounds(*a.args(), _vec3(B).ctypes.data_as(_d),
+                                                      _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[: a.ns, : a.ns]
+
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)
         out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
@@ -397,6 +405,13 @@ class Reference(_Backend):
                                                         ctypes.c_long(len(q)), _vec3(B).ctypes.data_as(_d),
                                                         _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
         return out[:total], offsets
+
+    def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:
+        a = self._basis(shells)
+        out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
+        self._check(self.lib.ref_eri_derivative_bounds(*self._bargs(a), _vec3(B).ctypes.data_as(_d),
+                                                       _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[: a.ns, : a.ns]
 
     def schwarz(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)

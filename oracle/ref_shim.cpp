@@ -11,6 +11,8 @@
 //   ref_eri_batch          <- src/bindings.cpp:672-731 (evaluate_eri_shell_quartets)
 //   ref_eri_full           <- src/bindings.cpp:640-671 (compute_eri_tensor)
 //   ref_schwarz            <- src/bindings.cpp:409-425 (EriSchwarzBounds)
+//   ref_eri_center_derivatives <- src/derivatives.cpp:954-959
+//   ref_eri_derivative_bounds  <- src/derivatives.cpp:1307-1372
 //   ref_cholesky_diagonal  <- src/bindings.cpp:2306-2314
 //   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
 #include "giao_integrals/boys.hpp"
@@ -221,6 +223,18 @@ int ref_schwarz(int ns, const double* centers, const int* ls, const int* nprims,
     return guarded([&] {
         auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
         giao::EriSchwarzBounds b(basis, make_field(B, O));
+        std::memcpy(out, b.values().data(), b.values().size() * sizeof(double));
+    });
+}
+
+// Derivative Schwarz factors per ordered shell pair
+// (EriDerivativeSchwarzBounds::values, src/derivatives.cpp:1307-1372).
+int ref_eri_derivative_bounds(int ns, const double* centers, const int* ls, const int* nprims,
+                              const int* ncontrs, const double* exps, const double* coefs,
+                              const int* normalize, const double* B, const double* O, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        giao::EriDerivativeSchwarzBounds b(basis, make_field(B, O));
         std::memcpy(out, b.values().data(), b.values().size() * sizeof(double));
     });
 }

@@ -176,3 +176,91 @@ def test_device_entry_matches_host(golden):
         nat.check(nat.lib().gx_eri_center_derivatives_device(
             ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O), nat.u32ptr(q), len(q), nat.i64ptr(offsets),
             ctypes.c_void_p(dev.data_ptr()), total - 1, ctypes.byref(ms)))
+
+
+def test_derivative_bounds_match_reference_and_bound_blocks(golden):
+    """GPU derivative Schwarz factors against the reference's
+    (EriDerivativeSchwarzBounds), and every block bounded by its quartet
+    bound (the reference's own property, test_eri_derivative_batches.py)."""
+    from giaoint_gb300.eri import _EriDerivativeSchwarzBounds
+
+    g = golden.derivatives
+    for name, specs, q in derivative_systems(g):
+        basis = _basis(specs)
+        for label, field in (("field", _field(g["field"], g["origin"])), ("zero", None)):
+            bounds = _EriDerivativeSchwarzBounds(basis, field=field)
+            ns = len(specs)
+            np.testing.assert_allclose(bounds.values.reshape(ns, ns), g[f"{name}_bounds_{label}"], rtol=1e-12)
+            np.testing.assert_allclose(bounds.ordinary.reshape(ns, ns), g[f"{name}_schwarz_{label}"], rtol=1e-12)
+            off = g[f"{name}_offsets"]
+            vals = g[f"{name}_{label}"]
+            qb = bounds.quartet_bounds(q)
+            for i in range(len(q)):
+                assert np.abs(vals[off[i]:off[i + 1]]).max() <= qb[i] * (1 + 1e-13)
+                assert qb[i] == bounds.quartet_bound(tuple(int(x) for x in q[i]))
+            with pytest.raises(IndexError):
+                bounds.quartet_bound((0, 0, 0, ns))
+
+
+def test_derivative_screening_is_safe_and_tied_to_basis_and_field(golden):
+    """Screening at the median quartet bound drops only quartets whose every
+    derivative component is below the threshold, keeps the rest unchanged,
+    and refuses bounds built for another basis object or field."""
+    from giaoint_gb300.eri import _EriDerivativeSchwarzBounds
+
+    shells = [gi.Shell((0.1, -0.2, 0.3), 0, [0.8], [1.0]), gi.Shell((4.0, 0.0, 0.0), 1, [0.9], [1.0]),
+              gi.Shell((0.5, 0.3, -0.2), 2, [1.1, 0.4], [0.6, 0.5])]
+    basis = gi.Basis(shells)
+    q = [tuple(int(x) for x in r) for r in np.ndindex(3, 3, 3, 3)]
+    for field in (None, gi.MagneticField((0.05, -0.02, 0.1), gauge_origin=(0.3, -0.1, 0.2))):
+        bounds = _EriDerivativeSchwarzBounds(basis, field=field)
+        threshold = float(np.median(bounds.quartet_bounds(q)))
+        full = {tuple(int(x) for x in r): b.block(i) for b in gi.eri_derivative_batches(basis, field=field, quartets=q)
+                for i, r in enumerate(b.quartets)}
+        batches = list(gi.eri_derivative_batches(basis, field=field, quartets=q, screening_threshold=threshold,
+                                                 target_bytes=4000))
+        assert sum(b.requested_count for b in batches) == len(q)
+        screened = sum(b.screened_count for b in batches)
+        assert 0 < screened < len(q)
+        kept = set()
+        for b in batches:
+            for i, r in enumerate(b.quartets):
+                r = tuple(int(x) for x in r)
+                kept.add(r)
+                np.testing.assert_array_equal(b.block(i), full[r])
+        dropped = [np.abs(full[r]).max() for r in q if r not in kept]
+        assert len(dropped) == screened
+        assert max(dropped) < threshold and any(v > 1e-20 for v in dropped)
+        other = gi.Basis(shells)
+        for changed_basis, changed_field in ((other, field), (basis, gi.MagneticField((0.0, 0.0, 0.3)))):
+            with pytest.raises(ValueError, match="do not match"):
+                _eri_derivative_batch(changed_basis, [(0, 0, 0, 0)], field=changed_field, screening_threshold=1e-8,
+                                      bounds=bounds)
+
+
+def test_derivatives_match_finite_differences():
+    """Slot derivatives of a shell moved as a whole (both occurrences of a
+    repeated shell) against a Richardson-extrapolated central difference of
+    the GPU's own ERIs with displaced centres."""
+    centers = np.array([[0.1, -0.2, 0.3], [-0.3, 0.4, 0.2]])
+
+    def shells(c):
+        return [gi.Shell(tuple(c[0]), 0, [0.8], [1.0]), gi.Shell(tuple(c[1]), 1, [0.6], [1.0])]
+
+    q = (0, 1, 0, 1)
+    for field in (None, gi.MagneticField((0.05, -0.1, 0.2), gauge_origin=(0.1, 0.2, -0.3))):
+        block = next(gi.eri_derivative_batches(gi.Basis(shells(centers)), quartets=[q], field=field)).block(0)
+        for center in range(2):
+            for axis in range(3):
+                def value(step):
+                    c = centers.copy()
+                    c[center, axis] += step
+                    s = shells(c)
+                    return gi.eri_shell(*[s[k] for k in q], field=field)
+
+                h = 1e-3
+                d1 = (value(h) - value(-h)) / (2 * h)
+                d2 = (value(h / 2) - value(-h / 2)) / h
+                expected = (4 * d2 - d1) / 3
+                actual = block[[k for k, s in enumerate(q) if s == center], axis].sum(axis=0)
+                np.testing.assert_allclose(actual, expected, atol=3e-10, rtol=3e-9)

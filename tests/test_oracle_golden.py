@@ -151,3 +151,19 @@ def test_eri_center_derivatives_translation_sum_rule_oracle(golden, oracle):
             r = derivative_sum_rule_residual(specs, q, g[f"{name}_offsets"], g[f"{name}_{label}"], eri, eoff,
                                              field, o)
             assert r <= 1e-11, (name, label, r)
+
+
+def test_eri_derivative_bounds_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of EriDerivativeSchwarzBounds
+    (src/derivatives.cpp:1307-1372) against the reference library's factors,
+    and the oracle's ordinary Schwarz factors against the reference's."""
+    from conftest import derivative_systems
+
+    g = golden.derivatives
+    B, origin = tuple(g["field"]), tuple(g["origin"])
+    for name, specs, _q in derivative_systems(g):
+        for label, field, o in (("field", B, origin), ("zero", None, None)):
+            np.testing.assert_allclose(oracle.eri_derivative_bounds(specs, field, o), g[f"{name}_bounds_{label}"],
+                                       rtol=1e-14, atol=0)
+            np.testing.assert_allclose(oracle.schwarz(specs, field, o), g[f"{name}_schwarz_{label}"],
+                                       rtol=1e-14, atol=0)
