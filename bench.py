@@ -57,6 +57,7 @@ def parse():
     p.add_argument("--no-autotune", action="store_true", help="keep the default per-class launch configurations")
     p.add_argument("--natoms", type=int, default=12)
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-derivatives", action="store_true")
     p.add_argument("--serving-requests", type=int, default=32)
     p.add_argument("--sweep", type=int, default=0,
                    help="field sweep: evaluate the molecule at this many fields |B| <= 0.5 in FP64 and mixed")
@@ -233,6 +234,78 @@ def full_tensor_leg(ctx, run_cpu: bool):
         out["cpu_port_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_port_threads"] = threads
         out["max_abs_diff_vs_cpu_port"] = float(np.max(np.abs(full - ref)))
+    return out
+
+
+def derivative_leg(ctx, recs, B, quartets, run_cpu: bool, count: int = 200000, seed: int = 5):
+    """ERI centre derivatives (4, 3, na, nb, nc, nd) of a seeded sample of
+    canonical quartets of the same molecule and field: device time of
+    gx_eri_center_derivatives_device (derived-basis integrals + combine,
+    output resident in HBM) and of the host-output call, with the oracle port
+    (single thread) on a bounded sub-sample beside it."""
+    import ctypes
+
+    import torch
+
+    import giaoint_gb300 as gi
+    from giaoint_gb300 import _native as nat
+
+    basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
+    rng = np.random.default_rng(seed)
+    q = np.ascontiguousarray(quartets[np.sort(rng.choice(len(quartets), min(count, len(quartets)), replace=False))],
+                             dtype=np.uint32)
+    sizes = np.array([gi.Shell.from_record(r).ao_count for r in recs], dtype=np.int64)
+    total = int(12 * np.prod(sizes[q.astype(np.int64)], axis=1).sum())
+    Bv = np.ascontiguousarray(B, dtype=np.float64)
+    Ov = np.zeros(3)
+    dev = torch.empty(total, dtype=torch.complex128, device="cuda:0")
+    offsets = np.zeros(len(q) + 1, dtype=np.int64)
+    ms = ctypes.c_float()
+    lib = nat.lib()
+    h = basis._device(ctx)
+
+    def device_call():
+        nat.check(lib.gx_eri_center_derivatives_device(ctx.handle, h, nat.dptr(Bv), nat.dptr(Ov), nat.u32ptr(q),
+                                                       len(q), nat.i64ptr(offsets), ctypes.c_void_p(dev.data_ptr()),
+                                                       total, ctypes.byref(ms)))
+
+    for _ in range(2):
+        device_call()
+    times, kms = [], []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        device_call()
+        times.append(time.perf_counter() - t0)
+        kms.append(ms.value)
+    host = torch.empty(total, dtype=torch.complex128).pin_memory()
+    hv = host.numpy()
+    t0 = time.perf_counter()
+    nat.check(lib.gx_eri_center_derivatives(ctx.handle, h, nat.dptr(Bv), nat.dptr(Ov), nat.u32ptr(q), len(q),
+                                            nat.i64ptr(offsets), nat.dptr(hv.view(np.float64)), total,
+                                            ctypes.byref(ms)))
+    host_s = time.perf_counter() - t0
+    dev_s = statistics.median(times)
+    out = {"workload": f"{len(q)} seeded canonical quartets of the 12-atom molecule, same field, "
+                       f"{total} derivative components (4 slots x 3 axes per ERI)",
+           "quartets": int(len(q)), "components": total, "seconds_device": dev_s,
+           "derived_integral_kernel_ms": statistics.median(kms),
+           "quartets_per_s": len(q) / dev_s, "components_per_s": total / dev_s,
+           "seconds_host_output": host_s, "host_output_components_per_s": total / host_s}
+    if run_cpu:
+        from oracle import oracle as O
+
+        sub = q[np.sort(rng.choice(len(q), 400, replace=False))]
+        t0 = time.perf_counter()
+        ref, roff = O.Oracle().eri_center_derivatives(recs, sub, tuple(B), (0.0, 0.0, 0.0))
+        cpu_s = time.perf_counter() - t0
+        idx = {tuple(x): i for i, x in enumerate(q.tolist())}
+        got = np.concatenate([hv[offsets[idx[tuple(x)]]:offsets[idx[tuple(x)] + 1]] for x in sub.tolist()])
+        out["cpu_port"] = {"components_per_s": len(ref) / cpu_s, "cores": 1,
+                           "sample": f"400 of the quartets ({len(ref)} components), {cpu_s:.2f} s, "
+                                     "oracle/giao_oracle.c single thread"}
+        out["max_abs_diff_vs_cpu_port"] = float(np.abs(got - ref).max())
+        out["speedup_vs_cpu_port_1_thread"] = (total / dev_s) / (len(ref) / cpu_s)
+    del dev
     return out
 
 
@@ -513,6 +586,10 @@ def run_gpu(args):
     if rank == 0:
         nat.check(lib.gx_context_set_stream(ctx.handle, None))
         full_tensor = full_tensor_leg(ctx, run_cpu=(world == 1 and not args.no_cpu))
+    derivatives = None
+    if rank == 0 and not args.no_derivatives:
+        nat.check(lib.gx_context_set_stream(ctx.handle, None))
+        derivatives = derivative_leg(ctx, recs, B, quartets, run_cpu=(world == 1 and not args.no_cpu))
     serving = None
     if rank == 0 and not args.no_serving:
         serving = serving_leg(args)
@@ -556,6 +633,7 @@ def run_gpu(args):
             "cholesky": chol,
             "field_sweep": sweep,
             "full_tensor": full_tensor,
+            "center_derivatives": derivatives,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

@@ -29,10 +29,12 @@ from .eri import (
     eri_batches,
     eri_center_derivatives_shell,
     eri_derivative_batches,
+    eri_magnetic_derivatives_shell,
     eri_schwarz_bounds,
     eri_shell,
     primitive_eri,
     primitive_eri_center_derivatives,
+    primitive_eri_magnetic_derivatives,
 )
 from .nuclear import nuclear_attraction, nuclear_attraction_shell, primitive_nuclear_attraction
 
@@ -60,12 +62,14 @@ __all__ = [
     "eri_batches",
     "eri_center_derivatives_shell",
     "eri_derivative_batches",
+    "eri_magnetic_derivatives_shell",
     "eri_schwarz_bounds",
     "eri_shell",
     "nuclear_attraction",
     "nuclear_attraction_shell",
     "primitive_eri",
     "primitive_eri_center_derivatives",
+    "primitive_eri_magnetic_derivatives",
     "primitive_nuclear_attraction",
     "primitive_normalization",
     "resolve_num_threads",

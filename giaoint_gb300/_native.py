@@ -88,6 +88,8 @@ SIGNATURES = {
                                                  ctypes.POINTER(ctypes.c_float)]),
     "gx_eri_center_derivatives_device": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _vp,
                                                         ctypes.c_int64, ctypes.POINTER(ctypes.c_float)]),
+    "gx_eri_magnetic_derivatives": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _d,
+                                                   ctypes.c_int64, ctypes.POINTER(ctypes.c_float)]),
     "gx_eri_derivative_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d, _d]),
     "gx_eri_shell": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d]),
     "gx_eri_full": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]),

@@ -1388,11 +1388,12 @@ void derivative_schwarz_impl(gx_context* ctx, gx_basis* b, const double* B, cons
     }
 }
 
-// Centre derivatives of nq shell quartets: blocks (4, 3, na, nb, nc, nd) at
-// offsets[i] (complex elements), in input order.
-int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
-                        int64_t nq, int64_t* offsets, void* out, bool out_is_device, int64_t capacity,
-                        float* kernel_ms) {
+// Centre (mode 0) or magnetic (mode 1) derivatives of nq shell quartets:
+// blocks (4, 3, na, nb, nc, nd) or (3, na, nb, nc, nd) at offsets[i] (complex
+// elements), in input order.
+int eri_derivative_impl(gx_context* ctx, gx_basis* b, int mode, const double* B, const double* O,
+                        const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out, bool out_is_device,
+                        int64_t capacity, float* kernel_ms) {
     return guarded([&] {
         if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
         if (nq < 0) raise(GX_EINVAL, "negative quartet count");
@@ -1412,7 +1413,7 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const dou
             }
             if (L + 1 > 32) raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
             offsets[i] = off;
-            off += 12 * size;
+            off += (mode == 0 ? 12 : 3) * size;
         }
         offsets[nq] = off;
         if (off > capacity) raise(GX_ELENGTH, "derivative output buffer is too small");
@@ -1426,9 +1427,11 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const dou
         std::vector<int> dix;
         gx_basis* db = derivative_basis(ctx, b, dix);
         const bool field = B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0;
-        // derived blocks per quartet: for each slot Z, [D], [U]; then [plain]
+        const bool has_u = mode == 1 || field;
+        // derived blocks per quartet: for each slot [Z, D if l > 0] (centre
+        // mode), [U]; then [plain]
         std::vector<uint32_t> dq;
-        dq.reserve((size_t)nq * 4 * (field ? 13 : 8));
+        dq.reserve((size_t)nq * 4 * (mode == 1 ? 5 : (field ? 13 : 8)));
         std::vector<long long> doff((size_t)nq);
         int64_t dtotal = 0;
         for (int64_t i = 0; i < nq; ++i) {
@@ -1443,11 +1446,13 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const dou
                 dtotal += size;
             };
             for (int k = 0; k < 4; ++k) {
-                add(k, kDerivZ);
-                if (b->l[x[k]] > 0) add(k, kDerivD);
-                if (field) add(k, kDerivU);
+                if (mode == 0) {
+                    add(k, kDerivZ);
+                    if (b->l[x[k]] > 0) add(k, kDerivD);
+                }
+                if (has_u) add(k, kDerivU);
             }
-            if (field) add(0, -1);
+            if (has_u) add(0, -1);
         }
         const int64_t dcount = (int64_t)dq.size() / 4;
         uint64_t h1 = 0x452821E638D01377ull ^ (uint64_t)dcount, h2 = 0xBE5466CF34E90C6Cull;
@@ -1493,6 +1498,7 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const dou
         }
         gx::DerivCombineArgs a{};
         a.nq = (int)nq;
+        a.mode = mode;
         a.field = field ? 1 : 0;
         a.quartets = reinterpret_cast<const uint32_t*>(meta);
         a.offsets = reinterpret_cast<const long long*>(meta + qbytes);
@@ -1503,7 +1509,10 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, const double* B, const dou
         a.shell_center = b->d_shell_center.as<double>();
         a.derived = ctx->deriv_vals.as<double2>();
         a.out = dout;
-        for (int k = 0; k < 3; ++k) a.B[k] = B[k];
+        for (int k = 0; k < 3; ++k) {
+            a.B[k] = B[k];
+            a.O[k] = O[k];
+        }
         double df = 1.0;  // (2n - 1)!!
         for (int n = 0; n < 18; ++n) {
             if (n > 0) df *= 2.0 * n - 1.0;
@@ -1719,7 +1728,13 @@ int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const
 int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
                               const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                               int64_t out_capacity, float* kernel_ms) {
-    return eri_derivative_impl(ctx, basis, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
+    return eri_derivative_impl(ctx, basis, 0, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
+}
+
+int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
+                                int64_t out_capacity, float* kernel_ms) {
+    return eri_derivative_impl(ctx, basis, 1, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
 }
 
 int gx_eri_derivative_schwarz(gx_context* ctx, gx_basis* basis, const double* B, const double* O, double* values,
@@ -1743,7 +1758,8 @@ int gx_eri_derivative_schwarz(gx_context* ctx, gx_basis* basis, const double* B,
 int gx_eri_center_derivatives_device(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
                                      const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out_device,
                                      int64_t out_capacity, float* kernel_ms) {
-    return eri_derivative_impl(ctx, basis, B, O, quartets, nq, offsets, out_device, true, out_capacity, kernel_ms);
+    return eri_derivative_impl(ctx, basis, 0, B, O, quartets, nq, offsets, out_device, true, out_capacity,
+                               kernel_ms);
 }
 
 int gx_eri_shell(gx_context* ctx, gx_basis* basis, int a, int b, int c, int d, const double* B, const double* O,

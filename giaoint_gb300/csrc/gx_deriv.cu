@@ -1,6 +1,8 @@
-// ERI centre derivatives d/dR_{slot,axis} (ab|cd) of London-orbital shell
-// quartets (compute_eri_center_derivatives and EriResponses::centers,
-// src/derivatives.cpp:53-87, 215-245, 556-640, 954-959 of the reference).
+// ERI centre derivatives d/dR_{slot,axis} (ab|cd) and magnetic derivatives
+// d/dB_b (ab|cd) of London-orbital shell quartets
+// (compute_eri_center_derivatives / compute_eri_magnetic_derivatives and
+// EriResponses::centers / magnetic, src/derivatives.cpp:53-106, 215-245,
+// 268-280, 556-640, 954-966 of the reference).
 //
 // For a Cartesian primitive with normalisation N(alpha, l) = g(alpha, l) h(l),
 //   g(alpha, l) = (2 alpha / pi)^{3/4} (4 alpha)^{|l|/2},
@@ -9,6 +11,8 @@
 //   h(l_k) [ Z_k(l_k + 1_x) - l_x D_k(l_k - 1_x)
 //            + i phi_k sum_c (B x e_x)_c U_k(l_k + 1_c) ]
 //   + i phi_k sum_c (B x e_x)_c R_{k,c} (ab|cd),
+// and the field derivative along b is the sum over the four slots of
+//   i phi_k sum_c (e_b x (R_k - O))_c [h(l_k) U_k(l_k + 1_c) + R_{k,c} (ab|cd)],
 // phi_k = +1/2 on the bra side of a pair (slots 0, 2), -1/2 on the ket side,
 // where Z_k, U_k and D_k are contracted integrals with slot k replaced by a
 // raw-primitive shell of angular momentum l + 1, l + 1 and l - 1 and
@@ -41,6 +45,8 @@ __device__ __forceinline__ void comp_of(int l, int c, int& lx, int& ly, int& lz)
 
 __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) {
     const long long total = a.offsets[a.nq];
+    const bool centre = a.mode == 0;
+    const bool has_u = !centre || a.field;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         // quartet of element e: last i with offsets[i] <= e
@@ -60,43 +66,38 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
             dim[k] = nc[k] * ncart(l[k]);
             size *= dim[k];
         }
-        long long rel = e - __ldg(&a.offsets[qi]);
+        const long long rel = e - __ldg(&a.offsets[qi]);
         const int d = (int)(rel / size);
-        long long r = rel - (long long)d * size;
-        const int k = d / 3, x = d - 3 * (d / 3);
+        const long long r0 = rel - (long long)d * size;
+        long long r = r0;
         int idx[4];
         for (int j = 3; j >= 0; --j) {
             idx[j] = (int)(r % dim[j]);
             r /= dim[j];
         }
-        // offsets of this quartet's derived blocks: per slot Z, [D], [U]; then [base]
+        // this quartet's derived blocks: per slot [Z, D if l > 0] (centre), [U]; then [plain]
         long long off = __ldg(&a.derived_offsets[qi]);
-        long long zoff = 0, doff = -1, uoff = -1, boff = -1;
+        long long zoff[4], doff[4], uoff[4], boff = -1;
         for (int j = 0; j < 4; ++j) {
             const long long up = size / dim[j] * (nc[j] * ncart(l[j] + 1));
-            const long long dn = l[j] > 0 ? size / dim[j] * (nc[j] * ncart(l[j] - 1)) : 0;
-            if (j == k) zoff = off;
-            off += up;
-            if (l[j] > 0) {
-                if (j == k) doff = off;
-                off += dn;
+            zoff[j] = doff[j] = uoff[j] = -1;
+            if (centre) {
+                zoff[j] = off;
+                off += up;
+                if (l[j] > 0) {
+                    doff[j] = off;
+                    off += size / dim[j] * (nc[j] * ncart(l[j] - 1));
+                }
             }
-            if (a.field) {
-                if (j == k) uoff = off;
+            if (has_u) {
+                uoff[j] = off;
                 off += up;
             }
         }
-        if (a.field) boff = off;
-
-        const int lk = l[k], nck = ncart(lk);
-        const int xk = idx[k] / nck, ck = idx[k] - xk * nck;
-        int ang[3];
-        comp_of(lk, ck, ang[0], ang[1], ang[2]);
-        const double hk = __ldg(&a.shell_raw[sh[k]]) ? 1.0 : a.inv_sqrt_df[ang[0]] * a.inv_sqrt_df[ang[1]] *
-                                                              a.inv_sqrt_df[ang[2]];
+        if (has_u) boff = off;
         // linear index of the derived block whose slot k has angular momentum
-        // lp and component (px, py, pz)
-        auto derived = [&](int lp, int px, int pz) {
+        // lp and component (px, py, pz), contraction xk
+        auto derived = [&](int k, int xk, int lp, int px, int pz) {
             long long li = 0;
             for (int j = 0; j < 4; ++j) {
                 const int dj = j == k ? nc[j] * ncart(lp) : dim[j];
@@ -105,38 +106,58 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
             }
             return li;
         };
-        int up[3] = {ang[0], ang[1], ang[2]};
-        ++up[x];
-        double2 v = __ldg(&a.derived[zoff + derived(lk + 1, up[0], up[2])]);
-        if (ang[x] > 0) {
-            int dn[3] = {ang[0], ang[1], ang[2]};
-            --dn[x];
-            const double2 w = __ldg(&a.derived[doff + derived(lk - 1, dn[0], dn[2])]);
-            v.x -= ang[x] * w.x;
-            v.y -= ang[x] * w.y;
-        }
-        double2 res = c2(hk * v.x, hk * v.y);
-        if (a.field) {
+        double2 res = c2(0.0, 0.0);
+        const double2 base = has_u ? __ldg(&a.derived[boff + r0]) : c2(0.0, 0.0);
+        // slots contributing: one (centre mode) or all four (magnetic mode)
+        const int k0 = centre ? d / 3 : 0, k1 = centre ? d / 3 + 1 : 4;
+        for (int k = k0; k < k1; ++k) {
+            const int lk = l[k], nck = ncart(lk);
+            const int xk = idx[k] / nck, ck = idx[k] - xk * nck;
+            int ang[3];
+            comp_of(lk, ck, ang[0], ang[1], ang[2]);
+            const double hk = __ldg(&a.shell_raw[sh[k]])
+                                  ? 1.0
+                                  : a.inv_sqrt_df[ang[0]] * a.inv_sqrt_df[ang[1]] * a.inv_sqrt_df[ang[2]];
             const double phi = (k % 2 == 0) ? 0.5 : -0.5;
-            // (B x e_x)_c
-            double bx[3];
-            bx[0] = x == 2 ? a.B[1] : (x == 1 ? -a.B[2] : 0.0);
-            bx[1] = x == 0 ? a.B[2] : (x == 2 ? -a.B[0] : 0.0);
-            bx[2] = x == 1 ? a.B[0] : (x == 0 ? -a.B[1] : 0.0);
-            const double2 base = __ldg(&a.derived[boff + rel - (long long)d * size]);
+            double w[3];  // phase derivative: B x e_x (centre) or e_b x (R_k - O) (magnetic)
+            if (centre) {
+                const int x = d - 3 * k;
+                int up[3] = {ang[0], ang[1], ang[2]};
+                ++up[x];
+                double2 v = __ldg(&a.derived[zoff[k] + derived(k, xk, lk + 1, up[0], up[2])]);
+                if (ang[x] > 0) {
+                    int dn[3] = {ang[0], ang[1], ang[2]};
+                    --dn[x];
+                    const double2 t = __ldg(&a.derived[doff[k] + derived(k, xk, lk - 1, dn[0], dn[2])]);
+                    v.x -= ang[x] * t.x;
+                    v.y -= ang[x] * t.y;
+                }
+                res = c2(hk * v.x, hk * v.y);
+                if (!a.field) break;
+                w[0] = x == 2 ? a.B[1] : (x == 1 ? -a.B[2] : 0.0);
+                w[1] = x == 0 ? a.B[2] : (x == 2 ? -a.B[0] : 0.0);
+                w[2] = x == 1 ? a.B[0] : (x == 0 ? -a.B[1] : 0.0);
+            } else {
+                const int b = d;
+                double D[3];
+                for (int c = 0; c < 3; ++c) D[c] = __ldg(&a.shell_center[3 * sh[k] + c]) - a.O[c];
+                w[0] = b == 1 ? D[2] : (b == 2 ? -D[1] : 0.0);
+                w[1] = b == 2 ? D[0] : (b == 0 ? -D[2] : 0.0);
+                w[2] = b == 0 ? D[1] : (b == 1 ? -D[0] : 0.0);
+            }
             double2 t = c2(0.0, 0.0);
             for (int c = 0; c < 3; ++c) {
-                const double coef = phi * bx[c];
+                const double coef = phi * w[c];
                 if (coef == 0.0) continue;
                 int uc[3] = {ang[0], ang[1], ang[2]};
                 ++uc[c];
-                const double2 u = __ldg(&a.derived[uoff + derived(lk + 1, uc[0], uc[2])]);
+                const double2 u = __ldg(&a.derived[uoff[k] + derived(k, xk, lk + 1, uc[0], uc[2])]);
                 const double R = __ldg(&a.shell_center[3 * sh[k] + c]);
                 // coef * (h U + R base)
                 t.x += coef * (hk * u.x + R * base.x);
                 t.y += coef * (hk * u.y + R * base.y);
             }
-            // i t
+            // + i t
             res.x -= t.y;
             res.y += t.x;
         }

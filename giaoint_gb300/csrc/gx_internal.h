@@ -136,11 +136,13 @@ cudaError_t launch_nuclear(const BasisDev& bs, const PairData& pp, const BoysTab
                            const double* charge, const double* center, const long long* seg_ao, long long n,
                            int max_pair_L, int max_nab, double2* out, DevStatus* status, cudaStream_t s);
 
-// ERI centre derivatives (gx_deriv.cu): gathers the derived-basis blocks of
-// nq quartets into (4, 3, na, nb, nc, nd) blocks at out + offsets[i].
+// ERI centre and magnetic derivatives (gx_deriv.cu): gathers the
+// derived-basis blocks of nq quartets into (4, 3, na, nb, nc, nd) or
+// (3, na, nb, nc, nd) blocks at out + offsets[i].
 struct DerivCombineArgs {
     int nq;
-    int field;                       // B != 0: U blocks and the plain block follow
+    int mode;                        // 0: centre derivatives (12 per element), 1: magnetic (3 per element)
+    int field;                       // centre mode with B != 0: U blocks and the plain block follow
     const uint32_t* quartets;        // [4 nq] original shells
     const long long* offsets;        // [nq + 1] output offsets (12 x block size each)
     const long long* derived_offsets;  // [nq] first derived block of each quartet
@@ -150,7 +152,7 @@ struct DerivCombineArgs {
     const double* shell_center;      // [3 ns]
     const double2* derived;          // derived-basis ERI blocks
     double2* out;
-    double B[3];
+    double B[3], O[3];
     double inv_sqrt_df[18];          // 1 / sqrt((2n - 1)!!)
 };
 cudaError_t launch_deriv_combine(const DerivCombineArgs& args, long long total, int sms, cudaStream_t s);

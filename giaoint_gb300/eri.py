@@ -294,7 +294,7 @@ def primitive_eri(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussi
 
 
 # ---------------------------------------------------------------------------
-# centre derivatives (src/derivatives.cpp:53-87, 215-245, 556-640, 954-959;
+# centre and magnetic derivatives (src/derivatives.cpp:53-106, 215-280, 556-640, 954-966;
 # python/giao_integrals/eri.py:210-284; src/bindings.cpp:979-992, 1308-1324,
 # 2255-2303)
 # ---------------------------------------------------------------------------
@@ -425,22 +425,75 @@ def primitive_eri_center_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussian,
     """Centre derivatives of one primitive quartet, complex (4, 3)
     (primitive_eri_center_derivatives; src/derivatives.cpp:836-842,
     src/bindings.cpp:979-992)."""
+    shells, picks, scale = _primitive_shells((a, b, c, d))
+    full = eri_center_derivatives_shell(*shells, field=field, context=context)
+    return full[:, :, picks[0], picks[1], picks[2], picks[3]] * scale
+
+
+def _eri_magnetic_derivative_blocks(basis: Basis, quartets, *, field: MagneticField | None = None, context=None):
+    """Magnetic-derivative blocks (3, na, nb, nc, nd) of ``quartets`` packed
+    in input order (gx_eri_magnetic_derivatives): returns (offsets, values)."""
+    ctx = context or nat.default_context()
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+    if len(q) and (q.min() < 0 or q.max() >= len(basis.shells)):
+        raise IndexError("derivative shell quartet index is out of range")
+    q = np.ascontiguousarray(q.astype(np.uint32))
+    sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+    total = int(3 * np.prod(sizes[q.astype(np.int64)], axis=1).sum()) if len(q) else 0
+    values = np.empty(max(total, 1), dtype=np.complex128)
+    offsets = np.zeros(len(q) + 1, dtype=np.int64)
+    if len(q):
+        B, O = field_arrays(field)
+        ms = ctypes.c_float()
+        nat.check(nat.lib().gx_eri_magnetic_derivatives(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                                        nat.u32ptr(q), len(q), nat.i64ptr(offsets),
+                                                        nat.dptr(values.view(np.float64)), total, ctypes.byref(ms)))
+    return offsets, values[:total]
+
+
+def eri_magnetic_derivatives_shell(a: Shell, b: Shell, c: Shell, d: Shell, *, field: MagneticField | None = None,
+                                   out=None, context=None) -> npt.NDArray[np.complex128]:
+    """Field derivatives d/dB_b of one shell quartet at fixed gauge origin,
+    complex (3, na, nb, nc, nd) (compute_eri_magnetic_derivatives;
+    src/bindings.cpp:1326-1342)."""
+    for s in (a, b, c, d):
+        if not isinstance(s, Shell):
+            raise TypeError("a, b, c and d must be Shell objects")
+    shape = (3, a.ao_count, b.ao_count, c.ao_count, d.ao_count)
+    result = _validate_out(out, shape)
+    _, values = _eri_magnetic_derivative_blocks(Basis([a, b, c, d]), [(0, 1, 2, 3)], field=field, context=context)
+    result[...] = values.reshape(shape)
+    return result
+
+
+def primitive_eri_magnetic_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussian,
+                                       d: PrimitiveGaussian, *, field: MagneticField | None = None,
+                                       context=None) -> npt.NDArray[np.complex128]:
+    """Field derivatives of one primitive quartet, complex (3,)
+    (primitive_eri_magnetic_derivatives; src/derivatives.cpp:844-850,
+    src/bindings.cpp:995-1010)."""
+    shells, picks, scale = _primitive_shells((a, b, c, d))
+    full = eri_magnetic_derivatives_shell(*shells, field=field, context=context)
+    return full[:, picks[0], picks[1], picks[2], picks[3]] * scale
+
+
+def _primitive_shells(prims):
+    """Unit-coefficient one-primitive shells whose components carry
+    N(alpha, component), the component index of each primitive, and the
+    scale (coefficients; unnormalised primitives divide N out again)."""
     shells, picks = [], []
     scale = 1.0
-    for g in (a, b, c, d):
+    for g in prims:
         if not isinstance(g, PrimitiveGaussian):
             raise TypeError("a, b, c and d must be PrimitiveGaussian objects")
         l = sum(g.angular)
-        # unit-coefficient shell whose components carry N(alpha, component);
-        # unnormalised primitives divide it out again
         shells.append(Shell(g.center, l, [g.exponent], [1.0], normalize=False))
         comps = [(x, y, l - x - y) for x in range(l, -1, -1) for y in range(l - x, -1, -1)]
         picks.append(comps.index(tuple(g.angular)))
         scale *= g.coefficient
         if not g.normalized:
             scale /= nat.lib().gx_primitive_normalization(g.exponent, *g.angular)
-    full = eri_center_derivatives_shell(*shells, field=field, context=context)
-    return full[:, :, picks[0], picks[1], picks[2], picks[3]] * scale
+    return shells, picks, scale
 
 
 class _EriDerivativeSchwarzBounds:

@@ -154,6 +154,16 @@ int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B,
                               const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                               int64_t out_capacity, float* kernel_ms);
 
+/* ERI magnetic derivatives d/dB_b (ab|cd) of nq shell quartets at fixed
+ * gauge origin, replacing compute_eri_magnetic_derivatives
+ * (src/derivatives.cpp:88-106, 268-280, 961-966; eri_magnetic_derivatives_shell,
+ * src/bindings.cpp:1326-1342): block i at offsets[i] is the C-order complex
+ * (3, na, nb, nc, nd) array, b the field axis.  Same limits and arguments as
+ * gx_eri_center_derivatives. */
+int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
+                                int64_t out_capacity, float* kernel_ms);
+
 /* Derivative-density Schwarz factors, replacing EriDerivativeSchwarzBounds
  * (src/derivatives.cpp:1307-1372, bindings.cpp:2242-2253): values[ns*ns]
  * receives the factor of every ordered shell pair (a, b) at a*ns + b, and

@@ -1272,11 +1272,49 @@ static int primitive_center_derivatives(const prim_t* pr, const pair_t* ab, cons
     return 0;
 }
 
-/* Blocks (4, 3, na, nb, nc, nd) of nq shell quartets packed in input order,
+/* d/dB_b of one primitive quartet (raw primitives): sum over slots k of
+ * i phi_k sum_c (e_b x (R_k - O))_c [e(l_k + 1_c) + R_{k,c} e(l)], phi = +1/2
+ * on slots 0, 2 and -1/2 on slots 1, 3 (src/derivatives.cpp:88-106, 268-280). */
+static int primitive_magnetic_derivatives(const prim_t* pr, const pair_t* ab, const pair_t* cd, const field_t* f,
+                                          int real_zero, ws_t* w, cplx* out3) {
+    cplx base;
+    int rc = eri_kernel(pr, ab, cd, real_zero, w, &base);
+    if (rc) return rc;
+    cplx up[4][3];
+    for (int k = 0; k < 4; ++k)
+        for (int c = 0; c < 3; ++c) {
+            int a[3] = {pr[k].ang[0], pr[k].ang[1], pr[k].ang[2]};
+            ++a[c];
+            if ((rc = eri_shifted(pr, k, a, ab, cd, real_zero, w, &up[k][c]))) return rc;
+        }
+    for (int b = 0; b < 3; ++b) {
+        cplx r = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            const double phi = (k % 2 == 0) ? 0.5 : -0.5;
+            double d[3], e[3] = {0.0, 0.0, 0.0};
+            for (int x = 0; x < 3; ++x) d[x] = pr[k].center[x] - f->O[x];
+            e[b] = 1.0;
+            const double ph[3] = {e[1] * d[2] - e[2] * d[1], e[2] * d[0] - e[0] * d[2], e[0] * d[1] - e[1] * d[0]};
+            cplx t = 0.0;
+            for (int c = 0; c < 3; ++c) {
+                const double coef = phi * ph[c];
+                if (coef == 0.0) continue;
+                t += CMPLX(0.0, coef) * (up[k][c] + pr[k].center[c] * base);
+            }
+            r += t;
+        }
+        out3[b] = r;
+    }
+    return 0;
+}
+
+/* Blocks (ncomp, na, nb, nc, nd) of nq shell quartets packed in input order,
  * primitive and component loops of compute_quartet_block
- * (src/derivatives.cpp:556-640). */
-int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
-                              double* out_) {
+ * (src/derivatives.cpp:556-640): ncomp = 12 centre derivatives (slot-major)
+ * or 3 magnetic derivatives. */
+static int derivative_blocks(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
+                             double* out_, int magnetic) {
+    const int ncomp = magnetic ? 3 : 12;
     basis_t bs;
     int rc = basis_init(&bs, ns, centers, ls, nprims, ncontrs, exps, coefs);
     cplx* out = (cplx*)out_;
@@ -1303,7 +1341,7 @@ int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, con
         if (rc) break;
         const size_t block = shape[0] * shape[1] * shape[2] * shape[3];
         cplx* o = out + off;
-        for (size_t i = 0; i < 12 * block; ++i) o[i] = 0.0;
+        for (size_t i = 0; i < (size_t)ncomp * block; ++i) o[i] = 0.0;
         w.boys_valid = 0;
         for (int pa = 0; pa < nprims[sh[0]] && !rc; ++pa)
             for (int pb = 0; pb < nprims[sh[1]] && !rc; ++pb) {
@@ -1333,7 +1371,9 @@ int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, con
                                                                                pr[k].ang[1], pr[k].ang[2]);
                                         }
                                         cplx d12[12];
-                                        rc = primitive_center_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12);
+                                        rc = magnetic
+                                                 ? primitive_magnetic_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12)
+                                                 : primitive_center_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12);
                                         if (rc) break;
                                         for (int xa = 0; xa < ncontrs[sh[0]]; ++xa)
                                             for (int xb = 0; xb < ncontrs[sh[1]]; ++xb)
@@ -1350,16 +1390,27 @@ int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, con
                                                               (size_t)xb * nc[1] + cb) * shape[2] +
                                                              (size_t)xc * nc[2] + cc) * shape[3] +
                                                             (size_t)xd * nc[3] + cdd;
-                                                        for (int dd = 0; dd < 12; ++dd) o[dd * block + e] += kk * d12[dd];
+                                                        for (int dd = 0; dd < ncomp; ++dd)
+                                                            o[dd * block + e] += kk * d12[dd];
                                                     }
                                     }
                     }
             }
-        off += 12 * block;
+        off += (size_t)ncomp * block;
     }
     ws_free(&w);
     basis_free(&bs);
     return rc;
+}
+
+int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
+                              double* out) {
+    return derivative_blocks(ns, centers, ls, nprims, ncontrs, exps, coefs, quartets, nq, B, O, out, 0);
+}
+
+int or_eri_magnetic_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
+                                double* out) {
+    return derivative_blocks(ns, centers, ls, nprims, ncontrs, exps, coefs, quartets, nq, B, O, out, 1);
 }
 
 /* Derivative-density Schwarz factors of every ordered shell pair

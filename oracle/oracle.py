@@ -157,11 +157,11 @@ def _nuclei(nuclei):
     return ch, cc
 
 
-def _derivative_layout(shells, quartets):
-    """Quartet array, offsets and total of packed (4, 3, na, nb, nc, nd) blocks."""
+def _derivative_layout(shells, quartets, ncomp: int = 12):
+    """Quartet array, offsets and total of packed (ncomp, na, nb, nc, nd) blocks."""
     q = np.ascontiguousarray(np.asarray(quartets, dtype=np.uint32).reshape(-1, 4))
     specs = as_specs(shells)
-    sizes = [12 * int(np.prod([specs[k].nao for k in row])) for row in q]
+    sizes = [ncomp * int(np.prod([specs[k].nao for k in row])) for row in q]
     offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     return q, offsets, int(offsets[-1])
 
@@ -298,6 +298,17 @@ class Oracle(_Backend):
                                                        out.ctypes.data_as(_d)))
         return out[:total], offsets
 
+    def eri_magnetic_derivatives(self, shells, quartets, B=None, O=None):
+        """Magnetic-derivative blocks (3, na, nb, nc, nd) of each quartet,
+        packed in input order; returns (values, offsets)."""
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets, 3)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.or_eri_magnetic_derivatives(*a.args(), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
+                                                         _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
+                                                         out.ctypes.data_as(_d)))
+        return out[:total], offsets
+
     def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:
         """Derivative Schwarz factors of every ordered shell pair, [ns, ns]."""
         a = self._basis(shells)
@@ -404,6 +415,17 @@ class Reference(_Backend):
         self._check(self.lib.ref_eri_center_derivatives(*self._bargs(a), q.ctypes.data_as(_u32),
                                                         ctypes.c_long(len(q)), _vec3(B).ctypes.data_as(_d),
                                                         _vec3(O).ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out[:total], offsets
+
+    def eri_magnetic_derivatives(self, shells, quartets, B=None, O=None):
+        """Magnetic-derivative blocks (3, na, nb, nc, nd) of each quartet,
+        packed in input order; returns (values, offsets)."""
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets, 3)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.ref_eri_magnetic_derivatives(*self._bargs(a), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
+                                                         _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
+                                                         out.ctypes.data_as(_d)))
         return out[:total], offsets
 
     def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:

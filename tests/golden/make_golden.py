@@ -27,8 +27,9 @@ Inputs and outputs:
   blocks (4, 3, na, nb, nc, nd) for a seeded three-atom molecule (seeded
   canonical and arbitrary quartets, repeated shells) and a hand-made f/g
   system with a two-contraction p shell, at a finite field with a shifted
-  gauge origin and at zero field, with the reference's derivative and
-  ordinary Schwarz factors of every ordered shell pair;
+  gauge origin and at zero field, with the magnetic-derivative blocks
+  (3, na, nb, nc, nd) of the same quartets and the reference's derivative
+  and ordinary Schwarz factors of every ordered shell pair;
 * ``cholesky.json`` -- the reference's own NumPy Cholesky driver
   (python/giao_integrals/cholesky.py, executed unmodified over the reference
   library's native diagonal/column generators) on the two-shell d/f system of
@@ -287,6 +288,7 @@ def derivative_fixture(ref):
         for label, B, origin in (("field", DERIV_FIELD, DERIV_ORIGIN), ("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))):
             vals, offsets = ref.eri_center_derivatives(specs, q, B, origin)
             out[f"{name}_{label}"] = vals
+            out[f"{name}_magnetic_{label}"] = ref.eri_magnetic_derivatives(specs, q, B, origin)[0]
             out[f"{name}_bounds_{label}"] = ref.eri_derivative_bounds(specs, B, origin)
             out[f"{name}_schwarz_{label}"] = ref.schwarz(specs, B, origin)
             out[f"{name}_offsets"] = offsets

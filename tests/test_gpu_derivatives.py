@@ -264,3 +264,68 @@ def test_derivatives_match_finite_differences():
                 expected = (4 * d2 - d1) / 3
                 actual = block[[k for k, s in enumerate(q) if s == center], axis].sum(axis=0)
                 np.testing.assert_allclose(actual, expected, atol=3e-10, rtol=3e-9)
+
+
+def test_magnetic_derivatives_match_reference(golden, oracle):
+    """d/dB_b blocks (3, na, nb, nc, nd) against the reference library's
+    (golden) and the oracle's, through the batch entry, the shell API and
+    the primitive API."""
+    from giaoint_gb300.eri import _eri_magnetic_derivative_blocks
+
+    g = golden.derivatives
+    for name, specs, q in derivative_systems(g):
+        basis = _basis(specs)
+        for label, field in (("field", _field(g["field"], g["origin"])), ("zero", None)):
+            offsets, values = _eri_magnetic_derivative_blocks(basis, q, field=field)
+            ref = g[f"{name}_magnetic_{label}"]
+            assert _close(values, ref), (name, label)
+            if name == "hand":
+                for i, x in enumerate(q):
+                    blk = gi.eri_magnetic_derivatives_shell(*(basis.shells[k] for k in x), field=field)
+                    assert _close(blk.ravel(), ref[offsets[i]:offsets[i + 1]])
+    field = _field(g["field"], g["origin"])
+    prims = [gi.PrimitiveGaussian(0.9, (0.2, -0.1, 0.0), (0, 1, 1), coefficient=1.2),
+             gi.PrimitiveGaussian(0.5, (-0.4, 0.3, 0.2), (1, 0, 0), normalized=False),
+             gi.PrimitiveGaussian(1.7, (0.1, 0.6, -0.3), (2, 0, 0), coefficient=0.7),
+             gi.PrimitiveGaussian(0.3, (0.0, -0.5, 0.4), (0, 0, 0))]
+    v = gi.primitive_eri_magnetic_derivatives(*prims, field=field)
+    recs = [syn.ShellRecord(p.center, sum(p.angular), (p.exponent,), ((1.0,),), False) for p in prims]
+    blk, _ = oracle.eri_magnetic_derivatives(recs, [(0, 1, 2, 3)], tuple(g["field"]), tuple(g["origin"]))
+    dims = [len(gi.cartesian_components(sum(p.angular))) for p in prims]
+    picks = [gi.cartesian_components(sum(p.angular)).index(tuple(p.angular)) for p in prims]
+    expect = blk.reshape([3] + dims)[:, picks[0], picks[1], picks[2], picks[3]] * (1.2 * 0.7)
+    expect = expect / gi.primitive_normalization(0.5, (1, 0, 0))
+    assert v.shape == (3,)
+    assert np.abs(v - expect).max() <= TOL * max(1.0, np.abs(expect).max())
+
+
+def test_magnetic_derivatives_match_field_differences():
+    """2000 canonical quartets of the 12-atom molecule: d/dB_b against a
+    Richardson-extrapolated central difference of the GPU's own FP64-exact
+    ERIs at B +- h e_b (fixed gauge origin), at zero and finite field."""
+    from giaoint_gb300.eri import _eri_magnetic_derivative_blocks
+
+    recs = syn.random_molecule(2026, natoms=12)
+    basis = basis_from_records(recs)
+    q = gi.canonical_quartets(len(recs))
+    q = q[np.random.default_rng(11).choice(len(q), 2000, replace=False)]
+    O = (0.4, 0.1, -0.6)
+    for B in ((0.0, 0.0, 0.0), (0.05, -0.08, 0.12)):
+        offsets, values = _eri_magnetic_derivative_blocks(basis, q, field=gi.MagneticField(B, gauge_origin=O))
+
+        def eri_at(b, step):
+            Bs = list(B)
+            Bs[b] += step
+            return _eri_batch(basis, q, field=gi.MagneticField(tuple(Bs), gauge_origin=O),
+                              precision="fp64_exact")[3]
+
+        _, _, eoff, _, _, _ = _eri_batch(basis, q, field=gi.MagneticField(B, gauge_origin=O))
+        sizes = np.diff(eoff)
+        for b in range(3):
+            h = 1e-3
+            d1 = (eri_at(b, h) - eri_at(b, -h)) / (2 * h)
+            d2 = (eri_at(b, h / 2) - eri_at(b, -h / 2)) / h
+            fd = (4 * d2 - d1) / 3
+            got = np.concatenate([values[offsets[i] + b * sizes[i]:offsets[i] + (b + 1) * sizes[i]]
+                                  for i in range(len(q))])
+            assert np.abs(got - fd).max() <= 1e-9 * max(1.0, np.abs(fd).max())

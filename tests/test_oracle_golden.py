@@ -167,3 +167,18 @@ def test_eri_derivative_bounds_oracle_matches_reference(golden, oracle):
                                        rtol=1e-14, atol=0)
             np.testing.assert_allclose(oracle.schwarz(specs, field, o), g[f"{name}_schwarz_{label}"],
                                        rtol=1e-14, atol=0)
+
+
+def test_eri_magnetic_derivatives_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of compute_eri_magnetic_derivatives
+    (src/derivatives.cpp:88-106, 268-280, 961-966) against the reference
+    library's (3, na, nb, nc, nd) blocks, zero and finite field."""
+    from conftest import derivative_systems
+
+    g = golden.derivatives
+    B, origin = tuple(g["field"]), tuple(g["origin"])
+    for name, specs, q in derivative_systems(g):
+        for label, field, o in (("field", B, origin), ("zero", None, None)):
+            vals, _ = oracle.eri_magnetic_derivatives(specs, q, field, o)
+            ref = g[f"{name}_magnetic_{label}"]
+            assert np.abs(vals - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (name, label)
