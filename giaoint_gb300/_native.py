@@ -63,7 +63,13 @@ class GxClassProfile(ctypes.Structure):
         ("kt", ctypes.c_int),
         ("ct", ctypes.c_int),
         ("min_blocks", ctypes.c_int),
+        ("stream", ctypes.c_int),
     ]
+
+
+class GxClassConfig(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_int) for name in ("per_group", "warps_per_block", "batch", "kt", "ct", "min_blocks",
+                                                   "nostage", "stream")]
 
 
 # name -> (restype, argtypes); every symbol of include/giao_gb300.h
@@ -91,6 +97,8 @@ SIGNATURES = {
     "gx_eri_magnetic_derivatives": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _d,
                                                    ctypes.c_int64, ctypes.POINTER(ctypes.c_float)]),
     "gx_eri_derivative_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d, _d]),
+    "gx_eri_plan_get_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(GxClassConfig)]),
+    "gx_eri_plan_set_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(GxClassConfig)]),
     "gx_eri_shell": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d]),
     "gx_eri_full": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.c_int, ctypes.c_double, ctypes.c_double, _d]),
     "gx_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d]),

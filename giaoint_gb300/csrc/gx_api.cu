@@ -488,6 +488,7 @@ struct ClassConf {
     int ct = 0;         // generic kernel: ket components per lane in the bra transform (1-4; 0 = by lane use)
     int minb = 0;       // generic kernel: register-budget variant (2 or 4 resident blocks; 0 = 2)
     int nostage = 0;    // generic kernel: 1 = read E~ records and class tables from global memory
+    int stream = 0;     // generic kernel: 1 = per-entry recurrences into a two-column buffer (stream mode)
 };
 
 // Warp work units of every class: (first task within the class, task count).
@@ -797,8 +798,12 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     }
     if (qc.CH < ncd) qc.CH = std::max(qc.CT, qc.CH / qc.CT * qc.CT);  // chunks hold whole CT tiles
     qc.nchunk = (ncd + qc.CH - 1) / qc.CH;
+    qc.stream = conf.stream ? 1 : 0;
     int B1 = conf.b1 > 0 ? std::min(32, conf.b1) : 32;
-    while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
+    if (qc.stream)
+        while (B1 > 1 && (size_t)qc.NL * 2 + (size_t)B1 * (qc.L + 4) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
+    else
+        while (B1 > 1 && (size_t)qc.NL * (B1 + 1) + (size_t)qc.Nab * qc.CH > 3584) B1 /= 2;
     qc.B1 = B1;
     {
         // cooperative recurrence when a batch has fewer entries than the
@@ -2640,9 +2645,53 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
             o.kt = tiles[3 * ci];
             o.ct = tiles[3 * ci + 1];
             o.min_blocks = tiles[3 * ci + 2];
+            o.stream = tuned.valid ? tuned.conf[ci].stream : 0;
         }
         for (auto& e : ev) cudaEventDestroy(e);
         check_status(ctx);
+    });
+}
+
+int gx_eri_plan_get_config(gx_eri_plan* plan, int precision, gx_class_config* out) {
+    return guarded([&] {
+        if (!plan || !out) raise(GX_EINVAL, "null plan or output");
+        check_precision(precision);
+        std::lock_guard<std::mutex> lock(plan->ctx->mu);
+        const PlanData& pd = plan->data;
+        const auto& tuned = pd.tuned[precision];
+        for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
+            const ClassConf c = tuned.valid ? tuned.conf[ci] : ClassConf{};
+            out[ci] = gx_class_config{c.per_group, c.wpb, c.b1, c.kt, c.ct, c.minb, c.nostage, c.stream};
+        }
+    });
+}
+
+int gx_eri_plan_set_config(gx_eri_plan* plan, int precision, const gx_class_config* confs) {
+    return guarded([&] {
+        if (!plan || !confs) raise(GX_EINVAL, "null plan or configuration");
+        check_precision(precision);
+        gx_context* ctx = plan->ctx;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        PlanData& pd = plan->data;
+        std::vector<ClassConf> conf(pd.classes.size());
+        for (size_t ci = 0; ci < conf.size(); ++ci) {
+            const gx_class_config& c = confs[ci];
+            if (c.per_group < 0 || c.warps_per_block < 0 || c.warps_per_block > 4 || c.batch < 0 || c.batch > 32 ||
+                (c.kt != 0 && c.kt != 1 && c.kt != 2 && c.kt != 4) || c.ct < 0 || c.ct > 4 ||
+                (c.min_blocks != 0 && c.min_blocks != 2 && c.min_blocks != 4) || (c.nostage != 0 && c.nostage != 1) ||
+                (c.stream != 0 && c.stream != 1))
+                raise(GX_EINVAL, "class configuration out of range");
+            conf[ci] = ClassConf{c.per_group, c.warps_per_block, c.batch, c.kt, c.ct, c.min_blocks, c.nostage,
+                                 c.stream};
+        }
+        auto& tuned = pd.tuned[precision];
+        make_group_set(ctx, pd, conf, tuned.groups);
+        tuned.conf = conf;
+        tuned.valid = true;
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        ++plan->generation;
+        plan->graph.reset();
     });
 }
 
@@ -2745,6 +2794,25 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
                             best[ci] = cf;
                         }
                     }
+            }
+            if (!gx::small_class(k[0], k[1], k[2], k[3])) {
+                // fourth stage: stream mode (per-entry recurrences, small
+                // shared footprint, more resident warps) on the chosen split
+                const ClassConf base = best[ci];
+                for (int minb : {2, 4})
+                    for (int b1 : {0, 16})
+                        for (int nostage : {0, 1}) {
+                            ClassConf cf = base;
+                            cf.stream = 1;
+                            cf.minb = minb;
+                            cf.b1 = b1 ? b1 : 32;
+                            cf.nostage = nostage;
+                            const double t = time_conf(cf);
+                            if (t < 0.97 * best_ms) {
+                                best_ms = t;
+                                best[ci] = cf;
+                            }
+                        }
             }
             tot_default += def_ms;
             tot_best += best_ms;

@@ -82,6 +82,8 @@ struct QuartetClass {
     int stage_e;           // words (complex) of the per-warp E~ staging buffer (0: read E~ from global memory)
     int tab_words;         // 32-bit words of the block-shared class tables (0: read them from global memory)
     int KT, CT;            // Hermite rows per lane in the ket transform, ket components per lane in the bra transform
+    int stream;            // 1: phase 1 keeps only the seeds of the batch; each entry's R is built by the warp
+                           //    into a two-column buffer right before its ket transform (small shared footprint)
     int ntask;
     const Task* tasks;
     int ngroup;

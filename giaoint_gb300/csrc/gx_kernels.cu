@@ -546,17 +546,21 @@ __device__ __forceinline__ void hermite_rec_any(const EriDev& d, int L, const T*
 struct WarpSmem {
     size_t R, W, W32, queue, flag, eoff, seed, stage, total;
 };
-__host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed, int stage_e) {
+// Per-warp shared layout.  Batched mode: R columns of all B1 entries
+// (stride B1 + 1) and one seed area; stream mode: a two-column R buffer and
+// the seeds and X' of every batch entry (L + 4 slots each).
+__host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed, int stage_e, int stream,
+                                              int L) {
     WarpSmem w;
     const size_t B1p = B1 + 1;
     w.R = 0;
-    w.W = w.R + (size_t)NL * B1p * 16;
+    w.W = w.R + (size_t)NL * (stream ? 2 : B1p) * 16;
     w.W32 = w.W + (size_t)Nab * CH * 16;
     w.queue = w.W32 + (mixed ? (((size_t)Nab * CH * 8 + 15) / 16) * 16 : 0);
     w.flag = w.queue + (((size_t)B1 * 4 + 15) / 16) * 16;
     w.eoff = w.flag + (((size_t)B1 * 4 + 15) / 16) * 16;
     w.seed = w.eoff + (((size_t)B1 * 8 + 15) / 16) * 16;
-    w.stage = w.seed + (size_t)(BOYS_MAX_ORDER + 1 + 3) * 16;
+    w.stage = w.seed + (stream ? (size_t)B1 * (L + 4) : (size_t)(BOYS_MAX_ORDER + 1 + 3)) * 16;
     // FP64 record (16 B per word) followed by its FP32 copy (8 B per word)
     w.total = w.stage + (((size_t)stage_e * 24 + 15) / 16) * 16;
     return w;
@@ -975,7 +979,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     const int wpb = blockDim.x >> 5;
     const int B1p = qc.B1 + 1;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
-    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e);
+    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e, qc.stream, qc.L);
     const size_t tab_bytes = (((size_t)qc.tab_words * 4 + 15) / 16) * 16;
     char* base = reinterpret_cast<char*>(sm) + tab_bytes + (size_t)wib * lay.total;
     double2* R = reinterpret_cast<double2*>(base + lay.R);
@@ -984,7 +988,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     int* queue = reinterpret_cast<int*>(base + lay.queue);
     int* flag = reinterpret_cast<int*>(base + lay.flag);
     long long* eoff = reinterpret_cast<long long*>(base + lay.eoff);  // E~ record of each entry's ket pair
-    double2* sseed = reinterpret_cast<double2*>(base + lay.seed);  // [L+1] seeds, then X'[3]
+    double2* sseed = reinterpret_cast<double2*>(base + lay.seed);  // [L+1] seeds, then X'[3] (per entry: stream)
+    const int sstride = qc.L + 4;  // stream mode: seed slots per entry
     double2* stg = qc.stage_e > 0 ? reinterpret_cast<double2*>(base + lay.stage) : nullptr;  // E~ staging
     const int nab = qc.bra.nab, ncd = qc.ket.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
@@ -1065,7 +1070,40 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                 }
                 __syncwarp();
                 if (nb == 0) break;
-                if (nb <= qc.coop) {
+                if (qc.stream) {
+                    // seeds and X' of every entry, lane-parallel; the
+                    // recurrences run per entry in phase 2
+                    if (lane < nb) {
+                        const int idx = queue[lane];
+                        const int g = idx / KK, r = idx - g * KK;
+                        const int P = r / Kcd, Q = r - P * Kcd;
+                        const Task tg = qc.tasks[gi.x + g];
+                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
+                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                        const QuartetArgs qa = quartet_args(pp, ip, iq);
+                        double2 Sh[BOYS_MAX_ORDER + 1];
+                        float2 S32[BOYS_MAX_ORDER + 1];
+                        const bool want32 = mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
+                                                             pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] <
+                                                         cut32;
+                        int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
+                        if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
+                        double2* es = sseed + (size_t)lane * sstride;
+                        if (f == 1) {
+                            for (int n = 0; n <= qc.L; ++n) es[n] = Sh[n];
+                            for (int x = 0; x < 3; ++x) es[qc.L + 1 + x] = qa.X[x];
+                            cnt64 += first_chunk;
+                        } else {
+                            float2* s32 = reinterpret_cast<float2*>(es);
+                            for (int n = 0; n <= qc.L; ++n) s32[n] = S32[n];
+                            for (int x = 0; x < 3; ++x)
+                                s32[qc.L + 1 + x] = make_float2((float)qa.X[x].x, (float)qa.X[x].y);
+                            cnt32 += first_chunk;
+                        }
+                        flag[lane] = f;
+                        eoff[lane] = pp.Eoff[iq];
+                    }
+                } else if (nb <= qc.coop) {
                     // few entries: one lane forms the seeds, the warp runs the
                     // recurrence level-parallel
                     for (int j = 0; j < nb; ++j) {
@@ -1163,7 +1201,26 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         has64 = has64 || flag[jj] == 1;
                         has32 = has32 || flag[jj] == 0;
                     }
-                    step_k_any(qc, tabs, d.herm_xyz, pp, R, R32s, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn, lane);
+                    if (qc.stream) {
+                        // entry by entry: the warp's recurrence into the
+                        // two-column buffer (level 0 in column 0), then the
+                        // ket transform of that column
+                        for (int jj = j0; jj < j1; ++jj) {
+                            __syncwarp();  // the previous entry's transform has read R
+                            const double2* es = sseed + (size_t)jj * sstride;
+                            if (flag[jj] == 1) {
+                                coop_rec<double2>(qc.L, es, es + qc.L + 1, R, 2, 0, 1, d.herm_xyz, lane);
+                            } else {
+                                const float2* s32 = reinterpret_cast<const float2*>(es);
+                                coop_rec<float2>(qc.L, s32, s32 + qc.L + 1, R32s, 4, 0, 2, d.herm_xyz, lane);
+                            }
+                            step_k_any(qc, tabs, d.herm_xyz, pp, R, R32s, 2, flag + jj, eoff + jj, 0, 1, W, W32, stg,
+                                       c0, chn, lane);
+                        }
+                    } else {
+                        step_k_any(qc, tabs, d.herm_xyz, pp, R, R32s, B1p, flag, eoff, j0, j1, W, W32, stg, c0, chn,
+                                   lane);
+                    }
                     any64 = any64 || has64;
                     any32 = any32 || has32;
                     j0 = j1;
@@ -1192,7 +1249,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
 
 size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed) {
     return (((size_t)qc.tab_words * 4 + 15) / 16) * 16 +
-           (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed, qc.stage_e).total;
+           (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed, qc.stage_e, qc.stream, qc.L).total;
 }
 
 static bool g_const_ready = false;

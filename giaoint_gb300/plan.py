@@ -122,6 +122,28 @@ class EriPlan:
                                                  ctypes.byref(before), ctypes.byref(after)))
         return before.value, after.value
 
+    def get_config(self, precision: str = "fp64") -> list[dict]:
+        """Launch configuration of every class for ``precision`` (zeros: default)."""
+        lib = nat.lib()
+        n = lib.gx_eri_plan_class_count(self._handle)
+        if n < 0:
+            nat.check(n)
+        arr = (nat.GxClassConfig * max(n, 1))()
+        nat.check(lib.gx_eri_plan_get_config(self._handle, _precision(precision), arr))
+        keys = [name for name, _ in nat.GxClassConfig._fields_]
+        return [{k: getattr(arr[i], k) for k in keys} for i in range(n)]
+
+    def set_config(self, configs: list[dict], precision: str = "fp64") -> None:
+        """Pin the launch configuration of every class for ``precision``."""
+        n = nat.lib().gx_eri_plan_class_count(self._handle)
+        if len(configs) != n:
+            raise ValueError(f"expected {n} class configurations")
+        arr = (nat.GxClassConfig * max(n, 1))()
+        for i, c in enumerate(configs):
+            for k, v in c.items():
+                setattr(arr[i], k, int(v))
+        nat.check(nat.lib().gx_eri_plan_set_config(self._handle, _precision(precision), arr))
+
     def close(self) -> None:
         if getattr(self, "_handle", None):
             nat.lib().gx_eri_plan_destroy(self._handle)
@@ -141,7 +163,7 @@ def _main(argv=None) -> None:
     through a plan, once per precision mode, and print the counts: a small,
     self-contained workload for profiling one kernel launch per mode.
 
-        python -m giaoint_gb300.plan --atoms 12 --class 1111 --precision fp64,mixed
+        python -m giaoint_gb300.plan --atoms 12 --class 1111 --precision fp64,mixed [--stream] [--min-blocks 4]
     """
     import argparse
 
@@ -155,6 +177,8 @@ def _main(argv=None) -> None:
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--class", dest="cls", default="1111", help="four digits la lb lc ld")
     p.add_argument("--precision", default="fp64,mixed")
+    p.add_argument("--stream", action="store_true", help="stream mode (per-entry recurrences) for the class")
+    p.add_argument("--min-blocks", type=int, default=0, choices=[0, 2, 4])
     a = p.parse_args(argv)
     key = tuple(int(c) for c in a.cls)
     recs = syn.random_molecule(a.seed, natoms=a.atoms)
@@ -166,6 +190,9 @@ def _main(argv=None) -> None:
     out = torch.empty(max(plan.total, 1), dtype=torch.complex128, device="cuda:0")
     field = MagneticField(syn.random_field(a.seed))
     for prec in a.precision.split(","):
+        if a.stream or a.min_blocks:
+            plan.set_config([dict(c, stream=int(a.stream), min_blocks=a.min_blocks) for c in plan.get_config(prec)],
+                            prec)
         plan.execute(out, field, precision=prec)
         plan.synchronize()
         print(prec, {"class": key, "quartets": len(sel), **plan.counts()}, flush=True)

@@ -288,6 +288,7 @@ typedef struct gx_class_profile {
     int64_t groups;                /* warp work units */
     int kt, ct;                    /* generic kernel: ket-transform rows and bra-transform components per lane */
     int min_blocks;                /* generic kernel: register-budget variant (resident blocks) */
+    int stream;                    /* generic kernel: 1 = per-entry recurrences (stream mode) */
 } gx_class_profile;
 int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                         void* out_device, gx_class_profile* out);
@@ -298,6 +299,22 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
  * class times before and after. */
 int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                          void* out_device, int repeats, double* default_ms, double* tuned_ms);
+
+/* Launch configuration of one class (zeros: the default), as the
+ * autotuner chooses it: primitive quartets per warp unit, warps per block
+ * cap (<= 4), phase-1 batch cap (<= 32), ket-transform rows per lane (1, 2,
+ * 4), bra-transform components per lane (1-4), register-budget variant (2
+ * or 4 resident blocks), 1 = no shared staging, 1 = stream mode (per-entry
+ * recurrences into a two-column buffer).  Fields other than per_group apply
+ * to the generic kernel only. */
+typedef struct gx_class_config {
+    int per_group, warps_per_block, batch, kt, ct, min_blocks, nostage, stream;
+} gx_class_config;
+/* Read / replace the configuration of every class (gx_eri_plan_class_count
+ * entries) for one precision mode; a set configuration is used by later
+ * executions in that mode (replaying a saved tuning, or pinning one). */
+int gx_eri_plan_get_config(gx_eri_plan* plan, int precision, gx_class_config* out);
+int gx_eri_plan_set_config(gx_eri_plan* plan, int precision, const gx_class_config* confs);
 
 /* Canonical shell quartets of an ns-shell basis: the lexicographic
  * minimum of each finite-field orbit {(ab|cd), (cd|ab), (ba|dc)*, (dc|ba)*}

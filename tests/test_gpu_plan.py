@@ -80,3 +80,43 @@ def test_mixed_precision_autotuned_within_1e10_of_fp64():
     assert err <= 1e-10, err
     prof = plan.profile(out, field, precision="mixed")
     assert sum(p["fp32_quartets"] for p in prof) == counts["fp32_quartets"]
+
+
+def test_pinned_stream_mode_matches_exact_and_batched():
+    """Every generic class pinned to stream mode (per-entry recurrences into
+    a two-column buffer), over its register variants, staging and batch
+    sizes: FP64 within 1e-13 of the batched launches and 1e-12 of the
+    FP64-exact path; mixed precision within 1e-10 of FP64-exact."""
+    torch = _torch()
+    recs, basis = molecule(seed=13, natoms=4)
+    field = gi.MagneticField((0.08, -0.12, 0.05))
+    plan = EriPlan(basis)
+    out = torch.empty(plan.total, dtype=torch.complex128, device="cuda:0")
+    plan.execute(out, field, precision="fp64_exact")
+    plan.synchronize()
+    exact = out.clone()
+    plan.execute(out, field, precision="fp64")
+    plan.synchronize()
+    batched = out.clone()
+    default = plan.get_config("fp64")
+    assert all(c["stream"] == 0 for c in default)
+    for minb in (2, 4):
+        for nostage in (0, 1):
+            for b1 in (32, 8):
+                cfg = [dict(c, stream=1, min_blocks=minb, nostage=nostage, batch=b1) for c in default]
+                plan.set_config(cfg, "fp64")
+                assert plan.get_config("fp64") == cfg
+                out.zero_()
+                plan.execute(out, field, precision="fp64")
+                plan.synchronize()
+                assert float((out - batched).abs().max()) <= 1e-13, (minb, nostage, b1)
+                assert float((out - exact).abs().max()) <= 1e-12, (minb, nostage, b1)
+    plan.set_config([dict(c, stream=1, min_blocks=4) for c in plan.get_config("mixed")], "mixed")
+    plan.execute(out, field, precision="mixed")
+    plan.synchronize()
+    assert plan.counts()["fp32_quartets"] > 0
+    assert float((out - exact).abs().max()) <= 1e-10
+    with pytest.raises(ValueError, match="out of range"):
+        plan.set_config([dict(c, stream=2) for c in default], "fp64")
+    with pytest.raises(ValueError, match="class configurations"):
+        plan.set_config(default[:-1], "fp64")
