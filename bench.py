@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--natoms", type=int, default=12)
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--no-derivatives", action="store_true")
+    p.add_argument("--derivatives-only", action="store_true",
+                   help="run only the centre-derivative leg and print its JSON (profiling)")
+    p.add_argument("--derivative-quartets", type=int, default=200000)
     p.add_argument("--serving-requests", type=int, default=32)
     p.add_argument("--sweep", type=int, default=0,
                    help="field sweep: evaluate the molecule at this many fields |B| <= 0.5 in FP64 and mixed")
@@ -433,6 +436,11 @@ def run_gpu(args):
     lib = nat.lib()
     ctx = nat.Context(local)
     recs, B = workload(args.natoms, rank)
+    if args.derivatives_only:
+        quartets = gi.canonical_quartets(len(recs))
+        leg = derivative_leg(ctx, recs, B, quartets, run_cpu=False, count=args.derivative_quartets)
+        print(json.dumps({"center_derivatives": leg}), flush=True)
+        return
     basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
     bh = basis._device(ctx)
     quartets = gi.canonical_quartets(len(recs))
@@ -589,7 +597,8 @@ def run_gpu(args):
     derivatives = None
     if rank == 0 and not args.no_derivatives:
         nat.check(lib.gx_context_set_stream(ctx.handle, None))
-        derivatives = derivative_leg(ctx, recs, B, quartets, run_cpu=(world == 1 and not args.no_cpu))
+        derivatives = derivative_leg(ctx, recs, B, quartets, run_cpu=(world == 1 and not args.no_cpu),
+                                     count=args.derivative_quartets)
     serving = None
     if rank == 0 and not args.no_serving:
         serving = serving_leg(args)
