@@ -36,6 +36,7 @@ from .eri import (
     primitive_eri_center_derivatives,
     primitive_eri_magnetic_derivatives,
 )
+from .molecule import Molecule
 from .nuclear import nuclear_attraction, nuclear_attraction_shell, primitive_nuclear_attraction
 
 __version__ = "0.1.0"
@@ -49,6 +50,7 @@ __all__ = [
     "EriBatch",
     "EriDerivativeBatch",
     "MagneticField",
+    "Molecule",
     "Nucleus",
     "PrimitiveGaussian",
     "Shell",

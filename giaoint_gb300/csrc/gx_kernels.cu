@@ -1296,14 +1296,39 @@ __global__ void scatter_full_kernel(const double2* packed, const long long* bloc
     const int sh = f[4];
     const int na = sh & 255, nb = (sh >> 8) & 255, nc = (sh >> 16) & 255, nd = (sh >> 24) & 255;
     const int total = na * nb * nc * nd;
+    const long long g[4] = {f[0], f[1], f[2], f[3]};
+    const int dims[4] = {na, nb, nc, nd};
+    // image m of element (x0, x1, x2, x3) sits at (x[perm[m][0]], ...):
+    // (ab|cd), (cd|ab), (ba|dc)*, (dc|ba)* (src/eri.cpp:777-805)
+    const int perm[4][4] = {{0, 1, 2, 3}, {2, 3, 0, 1}, {1, 0, 3, 2}, {3, 2, 1, 0}};
     for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int id = e % nd, ic = (e / nd) % nc, ib = (e / (nd * nc)) % nb, ia = e / (nd * nc * nb);
+        const int x[4] = {e / (nd * nc * nb), (e / (nd * nc)) % nb, (e / nd) % nc, e % nd};
         const double2 v = packed[block_off[bi] + e];
-        const long long a = f[0] + ia, b = f[1] + ib, c = f[2] + ic, dd = f[3] + id;
-        full[((a * n + b) * n + c) * n + dd] = v;
-        full[((c * n + dd) * n + a) * n + b] = v;
-        full[((b * n + a) * n + dd) * n + c] = cconj(v);
-        full[((dd * n + c) * n + b) * n + a] = cconj(v);
+        const long long G[4] = {g[0] + x[0], g[1] + x[1], g[2] + x[2], g[3] + x[3]};
+        for (int m = 0; m < 4; ++m) {
+            long long p[4];
+            for (int k = 0; k < 4; ++k) p[k] = G[perm[m][k]];
+            // The reference writes the four images element by element, so
+            // where images coincide (repeated shells) the last (element,
+            // image) in that order wins; write only if this one is it.
+            bool last = true;
+            for (int m2 = 0; m2 < 4 && last; ++m2) {
+                int y[4];
+                bool inside = true;
+                for (int k = 0; k < 4; ++k) {
+                    // position k of image m2 holds global index G'[perm[m2][k]]
+                    const int slot = perm[m2][k];
+                    const long long loc = p[k] - g[slot];
+                    inside = inside && loc >= 0 && loc < dims[slot];
+                    y[slot] = (int)loc;
+                }
+                if (!inside) continue;
+                const int e2 = ((y[0] * nb + y[1]) * nc + y[2]) * nd + y[3];
+                if (e2 > e || (e2 == e && m2 > m)) last = false;
+            }
+            if (!last) continue;
+            full[((p[0] * n + p[1]) * n + p[2]) * n + p[3]] = m < 2 ? v : cconj(v);
+        }
     }
 }
 
