@@ -30,11 +30,13 @@ from .eri import (
     eri_center_derivatives_shell,
     eri_derivative_batches,
     eri_magnetic_derivatives_shell,
+    eri_mixed_derivatives_shell,
     eri_schwarz_bounds,
     eri_shell,
     primitive_eri,
     primitive_eri_center_derivatives,
     primitive_eri_magnetic_derivatives,
+    primitive_eri_mixed_derivatives,
 )
 from .molecule import Molecule
 from .nuclear import nuclear_attraction, nuclear_attraction_shell, primitive_nuclear_attraction
@@ -65,6 +67,7 @@ __all__ = [
     "eri_center_derivatives_shell",
     "eri_derivative_batches",
     "eri_magnetic_derivatives_shell",
+    "eri_mixed_derivatives_shell",
     "eri_schwarz_bounds",
     "eri_shell",
     "nuclear_attraction",
@@ -72,6 +75,7 @@ __all__ = [
     "primitive_eri",
     "primitive_eri_center_derivatives",
     "primitive_eri_magnetic_derivatives",
+    "primitive_eri_mixed_derivatives",
     "primitive_nuclear_attraction",
     "primitive_normalization",
     "resolve_num_threads",

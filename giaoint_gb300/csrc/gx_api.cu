@@ -1393,107 +1393,225 @@ void derivative_schwarz_impl(gx_context* ctx, gx_basis* b, const double* B, cons
     }
 }
 
-// Centre (mode 0) or magnetic (mode 1) derivatives of nq shell quartets:
-// blocks (4, 3, na, nb, nc, nd) or (3, na, nb, nc, nd) at offsets[i] (complex
-// elements), in input order.
+// Validate nq quartets of b for derivative mode `mode` (0 centre, 1
+// magnetic, 2 mixed field/centre) and write their output offsets
+// (complex elements, nq + 1 values).
+int64_t derivative_offsets(const gx_basis* b, int mode, const uint32_t* quartets, int64_t nq, int64_t* offsets) {
+    if (nq < 0) raise(GX_EINVAL, "negative quartet count");
+    if (nq > (int64_t)INT32_MAX) raise(GX_ELENGTH, "derivative batch size overflow");
+    const uint32_t ns = (uint32_t)b->ns;
+    const int lmax = mode == 2 ? 14 : 15, extra = mode == 2 ? 2 : 1;
+    const int64_t ncomp = mode == 0 ? 12 : (mode == 1 ? 3 : 36);
+    int64_t off = 0;
+    for (int64_t i = 0; i < nq; ++i) {
+        const uint32_t* x = quartets + 4 * i;
+        int L = 0;
+        int64_t size = 1;
+        for (int k = 0; k < 4; ++k) {
+            if (x[k] >= ns) raise(GX_ERANGE, "derivative shell quartet index is out of range");
+            if (b->l[x[k]] > lmax)
+                raise(GX_EINVAL, mode == 2 ? "ERI mixed derivatives support shells through l = 14"
+                                           : "ERI centre derivatives support shells through l = 15");
+            L += b->l[x[k]];
+            size *= b->nao_of(x[k]);
+        }
+        if (L + extra > 32) raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
+        offsets[i] = off;
+        off += ncomp * size;
+    }
+    offsets[nq] = off;
+    return off;
+}
+
+double inv_sqrt_double_factorial(int n) {
+    double df = 1.0;  // (2n - 1)!!
+    for (int k = 1; k <= n; ++k) df *= 2.0 * k - 1.0;
+    return 1.0 / std::sqrt(df);
+}
+
+// Centre (mode 0) or magnetic (mode 1) derivative blocks of nq validated
+// quartets into device memory dout at offsets; the caller holds ctx->mu.
+void derivative_core(gx_context* ctx, gx_basis* b, int mode, const double* B, const double* O,
+                     const uint32_t* quartets, int64_t nq, const int64_t* offsets, double2* dout, float* kernel_ms) {
+    if (nq == 0) return;
+    const uint32_t ns = (uint32_t)b->ns;
+    std::vector<int> dix;
+    gx_basis* db = derivative_basis(ctx, b, dix);
+    const bool field = B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0;
+    const bool has_u = mode == 1 || field;
+    // derived blocks per quartet: for each slot [Z, D if l > 0] (centre
+    // mode), [U]; then [plain]
+    std::vector<uint32_t> dq;
+    dq.reserve((size_t)nq * 4 * (mode == 1 ? 5 : (field ? 13 : 8)));
+    std::vector<long long> doff((size_t)nq);
+    int64_t dtotal = 0;
+    for (int64_t i = 0; i < nq; ++i) {
+        const uint32_t* x = quartets + 4 * i;
+        doff[i] = dtotal;
+        auto add = [&](int k, int g) {
+            uint32_t y[4] = {x[0], x[1], x[2], x[3]};
+            int64_t size = 1;
+            if (g >= 0) y[k] = (uint32_t)dix[(size_t)g * ns + x[k]];
+            for (int j = 0; j < 4; ++j) size *= db->nao_of(y[j]);
+            dq.insert(dq.end(), y, y + 4);
+            dtotal += size;
+        };
+        for (int k = 0; k < 4; ++k) {
+            if (mode == 0) {
+                add(k, kDerivZ);
+                if (b->l[x[k]] > 0) add(k, kDerivD);
+            }
+            if (has_u) add(k, kDerivU);
+        }
+        if (has_u) add(0, -1);
+    }
+    const int64_t dcount = (int64_t)dq.size() / 4;
+    uint64_t h1 = 0x452821E638D01377ull ^ (uint64_t)dcount, h2 = 0xBE5466CF34E90C6Cull;
+    for (int64_t i = 0; i < dcount; ++i) {
+        uint64_t v0, v1;
+        std::memcpy(&v0, &dq[4 * i], 8);
+        std::memcpy(&v1, &dq[4 * i + 2], 8);
+        h1 = (((h1 ^ v0) * 0x9E3779B97F4A7C15ull) ^ v1) * 0xBF58476D1CE4E5B9ull;
+        h1 ^= h1 >> 31;
+        h2 = (h2 + v0 * 0xC2B2AE3D27D4EB4Full + (v1 ^ (uint64_t)i)) * 0x94D049BB133111EBull;
+        h2 ^= h2 >> 29;
+    }
+    PlanData& plan = lookup_plan(ctx, db, h1, h2, dcount, dtotal, [&] {
+        std::vector<QuartetRequest> req;
+        req.reserve((size_t)dcount);
+        int64_t o = 0;
+        for (int64_t i = 0; i < dcount; ++i) {
+            const uint32_t* y = &dq[4 * i];
+            req.push_back({y[0], y[1], y[2], y[3], o});
+            o += db->nao_of(y[0]) * db->nao_of(y[1]) * db->nao_of(y[2]) * db->nao_of(y[3]);
+        }
+        return req;
+    });
+    apply_recorded_tuning(ctx, db, GX_PRECISION_FP64, plan);
+    float ms = 0.f;
+    ctx->deriv_vals.reserve(std::max<int64_t>(dtotal, 1) * sizeof(double2));
+    run_plan(ctx, db, B, O, plan, ctx->deriv_vals.as<double2>(), kernel_ms ? &ms : nullptr, nullptr,
+             GX_PRECISION_FP64, 0.0, nullptr);
+    // metadata: quartets | offsets | derived offsets
+    const size_t qbytes = ((size_t)nq * 16 + 15) / 16 * 16;
+    const size_t obytes = (size_t)(nq + 1) * 8;
+    ctx->deriv_meta.reserve(qbytes + obytes + (size_t)nq * 8);
+    char* meta = ctx->deriv_meta.as<char>();
+    GX_CUDA(cudaMemcpyAsync(meta, quartets, (size_t)nq * 16, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(cudaMemcpyAsync(meta + qbytes, offsets, obytes, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(cudaMemcpyAsync(meta + qbytes + obytes, doff.data(), (size_t)nq * 8, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    gx::DerivCombineArgs a{};
+    a.nq = (int)nq;
+    a.mode = mode;
+    a.field = field ? 1 : 0;
+    a.quartets = reinterpret_cast<const uint32_t*>(meta);
+    a.offsets = reinterpret_cast<const long long*>(meta + qbytes);
+    a.derived_offsets = reinterpret_cast<const long long*>(meta + qbytes + obytes);
+    a.shell_l = b->d_shell_l.as<int>();
+    a.shell_ncontr = b->d_shell_ncontr.as<int>();
+    a.shell_raw = b->d_shell_raw.as<int>();
+    a.shell_center = b->d_shell_center.as<double>();
+    a.derived = ctx->deriv_vals.as<double2>();
+    a.out = dout;
+    for (int k = 0; k < 3; ++k) {
+        a.B[k] = B[k];
+        a.O[k] = O[k];
+    }
+    for (int n = 0; n < 18; ++n) a.inv_sqrt_df[n] = inv_sqrt_double_factorial(n);
+    GX_CUDA(gx::launch_deriv_combine(a, offsets[nq], ctx->sm_count, ctx->stream));
+    if (kernel_ms) *kernel_ms = ms;
+}
+
+// Mixed field/centre derivatives (4, 3, 3, na, nb, nc, nd) of nq validated
+// quartets: the centre derivatives of the quartets and of the four quartets
+// with one slot replaced by its U shell (the latter on the derived basis,
+// whose own derived basis supplies the doubly shifted shells), their plain
+// blocks, and deriv_mixed_kernel's linear combination.  Caller holds ctx->mu.
+void mixed_core(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
+                int64_t nq, const int64_t* offsets, double2* dout) {
+    if (nq == 0) return;
+    const int ns = b->ns;
+    std::vector<int> dix;
+    gx_basis* db = derivative_basis(ctx, b, dix);
+    std::vector<uint32_t> lists[5];
+    for (int t = 0; t < 5; ++t) {
+        lists[t].assign(quartets, quartets + 4 * nq);
+        if (t > 0)
+            for (int64_t i = 0; i < nq; ++i) {
+                uint32_t& s = lists[t][4 * i + (t - 1)];
+                s = (uint32_t)dix[(size_t)kDerivU * ns + s];
+            }
+    }
+    DeviceBuffer dbuf[5];
+    std::vector<long long> doff(5 * (size_t)nq), eoff(5 * (size_t)nq);
+    std::vector<int64_t> o(nq + 1);
+    for (int t = 0; t < 5; ++t) {
+        gx_basis* bt = t == 0 ? b : db;
+        const int64_t tot = derivative_offsets(bt, 0, lists[t].data(), nq, o.data());
+        for (int64_t i = 0; i < nq; ++i) doff[(size_t)t * nq + i] = o[i];
+        dbuf[t].reserve(std::max<int64_t>(tot, 1) * sizeof(double2));
+        derivative_core(ctx, bt, 0, B, O, lists[t].data(), nq, o.data(), dbuf[t].as<double2>(), nullptr);
+    }
+    // plain blocks of all five lists, on the derived basis (its first ns
+    // shells are the shells of b)
+    std::vector<QuartetRequest> req;
+    req.reserve(5 * (size_t)nq);
+    int64_t etot = 0;
+    for (int t = 0; t < 5; ++t)
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* y = &lists[t][4 * i];
+            eoff[(size_t)t * nq + i] = etot;
+            req.push_back({y[0], y[1], y[2], y[3], etot});
+            etot += db->nao_of(y[0]) * db->nao_of(y[1]) * db->nao_of(y[2]) * db->nao_of(y[3]);
+        }
+    DeviceBuffer ebuf, meta;
+    ebuf.reserve(std::max<int64_t>(etot, 1) * sizeof(double2));
+    run_quartets(ctx, db, B, O, req, ebuf.as<double2>(), nullptr);
+    const size_t qbytes = ((size_t)nq * 16 + 15) / 16 * 16;
+    const size_t obytes = (size_t)(nq + 1) * 8;
+    const size_t tbytes = 5 * (size_t)nq * 8;
+    meta.reserve(qbytes + obytes + 2 * tbytes);
+    char* m = meta.as<char>();
+    GX_CUDA(cudaMemcpyAsync(m, quartets, (size_t)nq * 16, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(cudaMemcpyAsync(m + qbytes, offsets, obytes, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(cudaMemcpyAsync(m + qbytes + obytes, doff.data(), tbytes, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(cudaMemcpyAsync(m + qbytes + obytes + tbytes, eoff.data(), tbytes, cudaMemcpyHostToDevice, ctx->stream));
+    gx::DerivMixedArgs a{};
+    a.nq = (int)nq;
+    a.quartets = reinterpret_cast<const uint32_t*>(m);
+    a.offsets = reinterpret_cast<const long long*>(m + qbytes);
+    a.doff = reinterpret_cast<const long long*>(m + qbytes + obytes);
+    a.eoff = reinterpret_cast<const long long*>(m + qbytes + obytes + tbytes);
+    for (int t = 0; t < 5; ++t) a.D[t] = dbuf[t].as<double2>();
+    a.E = ebuf.as<double2>();
+    a.shell_l = b->d_shell_l.as<int>();
+    a.shell_ncontr = b->d_shell_ncontr.as<int>();
+    a.shell_raw = b->d_shell_raw.as<int>();
+    a.shell_center = b->d_shell_center.as<double>();
+    a.out = dout;
+    for (int k = 0; k < 3; ++k) a.O[k] = O[k];
+    for (int n = 0; n < 18; ++n) a.inv_sqrt_df[n] = inv_sqrt_double_factorial(n);
+    GX_CUDA(gx::launch_deriv_mixed(a, offsets[nq], ctx->sm_count, ctx->stream));
+    // the local buffers are freed on return: finish their readers first
+    GX_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// Centre (mode 0), magnetic (mode 1) or mixed (mode 2) derivatives of nq
+// shell quartets: blocks (4, 3, ...), (3, ...) or (4, 3, 3, ...) of the
+// reference layout at offsets[i] (complex elements), in input order.
 int eri_derivative_impl(gx_context* ctx, gx_basis* b, int mode, const double* B, const double* O,
                         const uint32_t* quartets, int64_t nq, int64_t* offsets, void* out, bool out_is_device,
                         int64_t capacity, float* kernel_ms) {
     return guarded([&] {
         if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
-        if (nq < 0) raise(GX_EINVAL, "negative quartet count");
-        if (nq > (int64_t)INT32_MAX) raise(GX_ELENGTH, "derivative batch size overflow");
         check_field(B, O);
-        const uint32_t ns = (uint32_t)b->ns;
-        int64_t off = 0;
-        for (int64_t i = 0; i < nq; ++i) {
-            const uint32_t* x = quartets + 4 * i;
-            int L = 0;
-            int64_t size = 1;
-            for (int k = 0; k < 4; ++k) {
-                if (x[k] >= ns) raise(GX_ERANGE, "derivative shell quartet index is out of range");
-                if (b->l[x[k]] > 15) raise(GX_EINVAL, "ERI centre derivatives support shells through l = 15");
-                L += b->l[x[k]];
-                size *= b->nao_of(x[k]);
-            }
-            if (L + 1 > 32) raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
-            offsets[i] = off;
-            off += (mode == 0 ? 12 : 3) * size;
-        }
-        offsets[nq] = off;
+        const int64_t off = derivative_offsets(b, mode, quartets, nq, offsets);
         if (off > capacity) raise(GX_ELENGTH, "derivative output buffer is too small");
         std::lock_guard<std::mutex> lock(ctx->mu);
         GX_CUDA(cudaSetDevice(ctx->device));
-        float ms = 0.f;
-        if (nq == 0) {
-            if (kernel_ms) *kernel_ms = 0.f;
-            return;
-        }
-        std::vector<int> dix;
-        gx_basis* db = derivative_basis(ctx, b, dix);
-        const bool field = B[0] != 0.0 || B[1] != 0.0 || B[2] != 0.0;
-        const bool has_u = mode == 1 || field;
-        // derived blocks per quartet: for each slot [Z, D if l > 0] (centre
-        // mode), [U]; then [plain]
-        std::vector<uint32_t> dq;
-        dq.reserve((size_t)nq * 4 * (mode == 1 ? 5 : (field ? 13 : 8)));
-        std::vector<long long> doff((size_t)nq);
-        int64_t dtotal = 0;
-        for (int64_t i = 0; i < nq; ++i) {
-            const uint32_t* x = quartets + 4 * i;
-            doff[i] = dtotal;
-            auto add = [&](int k, int g) {
-                uint32_t y[4] = {x[0], x[1], x[2], x[3]};
-                int64_t size = 1;
-                if (g >= 0) y[k] = (uint32_t)dix[(size_t)g * ns + x[k]];
-                for (int j = 0; j < 4; ++j) size *= db->nao_of(y[j]);
-                dq.insert(dq.end(), y, y + 4);
-                dtotal += size;
-            };
-            for (int k = 0; k < 4; ++k) {
-                if (mode == 0) {
-                    add(k, kDerivZ);
-                    if (b->l[x[k]] > 0) add(k, kDerivD);
-                }
-                if (has_u) add(k, kDerivU);
-            }
-            if (has_u) add(0, -1);
-        }
-        const int64_t dcount = (int64_t)dq.size() / 4;
-        uint64_t h1 = 0x452821E638D01377ull ^ (uint64_t)dcount, h2 = 0xBE5466CF34E90C6Cull;
-        for (int64_t i = 0; i < dcount; ++i) {
-            uint64_t v0, v1;
-            std::memcpy(&v0, &dq[4 * i], 8);
-            std::memcpy(&v1, &dq[4 * i + 2], 8);
-            h1 = (((h1 ^ v0) * 0x9E3779B97F4A7C15ull) ^ v1) * 0xBF58476D1CE4E5B9ull;
-            h1 ^= h1 >> 31;
-            h2 = (h2 + v0 * 0xC2B2AE3D27D4EB4Full + (v1 ^ (uint64_t)i)) * 0x94D049BB133111EBull;
-            h2 ^= h2 >> 29;
-        }
-        PlanData& plan = lookup_plan(ctx, db, h1, h2, dcount, dtotal, [&] {
-            std::vector<QuartetRequest> req;
-            req.reserve((size_t)dcount);
-            int64_t o = 0;
-            for (int64_t i = 0; i < dcount; ++i) {
-                const uint32_t* y = &dq[4 * i];
-                req.push_back({y[0], y[1], y[2], y[3], o});
-                o += db->nao_of(y[0]) * db->nao_of(y[1]) * db->nao_of(y[2]) * db->nao_of(y[3]);
-            }
-            return req;
-        });
-        apply_recorded_tuning(ctx, db, GX_PRECISION_FP64, plan);
-        ctx->deriv_vals.reserve(std::max<int64_t>(dtotal, 1) * sizeof(double2));
-        run_plan(ctx, db, B, O, plan, ctx->deriv_vals.as<double2>(), kernel_ms ? &ms : nullptr, nullptr,
-                 GX_PRECISION_FP64, 0.0, nullptr);
-        // metadata: quartets | offsets | derived offsets
-        const size_t qbytes = ((size_t)nq * 16 + 15) / 16 * 16;
-        const size_t obytes = (size_t)(nq + 1) * 8;
-        ctx->deriv_meta.reserve(qbytes + obytes + (size_t)nq * 8);
-        char* meta = ctx->deriv_meta.as<char>();
-        GX_CUDA(cudaMemcpyAsync(meta, quartets, (size_t)nq * 16, cudaMemcpyHostToDevice, ctx->stream));
-        GX_CUDA(cudaMemcpyAsync(meta + qbytes, offsets, obytes, cudaMemcpyHostToDevice, ctx->stream));
-        GX_CUDA(cudaMemcpyAsync(meta + qbytes + obytes, doff.data(), (size_t)nq * 8, cudaMemcpyHostToDevice,
-                                ctx->stream));
+        if (kernel_ms) *kernel_ms = 0.f;
+        if (nq == 0) return;
         double2* dout;
         if (out_is_device) {
             dout = static_cast<double2*>(out);
@@ -1501,33 +1619,13 @@ int eri_derivative_impl(gx_context* ctx, gx_basis* b, int mode, const double* B,
             ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
             dout = ctx->out.as<double2>();
         }
-        gx::DerivCombineArgs a{};
-        a.nq = (int)nq;
-        a.mode = mode;
-        a.field = field ? 1 : 0;
-        a.quartets = reinterpret_cast<const uint32_t*>(meta);
-        a.offsets = reinterpret_cast<const long long*>(meta + qbytes);
-        a.derived_offsets = reinterpret_cast<const long long*>(meta + qbytes + obytes);
-        a.shell_l = b->d_shell_l.as<int>();
-        a.shell_ncontr = b->d_shell_ncontr.as<int>();
-        a.shell_raw = b->d_shell_raw.as<int>();
-        a.shell_center = b->d_shell_center.as<double>();
-        a.derived = ctx->deriv_vals.as<double2>();
-        a.out = dout;
-        for (int k = 0; k < 3; ++k) {
-            a.B[k] = B[k];
-            a.O[k] = O[k];
-        }
-        double df = 1.0;  // (2n - 1)!!
-        for (int n = 0; n < 18; ++n) {
-            if (n > 0) df *= 2.0 * n - 1.0;
-            a.inv_sqrt_df[n] = 1.0 / std::sqrt(df);
-        }
-        GX_CUDA(gx::launch_deriv_combine(a, off, ctx->sm_count, ctx->stream));
+        if (mode == 2)
+            mixed_core(ctx, b, B, O, quartets, nq, offsets, dout);
+        else
+            derivative_core(ctx, b, mode, B, O, quartets, nq, offsets, dout, kernel_ms);
         if (!out_is_device)
             GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (kernel_ms) *kernel_ms = ms;
     });
 }
 
@@ -1677,9 +1775,14 @@ void gx_basis_destroy(gx_basis* b) {
     std::lock_guard<std::mutex> lock(b->ctx->mu);
     cudaSetDevice(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
-    drop_cached_plans(b->ctx, b);
-    if (b->deriv) drop_cached_plans(b->ctx, b->deriv.get());
-    if (b->bound) drop_cached_plans(b->ctx, b->bound.get());
+    // plans and tunings of the basis and of the derived bases it owns
+    // (derivative bases nest: the mixed derivatives use two levels)
+    std::vector<const gx_basis*> owned{b};
+    for (size_t i = 0; i < owned.size(); ++i) {
+        if (owned[i]->deriv) owned.push_back(owned[i]->deriv.get());
+        if (owned[i]->bound) owned.push_back(owned[i]->bound.get());
+    }
+    for (const gx_basis* o : owned) drop_cached_plans(b->ctx, o);
     delete b;
 }
 
@@ -1740,6 +1843,11 @@ int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* 
                                 const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                                 int64_t out_capacity, float* kernel_ms) {
     return eri_derivative_impl(ctx, basis, 1, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
+}
+
+int gx_eri_mixed_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                             const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out, int64_t out_capacity) {
+    return eri_derivative_impl(ctx, basis, 2, B, O, quartets, nq, offsets, out, false, out_capacity, nullptr);
 }
 
 int gx_eri_derivative_schwarz(gx_context* ctx, gx_basis* basis, const double* B, const double* O, double* values,

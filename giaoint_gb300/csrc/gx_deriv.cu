@@ -165,6 +165,129 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
     }
 }
 
+// d2/dR_{k,r} dB_b (ab|cd) at fixed gauge origin, index (k 3 + r) 3 + b:
+//   M0 D0[k,r] + sum_j sum_c i phi_j (e_b x (R_j - O))_c
+//                  [h_j Dj[k,r](l_j + 1_c) + delta_jk delta_rc E0]
+//   + sum_c i phi_k (e_b x e_r)_c [h_k Ek(l_k + 1_c) + R_{k,c} E0],
+// M0 = sum_j sum_c i phi_j (e_b x (R_j - O))_c R_{j,c}; Dj / Ej are the
+// centre derivatives / plain blocks of the quartet with slot j replaced by its
+// U shell (raw primitives, coefficients w g(alpha, l)), D0 / E0 those of the
+// quartet itself.  This is the reference's centre response applied to the
+// field response plus the cross term (src/derivatives.cpp:160-181, 232-245),
+// regrouped by linearity.
+__global__ void __launch_bounds__(256) deriv_mixed_kernel(DerivMixedArgs a) {
+    const long long total = a.offsets[a.nq];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = a.nq - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&a.offsets[mid]) <= e) lo = mid;
+            else hi = mid - 1;
+        }
+        const int qi = lo;
+        int sh[4], l[4], nc[4], dim[4];
+        long long size = 1;
+        for (int k = 0; k < 4; ++k) {
+            sh[k] = (int)__ldg(&a.quartets[4 * qi + k]);
+            l[k] = __ldg(&a.shell_l[sh[k]]);
+            nc[k] = __ldg(&a.shell_ncontr[sh[k]]);
+            dim[k] = nc[k] * ncart(l[k]);
+            size *= dim[k];
+        }
+        const long long rel = e - __ldg(&a.offsets[qi]);
+        const int d = (int)(rel / size);
+        const long long r0 = rel - (long long)d * size;
+        const int k = d / 9, r = (d / 3) % 3, b = d % 3;
+        int idx[4], xs[4], ang[4][3];
+        double h[4];
+        {
+            long long t = r0;
+            for (int j = 3; j >= 0; --j) {
+                idx[j] = (int)(t % dim[j]);
+                t /= dim[j];
+            }
+            for (int j = 0; j < 4; ++j) {
+                const int nck = ncart(l[j]);
+                xs[j] = idx[j] / nck;
+                comp_of(l[j], idx[j] - xs[j] * nck, ang[j][0], ang[j][1], ang[j][2]);
+                h[j] = __ldg(&a.shell_raw[sh[j]])
+                           ? 1.0
+                           : a.inv_sqrt_df[ang[j][0]] * a.inv_sqrt_df[ang[j][1]] * a.inv_sqrt_df[ang[j][2]];
+            }
+        }
+        // linear index of element idx with slot j at component (px, py, pz) of l_j + 1
+        auto up_index = [&](int j, int px, int pz) {
+            long long li = 0;
+            for (int t = 0; t < 4; ++t) {
+                const int dt = t == j ? nc[t] * ncart(l[t] + 1) : dim[t];
+                const int it = t == j ? xs[t] * ncart(l[t] + 1) + comp_index(l[t] + 1, px, pz) : idx[t];
+                li = li * dt + it;
+            }
+            return li;
+        };
+        const double2 e0 = __ldg(&a.E[__ldg(&a.eoff[qi]) + r0]);
+        const double2 d0 = __ldg(&a.D[0][__ldg(&a.doff[qi]) + (long long)(k * 3 + r) * size + r0]);
+        double2 acc = c2(0.0, 0.0);
+        double m0 = 0.0;  // M0 = i m0
+        for (int j = 0; j < 4; ++j) {
+            const double phi = (j % 2 == 0) ? 0.5 : -0.5;
+            double D[3], R[3], w[3];
+            for (int c = 0; c < 3; ++c) {
+                R[c] = __ldg(&a.shell_center[3 * sh[j] + c]);
+                D[c] = R[c] - a.O[c];
+            }
+            w[0] = b == 1 ? D[2] : (b == 2 ? -D[1] : 0.0);
+            w[1] = b == 2 ? D[0] : (b == 0 ? -D[2] : 0.0);
+            w[2] = b == 0 ? D[1] : (b == 1 ? -D[0] : 0.0);
+            const long long sizej = size / dim[j] * (nc[j] * ncart(l[j] + 1));
+            const double2* Dj = a.D[1 + j] + __ldg(&a.doff[(long long)(1 + j) * a.nq + qi]) +
+                                (long long)(k * 3 + r) * sizej;
+            for (int c = 0; c < 3; ++c) {
+                const double coef = phi * w[c];
+                if (coef == 0.0) continue;
+                m0 += coef * R[c];
+                int up[3] = {ang[j][0], ang[j][1], ang[j][2]};
+                ++up[c];
+                const double2 v = __ldg(&Dj[up_index(j, up[0], up[2])]);
+                double tx = h[j] * v.x, ty = h[j] * v.y;
+                if (j == k && r == c) {
+                    tx += e0.x;
+                    ty += e0.y;
+                }
+                // += i coef (tx, ty)
+                acc.x -= coef * ty;
+                acc.y += coef * tx;
+            }
+        }
+        // + i m0 d0
+        acc.x -= m0 * d0.y;
+        acc.y += m0 * d0.x;
+        {
+            // cross term: (e_b x e_r)_c
+            const double phi = (k % 2 == 0) ? 0.5 : -0.5;
+            double cr[3] = {0.0, 0.0, 0.0};
+            if (b != r) {
+                const int c = 3 - b - r;  // the remaining axis; sign of the permutation (b, r, c)
+                cr[c] = ((b + 1) % 3 == r) ? 1.0 : -1.0;
+            }
+            const double2* Ek = a.E + __ldg(&a.eoff[(long long)(1 + k) * a.nq + qi]);
+            for (int c = 0; c < 3; ++c) {
+                const double coef = phi * cr[c];
+                if (coef == 0.0) continue;
+                int up[3] = {ang[k][0], ang[k][1], ang[k][2]};
+                ++up[c];
+                const double2 u = __ldg(&Ek[up_index(k, up[0], up[2])]);
+                const double Rc = __ldg(&a.shell_center[3 * sh[k] + c]);
+                const double tx = h[k] * u.x + Rc * e0.x, ty = h[k] * u.y + Rc * e0.y;
+                acc.x -= coef * ty;
+                acc.y += coef * tx;
+            }
+        }
+        a.out[e] = acc;
+    }
+}
+
 __global__ void __launch_bounds__(256) gather_abs_kernel(const double2* __restrict__ src,
                                                          const long long* __restrict__ idx, double* __restrict__ dst,
                                                          long long n) {
@@ -182,6 +305,14 @@ cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* 
     const long long want = (n + 255) / 256;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, (long long)sms * 8));
     gather_abs_kernel<<<blocks, 256, 0, s>>>(src, idx, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deriv_mixed(const DerivMixedArgs& args, long long total, int sms, cudaStream_t s) {
+    if (total == 0) return cudaSuccess;
+    const long long want = (total + 255) / 256;
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, (long long)sms * 8));
+    deriv_mixed_kernel<<<blocks, 256, 0, s>>>(args);
     return cudaGetLastError();
 }
 

@@ -158,6 +158,26 @@ struct DerivCombineArgs {
     double inv_sqrt_df[18];          // 1 / sqrt((2n - 1)!!)
 };
 cudaError_t launch_deriv_combine(const DerivCombineArgs& args, long long total, int sms, cudaStream_t s);
+// Mixed field/centre derivatives (4, 3, 3, ...) assembled from the centre
+// derivatives (D[0]: the quartets, D[1 + j]: the quartets with slot j
+// replaced by its U shell) and the plain blocks (E at eoff[0 .. 4]).
+struct DerivMixedArgs {
+    int nq;
+    const uint32_t* quartets;        // [4 nq] original shells
+    const long long* offsets;        // [nq + 1] output offsets (36 x block size each)
+    const long long* doff;           // [5 nq] centre-derivative block offsets per list
+    const long long* eoff;           // [5 nq] plain block offsets per list
+    const double2* D[5];
+    const double2* E;
+    const int* shell_l;
+    const int* shell_ncontr;
+    const int* shell_raw;
+    const double* shell_center;
+    double2* out;
+    double O[3];
+    double inv_sqrt_df[18];
+};
+cudaError_t launch_deriv_mixed(const DerivMixedArgs& args, long long total, int sms, cudaStream_t s);
 // dst[i] = |src[idx[i]]| (diagonal elements of the derivative-bound blocks)
 cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* dst, long long n, int sms,
                               cudaStream_t s);

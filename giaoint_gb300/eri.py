@@ -477,6 +477,53 @@ def primitive_eri_magnetic_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussia
     return full[:, picks[0], picks[1], picks[2], picks[3]] * scale
 
 
+def _eri_mixed_derivative_blocks(basis: Basis, quartets, *, field: MagneticField | None = None, context=None):
+    """Mixed field/centre derivative blocks (4, 3, 3, na, nb, nc, nd) of
+    ``quartets`` packed in input order (gx_eri_mixed_derivatives): returns
+    (offsets, values).  Meant for small bases (two levels of derived shells)."""
+    ctx = context or nat.default_context()
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+    if len(q) and (q.min() < 0 or q.max() >= len(basis.shells)):
+        raise IndexError("derivative shell quartet index is out of range")
+    q = np.ascontiguousarray(q.astype(np.uint32))
+    sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+    total = int(36 * np.prod(sizes[q.astype(np.int64)], axis=1).sum()) if len(q) else 0
+    values = np.empty(max(total, 1), dtype=np.complex128)
+    offsets = np.zeros(len(q) + 1, dtype=np.int64)
+    if len(q):
+        B, O = field_arrays(field)
+        nat.check(nat.lib().gx_eri_mixed_derivatives(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O),
+                                                     nat.u32ptr(q), len(q), nat.i64ptr(offsets),
+                                                     nat.dptr(values.view(np.float64)), total))
+    return offsets, values[:total]
+
+
+def eri_mixed_derivatives_shell(a: Shell, b: Shell, c: Shell, d: Shell, *, field: MagneticField | None = None,
+                                out=None, context=None) -> npt.NDArray[np.complex128]:
+    """Mixed second derivatives d2/dR dB of one shell quartet at fixed gauge
+    origin, complex (4, 3, 3, na, nb, nc, nd): centre slot, nuclear axis,
+    field axis (compute_eri_mixed_derivatives; src/bindings.cpp:2155-2165)."""
+    for s in (a, b, c, d):
+        if not isinstance(s, Shell):
+            raise TypeError("a, b, c and d must be Shell objects")
+    shape = (4, 3, 3, a.ao_count, b.ao_count, c.ao_count, d.ao_count)
+    result = _validate_out(out, shape)
+    _, values = _eri_mixed_derivative_blocks(Basis([a, b, c, d]), [(0, 1, 2, 3)], field=field, context=context)
+    result[...] = values.reshape(shape)
+    return result
+
+
+def primitive_eri_mixed_derivatives(a: PrimitiveGaussian, b: PrimitiveGaussian, c: PrimitiveGaussian,
+                                    d: PrimitiveGaussian, *, field: MagneticField | None = None,
+                                    context=None) -> npt.NDArray[np.complex128]:
+    """Mixed second derivatives of one primitive quartet, complex (4, 3, 3)
+    (primitive_eri_mixed_derivatives; src/derivatives.cpp:1252-1256,
+    src/bindings.cpp:2139-2145)."""
+    shells, picks, scale = _primitive_shells((a, b, c, d))
+    full = eri_mixed_derivatives_shell(*shells, field=field, context=context)
+    return full[:, :, :, picks[0], picks[1], picks[2], picks[3]] * scale
+
+
 def _primitive_shells(prims):
     """Unit-coefficient one-primitive shells whose components carry
     N(alpha, component), the component index of each primitive, and the

@@ -164,6 +164,17 @@ int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* 
                                 const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out,
                                 int64_t out_capacity, float* kernel_ms);
 
+/* Mixed field/centre second derivatives d2/dR_{slot,r} dB_b (ab|cd) of nq
+ * shell quartets at fixed gauge origin, replacing
+ * compute_eri_mixed_derivatives (src/derivatives.cpp:160-181, 232-259,
+ * 968-973; eri_mixed_derivatives_shell, src/bindings.cpp:2155-2165): block i
+ * at offsets[i] is the C-order complex (4, 3, 3, na, nb, nc, nd) array, index
+ * (slot 3 + r) 3 + b.  Shells through l = 14, combined order + 2 through 32.
+ * Builds derived bases of two levels (16 shells per shell of the basis):
+ * meant for small bases such as the four shells of one quartet. */
+int gx_eri_mixed_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                             const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out, int64_t out_capacity);
+
 /* Derivative-density Schwarz factors, replacing EriDerivativeSchwarzBounds
  * (src/derivatives.cpp:1307-1372, bindings.cpp:2242-2253): values[ns*ns]
  * receives the factor of every ordered shell pair (a, b) at a*ns + b, and

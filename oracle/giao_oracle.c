@@ -1308,13 +1308,108 @@ static int primitive_magnetic_derivatives(const prim_t* pr, const pair_t* ab, co
     return 0;
 }
 
+/* ERI of quartet q with slot j shifted by +1_c (j < 0: none). */
+static int eval_shift(const prim_t* q, int j, int c, const pair_t* ab, const pair_t* cd, int real_zero, ws_t* w,
+                      cplx* v) {
+    prim_t t[4];
+    memcpy(t, q, sizeof t);
+    if (j >= 0) ++t[j].ang[c];
+    return eri_kernel(t, ab, cd, real_zero, w, v);
+}
+
+/* d/dB_b of quartet q (all four slots' London response, src/derivatives.cpp:88-106, 268-280). */
+static int magnetic_of(const prim_t* q, int b, const pair_t* ab, const pair_t* cd, const field_t* f, int real_zero,
+                       ws_t* w, cplx* out) {
+    cplx base;
+    int rc = eval_shift(q, -1, 0, ab, cd, real_zero, w, &base);
+    if (rc) return rc;
+    cplx r = 0.0;
+    for (int j = 0; j < 4; ++j) {
+        const double phi = (j % 2 == 0) ? 0.5 : -0.5;
+        double d[3], e[3] = {0.0, 0.0, 0.0};
+        for (int x = 0; x < 3; ++x) d[x] = q[j].center[x] - f->O[x];
+        e[b] = 1.0;
+        const double ph[3] = {e[1] * d[2] - e[2] * d[1], e[2] * d[0] - e[0] * d[2], e[0] * d[1] - e[1] * d[0]};
+        for (int c = 0; c < 3; ++c) {
+            const double coef = phi * ph[c];
+            if (coef == 0.0) continue;
+            cplx up;
+            if ((rc = eval_shift(q, j, c, ab, cd, real_zero, w, &up))) return rc;
+            r += CMPLX(0.0, coef) * (up + q[j].center[c] * base);
+        }
+    }
+    *out = r;
+    return 0;
+}
+
+/* d2/dR_{k,r} dB_b of one primitive quartet, index (k*3 + r)*3 + b: the centre
+ * response of slot k applied to the field derivative, plus the cross term
+ * i phi_k sum_c (e_b x e_r)_c [e(l_k + 1_c) + R_{k,c} e]
+ * (src/derivatives.cpp:160-181, 232-245). */
+static int primitive_mixed_derivatives(const prim_t* pr, const pair_t* ab, const pair_t* cd, const field_t* f,
+                                       int real_zero, ws_t* w, cplx* out36) {
+    int rc;
+    cplx base;
+    if ((rc = eval_shift(pr, -1, 0, ab, cd, real_zero, w, &base))) return rc;
+    for (int k = 0; k < 4; ++k) {
+        const double phi = (k % 2 == 0) ? 0.5 : -0.5;
+        cplx up[3];
+        for (int c = 0; c < 3; ++c)
+            if ((rc = eval_shift(pr, k, c, ab, cd, real_zero, w, &up[c]))) return rc;
+        for (int b = 0; b < 3; ++b) {
+            /* field derivative of the quartet with slot k shifted: +1_c (c = 0..2), -1_r, raw */
+            cplx mup[3], mraw;
+            for (int c = 0; c < 3; ++c) {
+                prim_t q[4];
+                memcpy(q, pr, sizeof q);
+                ++q[k].ang[c];
+                if ((rc = magnetic_of(q, b, ab, cd, f, real_zero, w, &mup[c]))) return rc;
+            }
+            if ((rc = magnetic_of(pr, b, ab, cd, f, real_zero, w, &mraw))) return rc;
+            for (int r = 0; r < 3; ++r) {
+                cplx v = 2.0 * pr[k].alpha * mup[r];
+                if (pr[k].ang[r] > 0) {
+                    prim_t q[4];
+                    memcpy(q, pr, sizeof q);
+                    --q[k].ang[r];
+                    cplx mdn;
+                    if ((rc = magnetic_of(q, b, ab, cd, f, real_zero, w, &mdn))) return rc;
+                    v -= (double)pr[k].ang[r] * mdn;
+                }
+                double e[3] = {0.0, 0.0, 0.0};
+                e[r] = 1.0;
+                const double bx[3] = {f->B[1] * e[2] - f->B[2] * e[1], f->B[2] * e[0] - f->B[0] * e[2],
+                                      f->B[0] * e[1] - f->B[1] * e[0]};
+                for (int c = 0; c < 3; ++c) {
+                    const double coef = phi * bx[c];
+                    if (coef == 0.0) continue;
+                    v += CMPLX(0.0, coef) * (mup[c] + pr[k].center[c] * mraw);
+                }
+                /* (e_b x e_r) */
+                double eb[3] = {0.0, 0.0, 0.0};
+                eb[b] = 1.0;
+                const double cr[3] = {eb[1] * e[2] - eb[2] * e[1], eb[2] * e[0] - eb[0] * e[2],
+                                      eb[0] * e[1] - eb[1] * e[0]};
+                for (int c = 0; c < 3; ++c) {
+                    const double coef = phi * cr[c];
+                    if (coef == 0.0) continue;
+                    v += CMPLX(0.0, coef) * (up[c] + pr[k].center[c] * base);
+                }
+                out36[(k * 3 + r) * 3 + b] = v;
+            }
+        }
+    }
+    return 0;
+}
+
 /* Blocks (ncomp, na, nb, nc, nd) of nq shell quartets packed in input order,
  * primitive and component loops of compute_quartet_block
  * (src/derivatives.cpp:556-640): ncomp = 12 centre derivatives (slot-major)
  * or 3 magnetic derivatives. */
 static int derivative_blocks(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
-                             double* out_, int magnetic) {
-    const int ncomp = magnetic ? 3 : 12;
+                             double* out_, int mode) {
+    const int magnetic = mode == 1;
+    const int ncomp = mode == 2 ? 36 : (magnetic ? 3 : 12);
     basis_t bs;
     int rc = basis_init(&bs, ns, centers, ls, nprims, ncontrs, exps, coefs);
     cplx* out = (cplx*)out_;
@@ -1370,8 +1465,9 @@ static int derivative_blocks(BASIS_ARGS, const uint32_t* quartets, long nq, cons
                                             norm *= or_primitive_normalization(pr[k].alpha, pr[k].ang[0],
                                                                                pr[k].ang[1], pr[k].ang[2]);
                                         }
-                                        cplx d12[12];
-                                        rc = magnetic
+                                        cplx d12[36];
+                                        rc = mode == 2 ? primitive_mixed_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12)
+                                             : magnetic
                                                  ? primitive_magnetic_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12)
                                                  : primitive_center_derivatives(pr, &ab, &cd, &f, real_zero, &w, d12);
                                         if (rc) break;
@@ -1411,6 +1507,11 @@ int or_eri_center_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, con
 int or_eri_magnetic_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
                                 double* out) {
     return derivative_blocks(ns, centers, ls, nprims, ncontrs, exps, coefs, quartets, nq, B, O, out, 1);
+}
+
+int or_eri_mixed_derivatives(BASIS_ARGS, const uint32_t* quartets, long nq, const double* B, const double* O,
+                             double* out) {
+    return derivative_blocks(ns, centers, ls, nprims, ncontrs, exps, coefs, quartets, nq, B, O, out, 2);
 }
 
 /* Derivative-density Schwarz factors of every ordered shell pair

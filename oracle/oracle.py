@@ -309,6 +309,17 @@ class Oracle(_Backend):
                                                          out.ctypes.data_as(_d)))
         return out[:total], offsets
 
+    def eri_mixed_derivatives(self, shells, quartets, B=None, O=None):
+        """Mixed field/centre derivative blocks (4, 3, 3, na, nb, nc, nd) of
+        each quartet, packed in input order; returns (values, offsets)."""
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets, 36)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.or_eri_mixed_derivatives(*a.args(), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
+                                                      _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
+                                                      out.ctypes.data_as(_d)))
+        return out[:total], offsets
+
     def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:
         """Derivative Schwarz factors of every ordered shell pair, [ns, ns]."""
         a = self._basis(shells)
@@ -426,6 +437,17 @@ class Reference(_Backend):
         self._check(self.lib.ref_eri_magnetic_derivatives(*self._bargs(a), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
                                                          _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
                                                          out.ctypes.data_as(_d)))
+        return out[:total], offsets
+
+    def eri_mixed_derivatives(self, shells, quartets, B=None, O=None):
+        """Mixed field/centre derivative blocks (4, 3, 3, na, nb, nc, nd) of
+        each quartet, packed in input order; returns (values, offsets)."""
+        a = self._basis(shells)
+        q, offsets, total = _derivative_layout(shells, quartets, 36)
+        out = np.zeros(max(total, 1), dtype=np.complex128)
+        self._check(self.lib.ref_eri_mixed_derivatives(*self._bargs(a), q.ctypes.data_as(_u32), ctypes.c_long(len(q)),
+                                                      _vec3(B).ctypes.data_as(_d), _vec3(O).ctypes.data_as(_d),
+                                                      out.ctypes.data_as(_d)))
         return out[:total], offsets
 
     def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:

@@ -13,6 +13,7 @@
 //   ref_schwarz            <- src/bindings.cpp:409-425 (EriSchwarzBounds)
 //   ref_eri_center_derivatives <- src/derivatives.cpp:954-959
 //   ref_eri_magnetic_derivatives <- src/derivatives.cpp:961-966
+//   ref_eri_mixed_derivatives  <- src/derivatives.cpp:968-973
 //   ref_eri_derivative_bounds  <- src/derivatives.cpp:1307-1372
 //   ref_cholesky_diagonal  <- src/bindings.cpp:2306-2314
 //   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
@@ -236,6 +237,31 @@ int ref_eri_magnetic_derivatives(int ns, const double* centers, const int* ls, c
             const auto& d = sh[quartets[4 * i + 3]];
             const std::size_t size = 3 * giao::shell_quartet_size(a, b, c, d);
             giao::compute_eri_magnetic_derivatives(
+                a, b, c, d, field, std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out) + off, size));
+            off += size;
+        }
+    });
+}
+
+// Mixed field/centre derivative blocks (4, 3, 3, na, nb, nc, nd) of nq
+// quartets, packed in input order (compute_eri_mixed_derivatives,
+// src/derivatives.cpp:968-973).
+int ref_eri_mixed_derivatives(int ns, const double* centers, const int* ls, const int* nprims,
+                              const int* ncontrs, const double* exps, const double* coefs,
+                              const int* normalize, const uint32_t* quartets, long nq, const double* B,
+                              const double* O, double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        const auto field = make_field(B, O);
+        std::size_t off = 0;
+        for (long i = 0; i < nq; ++i) {
+            const auto& sh = basis.shells();
+            const auto& a = sh[quartets[4 * i]];
+            const auto& b = sh[quartets[4 * i + 1]];
+            const auto& c = sh[quartets[4 * i + 2]];
+            const auto& d = sh[quartets[4 * i + 3]];
+            const std::size_t size = 36 * giao::shell_quartet_size(a, b, c, d);
+            giao::compute_eri_mixed_derivatives(
                 a, b, c, d, field, std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out) + off, size));
             off += size;
         }

@@ -28,7 +28,8 @@ Inputs and outputs:
   canonical and arbitrary quartets, repeated shells) and a hand-made f/g
   system with a two-contraction p shell, at a finite field with a shifted
   gauge origin and at zero field, with the magnetic-derivative blocks
-  (3, na, nb, nc, nd) of the same quartets and the reference's derivative
+  (3, na, nb, nc, nd) of the same quartets, the mixed field/centre blocks
+  (4, 3, 3, na, nb, nc, nd) of a subset, and the reference's derivative
   and ordinary Schwarz factors of every ordered shell pair;
 * ``cholesky.json`` -- the reference's own NumPy Cholesky driver
   (python/giao_integrals/cholesky.py, executed unmodified over the reference
@@ -279,6 +280,11 @@ def derivative_cases():
     return {"molecule3": (mol, quartets), "hand": (hand, hq)}
 
 
+# quartets (indices into each system's list) of the mixed field/centre
+# derivative fixture: (4, 3, 3, ...) blocks are 36 components per element
+MIXED_SUBSET = {"molecule3": [0, 1, 2, 3, 30], "hand": [0, 3, 4]}
+
+
 def derivative_fixture(ref):
     out = {}
     for name, (specs, quartets) in derivative_cases().items():
@@ -289,6 +295,9 @@ def derivative_fixture(ref):
             vals, offsets = ref.eri_center_derivatives(specs, q, B, origin)
             out[f"{name}_{label}"] = vals
             out[f"{name}_magnetic_{label}"] = ref.eri_magnetic_derivatives(specs, q, B, origin)[0]
+            mq = q[MIXED_SUBSET[name]]
+            out[f"{name}_mixed_quartets"] = mq
+            out[f"{name}_mixed_{label}"] = ref.eri_mixed_derivatives(specs, mq, B, origin)[0]
             out[f"{name}_bounds_{label}"] = ref.eri_derivative_bounds(specs, B, origin)
             out[f"{name}_schwarz_{label}"] = ref.schwarz(specs, B, origin)
             out[f"{name}_offsets"] = offsets

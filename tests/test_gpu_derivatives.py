@@ -329,3 +329,67 @@ def test_magnetic_derivatives_match_field_differences():
             got = np.concatenate([values[offsets[i] + b * sizes[i]:offsets[i] + (b + 1) * sizes[i]]
                                   for i in range(len(q))])
             assert np.abs(got - fd).max() <= 1e-9 * max(1.0, np.abs(fd).max())
+
+
+def test_mixed_derivatives_match_reference(golden, oracle):
+    """d2/dR dB blocks (4, 3, 3, na, nb, nc, nd) against the reference
+    library's (golden) through the quartet entry and the shell API, and the
+    primitive API against the oracle's one-primitive shells."""
+    from giaoint_gb300.eri import _eri_mixed_derivative_blocks
+
+    g = golden.derivatives
+    for name, specs, _q in derivative_systems(g):
+        basis = _basis(specs)
+        q = g[f"{name}_mixed_quartets"]
+        for label, field in (("field", _field(g["field"], g["origin"])), ("zero", None)):
+            offsets, values = _eri_mixed_derivative_blocks(basis, q, field=field)
+            ref = g[f"{name}_mixed_{label}"]
+            assert _close(values, ref), (name, label)
+            x = q[0]
+            blk = gi.eri_mixed_derivatives_shell(*(basis.shells[k] for k in x), field=field)
+            assert blk.shape[:3] == (4, 3, 3)
+            assert _close(blk.ravel(), ref[offsets[0]:offsets[1]])
+    field = _field(g["field"], g["origin"])
+    prims = [gi.PrimitiveGaussian(0.9, (0.2, -0.1, 0.0), (0, 1, 0), coefficient=1.2),
+             gi.PrimitiveGaussian(0.5, (-0.4, 0.3, 0.2), (1, 0, 0), normalized=False),
+             gi.PrimitiveGaussian(1.7, (0.1, 0.6, -0.3), (0, 0, 1), coefficient=0.7),
+             gi.PrimitiveGaussian(0.3, (0.0, -0.5, 0.4), (0, 0, 0))]
+    v = gi.primitive_eri_mixed_derivatives(*prims, field=field)
+    recs = [syn.ShellRecord(p.center, sum(p.angular), (p.exponent,), ((1.0,),), False) for p in prims]
+    blk, _ = oracle.eri_mixed_derivatives(recs, [(0, 1, 2, 3)], tuple(g["field"]), tuple(g["origin"]))
+    dims = [len(gi.cartesian_components(sum(p.angular))) for p in prims]
+    picks = [gi.cartesian_components(sum(p.angular)).index(tuple(p.angular)) for p in prims]
+    expect = blk.reshape([4, 3, 3] + dims)[:, :, :, picks[0], picks[1], picks[2], picks[3]] * (1.2 * 0.7)
+    expect = expect / gi.primitive_normalization(0.5, (1, 0, 0))
+    assert v.shape == (4, 3, 3)
+    assert np.abs(v - expect).max() <= TOL * max(1.0, np.abs(expect).max())
+
+
+def test_mixed_derivatives_match_field_differences_of_centre_derivatives():
+    """d2/dR dB against a Richardson central difference in B of the GPU's
+    own centre derivatives (fixed gauge origin), on 40 quartets of a
+    three-atom molecule."""
+    from giaoint_gb300.eri import _eri_mixed_derivative_blocks
+
+    recs = syn.random_molecule(5, natoms=3, box=4.0)
+    basis = basis_from_records(recs)
+    q = gi.canonical_quartets(len(recs))
+    q = q[np.random.default_rng(17).choice(len(q), 40, replace=False)]
+    B0, O = np.array([0.04, -0.06, 0.09]), (0.3, -0.2, 0.1)
+    offsets, mixed = _eri_mixed_derivative_blocks(basis, q, field=gi.MagneticField(tuple(B0), gauge_origin=O))
+
+    def centre(Bv):
+        return _eri_derivative_batch(basis, q, field=gi.MagneticField(tuple(Bv), gauge_origin=O))
+
+    _, _, coff, _, _, _ = centre(B0)
+    sizes = np.diff(coff) // 12
+    for b in range(3):
+        h = 1e-3
+        e = np.eye(3)[b]
+        d1 = (centre(B0 + h * e)[3] - centre(B0 - h * e)[3]) / (2 * h)
+        d2 = (centre(B0 + h / 2 * e)[3] - centre(B0 - h / 2 * e)[3]) / h
+        fd = (4 * d2 - d1) / 3
+        for i in range(len(q)):
+            m = mixed[offsets[i]:offsets[i + 1]].reshape(4, 3, 3, -1)[:, :, b, :]
+            f = fd[coff[i]:coff[i + 1]].reshape(4, 3, -1)
+            assert np.abs(m - f).max() <= 1e-8 * max(1.0, np.abs(f).max())

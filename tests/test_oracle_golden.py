@@ -182,3 +182,19 @@ def test_eri_magnetic_derivatives_oracle_matches_reference(golden, oracle):
             vals, _ = oracle.eri_magnetic_derivatives(specs, q, field, o)
             ref = g[f"{name}_magnetic_{label}"]
             assert np.abs(vals - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (name, label)
+
+
+def test_eri_mixed_derivatives_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of compute_eri_mixed_derivatives
+    (src/derivatives.cpp:160-181, 232-259, 968-973) against the reference
+    library's (4, 3, 3, na, nb, nc, nd) blocks, zero and finite field."""
+    from conftest import derivative_systems
+
+    g = golden.derivatives
+    B, origin = tuple(g["field"]), tuple(g["origin"])
+    for name, specs, _q in derivative_systems(g):
+        q = g[f"{name}_mixed_quartets"]
+        for label, field, o in (("field", B, origin), ("zero", None, None)):
+            vals, _ = oracle.eri_mixed_derivatives(specs, q, field, o)
+            ref = g[f"{name}_mixed_{label}"]
+            assert np.abs(vals - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (name, label)
