@@ -21,6 +21,7 @@ from ._types import (
 )
 from .boys import BoysRegion, boys, boys_with_diagnostics
 from .cholesky import CholeskyERI, cholesky_eri
+from .derivative_assembly import eri_derivative_contraction
 from .eri import (
     EriBatch,
     EriDerivativeBatch,
@@ -65,6 +66,7 @@ __all__ = [
     "eri",
     "eri_batches",
     "eri_center_derivatives_shell",
+    "eri_derivative_contraction",
     "eri_derivative_batches",
     "eri_magnetic_derivatives_shell",
     "eri_mixed_derivatives_shell",

@@ -97,6 +97,9 @@ SIGNATURES = {
     "gx_eri_magnetic_derivatives": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _d,
                                                    ctypes.c_int64, ctypes.POINTER(ctypes.c_float)]),
     "gx_eri_mixed_derivatives": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _d, ctypes.c_int64]),
+    "gx_eri_derivative_contraction": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, ctypes.c_int,
+                                                     ctypes.c_int, _d, ctypes.c_int, _d, _d, ctypes.c_int,
+                                                     ctypes.c_int64, _d]),
     "gx_eri_derivative_schwarz": (ctypes.c_int, [_vp, _vp, _d, _d, _d, _d]),
     "gx_eri_plan_get_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(GxClassConfig)]),
     "gx_eri_plan_set_config": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(GxClassConfig)]),

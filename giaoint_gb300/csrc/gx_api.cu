@@ -1845,6 +1845,103 @@ int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* 
     return eri_derivative_impl(ctx, basis, 1, B, O, quartets, nq, offsets, out, false, out_capacity, kernel_ms);
 }
 
+int gx_eri_derivative_contraction(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                  const uint32_t* quartets, int64_t nq, const int64_t* shell_atoms, int natom,
+                                  int npc, const double* coulomb, int npx, const double* exchange,
+                                  const double* gamma, int gamma_complex, int64_t batch_elements, double* out) {
+    return guarded([&] {
+        if (!ctx || !basis || !out) raise(GX_EINVAL, "null context, basis or output");
+        check_field(B, O);
+        gx_basis* b = basis;
+        const int ns = b->ns;
+        if (natom < 0) raise(GX_EINVAL, "natom must be non-negative");
+        for (int s2 = 0; s2 < ns; ++s2)
+            if (shell_atoms[s2] < 0 || shell_atoms[s2] >= natom) raise(GX_ERANGE, "shell atom index is out of range");
+        if (npc < 0 || npx < 0) raise(GX_EINVAL, "negative density pair count");
+        if (npc == 0 && npx == 0 && !gamma) raise(GX_EINVAL, "at least one density pair or gamma is required");
+        if (batch_elements <= 0) raise(GX_EINVAL, "batch size must be positive");
+        // canonical quartets only (src/assembly.cpp:112-114)
+        for (int64_t i = 0; i < nq; ++i) {
+            const uint32_t* x = quartets + 4 * i;
+            for (int k = 0; k < 4; ++k)
+                if (x[k] >= (uint32_t)ns) raise(GX_ERANGE, "quartet index out of range");
+            const std::array<uint32_t, 4> img[4] = {{x[0], x[1], x[2], x[3]}, {x[2], x[3], x[0], x[1]},
+                                                    {x[1], x[0], x[3], x[2]}, {x[3], x[2], x[1], x[0]}};
+            if (*std::min_element(img, img + 4) != img[0])
+                raise(GX_EINVAL, "contraction requires canonical quartets");
+        }
+        std::vector<int64_t> all(nq + 1);
+        derivative_offsets(b, 0, quartets, nq, all.data());
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        if (nq == 0) return;
+        const int64_t n = b->nao;
+        DeviceBuffer dj, dk, dg, dstart, dbuf, meta, dpart;
+        auto up = [&](DeviceBuffer& d, const void* src, size_t bytes) {
+            d.reserve(std::max<size_t>(bytes, 16));
+            if (bytes) GX_CUDA(cudaMemcpyAsync(d.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        };
+        up(dj, coulomb, (size_t)2 * npc * n * n * sizeof(double2));
+        up(dk, exchange, (size_t)2 * npx * n * n * sizeof(double2));
+        if (gamma) up(dg, gamma, (size_t)n * n * n * n * (gamma_complex ? sizeof(double2) : sizeof(double)));
+        up(dstart, b->ao_off.data(), (size_t)ns * sizeof(int64_t));
+        std::vector<int64_t> loff;
+        std::vector<double2> part;
+        std::vector<std::complex<double>> acc((size_t)natom * 3, 0.0);
+        for (int64_t i0 = 0; i0 < nq;) {
+            int64_t i1 = i0 + 1;
+            while (i1 < nq && all[i1 + 1] - all[i0] <= batch_elements) ++i1;
+            const int64_t cnt = i1 - i0;
+            loff.assign(cnt + 1, 0);
+            const int64_t tot = derivative_offsets(b, 0, quartets + 4 * i0, cnt, loff.data());
+            dbuf.reserve(std::max<int64_t>(tot, 1) * sizeof(double2));
+            derivative_core(ctx, b, 0, B, O, quartets + 4 * i0, cnt, loff.data(), dbuf.as<double2>(), nullptr);
+            const size_t qbytes = ((size_t)cnt * 16 + 15) / 16 * 16;
+            meta.reserve(qbytes + (size_t)cnt * 8);
+            GX_CUDA(cudaMemcpyAsync(meta.ptr, quartets + 4 * i0, (size_t)cnt * 16, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+            GX_CUDA(cudaMemcpyAsync(meta.as<char>() + qbytes, loff.data(), (size_t)cnt * 8, cudaMemcpyHostToDevice,
+                                    ctx->stream));
+            dpart.reserve((size_t)cnt * 12 * sizeof(double2));
+            gx::DerivContractArgs a{};
+            a.nq = (int)cnt;
+            a.quartets = meta.as<uint32_t>();
+            a.offsets = reinterpret_cast<const long long*>(meta.as<char>() + qbytes);
+            a.D = dbuf.as<double2>();
+            a.shell_l = b->d_shell_l.as<int>();
+            a.shell_ncontr = b->d_shell_ncontr.as<int>();
+            a.ao_start = dstart.as<long long>();
+            a.n = n;
+            a.npc = npc;
+            a.npx = npx;
+            a.coulomb = dj.as<double2>();
+            a.exchange = dk.as<double2>();
+            a.gamma = gamma && gamma_complex ? dg.as<double2>() : nullptr;
+            a.gamma_real = gamma && !gamma_complex ? dg.as<double>() : nullptr;
+            a.partials = dpart.as<double2>();
+            GX_CUDA(gx::launch_deriv_contract(a, ctx->sm_count, ctx->stream));
+            part.resize((size_t)cnt * 12);
+            GX_CUDA(cudaMemcpyAsync(part.data(), dpart.ptr, part.size() * sizeof(double2), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            GX_CUDA(cudaStreamSynchronize(ctx->stream));
+            // fixed canonical-quartet and slot order (src/assembly.cpp:151-157)
+            for (int64_t r = 0; r < cnt; ++r)
+                for (int slot = 0; slot < 4; ++slot) {
+                    const int64_t atom = shell_atoms[quartets[4 * (i0 + r) + slot]];
+                    for (int axis = 0; axis < 3; ++axis) {
+                        const double2 v = part[(size_t)r * 12 + slot * 3 + axis];
+                        acc[(size_t)atom * 3 + axis] += std::complex<double>(v.x, v.y);
+                    }
+                }
+            i0 = i1;
+        }
+        for (size_t i = 0; i < acc.size(); ++i) {
+            out[2 * i] += acc[i].real();
+            out[2 * i + 1] += acc[i].imag();
+        }
+    });
+}
+
 int gx_eri_mixed_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
                              const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out, int64_t out_capacity) {
     return eri_derivative_impl(ctx, basis, 2, B, O, quartets, nq, offsets, out, false, out_capacity, nullptr);

@@ -288,6 +288,90 @@ __global__ void __launch_bounds__(256) deriv_mixed_kernel(DerivMixedArgs a) {
     }
 }
 
+// Per-atom contraction of centre derivatives (src/assembly.cpp:87-158), one
+// warp per canonical quartet: for every local element and every distinct
+// orbit image (identity, pair exchange, conjugate reversal, conjugate
+// exchanged reversal) the weight
+//   sum P[nu,mu] Q[sig,lam] (Coulomb) + sum P[nu,lam] Q[sig,mu] (exchange)
+//   + gamma[mu,nu,lam,sig]
+// at the image's AO indices multiplies the derivative (conjugated for the
+// last two images); lanes stride over the elements and a fixed shuffle tree
+// sums the twelve partial sums, so the result does not depend on scheduling.
+__global__ void __launch_bounds__(128) deriv_contract_kernel(DerivContractArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int perm[4][4] = {{0, 1, 2, 3}, {2, 3, 0, 1}, {1, 0, 3, 2}, {3, 2, 1, 0}};
+    const long long n = a.n;
+    for (int qi = warp; qi < a.nq; qi += nwarps) {
+        int sh[4], dim[4];
+        long long st[4], size = 1;
+        for (int k = 0; k < 4; ++k) {
+            sh[k] = (int)__ldg(&a.quartets[4 * qi + k]);
+            dim[k] = __ldg(&a.shell_ncontr[sh[k]]) * ncart(__ldg(&a.shell_l[sh[k]]));
+            st[k] = __ldg(&a.ao_start[sh[k]]);
+            size *= dim[k];
+        }
+        bool active[4] = {true, true, true, true};
+        for (int o = 1; o < 4; ++o)
+            for (int p = 0; p < o && active[o]; ++p) {
+                bool same = true;
+                for (int k = 0; k < 4; ++k) same = same && sh[perm[o][k]] == sh[perm[p][k]];
+                if (same) active[o] = false;
+            }
+        const double2* blk = a.D + __ldg(&a.offsets[qi]);
+        double2 acc[12];
+#pragma unroll
+        for (int t = 0; t < 12; ++t) acc[t] = c2(0.0, 0.0);
+        for (long long loc = lane; loc < size; loc += 32) {
+            long long ao[4];
+            long long rest = loc;
+            for (int k = 3; k >= 0; --k) {
+                ao[k] = st[k] + rest % dim[k];
+                rest /= dim[k];
+            }
+            double2 wd = c2(0.0, 0.0), wc = c2(0.0, 0.0);  // direct / conjugated images
+            for (int o = 0; o < 4; ++o) {
+                if (!active[o]) continue;
+                const long long mu = ao[perm[o][0]], nu = ao[perm[o][1]], la = ao[perm[o][2]], si = ao[perm[o][3]];
+                double2 w = c2(0.0, 0.0);
+                for (int p = 0; p < a.npc; ++p) {
+                    const double2* P = a.coulomb + (2 * p) * n * n;
+                    const double2* Q = P + n * n;
+                    w = cmac(w, __ldg(&P[nu * n + mu]), __ldg(&Q[si * n + la]));
+                }
+                for (int p = 0; p < a.npx; ++p) {
+                    const double2* P = a.exchange + (2 * p) * n * n;
+                    const double2* Q = P + n * n;
+                    w = cmac(w, __ldg(&P[nu * n + la]), __ldg(&Q[si * n + mu]));
+                }
+                const long long gi = ((mu * n + nu) * n + la) * n + si;
+                if (a.gamma) w = cadd(w, __ldg(&a.gamma[gi]));
+                if (a.gamma_real) w.x += __ldg(&a.gamma_real[gi]);
+                if (o < 2)
+                    wd = cadd(wd, w);
+                else
+                    wc = cadd(wc, w);
+            }
+#pragma unroll
+            for (int t = 0; t < 12; ++t) {
+                const double2 dv = __ldg(&blk[(long long)t * size + loc]);
+                // d wd + conj(d) wc
+                acc[t].x += dv.x * wd.x - dv.y * wd.y + dv.x * wc.x + dv.y * wc.y;
+                acc[t].y += dv.x * wd.y + dv.y * wd.x + dv.x * wc.y - dv.y * wc.x;
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 12; ++t)
+            for (int off = 16; off > 0; off >>= 1) {
+                acc[t].x += __shfl_xor_sync(0xffffffffu, acc[t].x, off);
+                acc[t].y += __shfl_xor_sync(0xffffffffu, acc[t].y, off);
+            }
+        if (lane == 0)
+            for (int t = 0; t < 12; ++t) a.partials[(long long)qi * 12 + t] = acc[t];
+    }
+}
+
 __global__ void __launch_bounds__(256) gather_abs_kernel(const double2* __restrict__ src,
                                                          const long long* __restrict__ idx, double* __restrict__ dst,
                                                          long long n) {
@@ -305,6 +389,14 @@ cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* 
     const long long want = (n + 255) / 256;
     const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, (long long)sms * 8));
     gather_abs_kernel<<<blocks, 256, 0, s>>>(src, idx, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deriv_contract(const DerivContractArgs& args, int sms, cudaStream_t s) {
+    if (args.nq == 0) return cudaSuccess;
+    const long long want = ((long long)args.nq + 3) / 4;  // 4 warps per block
+    const unsigned blocks = (unsigned)std::max<long long>(1, std::min(want, (long long)sms * 16));
+    deriv_contract_kernel<<<blocks, 128, 0, s>>>(args);
     return cudaGetLastError();
 }
 

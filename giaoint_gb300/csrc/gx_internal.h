@@ -178,6 +178,25 @@ struct DerivMixedArgs {
     double inv_sqrt_df[18];
 };
 cudaError_t launch_deriv_mixed(const DerivMixedArgs& args, long long total, int sms, cudaStream_t s);
+// Twelve partial sums per canonical quartet of the per-atom contraction of
+// centre derivatives with density pairs and a two-particle density.
+struct DerivContractArgs {
+    int nq;
+    const uint32_t* quartets;        // [4 nq]
+    const long long* offsets;        // [nq] derivative block offsets in D
+    const double2* D;
+    const int* shell_l;
+    const int* shell_ncontr;
+    const long long* ao_start;       // per shell
+    long long n;                     // AO count
+    int npc, npx;                    // Coulomb / exchange pairs
+    const double2* coulomb;          // [2 npc] (n, n): P, Q, P, Q, ...
+    const double2* exchange;         // [2 npx] (n, n)
+    const double2* gamma;            // complex n^4 or null
+    const double* gamma_real;        // real n^4 or null
+    double2* partials;               // [nq][12]
+};
+cudaError_t launch_deriv_contract(const DerivContractArgs& args, int sms, cudaStream_t s);
 // dst[i] = |src[idx[i]]| (diagonal elements of the derivative-bound blocks)
 cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* dst, long long n, int sms,
                               cudaStream_t s);

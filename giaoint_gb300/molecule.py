@@ -25,6 +25,7 @@ import numpy as np
 
 from ._types import Basis, MagneticField, Nucleus, Shell
 from .cholesky import cholesky_eri as _cholesky_eri
+from .derivative_assembly import eri_derivative_contraction as _eri_derivative_contraction
 from .eri import eri as _eri
 from .eri import eri_batches as _eri_batches
 from .eri import eri_derivative_batches as _eri_derivative_batches
@@ -278,3 +279,12 @@ class Molecule:
         maps shells to atoms (repeated slots add)."""
         return _eri_derivative_batches(self._basis, field=self._field, quartets=quartets, target_bytes=target_bytes,
                                        screening_threshold=screening_threshold, threads=threads)
+
+    def eri_derivative_contraction(self, *, coulomb_pairs=(), exchange_pairs=(), gamma=None,
+                                   target_bytes=64 * 1024 ** 2, screening_threshold=0.0, threads=None, out=None):
+        """Per-atom contraction of the ERI centre derivatives with this
+        molecule's field and shell owners, complex128 (natom, 3)."""
+        return _eri_derivative_contraction(self._basis, self._shell_atoms, len(self._atoms), field=self._field,
+                                           coulomb_pairs=coulomb_pairs, exchange_pairs=exchange_pairs, gamma=gamma,
+                                           target_bytes=target_bytes, screening_threshold=screening_threshold,
+                                           threads=threads, out=out)

@@ -175,6 +175,24 @@ int gx_eri_magnetic_derivatives(gx_context* ctx, gx_basis* basis, const double* 
 int gx_eri_mixed_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
                              const uint32_t* quartets, int64_t nq, int64_t* offsets, double* out, int64_t out_capacity);
 
+/* Per-atom contraction of ERI centre derivatives with fixed densities,
+ * replacing detail::contract_eri_derivatives behind _contract_eri_derivative_batch
+ * (src/assembly.cpp:87-158, bindings.cpp:2418-2456): for every canonical
+ * quartet (an error otherwise) and each of its distinct orbit images, the
+ * derivative (conjugated for the two reversed images) times
+ *   sum_pairs P[nu,mu] Q[sig,lam] (coulomb) + sum_pairs P[nu,lam] Q[sig,mu]
+ *   (exchange) + gamma[mu,nu,lam,sig]
+ * is added to out[shell_atoms[slot shell]][axis], in quartet and slot order.
+ * coulomb / exchange: npc / npx pairs of complex (n, n) matrices (P then Q);
+ * gamma: n^4 values, complex (gamma_complex != 0) or real, may be NULL;
+ * out: complex (natom, 3), accumulated (not cleared).  The derivative blocks
+ * stay on the device, computed in batches of at most batch_elements complex
+ * values (a single larger quartet alone). */
+int gx_eri_derivative_contraction(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                                  const uint32_t* quartets, int64_t nq, const int64_t* shell_atoms, int natom,
+                                  int npc, const double* coulomb, int npx, const double* exchange,
+                                  const double* gamma, int gamma_complex, int64_t batch_elements, double* out);
+
 /* Derivative-density Schwarz factors, replacing EriDerivativeSchwarzBounds
  * (src/derivatives.cpp:1307-1372, bindings.cpp:2242-2253): values[ns*ns]
  * receives the factor of every ordered shell pair (a, b) at a*ns + b, and

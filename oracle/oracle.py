@@ -450,6 +450,26 @@ class Reference(_Backend):
                                                       out.ctypes.data_as(_d)))
         return out[:total], offsets
 
+    def contract_eri_derivatives(self, shells, atoms, natom, quartets, offsets, values, coulomb=(), exchange=(),
+                                 gamma=None) -> np.ndarray:
+        """Reference per-atom contraction (complex (natom, 3))."""
+        a = self._basis(shells)
+        n = a.nao
+        q = np.ascontiguousarray(np.asarray(quartets, dtype=np.uint32).reshape(-1, 4))
+        at = np.ascontiguousarray(atoms, dtype=np.int64)
+        off = np.ascontiguousarray(offsets, dtype=np.int64)
+        vals = np.ascontiguousarray(values, dtype=np.complex128)
+        cj = np.ascontiguousarray([m for pair in coulomb for m in pair] or [np.zeros((n, n))], dtype=np.complex128)
+        kx = np.ascontiguousarray([m for pair in exchange for m in pair] or [np.zeros((n, n))], dtype=np.complex128)
+        g = None if gamma is None else np.ascontiguousarray(gamma, dtype=np.complex128)
+        out = np.zeros((natom, 3), dtype=np.complex128)
+        self._check(self.lib.ref_contract_eri_derivatives(
+            *self._bargs(a), at.ctypes.data_as(_l), ctypes.c_long(natom), q.ctypes.data_as(_u32),
+            ctypes.c_long(len(q)), off.ctypes.data_as(_l), vals.ctypes.data_as(_d), ctypes.c_int(len(coulomb)),
+            cj.ctypes.data_as(_d), ctypes.c_int(len(exchange)), kx.ctypes.data_as(_d),
+            None if g is None else g.ctypes.data_as(_d), out.ctypes.data_as(_d)))
+        return out
+
     def eri_derivative_bounds(self, shells, B=None, O=None) -> np.ndarray:
         a = self._basis(shells)
         out = np.zeros((max(a.ns, 1), max(a.ns, 1)), dtype=np.float64)
@@ -618,3 +638,55 @@ def cholesky_eri(backend: _Backend, shells, B=None, O=None, threshold: float = 1
     vectors = np.array(factors[: len(pivots)], dtype=np.complex128).reshape(len(pivots), n, n)
     return CholeskyResult(vectors, np.asarray(pivots, dtype=np.int64).reshape(-1, 2), threshold,
                           float(np.max(residual, initial=0.0)))
+
+
+# --------------------------------------------------------------------------
+# per-atom contraction of ERI centre derivatives (src/assembly.cpp:87-158)
+# --------------------------------------------------------------------------
+
+_ORBIT = ((0, 1, 2, 3), (2, 3, 0, 1), (1, 0, 3, 2), (3, 2, 1, 0))
+
+
+def contract_eri_derivatives(shells, atoms, natom, quartets, offsets, values, coulomb=(), exchange=(), gamma=None):
+    """Restatement of detail::contract_eri_derivatives: for every canonical
+    quartet, every distinct orbit image (identity, pair exchange, conjugate
+    reversal, conjugate exchanged reversal; images with equal shell quartets
+    counted once) contributes derivative x weight, the weight being
+    sum_pairs P[nu,mu] Q[sig,lam] (Coulomb), P[nu,lam] Q[sig,mu] (exchange)
+    and gamma[mu,nu,lam,sig] at the image's AO indices; the derivative is
+    conjugated for the last two images.  Twelve partial sums per quartet,
+    added to the slot shells' atoms in quartet and slot order.  NumPy, one
+    quartet at a time (small cases)."""
+    specs = as_specs(shells)
+    nao = [s.nao for s in specs]
+    start = np.concatenate([[0], np.cumsum(nao)]).astype(np.int64)
+    out = np.zeros((natom, 3), dtype=np.complex128)
+    q = np.asarray(quartets, dtype=np.int64).reshape(-1, 4)
+    for row, x in enumerate(q):
+        shape = [nao[s] for s in x]
+        size = int(np.prod(shape))
+        blk = np.asarray(values[offsets[row]:offsets[row + 1]]).reshape(4, 3, size)
+        grids = np.meshgrid(*[start[s] + np.arange(nao[s]) for s in x], indexing="ij")
+        ao = [g.ravel() for g in grids]
+        active = []
+        for orbit, perm in enumerate(_ORBIT):
+            image = tuple(x[perm[k]] for k in range(4))
+            if any(image == tuple(x[_ORBIT[p][k]] for k in range(4)) for p in range(orbit)):
+                continue
+            active.append(orbit)
+        partial = np.zeros((4, 3), dtype=np.complex128)
+        for orbit in active:
+            perm = _ORBIT[orbit]
+            mu, nu, lam, sig = (ao[perm[k]] for k in range(4))
+            w = np.zeros(size, dtype=np.complex128)
+            for P, Q in coulomb:
+                w += np.asarray(P)[nu, mu] * np.asarray(Q)[sig, lam]
+            for P, Q in exchange:
+                w += np.asarray(P)[nu, lam] * np.asarray(Q)[sig, mu]
+            if gamma is not None:
+                w += np.asarray(gamma)[mu, nu, lam, sig]
+            d = np.conj(blk) if orbit >= 2 else blk
+            partial += (d * w[None, None, :]).sum(axis=2)
+        for slot in range(4):
+            out[atoms[x[slot]]] += partial[slot]
+    return out

@@ -15,9 +15,11 @@
 //   ref_eri_magnetic_derivatives <- src/derivatives.cpp:961-966
 //   ref_eri_mixed_derivatives  <- src/derivatives.cpp:968-973
 //   ref_eri_derivative_bounds  <- src/derivatives.cpp:1307-1372
+//   ref_contract_eri_derivatives <- src/assembly.cpp:87-158
 //   ref_cholesky_diagonal  <- src/bindings.cpp:2306-2314
 //   ref_cholesky_columns   <- src/bindings.cpp:2315-2330
 #include "giao_integrals/boys.hpp"
+#include "assembly.hpp"
 #include "giao_integrals/derivatives.hpp"
 #include "giao_integrals/eri.hpp"
 #include "giao_integrals/nuclear.hpp"
@@ -265,6 +267,39 @@ int ref_eri_mixed_derivatives(int ns, const double* centers, const int* ls, cons
                 a, b, c, d, field, std::span<giao::Complex>(reinterpret_cast<giao::Complex*>(out) + off, size));
             off += size;
         }
+    });
+}
+
+// Per-atom contraction of canonical centre-derivative blocks with density
+// pairs and an optional complex two-particle density
+// (detail::contract_eri_derivatives, src/assembly.cpp:87-158).  coulomb /
+// exchange: npc / npx pairs of complex (n, n) matrices, P then Q; gamma:
+// complex n^4 or null; out: complex (natom, 3), accumulated.
+int ref_contract_eri_derivatives(int ns, const double* centers, const int* ls, const int* nprims,
+                                 const int* ncontrs, const double* exps, const double* coefs,
+                                 const int* normalize, const long* atoms, long natom, const uint32_t* quartets,
+                                 long nq, const long* offsets, const double* values, int npc,
+                                 const double* coulomb, int npx, const double* exchange, const double* gamma,
+                                 double* out) {
+    return guarded([&] {
+        auto basis = make_basis(ns, centers, ls, nprims, ncontrs, exps, coefs, normalize);
+        const std::size_t n = basis.ao_count();
+        std::vector<std::size_t> at(atoms, atoms + ns);
+        std::vector<giao::ShellQuartetIndex> q;
+        for (long i = 0; i < nq; ++i)
+            q.push_back({quartets[4 * i], quartets[4 * i + 1], quartets[4 * i + 2], quartets[4 * i + 3]});
+        std::vector<std::size_t> off(offsets, offsets + nq + 1);
+        auto cx = [](const double* p) { return reinterpret_cast<const giao::Complex*>(p); };
+        std::vector<giao::detail::DensityPair> jp, kp;
+        for (int i = 0; i < npc; ++i)
+            jp.push_back({{cx(coulomb) + 2 * i * n * n, n * n}, {cx(coulomb) + (2 * i + 1) * n * n, n * n}});
+        for (int i = 0; i < npx; ++i)
+            kp.push_back({{cx(exchange) + 2 * i * n * n, n * n}, {cx(exchange) + (2 * i + 1) * n * n, n * n}});
+        std::span<const giao::Complex> g;
+        if (gamma) g = {cx(gamma), n * n * n * n};
+        giao::detail::contract_eri_derivatives(basis, at, (std::size_t)natom, q, off,
+                                               {cx(values), (std::size_t)off.back()}, jp, kp, g, {},
+                                               {reinterpret_cast<giao::Complex*>(out), (std::size_t)natom * 3}, 1);
     });
 }
 

@@ -23,6 +23,7 @@ def golden():
         blocks = dict(np.load(GOLDEN / "eri_blocks.npz"))
         nuclear = dict(np.load(GOLDEN / "nuclear.npz"))
         derivatives = dict(np.load(GOLDEN / "derivatives.npz"))
+        contraction = dict(np.load(GOLDEN / "contraction.npz"))
 
     return G
 
@@ -44,3 +45,11 @@ def derivative_systems(g):
                  for d in json.loads(str(g[f"{name}_shells"]))]
         out.append((name, specs, g[f"{name}_quartets"]))
     return out
+
+
+def contraction_setup():
+    """Systems and closed-form densities of the contraction fixture."""
+    sys.path.insert(0, str(GOLDEN))
+    import make_golden as mg
+
+    return mg

@@ -5,7 +5,7 @@ read-only reference path used to build oracle/_ref):
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py nuclear    # one fixture (boys, m8, blocks, nuclear,
-                                                  # derivatives, cholesky)
+                                                  # derivatives, contraction, cholesky)
 
 Inputs and outputs:
 
@@ -31,6 +31,10 @@ Inputs and outputs:
   (3, na, nb, nc, nd) of the same quartets, the mixed field/centre blocks
   (4, 3, 3, na, nb, nc, nd) of a subset, and the reference's derivative
   and ordinary Schwarz factors of every ordered shell pair;
+* ``contraction.npz`` -- reference ``contract_eri_derivatives`` (per-atom
+  (natom, 3)) over all canonical quartets of the hand-made f/g system and a
+  seeded two-atom molecule, with the closed-form densities of
+  ``contraction_densities`` (complex and real gamma), zero and finite field;
 * ``cholesky.json`` -- the reference's own NumPy Cholesky driver
   (python/giao_integrals/cholesky.py, executed unmodified over the reference
   library's native diagonal/column generators) on the two-shell d/f system of
@@ -306,6 +310,48 @@ def derivative_fixture(ref):
     np.savez_compressed(HERE / "derivatives.npz", **out)
 
 
+def contraction_densities(n: int, complex_gamma: bool):
+    """Closed-form (reproducible anywhere) Coulomb pair, two exchange pairs
+    and a two-particle density of an n-AO system."""
+    i = np.arange(n)[:, None]
+    j = np.arange(n)[None, :]
+    mats = [np.cos(0.3 * i + 0.7 * j + t) + 1j * np.sin(0.5 * i - 0.2 * j + 2 * t) for t in range(6)]
+    coulomb = [(mats[0], mats[1])]
+    exchange = [(mats[2], mats[3]), (mats[4], mats[5])]
+    a, b, c, d = np.meshgrid(*(np.arange(n),) * 4, indexing="ij")
+    gamma = 0.1 * np.sin(a + 2.0 * b + 3.0 * c + 5.0 * d)
+    if complex_gamma:
+        gamma = gamma + 0.1j * np.cos(7.0 * a - b + c - 2.0 * d)
+    return coulomb, exchange, np.ascontiguousarray(gamma)
+
+
+def contraction_cases():
+    """(name, shell specs, shell atoms, natom, complex gamma) of the
+    contraction fixture."""
+    hand = derivative_cases()["hand"][0]
+    small = O.as_specs(syn.random_molecule(9, natoms=2, box=3.0))
+    cen = []
+    small_atoms = []
+    for s in small:
+        if s.center not in cen:
+            cen.append(s.center)
+        small_atoms.append(cen.index(s.center))
+    return [("hand", hand, [0, 1, 0, 2], 3, True), ("small", small, small_atoms, len(cen), False)]
+
+
+def contraction_fixture(ref, orc):
+    out = {}
+    for name, specs, atoms, natom, cg in contraction_cases():
+        n = sum(s.nao for s in specs)
+        coulomb, exchange, gamma = contraction_densities(n, cg)
+        q = orc.canonical_quartets(len(specs))
+        for label, B, origin in (("field", DERIV_FIELD, DERIV_ORIGIN), ("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0))):
+            vals, offsets = ref.eri_center_derivatives(specs, q, B, origin)
+            out[f"{name}_{label}"] = ref.contract_eri_derivatives(specs, atoms, natom, q, offsets, vals, coulomb,
+                                                                  exchange, gamma)
+    np.savez_compressed(HERE / "contraction.npz", **out)
+
+
 def main():
     if build_ref.build() is None:
         raise SystemExit("the reference checkout is required to generate fixtures")
@@ -322,6 +368,8 @@ def main():
         nuclear_fixture(ref)
     if not only or "derivatives" in only:
         derivative_fixture(ref)
+    if not only or "contraction" in only:
+        contraction_fixture(ref, orc)
     if not only or "cholesky" in only:
         (HERE / "cholesky.json").write_text(json.dumps(cholesky_fixture(ref)))
     for p in sorted(HERE.iterdir()):

@@ -198,3 +198,22 @@ def test_eri_mixed_derivatives_oracle_matches_reference(golden, oracle):
             vals, _ = oracle.eri_mixed_derivatives(specs, q, field, o)
             ref = g[f"{name}_mixed_{label}"]
             assert np.abs(vals - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max()), (name, label)
+
+
+def test_eri_derivative_contraction_oracle_matches_reference(golden, oracle):
+    """Oracle restatement of detail::contract_eri_derivatives
+    (src/assembly.cpp:87-158) over all 5292 canonical quartets of a two-atom
+    molecule at finite field, with the fixture's closed-form Coulomb,
+    exchange and real two-particle densities, against the reference library."""
+    from conftest import contraction_setup
+    from oracle.oracle import contract_eri_derivatives
+
+    mg = contraction_setup()
+    name, specs, atoms, natom, complex_gamma = mg.contraction_cases()[1]
+    n = sum(s.nao for s in specs)
+    coulomb, exchange, gamma = mg.contraction_densities(n, complex_gamma)
+    q = oracle.canonical_quartets(len(specs))
+    vals, off = oracle.eri_center_derivatives(specs, q, mg.DERIV_FIELD, mg.DERIV_ORIGIN)
+    got = contract_eri_derivatives(specs, atoms, natom, q, off, vals, coulomb, exchange, gamma)
+    ref = golden.contraction[f"{name}_field"]
+    assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
