@@ -291,7 +291,8 @@ struct gx_basis {
     // followed by their Z, U and D shells, and per-shell arrays for the
     // combine kernel
     std::unique_ptr<gx_basis> deriv;
-    DeviceBuffer d_shell_l, d_shell_ncontr, d_shell_raw, d_shell_center;
+    DeviceBuffer d_shell_l, d_shell_ncontr, d_shell_raw, d_shell_center, d_shell_inv2a;
+    std::vector<double> shell_inv2a;  // 1 / (2 alpha) of single-primitive shells (l <= 15), else 0
     // derivative-bound basis (built on first use): one raw single-primitive
     // shell per (primitive, variant l / l + 1 / l - 1); bound_index[3 * g + v]
     // for the g-th primitive of the basis (-1: absent)
@@ -1220,6 +1221,13 @@ gx_basis* derivative_basis(gx_context* ctx, gx_basis* b, std::vector<int>& index
         upload(b->d_shell_ncontr, sn, ctx->stream);
         upload(b->d_shell_raw, sr, ctx->stream);
         upload(b->d_shell_center, b->center, ctx->stream);
+        b->shell_inv2a.assign(ns, 0.0);
+        size_t e = 0;
+        for (int s2 = 0; s2 < ns; ++s2) {
+            if (b->nprim[s2] == 1 && b->l[s2] <= 15) b->shell_inv2a[s2] = 1.0 / (2.0 * b->exps[e]);
+            e += b->nprim[s2];
+        }
+        upload(b->d_shell_inv2a, b->shell_inv2a, ctx->stream);
     }
     return b->deriv.get();
 }
@@ -1461,7 +1469,8 @@ void derivative_core(gx_context* ctx, gx_basis* b, int mode, const double* B, co
                 add(k, kDerivZ);
                 if (b->l[x[k]] > 0) add(k, kDerivD);
             }
-            if (has_u) add(k, kDerivU);
+            // centre mode: a single-primitive shell's U block is Z / (2 alpha)
+            if (has_u && !(mode == 0 && b->shell_inv2a[x[k]] != 0.0)) add(k, kDerivU);
         }
         if (has_u) add(0, -1);
     }
@@ -1512,6 +1521,7 @@ void derivative_core(gx_context* ctx, gx_basis* b, int mode, const double* B, co
     a.shell_ncontr = b->d_shell_ncontr.as<int>();
     a.shell_raw = b->d_shell_raw.as<int>();
     a.shell_center = b->d_shell_center.as<double>();
+    a.shell_inv2a = b->d_shell_inv2a.as<double>();
     a.derived = ctx->deriv_vals.as<double2>();
     a.out = dout;
     for (int k = 0; k < 3; ++k) {

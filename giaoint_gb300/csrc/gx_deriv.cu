@@ -78,9 +78,11 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
         // this quartet's derived blocks: per slot [Z, D if l > 0] (centre), [U]; then [plain]
         long long off = __ldg(&a.derived_offsets[qi]);
         long long zoff[4], doff[4], uoff[4], boff = -1;
+        double uscale[4];  // U = Z / (2 alpha) for a single-primitive shell in centre mode
         for (int j = 0; j < 4; ++j) {
             const long long up = size / dim[j] * (nc[j] * ncart(l[j] + 1));
             zoff[j] = doff[j] = uoff[j] = -1;
+            uscale[j] = 1.0;
             if (centre) {
                 zoff[j] = off;
                 off += up;
@@ -89,7 +91,11 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
                     off += size / dim[j] * (nc[j] * ncart(l[j] - 1));
                 }
             }
-            if (has_u) {
+            const double inv2a = centre ? __ldg(&a.shell_inv2a[sh[j]]) : 0.0;
+            if (has_u && inv2a != 0.0) {
+                uoff[j] = zoff[j];
+                uscale[j] = inv2a;
+            } else if (has_u) {
                 uoff[j] = off;
                 off += up;
             }
@@ -153,9 +159,10 @@ __global__ void __launch_bounds__(256) deriv_combine_kernel(DerivCombineArgs a) 
                 ++uc[c];
                 const double2 u = __ldg(&a.derived[uoff[k] + derived(k, xk, lk + 1, uc[0], uc[2])]);
                 const double R = __ldg(&a.shell_center[3 * sh[k] + c]);
+                const double hu = hk * uscale[k];
                 // coef * (h U + R base)
-                t.x += coef * (hk * u.x + R * base.x);
-                t.y += coef * (hk * u.y + R * base.y);
+                t.x += coef * (hu * u.x + R * base.x);
+                t.y += coef * (hu * u.y + R * base.y);
             }
             // + i t
             res.x -= t.y;

@@ -152,6 +152,8 @@ struct DerivCombineArgs {
     const int* shell_ncontr;
     const int* shell_raw;
     const double* shell_center;      // [3 ns]
+    const double* shell_inv2a;       // 1 / (2 alpha) of single-primitive shells, else 0: their U block
+                                     // (centre mode) is omitted and read as Z / (2 alpha)
     const double2* derived;          // derived-basis ERI blocks
     double2* out;
     double B[3], O[3];
