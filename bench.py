@@ -544,8 +544,8 @@ def run_gpu(args):
         off2 = np.zeros(nq + 1, dtype=np.int64)
         stats = nat.GxStats()
         times = []
-        reps = max(1, min(args.steps, 3))
-        warm = max(2, args.warmup)  # the first call is the cold one, reported separately
+        reps = max(1, min(args.steps, 5))
+        warm = max(3, args.warmup)  # the first call is the cold one, reported separately
         for i in range(warm + reps):
             t0 = time.perf_counter()
             nat.check(lib.gx_eri_batch(ctx.handle, bh, nat.dptr(Bv), nat.dptr(Ov),
@@ -594,7 +594,8 @@ def run_gpu(args):
                "cold_call_seconds": cold_s, "cold_h2d_bytes": int(ntask.value * 40 + 48),
                "d2h_copy_seconds": d2h_s, "d2h_gb_per_s": total * 16 / d2h_s / 1e9,
                "api": "gx_eri_batch (C ABI, pinned host buffers)", "max_abs_diff_vs_device_path": e2e_diff,
-               "call_seconds": times, "device_output_call_seconds": dev_times}
+               "call_seconds": times, "call_seconds_median": float(statistics.median(times)),
+               "device_output_call_seconds": dev_times}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample_rate(recs, B, quartets, target_seconds=10.0)
