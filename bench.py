@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--derivatives-only", action="store_true",
                    help="run only the centre-derivative leg and print its JSON (profiling)")
     p.add_argument("--derivative-quartets", type=int, default=200000)
+    p.add_argument("--cholesky-only", action="store_true",
+                   help="run only the Cholesky leg (no CPU port) and print its JSON (profiling)")
     p.add_argument("--serving-requests", type=int, default=32)
     p.add_argument("--sweep", type=int, default=0,
                    help="field sweep: evaluate the molecule at this many fields |B| <= 0.5 in FP64 and mixed")
@@ -436,6 +438,9 @@ def run_gpu(args):
     lib = nat.lib()
     ctx = nat.Context(local)
     recs, B = workload(args.natoms, rank)
+    if args.cholesky_only:
+        print(json.dumps({"cholesky": cholesky_leg(gi, nat, ctx, run_cpu=False)}), flush=True)
+        return
     if args.derivatives_only:
         quartets = gi.canonical_quartets(len(recs))
         leg = derivative_leg(ctx, recs, B, quartets, run_cpu=False, count=args.derivative_quartets)

@@ -2405,9 +2405,14 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         // ---- pivot loop ----
         bool reuse = !single;
         for (int s = 0; s < ns; ++s) reuse = reuse || b->ncontr[s] > 1 || b->nprim[s] > 1;
-        const int candidate_count = reuse ? 32 : 8;
+        // Columns kept per pivot-block evaluation.  The evaluation computes
+        // every column of the pivot's shell-pair block; without the
+        // contracted-variant rule the pivot is always the global argmax, so
+        // keeping more of them (and the raw-column cache below) changes only
+        // how often a block is evaluated, never a result.
+        const int candidate_count = reuse ? 32 : 256;
         ColumnPool pool;
-        pool.init(32 + 1024 + 64, N * esz);
+        pool.init(candidate_count + 1024 + 64, N * esz);
         d_work.reserve(N * esz);
         d_L.reserve(std::max<int64_t>(limit, 1) * N * esz);
         std::vector<int64_t> cands;               // current batch candidates (flat indices)
@@ -2462,7 +2467,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                 raise(GX_ENOMEM, "Cholesky rank capacity exceeded");
             }
             auto cached = lru_pos.find(pivot);
-            if (reuse && cached != lru_pos.end()) {
+            if (cached != lru_pos.end()) {
                 const int slot = cached->second->second;
                 lru.erase(cached->second);
                 lru_pos.erase(cached);
@@ -2554,7 +2559,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                 GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), cp->boff.as<long long>(),
                                              column_info.as<int>(), cp->nblocks, d_cand.as<int>(), (int)cands.size(),
                                              (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
-                if (reuse) {
+                {
                     for (size_t k = 0; k < cands.size(); ++k) {
                         if (cands[k] == pivot) continue;
                         // assignment to an existing key keeps its LRU position (OrderedDict semantics)
@@ -2577,7 +2582,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                 }
                 it = std::find(cands.begin(), cands.end(), pivot);
             }
-            if (reuse) {
+            {
                 auto c2it = lru_pos.find(pivot);
                 if (c2it != lru_pos.end()) {
                     pool.release(c2it->second->second);
