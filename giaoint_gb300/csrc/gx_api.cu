@@ -2412,7 +2412,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         // how often a block is evaluated, never a result.
         const int candidate_count = reuse ? 32 : 256;
         ColumnPool pool;
-        pool.init(candidate_count + 1024 + 64, N * esz);
+        pool.init(256 + 1024 + 64, N * esz);
         d_work.reserve(N * esz);
         d_L.reserve(std::max<int64_t>(limit, 1) * N * esz);
         std::vector<int64_t> cands;               // current batch candidates (flat indices)
@@ -2513,6 +2513,23 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                 }
                 block_cands.assign(keep.begin(), keep.begin() + std::min<size_t>(keep.size(),
                                                                                  std::min(32, opt->pivot_batch_size)));
+                if (reuse) {
+                    // the evaluation below computes every column of the block:
+                    // keep the other entries above the threshold too (largest
+                    // residual first) for the raw-column cache; the pivot rule
+                    // above uses only the contraction variants
+                    std::vector<int64_t> extra;
+                    for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + na; ++i)
+                        for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + nc; ++j) {
+                            const int64_t f = i * n + j;
+                            if (rv(f) > tol && std::find(keep.begin(), keep.end(), f) == keep.end())
+                                extra.push_back(f);
+                        }
+                    std::stable_sort(extra.begin(), extra.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
+                    const size_t room = keep.size() < 256 ? 256 - keep.size() : 0;
+                    if (extra.size() > room) extra.resize(room);
+                    keep.insert(keep.end(), extra.begin(), extra.end());
+                }
                 drop_batch();
                 cands = keep;
                 // columns (mu nu | p1 p0) for all shell pairs (real: b >= a).  The
