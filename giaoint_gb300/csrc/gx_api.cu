@@ -2590,7 +2590,9 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
                             lru_pos[cands[k]] = std::prev(lru.end());
                         }
                     }
-                    const size_t cap = (size_t)std::min<int64_t>(1024, std::max<int64_t>(8, rank + 8));
+                    // raw columns are exact whenever they were computed, so the
+                    // cache size changes only how often a block is evaluated
+                    const size_t cap = 1024;
                     while (lru.size() > cap) {
                         pool.release(lru.front().second);
                         lru_pos.erase(lru.front().first);
