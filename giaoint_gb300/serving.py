@@ -56,8 +56,8 @@ def footprint_bytes(request) -> int:
     n = int(sizes.sum())
     N = n * n
     rank_guess = min(N, max(64, 8 * n))
-    # factors, column pool (1120 columns), residual/diagonal/work vectors
-    return _BASE_BYTES + (rank_guess + 1120 + 4) * N * 16
+    # factors, column pool (1344 columns), residual/diagonal/work vectors
+    return _BASE_BYTES + (rank_guess + 1344 + 4) * N * 16
 
 
 @dataclass
