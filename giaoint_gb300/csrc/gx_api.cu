@@ -2414,6 +2414,9 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
         ColumnPool pool;
         pool.init(256 + 1024 + 64, N * esz);
         d_work.reserve(N * esz);
+        constexpr int kGemvChunks = 8;  // rank chunks of the factor update (partial sums)
+        DeviceBuffer d_gemv;
+        d_gemv.reserve((size_t)kGemvChunks * N * esz);
         d_L.reserve(std::max<int64_t>(limit, 1) * N * esz);
         std::vector<int64_t> cands;               // current batch candidates (flat indices)
         std::vector<int> cand_slot;               // their column slots
@@ -2613,7 +2616,7 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
             void* Lrow = static_cast<char*>(d_L.ptr) + (size_t)rank * N * esz;
             GX_CUDA(gx::launch_chol_step(real, d_L.ptr, N, (int)rank, pivot, pool.ptr(slot), d_work.ptr, (int)n,
                                          d_res.as<double>(), d_scale.as<double>(), Lrow, d_partial.ptr, d_red.ptr,
-                                         st));
+                                         st, d_gemv.ptr, kGemvChunks, ctx->sm_count));
             fetch_red();
             pivots_out[2 * rank] = pivot / n;
             pivots_out[2 * rank + 1] = pivot % n;

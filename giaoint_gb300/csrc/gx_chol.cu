@@ -12,6 +12,8 @@
 //                        clamp, zeroed pivot and the next argmax, fused
 //                        (cholesky.py:269-281)
 //   argmax reductions    lowest flat index on ties (NumPy argmax order)
+#include <algorithm>
+
 #include "gx_internal.h"
 
 namespace gx {
@@ -188,6 +190,57 @@ __global__ void chol_gemv_kernel(const T* L, long long ld, int rank, long long p
     if (j < N) col_out[j] = acc;
 }
 
+// The same update with the rank split over blockIdx.y: block (x, y) sums
+// conj(L[r, piv]) L[r, j] over its rows into partials[y][j], and
+// chol_gemv_sum_kernel subtracts the chunks in order.  Small n (few column
+// entries) otherwise leaves too few loads in flight to stream L at HBM speed.
+template <typename T>
+__global__ void chol_gemv_split_kernel(const T* L, long long ld, int rank, long long piv, int chunk, T* partials,
+                                       long long N) {
+    __shared__ T coef[256];
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int rbeg = blockIdx.y * chunk, rend = min(rank, rbeg + chunk);
+    T acc;
+    if constexpr (sizeof(T) == 8) {
+        acc = T(0);
+    } else {
+        acc = c2(0.0, 0.0);
+    }
+    for (int r0 = rbeg; r0 < rend; r0 += 256) {
+        const int nr = min(256, rend - r0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) coef[i] = L[(long long)(r0 + i) * ld + piv];
+        __syncthreads();
+        if (j < N) {
+#pragma unroll 8
+            for (int r = 0; r < nr; ++r) {
+                const T lv = __ldg(&L[(long long)(r0 + r) * ld + j]);
+                if constexpr (sizeof(T) == 8) {
+                    acc += coef[r] * lv;
+                } else {
+                    acc = cadd(acc, conj_mul(coef[r], lv));
+                }
+            }
+        }
+    }
+    if (j < N) partials[(long long)blockIdx.y * N + j] = acc;
+}
+
+template <typename T>
+__global__ void chol_gemv_sum_kernel(const T* col_in, const T* partials, int nchunks, long long N, T* col_out) {
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        T acc = col_in[j];
+        for (int y = 0; y < nchunks; ++y) {
+            if constexpr (sizeof(T) == 8) {
+                acc -= partials[(long long)y * N + j];
+            } else {
+                acc = csub(acc, partials[(long long)y * N + j]);
+            }
+        }
+        col_out[j] = acc;
+    }
+}
+
 // scale = 1/sqrt(residual[piv]) (read before the update)
 __global__ void chol_scale_kernel(const double* res, long long piv, double* scale) { *scale = rsqrt(res[piv]); }
 
@@ -220,10 +273,32 @@ __global__ void chol_update_kernel(const T* col, int n, long long piv, const dou
 
 cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, long long piv, const void* column,
                              void* work, int n, double* res, double* scale, void* Lrow, void* partial, void* out,
-                             cudaStream_t s) {
+                             cudaStream_t s, void* gemv_partials, int max_chunks, int sms) {
     const long long N = (long long)n * n;
     const int blocks = (int)((N + 127) / 128);
-    if (real) {
+    // rank chunks: enough blocks for about eight per SM, at least 32 rows each
+    int nchunks = 1;
+    if (gemv_partials && max_chunks > 1 && rank >= 64 && sms > 0) {
+        nchunks = std::max(1, std::min({max_chunks, (8 * sms) / std::max(blocks, 1), (rank + 31) / 32}));
+    }
+    if (nchunks > 1) {
+        const int chunk = (rank + nchunks - 1) / nchunks;
+        const dim3 grid(blocks, nchunks);
+        const int sblocks = (int)std::min<long long>((N + 255) / 256, 8LL * sms);
+        if (real) {
+            chol_gemv_split_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(L), ld, rank, piv, chunk,
+                                                                static_cast<double*>(gemv_partials), N);
+            chol_gemv_sum_kernel<double><<<sblocks, 256, 0, s>>>(static_cast<const double*>(column),
+                                                                  static_cast<const double*>(gemv_partials), nchunks,
+                                                                  N, static_cast<double*>(work));
+        } else {
+            chol_gemv_split_kernel<double2><<<grid, 128, 0, s>>>(static_cast<const double2*>(L), ld, rank, piv, chunk,
+                                                                 static_cast<double2*>(gemv_partials), N);
+            chol_gemv_sum_kernel<double2><<<sblocks, 256, 0, s>>>(static_cast<const double2*>(column),
+                                                                   static_cast<const double2*>(gemv_partials), nchunks,
+                                                                   N, static_cast<double2*>(work));
+        }
+    } else if (real) {
         chol_gemv_kernel<double><<<blocks, 128, 0, s>>>(static_cast<const double*>(L), ld, rank, piv,
                                                         static_cast<const double*>(column),
                                                         static_cast<double*>(work), N);

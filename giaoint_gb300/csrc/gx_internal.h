@@ -213,9 +213,11 @@ cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const
 cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info, int nblocks,
                              const int* cand, int ncand, int nc, int nd, int n, void* const* dst, cudaStream_t s);
 cudaError_t launch_chol_scan(const double* res, long long N, void* partial, void* out, cudaStream_t s);
+// gemv_partials (max_chunks x n^2 values, may be null): splits the factor
+// update over rank chunks when that gives more blocks; sms: SM count.
 cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, long long piv, const void* column,
                              void* work, int n, double* res, double* scale, void* Lrow, void* partial, void* out,
-                             cudaStream_t s);
+                             cudaStream_t s, void* gemv_partials = nullptr, int max_chunks = 0, int sms = 0);
 cudaError_t launch_chol_final_residual(bool real, const double* D, const void* L, int rank, long long N, double* res,
                                        cudaStream_t s);
 size_t chol_red_bytes();
