@@ -647,6 +647,9 @@ def run_gpu(args):
                       "speedup_vs_fp64_exact": ms_ex / ms_mx, "clocks": clocks_mx},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value, "traffic": None,
+                         "traffic_note": "per-step DRAM bytes not captured (81 class launches over a 4.2 GB output); "
+                                         "per-class ncu captures: DRAM traffic is the packed output write plus a few "
+                                         "MB of reads (profiles/quartet_kernel_*)",
                          "kernel": "FP64 path (quartet_kernel + small_kernel launches of one step)",
                          "achieved_basis": "FP64 FLOP model per primitive quartet x primitive quartets evaluated "
                                            "(screened ones excluded) / event-timed FP64 step",
