@@ -41,6 +41,31 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GIAO ERIs/s & Cholesky time, mixed vs FP64 GPU @1e-10; p50/p99 req latency"
 UNIT = "ERIs/s"
 WORKLOAD = "12-atom s6 s1 s1 p3 p1 d1 molecule, seed 2026, |B|<=0.2, all 6722352 canonical quartets, complex128"
+DTYPE = "f64+f32 (mixed: FP32 primitive quartets under the cutoff, FP64 elsewhere and for every sum)"
+
+
+# DRAM bytes (read + write) of one plan execution, from an ncu capture of
+# every class launch of one step (dram__bytes_read.sum + dram__bytes_write.sum
+# summed over the launches; see the traffic basis); None until captured.
+TRAFFIC_PER_STEP: dict = {}
+TRAFFIC_BASIS = "not captured"
+
+
+def _measured_peaks() -> dict:
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+MEASURED = _measured_peaks()
+
+
+def config_block(natoms: int) -> dict:
+    """The workload description shared by both arms (same keys and values)."""
+    return {"workload": WORKLOAD if natoms == 12 else WORKLOAD.replace("12-atom", f"{natoms}-atom"),
+            "molecule_seed": 2026, "field": "seeded, |B| <= 0.2", "quartets": "all canonical",
+            "l2": "flushed (256 MB write) between timed GPU steps; the 4.2 GB output is also larger than L2"}
 
 
 def parse():
@@ -64,9 +89,15 @@ def parse():
     p.add_argument("--cholesky-only", action="store_true",
                    help="run only the Cholesky leg (no CPU port) and print its JSON (profiling)")
     p.add_argument("--serving-requests", type=int, default=32)
-    p.add_argument("--sweep", type=int, default=0,
+    p.add_argument("--profile-step", default="", choices=["", "fp64", "mixed", "fp64_exact"],
+                   help="run warm-up steps and one step of this mode inside an NVTX range, then exit (profiling)")
+    p.add_argument("--sweep", type=int, default=64,
                    help="field sweep: evaluate the molecule at this many fields |B| <= 0.5 in FP64 and mixed")
+    p.add_argument("--sweep-oracle-quartets", type=int, default=4000,
+                   help="seeded canonical quartets per sweep field compared with the CPU oracle")
     p.add_argument("--sweep-cholesky", type=int, default=2, help="fields of the sweep that also run Cholesky 1e-6")
+    p.add_argument("--sweep-cholesky-pivots", type=int, default=48,
+                   help="leading pivots of each sweep Cholesky compared with the CPU oracle's")
     return p.parse_args()
 
 
@@ -139,32 +170,119 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample_rate(recs, B, quartets, target_seconds: float, seed: int = 1):
-    """Oracle (CPU port of the reference) on a bounded seeded quartet sample."""
+def cpu_sample_rate(recs, B, quartets, target_seconds: float, seed: int = 1, threads: int | None = None,
+                    keep: bool = False):
+    """Oracle (CPU port of the reference) on a bounded seeded quartet sample.
+    With ``keep``, the sample's quartet indices and ERI values are returned
+    too (for the full-size parity check of the GPU outputs)."""
     from oracle import oracle as O
 
     orc = O.Oracle()
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     rng = np.random.default_rng(seed)
-    probe = quartets[np.sort(rng.choice(len(quartets), 2000, replace=False))]
+    probe_n = min(len(quartets), 2000 if threads > 1 else 300)
+    probe = quartets[np.sort(rng.choice(len(quartets), probe_n, replace=False))]
     t0 = time.perf_counter()
-    vals, _ = orc.eri_batch(recs, probe, B, None, threads)
-    rate = 2000 / max(time.perf_counter() - t0, 1e-6)
-    count = int(min(len(quartets), max(2000, rate * target_seconds)))
-    sample = quartets[np.sort(rng.choice(len(quartets), count, replace=False))]
+    orc.eri_batch(recs, probe, B, None, threads)
+    rate = probe_n / max(time.perf_counter() - t0, 1e-6)
+    count = int(min(len(quartets), max(probe_n, rate * target_seconds)))
+    idx = np.sort(rng.choice(len(quartets), count, replace=False))
     t0 = time.perf_counter()
-    vals, _ = orc.eri_batch(recs, sample, B, None, threads)
+    vals, _ = orc.eri_batch(recs, quartets[idx], B, None, threads)
     dt = time.perf_counter() - t0
-    return {"value": len(vals) / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{count} seeded canonical quartets ({len(vals)} ERIs) of the same molecule and field, "
-                      f"{dt:.2f} s on {threads} threads (oracle/giao_oracle.c, OpenMP)",
-            "quartets_per_s": count / dt}
+    out = {"value": len(vals) / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{count} seeded canonical quartets ({len(vals)} ERIs) of the same molecule and field, "
+                     f"{dt:.2f} s on {threads} threads (oracle/giao_oracle.c, OpenMP)",
+           "quartets_per_s": count / dt}
+    if keep:
+        return out, idx, vals
+    return out
 
 
-def cholesky_leg(gi, nat, ctx, run_cpu: bool):
+def gather_blocks(out_c, offsets, idx):
+    """Packed values of quartets ``idx`` (sorted indices into the plan's
+    quartet list) from the device output ``out_c`` (complex128), in order."""
+    import torch
+
+    starts = offsets[idx]
+    lens = offsets[idx + 1] - starts
+    firsts = np.concatenate(([0], np.cumsum(lens)[:-1]))
+    pos = np.repeat(starts - firsts, lens) + np.arange(int(lens.sum()), dtype=np.int64)
+    return out_c.index_select(0, torch.from_numpy(pos).to(out_c.device)).cpu().numpy()
+
+
+def pivot_agreement(recs, field_int, gpu_pivots, gpu_vectors, ref, threads: int, gap: float = 1e-10) -> dict:
+    """Pivots of the GPU factorisation against the oracle's: the common
+    prefix, and at the first divergence the residual-diagonal gap of the two
+    choices from the oracle's own factors (pivots must agree wherever that
+    gap exceeds 1e-10); the largest factor difference over the common prefix."""
+    from oracle import oracle as O
+
+    n = gpu_vectors.shape[1]
+    m = min(len(ref.pivots), len(gpu_pivots))
+    k = 0
+    while k < m and tuple(ref.pivots[k]) == tuple(gpu_pivots[k]):
+        k += 1
+    out = {"compared_pivots": m, "pivots_equal_prefix": k,
+           "max_abs_vector_diff_prefix": float(np.abs(gpu_vectors[:k] - ref.vectors[:k]).max()) if k else 0.0}
+    if k < m:
+        L = ref.vectors[:k].reshape(k, n * n)
+        pairs = [(a_, b_) for a_ in range(len(recs)) for b_ in range(a_, len(recs))]
+        diag = O.Oracle().cholesky_diagonal(recs, pairs, tuple(field_int), (0.0, 0.0, 0.0), threads).ravel()
+        rk = diag - (np.abs(L) ** 2).sum(axis=0)  # the residual diagonal before pivot k
+        a = int(ref.pivots[k][0]) * n + int(ref.pivots[k][1])
+        b = int(gpu_pivots[k][0]) * n + int(gpu_pivots[k][1])
+        out["first_divergence_residual_gap"] = float(abs(rk[a] - rk[b]))
+        out["first_divergence_is_tie"] = bool(abs(rk[a] - rk[b]) <= gap)
+    else:
+        out["first_divergence_is_tie"] = True
+    return out
+
+
+def reconstruction_error(res, basis, field, ctx, count: int = 24, seed: int = 11) -> float:
+    """Largest |(mu nu|lam sig) - sum_P L[P,mu,nu] conj(L[P,sig,lam])| over
+    seeded shell quartets, against FP64-exact GPU ERI blocks (size-independent
+    check: bounded by the final residual diagonal)."""
+    from giaoint_gb300.eri import _eri_batch
+
+    rng = np.random.default_rng(seed)
+    ns = len(basis.shells)
+    qs = rng.integers(0, ns, size=(count, 4))
+    _, shapes, offs, vals, _, _ = _eri_batch(basis, qs, field=field, precision="fp64_exact", context=ctx)
+    off = basis.ao_offsets
+    err = 0.0
+    for i, q in enumerate(qs):
+        sl = tuple(slice(off[x], off[x] + basis.shells[x].ao_count) for x in q)
+        blk = vals[offs[i]:offs[i + 1]].reshape(tuple(shapes[i]))
+        err = max(err, float(np.abs(res.reconstruct(sl) - blk).max()))
+    return err
+
+
+def cholesky_roofline(stats: dict, peak64: float) -> dict:
+    """Rooflines of one factorisation: the column evaluations against the
+    FP64 peak (FLOP model of the primitive quartets evaluated), the factor
+    update against HBM (algorithmic bytes: L read once per pivot) and FP64."""
+    col_s = stats["column_ms"] * 1e-3
+    upd_s = stats["update_ms"] * 1e-3
+    hbm = float(MEASURED.get("hbm_gbs") or 6800.0)
+    col_tf = stats["column_model_flops"] / col_s / 1e12 if col_s > 0 else 0.0
+    upd_gbs = stats["update_bytes"] / upd_s / 1e9 if upd_s > 0 else 0.0
+    upd_tf = stats["update_flops"] / upd_s / 1e12 if upd_s > 0 else 0.0
+    return {"columns": {"bound": "fp64", "achieved": col_tf, "peak": peak64, "unit": "TFLOP/s",
+                        "frac": col_tf / peak64 if peak64 else None, "ms": stats["column_ms"],
+                        "block_evaluations": stats["block_evaluations"]},
+            "update": {"bound": "hbm", "achieved": upd_gbs, "peak": hbm, "unit": "GB/s", "frac": upd_gbs / hbm,
+                       "fp64_tflops": upd_tf, "fp64_frac": upd_tf / peak64 if peak64 else None,
+                       "ms": stats["update_ms"], "bytes": stats["update_bytes"], "flops": stats["update_flops"],
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}}
+
+
+def cholesky_leg(gi, nat, ctx, run_cpu: bool, peak64: float):
     """Streamed pivoted Cholesky of the 140-AO atom (10s 8p 6d 4f 2g, ratio
     2.5 from 0.05) at B = (0, 0, 0.1), threshold 1e-8: device driver time,
-    rank and residual; the oracle port on all host cores beside it."""
+    rank, residual, rooflines of the column evaluations and the factor
+    update, and the reconstruction error on seeded blocks; the oracle port on
+    all host cores beside it with the pivot agreement."""
     from giaoint_gb300 import synthetic as syn
     from giaoint_gb300.cholesky import _cholesky_device
 
@@ -172,11 +290,15 @@ def cholesky_leg(gi, nat, ctx, run_cpu: bool):
     basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
     field = gi.MagneticField((0.0, 0.0, 0.1))
     _cholesky_device(basis, field, 1e-4, 0.0, None, 32, context=ctx)  # warm-up (pairs, plans, pools)
+    stats: dict = {}
     t0 = time.perf_counter()
-    res = _cholesky_device(basis, field, 1e-8, 0.0, None, 32, context=ctx)
+    res = _cholesky_device(basis, field, 1e-8, 0.0, None, 32, context=ctx, stats=stats)
     gpu_s = time.perf_counter() - t0
     out = {"workload": "140-AO atom 10s8p6d4f2g, B=(0,0,0.1), threshold 1e-8", "seconds": gpu_s,
-           "rank": int(len(res.pivots)), "max_residual_diagonal": res.max_residual_diagonal}
+           "rank": int(len(res.pivots)), "max_residual_diagonal": res.max_residual_diagonal,
+           "stats": stats, "roofline": cholesky_roofline(stats, peak64),
+           "update_gbs": stats["update_bytes"] / max(stats["update_ms"], 1e-9) / 1e6,
+           "reconstruction_max_abs_error": reconstruction_error(res, basis, field, ctx)}
     if run_cpu:
         from oracle import oracle as O
 
@@ -187,24 +309,44 @@ def cholesky_leg(gi, nat, ctx, run_cpu: bool):
         out["cpu_port_seconds"] = cpu_s
         out["cpu_port_threads"] = threads
         out["cpu_port_rank"] = int(len(ref.pivots))
-        k = 0
-        while k < min(len(ref.pivots), len(res.pivots)) and tuple(ref.pivots[k]) == tuple(res.pivots[k]):
-            k += 1
-        out["pivots_equal_prefix"] = k
-        if k < min(len(ref.pivots), len(res.pivots)):
-            # residual gap of the two choices at the first divergence, from the
-            # port's own factors: parity requires equal pivots only where it
-            # exceeds 1e-10 (a near tie otherwise)
-            n = res.vectors.shape[1]
-            L = ref.vectors[:k].reshape(k, n * n)
-            orc = O.Oracle()
-            pairs = [(a_, b_) for a_ in range(len(recs)) for b_ in range(a_, len(recs))]
-            diag = orc.cholesky_diagonal(recs, pairs, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), threads).ravel()
-            rk = diag - (np.abs(L) ** 2).sum(axis=0)  # the residual diagonal before pivot k
-            a = int(ref.pivots[k][0]) * n + int(ref.pivots[k][1])
-            b = int(res.pivots[k][0]) * n + int(res.pivots[k][1])
-            out["first_divergence_residual_gap"] = float(abs(rk[a] - rk[b]))
+        out["cpu_port_max_residual_diagonal"] = ref.max_residual_diagonal
+        # single centre: the oracle's diagonal at zero field
+        out.update(pivot_agreement(recs, (0.0, 0.0, 0.0), res.pivots, res.vectors, ref, threads))
         out["speedup_vs_cpu_port"] = cpu_s / gpu_s
+    return out
+
+
+def sweep_cholesky_leg(args, gi, ctx, fields, run_cpu: bool, peak64: float) -> list:
+    """Cholesky (threshold 1e-6) of the 12-atom molecule at the first sweep
+    fields: device time, rank, residual, rooflines and reconstruction error;
+    against the oracle port, the first ``--sweep-cholesky-pivots`` pivots and
+    factors (the oracle's full factorisation of this molecule takes minutes
+    per field on the host)."""
+    from giaoint_gb300.cholesky import _cholesky_device
+
+    recs, _ = workload(args.natoms, 0)
+    basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
+    out = []
+    for b in fields[: args.sweep_cholesky]:
+        field = gi.MagneticField(tuple(b))
+        stats: dict = {}
+        t0 = time.perf_counter()
+        res = _cholesky_device(basis, field, 1e-6, 0.0, None, 32, context=ctx, stats=stats)
+        rec = {"B": list(b), "threshold": 1e-6, "seconds": time.perf_counter() - t0, "rank": int(len(res.pivots)),
+               "max_residual_diagonal": res.max_residual_diagonal, "roofline": cholesky_roofline(stats, peak64),
+               "block_evaluations": stats["block_evaluations"],
+               "reconstruction_max_abs_error": reconstruction_error(res, basis, field, ctx)}
+        if run_cpu and args.sweep_cholesky_pivots > 0:
+            from oracle import oracle as O
+
+            threads = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            ref = O.cholesky_eri(O.Oracle(), recs, tuple(b), None, threshold=1e-6, threads=threads,
+                                 max_pivots=args.sweep_cholesky_pivots)
+            rec["cpu_port_prefix_seconds"] = time.perf_counter() - t0
+            rec["cpu_port_threads"] = threads
+            rec.update(pivot_agreement(recs, tuple(b), res.pivots, res.vectors, ref, threads))
+        out.append(rec)
     return out
 
 
@@ -346,21 +488,31 @@ def serving_leg(args):
     return out
 
 
-def sweep_leg(args, lib, nat, plan, outp, out, stream, torch, ctx):
-    """Field sweep on the same molecule: every field evaluated in FP64 and in
-    mixed precision through the plan; max |mixed - FP64| per field, and the
-    device Cholesky (threshold 1e-6) for the first fields."""
+def sweep_leg(args, lib, nat, plan, outp, out, stream, torch, ctx, recs, quartets, offsets, peak64: float,
+              run_cpu: bool):
+    """Field sweep on the same molecule (config 4): every field evaluated in
+    FP64 and in mixed precision through the plan (all 262.8M ERIs per field,
+    kept on the device); per field the times, max |mixed - FP64| over every
+    ERI, and max |GPU - oracle| of both modes on a seeded subset of canonical
+    quartets; then the Cholesky (1e-6) of the first fields."""
     from giaoint_gb300 import synthetic as syn
+    from oracle import oracle as O
 
     fields = syn.field_grid(args.sweep, 0.5)
     nat.check(lib.gx_context_set_stream(ctx.handle, ctypes.c_void_p(stream.cuda_stream)))
     ref = torch.empty_like(out)
+    out_c, ref_c = out.view(torch.complex128), ref.view(torch.complex128)
+    orc = O.Oracle() if run_cpu else None
+    threads = os.cpu_count() or 1
     per_field = []
     t64 = tmx = 0.0
     Ov = np.zeros(3)
+    nq = len(quartets)
     with torch.cuda.stream(stream):
         for k, b in enumerate(fields):
             Bv = np.ascontiguousarray(b, dtype=np.float64)
+            # the pair records of a new field are built outside the timed region
+            nat.check(lib.gx_eri_plan_execute(plan, nat.dptr(Bv), nat.dptr(Ov), 0, args.mixed_cutoff, outp))
             e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
             e[0].record(stream)
             nat.check(lib.gx_eri_plan_execute(plan, nat.dptr(Bv), nat.dptr(Ov), 0, args.mixed_cutoff, outp))
@@ -375,37 +527,53 @@ def sweep_leg(args, lib, nat, plan, outp, out, stream, torch, ctx):
             ms64, msmx = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
             t64 += ms64
             tmx += msmx
-            per_field.append({"B": list(b), "fp64_ms": ms64, "mixed_ms": msmx, "max_abs_err_mixed_vs_fp64": err})
+            rec = {"B": list(b), "B_norm": float(np.linalg.norm(b)), "fp64_ms": ms64, "mixed_ms": msmx,
+                   "max_abs_err_mixed_vs_fp64": err}
+            if orc is not None and args.sweep_oracle_quartets > 0:
+                rng = np.random.default_rng(500 + k)
+                idx = np.sort(rng.choice(nq, min(nq, args.sweep_oracle_quartets), replace=False))
+                vals, _ = orc.eri_batch(recs, quartets[idx], tuple(b), None, threads)
+                stream.synchronize()
+                rec["oracle_quartets"] = int(len(idx))
+                rec["max_abs_err_fp64_vs_oracle"] = float(np.abs(gather_blocks(ref_c, offsets, idx) - vals).max())
+                rec["max_abs_err_mixed_vs_oracle"] = float(np.abs(gather_blocks(out_c, offsets, idx) - vals).max())
+            per_field.append(rec)
     nat.check(lib.gx_context_synchronize(ctx.handle))
     nat.check(lib.gx_context_set_stream(ctx.handle, None))
-    out_d = {"fields": len(fields), "bmax": 0.5, "fp64_ms_total": t64, "mixed_ms_total": tmx,
+    del ref
+    eris = int(offsets[-1])
+    out_d = {"workload": "12-atom molecule (seed 2026) at 64 seeded fields |B| <= 0.5 sorted by |B|; all canonical "
+                         "quartets per field in FP64 and mixed (cutoff %g)" % args.mixed_cutoff,
+             "fields": len(fields), "bmax": 0.5, "fp64_ms_total": t64, "mixed_ms_total": tmx,
+             "fp64_eris_per_s": eris * len(fields) / (t64 * 1e-3), "mixed_eris_per_s": eris * len(fields) / (tmx * 1e-3),
              "speedup_mixed_vs_fp64": t64 / max(tmx, 1e-9),
              "max_abs_err_mixed_vs_fp64": max(f["max_abs_err_mixed_vs_fp64"] for f in per_field),
              "per_field": per_field}
+    if per_field and "max_abs_err_mixed_vs_oracle" in per_field[0]:
+        out_d["max_abs_err_mixed_vs_oracle"] = max(f["max_abs_err_mixed_vs_oracle"] for f in per_field)
+        out_d["max_abs_err_fp64_vs_oracle"] = max(f["max_abs_err_fp64_vs_oracle"] for f in per_field)
     if args.sweep_cholesky > 0:
         import giaoint_gb300 as gi
-        from giaoint_gb300.cholesky import _cholesky_device
 
-        recs, _ = workload(args.natoms, 0)
-        basis = gi.Basis([gi.Shell.from_record(r) for r in recs])
-        chol = []
-        for b in fields[: args.sweep_cholesky]:
-            t0 = time.perf_counter()
-            res = _cholesky_device(basis, gi.MagneticField(tuple(b)), 1e-6, 0.0, None, 32, context=ctx)
-            chol.append({"B": list(b), "seconds": time.perf_counter() - t0, "rank": int(len(res.pivots)),
-                         "max_residual_diagonal": res.max_residual_diagonal})
-        out_d["cholesky_1e-6"] = chol
+        out_d["cholesky_1e-6"] = sweep_cholesky_leg(args, gi, ctx, fields, run_cpu, peak64)
     return out_d
 
 
 def run_reference(args):
+    """The reference algorithm on the host cores: the oracle port (a C
+    restatement of the reference library) with all host threads, on a
+    bounded seeded sample of the same quartets per step.  Nothing of the GPU
+    library is loaded on this path."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    import giaoint_gb300 as gi
+    from giaoint_gb300 import synthetic as syn
+    from giaoint_gb300.replicas import field_for_rank
+    from oracle import oracle as O
 
-    recs, B = workload(args.natoms, 0)
-    quartets = gi.canonical_quartets(len(recs))
+    recs = syn.random_molecule(2026, natoms=args.natoms)
+    B = field_for_rank(0)
+    quartets = O.Oracle().canonical_quartets(len(recs))
     per_step = []
     info = None
     for i in range(args.warmup + args.steps):
@@ -415,8 +583,8 @@ def run_reference(args):
     value = float(statistics.mean(per_step))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": "fp64", "arm": "CPU reference algorithm"},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_block(args.natoms),
+            "arm": "CPU reference algorithm (oracle port of the reference library, FP64, every primitive quartet)",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
                              "sample": info["sample"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -439,7 +607,9 @@ def run_gpu(args):
     ctx = nat.Context(local)
     recs, B = workload(args.natoms, rank)
     if args.cholesky_only:
-        print(json.dumps({"cholesky": cholesky_leg(gi, nat, ctx, run_cpu=False)}), flush=True)
+        pk = ctypes.c_double()
+        nat.check(lib.gx_measure_fp64_peak(ctx.handle, ctypes.byref(pk)))
+        print(json.dumps({"cholesky": cholesky_leg(gi, nat, ctx, run_cpu=False, peak64=pk.value)}), flush=True)
         return
     if args.derivatives_only:
         quartets = gi.canonical_quartets(len(recs))
@@ -518,26 +688,50 @@ def run_gpu(args):
                                          ctypes.byref(f32)))
         return ms, clock_info, (n64.value, n32.value, f64.value, f32.value)
 
+    if args.profile_step:
+        # one step of one mode inside an NVTX range "step" (for an ncu capture
+        # of every class launch of the step: --nvtx --nvtx-include "step/")
+        prec = {"fp64": 0, "mixed": 1, "fp64_exact": 2}[args.profile_step]
+        if not args.no_autotune:
+            autotune(prec)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                step(prec)
+            torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push("step")
+            step(prec)
+            torch.cuda.nvtx.range_pop()
+            torch.cuda.synchronize()
+        nat.check(lib.gx_context_synchronize(ctx.handle))
+        print(json.dumps({"profile_step": args.profile_step, "classes": int(lib.gx_eri_plan_class_count(plan))}),
+              flush=True)
+        lib.gx_eri_plan_destroy(plan)
+        return
     ms_ex, clocks_ex, cnt_ex = timed(2)
     exact = out.clone()
     ms64, clocks64, cnt64 = timed(0)
     d64 = (out - exact).view(-1, 2)
     err64 = float(torch.sqrt((d64 * d64).sum(dim=1)).max().item())
     del d64
-    ref64 = out.clone()
+    fp64_out = out.clone()
     ms_mx, clocks_mx, cnt_mx = timed(1)
     diff = (out - exact).view(-1, 2)
     max_err = float(torch.sqrt((diff * diff).sum(dim=1)).max().item())
-    del diff, ref64, exact
+    del diff
+    mixed_out = out.clone()  # out is reused by the e2e leg
     headline_mixed = args.precision == "mixed"
     ms = ms_mx if headline_mixed else ms64
     clock_info = clocks_mx if headline_mixed else clocks64
     value = world * total / (ms * 1e-3)
-    # live FP64 roofline denominator
-    peak = ctypes.c_double()
+    # live roofline denominators: FP64 and FP32 FMA probes
+    peak, peak32 = ctypes.c_double(), ctypes.c_double()
     nat.check(lib.gx_measure_fp64_peak(ctx.handle, ctypes.byref(peak)))
+    nat.check(lib.gx_measure_fp32_peak(ctx.handle, ctypes.byref(peak32)))
     achieved64 = cnt64[2] / (ms64 * 1e-3) / 1e12
-    achieved = achieved64
+    # mixed: FLOPs_fp64 / (t P64) + FLOPs_fp32 / (t P32) (FLOP model per primitive quartet)
+    mx_tf64 = cnt_mx[2] / (ms_mx * 1e-3) / 1e12
+    mx_tf32 = cnt_mx[3] / (ms_mx * 1e-3) / 1e12
+    frac_mixed = mx_tf64 / peak.value + mx_tf32 / peak32.value
     prec = {"fp64": 0, "mixed": 1}[args.precision]
     # e2e through the host-buffer C ABI call (pinned host memory)
     e2e = None
@@ -602,15 +796,29 @@ def run_gpu(args):
                "call_seconds": times, "call_seconds_median": float(statistics.median(times)),
                "device_output_call_seconds": dev_times}
     cpu = None
+    parity = {"bar": {"fp64": 1e-12, "fp64_exact": 1e-12, "mixed": 1e-10}}
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_sample_rate(recs, B, quartets, target_seconds=10.0)
+        cpu, cpu_idx, cpu_vals = cpu_sample_rate(recs, B, quartets, target_seconds=10.0, keep=True)
+        # the same port on one thread (a smaller sample), the figure beside the all-core one
+        single = cpu_sample_rate(recs, B, quartets, target_seconds=4.0, seed=2, threads=1)
+        cpu["single_thread"] = {"value": single["value"], "cores": 1, "sample": single["sample"]}
+        # full-size parity: every mode's output against the oracle on the sample
+        for name, t in (("fp64_exact", exact), ("fp64", fp64_out), ("mixed", mixed_out)):
+            got = gather_blocks(t.view(torch.complex128), offsets, cpu_idx)
+            parity[name] = float(np.abs(got - cpu_vals).max())
+        parity["quartets"] = int(len(cpu_idx))
+        parity["eris"] = int(len(cpu_vals))
+        parity["ok"] = all(parity[k] <= parity["bar"][k] for k in ("fp64", "fp64_exact", "mixed"))
+        del cpu_vals
+    del exact, fp64_out, mixed_out
     sweep = None
     if args.sweep > 0:
-        sweep = sweep_leg(args, lib, nat, plan, outp, out, stream, torch, ctx)
+        sweep = sweep_leg(args, lib, nat, plan, outp, out, stream, torch, ctx, recs, quartets, offsets, peak.value,
+                          run_cpu=(rank == 0 and world == 1 and not args.no_cpu))
     chol = None
     if rank == 0 and not args.no_cholesky:
         nat.check(lib.gx_context_set_stream(ctx.handle, None))
-        chol = cholesky_leg(gi, nat, ctx, run_cpu=(world == 1 and not args.no_cpu))
+        chol = cholesky_leg(gi, nat, ctx, run_cpu=(world == 1 and not args.no_cpu), peak64=peak.value)
     full_tensor = None
     if rank == 0:
         nat.check(lib.gx_context_set_stream(ctx.handle, None))
@@ -627,12 +835,11 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "precision": args.precision, "quartets_per_step": nq,
-                       "eris_per_step": total, "primitive_quartets_per_step": int(nprim.value),
-                       "mixed_cutoff": args.mixed_cutoff,
-                       "parallelism": f"replicas{world} (one field per rank)", "l2": "flushed (256 MB write) "
-                       "between timed steps; the 4.2 GB output is also larger than L2"},
+            "vs_baseline": None, "dtype": DTYPE if headline_mixed else "f64", "data": "synthetic",
+            "config": config_block(args.natoms),
+            "run": {"precision": args.precision, "quartets_per_step": nq, "eris_per_step": total,
+                    "primitive_quartets_per_step": int(nprim.value), "mixed_cutoff": args.mixed_cutoff,
+                    "parallelism": f"replicas{world} (one field per rank)"},
             "quartets_per_s": world * nq / (ms * 1e-3),
             "fp64_exact": {"ms_per_step": ms_ex, "eris_per_s": world * total / (ms_ex * 1e-3),
                            "primitive_quartets_evaluated": cnt_ex[0], "clocks": clocks_ex,
@@ -645,16 +852,30 @@ def run_gpu(args):
                       "fp64_primitive_quartets": cnt_mx[0], "fp32_primitive_quartets": cnt_mx[1],
                       "max_abs_error_vs_fp64_exact": max_err, "speedup_vs_fp64": ms64 / ms_mx,
                       "speedup_vs_fp64_exact": ms_ex / ms_mx, "clocks": clocks_mx},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                         "frac": achieved / peak.value, "traffic": None,
-                         "traffic_note": "per-step DRAM bytes not captured (81 class launches over a 4.2 GB output); "
-                                         "per-class ncu captures: DRAM traffic is the packed output write plus a few "
-                                         "MB of reads (profiles/quartet_kernel_*)",
-                         "kernel": "FP64 path (quartet_kernel + small_kernel launches of one step)",
-                         "achieved_basis": "FP64 FLOP model per primitive quartet x primitive quartets evaluated "
-                                           "(screened ones excluded) / event-timed FP64 step",
+            "roofline": {"bound": "fp64", "unit": "TFLOP/s",
+                         # FP64-equivalent rate: FLOPs_fp64 + FLOPs_fp32 * P64 / P32 per second of the
+                         # headline step, so that achieved / peak is the two-term fraction
+                         "achieved": (frac_mixed if headline_mixed else achieved64 / peak.value) * peak.value,
+                         "peak": peak.value,
+                         "frac": frac_mixed if headline_mixed else achieved64 / peak.value,
+                         "terms": {"fp64": {"achieved": mx_tf64, "peak": peak.value,
+                                            "frac": mx_tf64 / peak.value, "flops": cnt_mx[2]},
+                                   "fp32": {"achieved": mx_tf32, "peak": peak32.value,
+                                            "frac": mx_tf32 / peak32.value, "flops": cnt_mx[3]}},
+                         "fp64_mode": {"achieved": achieved64, "frac": achieved64 / peak.value,
+                                       "ms_per_step": ms64},
+                         "traffic": TRAFFIC_PER_STEP.get(args.precision),
+                         "traffic_basis": TRAFFIC_BASIS,
+                         "kernel": "one plan execution: quartet_kernel + small_kernel launches of the 81 classes",
+                         "achieved_basis": "FLOP model per primitive quartet (reference-structured MD count) x "
+                                           "primitive quartets evaluated per precision / event-timed step; "
+                                           "frac = FLOPs_fp64/(t P64) + FLOPs_fp32/(t P32)",
                          "model_flops_all_primitive_quartets": model.value,
-                         "peak_source": "measured live: FP64 FMA-chain probe kernel (gx_measure_fp64_peak)"},
+                         "peak_source": "measured live: FP64 and FP32 FMA-chain probe kernels "
+                                        "(gx_measure_fp64_peak, gx_measure_fp32_peak); MEASURED_PEAKS.json holds "
+                                        "no FP64/FP32 CUDA-core peak",
+                         "peak32": peak32.value},
+            "parity": parity,
             # one kernel per (la, lb, lc, ld) class per step; the pair records
             # are computed once per field, before the timed steps
             "gpu_launches": int(lib.gx_eri_plan_class_count(plan)) * args.steps,
@@ -673,6 +894,9 @@ def run_gpu(args):
     lib.gx_eri_plan_destroy(plan)
     if world > 1:
         torch.distributed.destroy_process_group()
+    if rank == 0 and parity.get("ok") is False:
+        print(f"parity failure against the oracle sample: {parity}", file=sys.stderr, flush=True)
+        sys.exit(1)
 
 
 def main():

@@ -47,6 +47,27 @@ class GxCholeskyOptions(ctypes.Structure):
     ]
 
 
+class GxCholeskyStats(ctypes.Structure):
+    _fields_ = [
+        ("rank", ctypes.c_int64),
+        ("block_evaluations", ctypes.c_int64),
+        ("column_entries", ctypes.c_int64),
+        ("column_primitive_quartets", ctypes.c_int64),
+        ("diagonal_primitive_quartets", ctypes.c_int64),
+        ("column_cache_capacity", ctypes.c_int64),
+        ("column_model_flops", ctypes.c_double),
+        ("column_ms", ctypes.c_double),
+        ("update_ms", ctypes.c_double),
+        ("update_bytes", ctypes.c_double),
+        ("update_flops", ctypes.c_double),
+        ("column_pool_bytes", ctypes.c_double),
+        ("seconds", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class GxClassProfile(ctypes.Structure):
     _fields_ = [
         ("la", ctypes.c_int), ("lb", ctypes.c_int), ("lc", ctypes.c_int), ("ld", ctypes.c_int),
@@ -69,7 +90,7 @@ class GxClassProfile(ctypes.Structure):
 
 class GxClassConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in ("per_group", "warps_per_block", "batch", "kt", "ct", "min_blocks",
-                                                   "nostage", "stream")]
+                                                   "nostage", "stream", "nolane")]
 
 
 # name -> (restype, argtypes); every symbol of include/giao_gb300.h
@@ -110,6 +131,13 @@ SIGNATURES = {
     "gx_cholesky_diagonal": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
     "gx_cholesky_columns": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_int64, _d, _d, _d]),
     "gx_cholesky": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.POINTER(GxCholeskyOptions), _d, _i64, _i64, _d]),
+    "gx_cholesky_factor": (ctypes.c_int, [_vp, _vp, _d, _d, ctypes.POINTER(GxCholeskyOptions), ctypes.POINTER(_vp)]),
+    "gx_cholesky_factors_info": (ctypes.c_int, [_vp, _i64, _i64, _d, _i]),
+    "gx_cholesky_factors_copy": (ctypes.c_int, [_vp, _d, _i64]),
+    "gx_cholesky_factors_device": (_vp, [_vp]),
+    "gx_cholesky_factors_stats": (ctypes.c_int, [_vp, ctypes.POINTER(GxCholeskyStats)]),
+    "gx_cholesky_factors_destroy": (None, [_vp]),
+    "gx_cholesky_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(GxCholeskyStats)]),
     "gx_context_set_stream": (ctypes.c_int, [_vp, _vp]),
     "gx_context_synchronize": (ctypes.c_int, [_vp]),
     "gx_eri_plan_create": (ctypes.c_int, [_vp, _vp, _u32, ctypes.c_int64, _i64, ctypes.POINTER(_vp)]),
@@ -123,6 +151,7 @@ SIGNATURES = {
                                            ctypes.POINTER(GxClassProfile)]),
     "gx_eri_plan_autotune": (ctypes.c_int, [_vp, _d, _d, ctypes.c_int, ctypes.c_double, _vp, ctypes.c_int, _d, _d]),
     "gx_measure_fp64_peak": (ctypes.c_int, [_vp, _d]),
+    "gx_measure_fp32_peak": (ctypes.c_int, [_vp, _d]),
     "gx_canonical_quartets": (ctypes.c_int64, [ctypes.c_int, _u32]),
     "gx_cholesky_step_noalloc": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int, ctypes.c_int,
                                                 _vp, _vp, _vp, _vp]),

@@ -5,6 +5,7 @@
 // reference's error semantics.
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <limits>
 #include <cmath>
 #include <complex>
@@ -17,6 +18,7 @@
 #include <numeric>
 #include <string>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/giao_gb300.h"
@@ -190,6 +192,7 @@ struct gx_context {
     // scratch
     DeviceBuffer out, tasks, scratch_a, scratch_b, scratch_c;
     DeviceBuffer deriv_vals, deriv_meta;
+    gx_cholesky_stats last_cholesky{};  // of the last factorisation on this context
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -490,12 +493,14 @@ struct ClassConf {
     int minb = 0;       // generic kernel: register-budget variant (2 or 4 resident blocks; 0 = 2)
     int nostage = 0;    // generic kernel: 1 = read E~ records and class tables from global memory
     int stream = 0;     // generic kernel: 1 = per-entry recurrences into a two-column buffer (stream mode)
+    int nolane = 0;     // 1 = the generic kernel also takes the FP32 entries (no FP32 lane kernel)
 };
 
 // Warp work units of every class: (first task within the class, task count).
 struct GroupSet {
     DeviceBuffer dev;
     std::vector<std::pair<size_t, size_t>> range;  // per class: first group, count
+    std::vector<std::pair<size_t, size_t>> lane;   // per class: groups of the FP32 lane kernel (count 0: none)
 };
 
 struct PlanData {
@@ -586,10 +591,11 @@ void record_tuning(const gx_context* ctx, const gx_basis* b, int precision, cons
 // generic kernel about `per_group` (default 32) primitive quartets and at
 // most 1024 tasks per unit, fewer tasks when the class is too small to give
 // every SM eight warps.
-std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_t ci, const ClassConf& conf) {
+std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_t ci, const ClassConf& conf,
+                              bool lane_units = false) {
     const PlanClass& pc = plan.classes[ci];
-    const bool small = gx::small_class(pc.key[0], pc.key[1], pc.key[2], pc.key[3]);
-    const int per = conf.per_group > 0 ? conf.per_group : (small ? 1024 : 32);
+    const bool small = lane_units || gx::small_class(pc.key[0], pc.key[1], pc.key[2], pc.key[3]);
+    const int per = lane_units ? 1024 : (conf.per_group > 0 ? conf.per_group : (small ? 1024 : 32));
     const int spread = std::max<int>(1, (int)(pc.count / (size_t)(8 * std::max(ctx->sm_count, 1))));
     std::vector<int2> groups;
     size_t i = pc.first;
@@ -607,12 +613,27 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
     return groups;
 }
 
+bool lane_class(const PlanClass& pc) { return gx::lane32_class(pc.key[0], pc.key[1], pc.key[2], pc.key[3]); }
+
+// Work units of every class, and for the classes with an FP32 lane kernel its
+// units (one lane per primitive quartet: up to 1024 primitive quartets and 128
+// tasks per warp), in one device array.
 void make_group_set(gx_context* ctx, const PlanData& plan, const std::vector<ClassConf>& conf, GroupSet& out) {
     std::vector<int2> all;
     out.range.clear();
+    out.lane.clear();
     for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
         const auto g = make_groups(ctx, plan, ci, conf[ci]);
         out.range.push_back({all.size(), g.size()});
+        all.insert(all.end(), g.begin(), g.end());
+    }
+    for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
+        if (!lane_class(plan.classes[ci])) {
+            out.lane.push_back({0, 0});
+            continue;
+        }
+        const auto g = make_groups(ctx, plan, ci, conf[ci], true);
+        out.lane.push_back({all.size(), g.size()});
         all.insert(all.end(), g.begin(), g.end());
     }
     upload(out.dev, all, ctx->stream);
@@ -732,7 +753,8 @@ gx::EriDev make_dev(gx_context* ctx, gx_basis* b, FieldPairs& fp, double2* out, 
 // optional pointers.
 void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t ci, const ClassConf& conf,
                   const int2* groups, int ngroup, unsigned long long* counters, cudaStream_t s, int* used_b1 = nullptr,
-                  int* used_wpb = nullptr, int* used_tiles = nullptr) {
+                  int* used_wpb = nullptr, int* used_tiles = nullptr, const int2* lane_groups = nullptr,
+                  int nlane = 0) {
     const auto& pc = plan.classes[ci];
     const auto& k = pc.key;
     dev.counters = counters ? counters + 2 * ci : nullptr;
@@ -748,7 +770,7 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
         if (used_wpb) *used_wpb = 4;
         return;
     }
-    gx::QuartetClass qc;
+    gx::QuartetClass qc{};
     qc.bra = ctx->pair_class(k[0], k[1]).dev();
     qc.ket = ctx->pair_class(k[2], k[3]).dev();
     qc.L = k[0] + k[1] + k[2] + k[3];
@@ -834,7 +856,21 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     const int cap = conf.wpb > 0 ? std::min(4, conf.wpb) : 4;
     const int wpb = (int)std::max<size_t>(1, std::min<size_t>(cap, (200 * 1024) / per_warp));
     const int grid = (int)std::min<long long>(((long long)qc.ngroup * qc.nchunk + wpb - 1) / wpb, 1 << 30);
+    // mixed precision: the FP32 entries of a 3 <= L <= 4 class go to the FP32
+    // lane kernel, launched after this one on the same stream
+    const bool lane = dev.fp32_cut > 0.0f && lane_groups && nlane > 0 && !conf.nolane &&
+                      gx::lane32_class(k[0], k[1], k[2], k[3]);
+    qc.no32 = lane ? 1 : 0;
     GX_CUDA(gx::launch_quartets(dev, qc, wpb, grid, s));
+    if (lane) {
+        gx::QuartetClass lq{};
+        lq.L = qc.L;
+        lq.ntask = qc.ntask;
+        lq.tasks = qc.tasks;
+        lq.ngroup = nlane;
+        lq.groups = lane_groups;
+        GX_CUDA(gx::launch_lane32(k[0], k[1], k[2], k[3], dev, lq, s));
+    }
     if (used_b1) *used_b1 = B1;
     if (used_wpb) *used_wpb = wpb;
     if (used_tiles) {
@@ -847,14 +883,15 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
 // Enqueue the pair records for (B, O) and every class launch; no host sync
 // unless the field changed (the pair bounds are sorted on the host).  Uses
 // the autotuned configuration of the precision mode when there is one.
-// counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null.
+// counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null;
+// zeroed first unless `accumulate`.
 int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
                  double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
-                 unsigned long long* counters = nullptr) {
+                 unsigned long long* counters = nullptr, bool accumulate = false) {
     cudaStream_t s = ctx->stream;
     FieldPairs& fp = field_pairs(b, B, O);
     const gx::EriDev dev = make_dev(ctx, b, fp, out, precision, mixed_cutoff);
-    if (counters) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
+    if (counters && !accumulate) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
     ctx->reset_status();
     const auto& tuned = plan.tuned[precision];
     const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
@@ -882,7 +919,8 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
         for (size_t ci = 0; ci < nc; ++ci)
             launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters,
-                         ctx->aux[ci % K]);
+                         ctx->aux[ci % K], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
+                         (int)gs.lane[ci].second);
         for (int k = 0; k < K; ++k) {
             GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
             GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
@@ -890,7 +928,8 @@ int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O,
     } else {
         for (size_t ci = 0; ci < nc; ++ci)
             launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
-                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s);
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, nullptr,
+                         nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first, (int)gs.lane[ci].second);
     }
     return 1 + (int)nc;
 }
@@ -2266,7 +2305,7 @@ struct CholRed {
 };
 
 // Device column slots shared by the current candidate batch and the raw-column
-// LRU (python/giao_integrals/cholesky.py:180-265).
+// cache (python/giao_integrals/cholesky.py:180-265).
 struct ColumnPool {
     DeviceBuffer buf;
     size_t col_bytes = 0;
@@ -2294,6 +2333,544 @@ struct ColumnPool {
     void* ptr(int s) const { return static_cast<char*>(buf.ptr) + (size_t)s * col_bytes; }
 };
 
+// Least-recently-inserted key set with the assignment semantics of a Python
+// OrderedDict: inserting a present key keeps its position.
+struct KeyOrder {
+    std::list<int64_t> order;
+    std::unordered_map<int64_t, std::list<int64_t>::iterator> pos;
+    bool contains(int64_t k) const { return pos.count(k) != 0; }
+    void insert(int64_t k) {
+        if (!contains(k)) pos[k] = order.insert(order.end(), k);
+    }
+    void erase(int64_t k) {
+        auto it = pos.find(k);
+        if (it == pos.end()) return;
+        order.erase(it->second);
+        pos.erase(it);
+    }
+    void trim(size_t cap) {
+        while (order.size() > cap) {
+            pos.erase(order.front());
+            order.pop_front();
+        }
+    }
+};
+
+}  // namespace
+
+// Factors of one pivoted Cholesky, resident on the device until destroyed.
+struct gx_cholesky_factors {
+    gx_context* ctx = nullptr;
+    DeviceBuffer L;              // rank rows of n*n (float64 on the real path, complex128 otherwise)
+    int64_t cap_rows = 0;
+    std::vector<int64_t> pivots;  // 2 * rank
+    int64_t n = 0, rank = 0;
+    bool real = false;
+    double max_residual = 0.0;
+    gx_cholesky_stats stats{};
+};
+
+namespace {
+
+// The pivot loop of python/giao_integrals/cholesky.py:60-297 on the device:
+// residual diagonal, argmax (lowest flat index on ties), column generation,
+// factor update and PSD check stay resident; the host sees one reduction
+// record per pivot.  The factor rows grow in f.L (doubling) up to `limit`.
+void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double* Of, const gx_cholesky_options* opt,
+                   gx_cholesky_factors& f) {
+    const auto wall0 = std::chrono::steady_clock::now();
+    const double threshold = opt->threshold, screening = opt->screening_threshold;
+    if (!std::isfinite(threshold) || threshold < 0.0) raise(GX_EINVAL, "threshold must be finite and non-negative");
+    if (!std::isfinite(screening) || screening < 0.0)
+        raise(GX_EINVAL, "screening_threshold must be finite and non-negative");
+    if (opt->pivot_batch_size < 1) raise(GX_EINVAL, "pivot_batch_size must be a positive integer");
+    GX_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int ns = b->ns;
+    const int64_t n = b->nao, N = n * n;
+    gx_cholesky_stats& stats = f.stats;
+    stats = gx_cholesky_stats{};
+    f.ctx = ctx;
+    f.n = n;
+    f.rank = 0;
+    f.max_residual = 0.0;
+    f.pivots.clear();
+    if (n == 0) return;
+    // single centre: the London phase cancels; use zero-field integrals (cholesky.py:130-133)
+    bool single = true;
+    for (int s = 1; s < ns; ++s)
+        for (int k = 0; k < 3; ++k) single = single && b->center[3 * s + k] == b->center[k];
+    const double zero3[3] = {0.0, 0.0, 0.0};
+    const double* iB = single ? zero3 : Bf;
+    const double* iO = single ? zero3 : Of;
+    const bool real = (Bf[0] == 0.0 && Bf[1] == 0.0 && Bf[2] == 0.0) || single;
+    f.real = real;
+    const size_t esz = real ? sizeof(double) : sizeof(double2);
+    std::vector<int> owner(n);
+    for (int s = 0; s < ns; ++s)
+        for (int64_t i = b->ao_off[s]; i < b->ao_off[s] + b->nao_of(s); ++i) owner[i] = s;
+
+    // event timing of the column evaluations and of the factor update
+    struct EventPair {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~EventPair() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev_col, ev_upd;
+    GX_CUDA(cudaEventCreate(&ev_col.a));
+    GX_CUDA(cudaEventCreate(&ev_col.b));
+    GX_CUDA(cudaEventCreate(&ev_upd.a));
+    GX_CUDA(cudaEventCreate(&ev_upd.b));
+    bool col_pending = false, upd_pending = false;
+    auto collect_times = [&] {  // after a stream synchronisation
+        float ms = 0.0f;
+        if (col_pending) {
+            GX_CUDA(cudaEventElapsedTime(&ms, ev_col.a, ev_col.b));
+            stats.column_ms += ms;
+            col_pending = false;
+        }
+        if (upd_pending) {
+            GX_CUDA(cudaEventElapsedTime(&ms, ev_upd.a, ev_upd.b));
+            stats.update_ms += ms;
+            upd_pending = false;
+        }
+    };
+
+    // ---- diagonal (with optional Schwarz skip of initial blocks) ----
+    DeviceBuffer d_D, d_res, d_partial, d_red, d_scale, d_work, d_boff, d_info, d_cand, d_dst;
+    d_D.reserve(N * sizeof(double));
+    d_res.reserve(N * sizeof(double));
+    d_partial.reserve(gx::chol_partial_bytes());
+    d_red.reserve(gx::chol_red_bytes());
+    d_scale.reserve(sizeof(double));
+    GX_CUDA(cudaMemsetAsync(d_D.ptr, 0, N * sizeof(double), st));
+    std::vector<double> q;
+    if (screening > 0.0) q = schwarz_values(ctx, b, iB, iO);
+    std::vector<std::pair<int, int>> measured, skipped;
+    std::vector<double> skip_fill;
+    for (int a = 0; a < ns; ++a)
+        for (int c = a; c < ns; ++c) {
+            const double qq = screening > 0.0 ? q[(size_t)a * ns + c] * q[(size_t)a * ns + c] : 0.0;
+            if (screening > 0.0 && qq <= std::min(threshold, screening)) {
+                skipped.push_back({a, c});
+                skip_fill.push_back(qq);
+            } else {
+                measured.push_back({a, c});
+            }
+        }
+    auto read_diagonal = [&](const std::vector<std::pair<int, int>>& pairs, double* target) {
+        if (pairs.empty()) return;
+        std::vector<QuartetRequest> req;
+        std::vector<long long> boff;
+        std::vector<int> info;
+        int64_t off = 0;
+        for (const auto& pr : pairs) {
+            const uint32_t a = pr.first, c = pr.second;
+            req.push_back({a, c, c, a, off});
+            boff.push_back(off);
+            info.insert(info.end(), {(int)b->ao_off[a], (int)b->ao_off[c], (int)b->nao_of(a), (int)b->nao_of(c)});
+            off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
+        }
+        ctx->scratch_a.reserve(off * sizeof(double2));
+        PlanData dplan;
+        build_plan(ctx, b, req, dplan);
+        int64_t evaluated[2] = {0, 0};
+        run_plan(ctx, b, iB, iO, dplan, ctx->scratch_a.as<double2>(), nullptr, nullptr, GX_PRECISION_FP64, 0.0,
+                 evaluated);
+        stats.diagonal_primitive_quartets += evaluated[0];
+        upload(d_boff, boff, st);
+        upload(d_info, info, st);
+        GX_CUDA(gx::launch_chol_diag(ctx->scratch_a.as<double2>(), d_boff.as<long long>(), d_info.as<int>(),
+                                     (int)pairs.size(), (int)n, target, st));
+    };
+    read_diagonal(measured, d_D.as<double>());
+    if (!skipped.empty()) {
+        std::vector<double> D(N);
+        GX_CUDA(cudaMemcpyAsync(D.data(), d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        for (size_t k = 0; k < skipped.size(); ++k) {
+            const int a = skipped[k].first, c = skipped[k].second;
+            for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
+                for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) {
+                    D[i * n + j] = skip_fill[k];
+                    D[j * n + i] = skip_fill[k];
+                }
+        }
+        GX_CUDA(cudaMemcpyAsync(d_D.ptr, D.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    GX_CUDA(cudaMemcpyAsync(d_res.ptr, d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CholRed red;
+    int status_code = 0;
+    auto fetch_red = [&] {
+        // the reduction result and the kernels' status word in one wait (a
+        // failure in a column batch is reported before the next pivot)
+        GX_CUDA(cudaMemcpyAsync(&red, d_red.ptr, sizeof red, cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaMemcpyAsync(&status_code, ctx->status.ptr, sizeof status_code, cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        collect_times();
+        if (status_code) check_status(ctx);
+    };
+    GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
+    fetch_red();
+    const double floor = 64 * 2.220446049250313e-16 * std::max(red.maxv, 0.0);
+    const double tol = std::max(threshold, floor);
+    const int64_t limit = std::min<int64_t>(N, opt->max_rank);
+
+    // ---- pivot loop ----
+    bool reuse = !single;
+    for (int s = 0; s < ns; ++s) reuse = reuse || b->ncontr[s] > 1 || b->nprim[s] > 1;
+    // The local block rule of complex contracted systems (cholesky.py:195-206).
+    const bool local_rule = reuse && !real && opt->pivot_batch_size > 1;
+    // Columns kept per pivot-block evaluation: the evaluation computes every
+    // column of the pivot's shell-pair block, and raw columns are exact
+    // whenever they are computed, so keeping more of them (and the raw-column
+    // cache below) changes only how often a block is evaluated.  Pivots are
+    // decided by the reference's own candidate and cache state, tracked
+    // separately (ref_* below) when its local rule is in force.
+    constexpr int kBatchColumns = 256;
+    const size_t col_bytes = N * esz;
+    int cache_cap = 1024;
+    {
+        // the raw-column cache only saves re-evaluations: fit it into half of
+        // the free device memory left after the first factor rows
+        size_t free_b = 0, total_b = 0;
+        GX_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const int64_t first_rows = std::min<int64_t>(std::max<int64_t>(limit, 1), std::max<int64_t>(64, 8 * n));
+        const double room = (double)free_b * 0.5 - (double)first_rows * col_bytes - 8.0 * col_bytes;
+        const int64_t fit = (int64_t)(room / (double)col_bytes) - kBatchColumns - 64;
+        cache_cap = (int)std::max<int64_t>(0, std::min<int64_t>(1024, fit));
+    }
+    ColumnPool pool;
+    pool.init(kBatchColumns + cache_cap + 64, col_bytes);
+    stats.column_cache_capacity = cache_cap;
+    d_work.reserve(col_bytes);
+    constexpr int kGemvChunks = 8;  // rank chunks of the factor update (partial sums)
+    DeviceBuffer d_gemv;
+    d_gemv.reserve((size_t)kGemvChunks * col_bytes);
+    f.cap_rows = std::min<int64_t>(std::max<int64_t>(limit, 1), std::max<int64_t>(64, 8 * n));
+    f.L.reserve((size_t)f.cap_rows * col_bytes);
+    std::vector<int64_t> cands;               // current batch candidates (flat indices)
+    std::vector<int> cand_slot;               // their column slots
+    std::list<std::pair<int64_t, int>> lru;   // raw-column cache, oldest first
+    std::map<int64_t, std::list<std::pair<int64_t, int>>::iterator> lru_pos;
+    // the reference's candidate batch, block candidates and raw-column cache keys
+    std::vector<int64_t> ref_cands, block_cands;
+    KeyOrder ref_cache;
+    std::vector<double> hostblk;
+    // Column evaluation of one pivot shell pair: its plan, block offsets and
+    // primitive-quartet counters (accumulated over its evaluations).
+    struct ColumnPlan {
+        PlanData plan;
+        DeviceBuffer boff, counters;
+        int nblocks = 0;
+        int64_t entries = 0;
+    };
+    std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
+    DeviceBuffer column_info;
+    {
+        // largest column batch: all (x, y) blocks against the largest pivot pair
+        int64_t sum_xy = 0, max_ao = 0;
+        for (int x = 0; x < ns; ++x) {
+            max_ao = std::max<int64_t>(max_ao, b->nao_of(x));
+            for (int y = real ? x : 0; y < ns; ++y) sum_xy += b->nao_of(x) * b->nao_of(y);
+        }
+        ctx->scratch_a.reserve(std::max<int64_t>(sum_xy * max_ao * max_ao, 1) * sizeof(double2));
+    }
+    int64_t rank = 0;
+    auto residual_at = [&](const std::vector<int64_t>& idx, std::vector<double>& vals) {
+        vals.resize(idx.size());
+        for (size_t k = 0; k < idx.size(); ++k)
+            GX_CUDA(cudaMemcpyAsync(&vals[k], d_res.as<double>() + idx[k], sizeof(double), cudaMemcpyDeviceToHost,
+                                    st));
+        GX_CUDA(cudaStreamSynchronize(st));
+    };
+    auto drop_batch = [&] {
+        for (int s : cand_slot) pool.release(s);
+        cands.clear();
+        cand_slot.clear();
+    };
+    // Residual of the pivot's shell-pair block on the host (one strided 2-D
+    // copy) and the reference's candidate list: the contraction variants of
+    // the pivot (reuse) or the whole block, above the tolerance, largest
+    // residual first (stable), at most `count`, the pivot forced in
+    // (cholesky.py:225-242).
+    int blk_a = -1, blk_c = -1;
+    int64_t blk_rank = -1;
+    auto load_block = [&](int64_t pivot) {
+        const int64_t mu = pivot / n, nu = pivot % n;
+        const int a = owner[mu], c = owner[nu];
+        if (a == blk_a && c == blk_c && blk_rank == rank) return;
+        const int64_t na = b->nao_of(a), nc = b->nao_of(c);
+        hostblk.resize(na * nc);
+        GX_CUDA(cudaMemcpy2DAsync(hostblk.data(), nc * sizeof(double),
+                                  d_res.as<double>() + b->ao_off[a] * n + b->ao_off[c], n * sizeof(double),
+                                  nc * sizeof(double), na, cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        blk_a = a;
+        blk_c = c;
+        blk_rank = rank;
+    };
+    auto rv = [&](int64_t f_) {
+        return hostblk[(f_ / n - b->ao_off[blk_a]) * b->nao_of(blk_c) + (f_ % n - b->ao_off[blk_c])];
+    };
+    auto reference_candidates = [&](int64_t pivot, int count) {
+        load_block(pivot);
+        const int a = blk_a, c = blk_c;
+        const int64_t mu = pivot / n, nu = pivot % n;
+        std::vector<int64_t> idx;
+        if (reuse) {
+            const int ca = b->ncart_of(a), cc = b->ncart_of(c);
+            for (int xa = 0; xa < b->ncontr[a]; ++xa)
+                for (int xc = 0; xc < b->ncontr[c]; ++xc)
+                    idx.push_back((b->ao_off[a] + (mu - b->ao_off[a]) % ca + (int64_t)ca * xa) * n + b->ao_off[c] +
+                                  (nu - b->ao_off[c]) % cc + (int64_t)cc * xc);
+        } else {
+            for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
+                for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) idx.push_back(i * n + j);
+        }
+        std::vector<int64_t> keep;
+        for (int64_t x : idx)
+            if (rv(x) > tol) keep.push_back(x);
+        std::stable_sort(keep.begin(), keep.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
+        if ((int)keep.size() > count) keep.resize(count);
+        if (std::find(keep.begin(), keep.end(), pivot) == keep.end()) {
+            if (keep.empty())
+                keep.push_back(pivot);
+            else
+                keep.back() = pivot;
+        }
+        return keep;
+    };
+    while (red.maxv > tol) {
+        int64_t pivot = red.idx;
+        if (local_rule && !block_cands.empty()) {
+            std::vector<double> v;
+            residual_at(block_cands, v);
+            size_t best = 0;
+            for (size_t k = 1; k < v.size(); ++k)
+                if (v[k] > v[best]) best = k;
+            if (v[best] > tol && v[best] >= 0.01 * red.maxv) pivot = block_cands[best];
+        }
+        if (rank >= limit) {
+            f.rank = rank;
+            stats.rank = rank;
+            raise(GX_ENOMEM, "Cholesky rank capacity exceeded");
+        }
+        if (rank >= f.cap_rows) {
+            // grow the factor rows (doubling, at most `limit`)
+            const int64_t cap2 = std::min<int64_t>(limit, 2 * f.cap_rows);
+            DeviceBuffer grown;
+            grown.reserve((size_t)cap2 * col_bytes);
+            GX_CUDA(cudaMemcpyAsync(grown.ptr, f.L.ptr, (size_t)rank * col_bytes, cudaMemcpyDeviceToDevice, st));
+            GX_CUDA(cudaStreamSynchronize(st));
+            std::swap(grown.ptr, f.L.ptr);
+            std::swap(grown.bytes, f.L.bytes);
+            f.cap_rows = cap2;
+        }
+        // The reference's state decides the local rule's candidates: a pivot
+        // found in its raw-column cache replaces its batch by the pivot alone;
+        // a pivot outside its batch makes it evaluate the pivot's block, whose
+        // contraction variants become the block candidates and enter its cache
+        // (capacity min(1024, max(8, rank + 8))).
+        if (local_rule) {
+            if (ref_cache.contains(pivot)) {
+                ref_cands.assign(1, pivot);
+                ref_cache.erase(pivot);
+            }
+            if (std::find(ref_cands.begin(), ref_cands.end(), pivot) == ref_cands.end()) {
+                ref_cands = reference_candidates(pivot, 32);
+                block_cands.assign(ref_cands.begin(),
+                                   ref_cands.begin() + std::min<size_t>(ref_cands.size(),
+                                                                        std::min(32, opt->pivot_batch_size)));
+                for (int64_t x : ref_cands)
+                    if (x != pivot) ref_cache.insert(x);
+                ref_cache.trim((size_t)std::min<int64_t>(1024, std::max<int64_t>(8, rank + 8)));
+            }
+            ref_cache.erase(pivot);
+        }
+        // Physical supply of the raw column: the current batch, the raw-column
+        // cache, or a new evaluation of the pivot's block.
+        auto cached = lru_pos.find(pivot);
+        if (cached != lru_pos.end() &&
+            std::find(cands.begin(), cands.end(), pivot) == cands.end()) {
+            const int slot = cached->second->second;
+            lru.erase(cached->second);
+            lru_pos.erase(cached);
+            drop_batch();
+            cands.push_back(pivot);
+            cand_slot.push_back(slot);  // cache reference moves to the batch
+        }
+        auto it = std::find(cands.begin(), cands.end(), pivot);
+        if (it == cands.end()) {
+            const int64_t mu = pivot / n, nu = pivot % n;
+            const int a = owner[mu], c = owner[nu];
+            std::vector<int64_t> keep = reference_candidates(pivot, reuse ? 32 : kBatchColumns);
+            {
+                // the evaluation computes every column of the block: keep the
+                // other entries above the threshold too (largest residual
+                // first) for the raw-column cache
+                std::vector<int64_t> extra;
+                const int64_t na = b->nao_of(a), nc = b->nao_of(c);
+                for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + na; ++i)
+                    for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + nc; ++j) {
+                        const int64_t fl = i * n + j;
+                        if (rv(fl) > tol && std::find(keep.begin(), keep.end(), fl) == keep.end()) extra.push_back(fl);
+                    }
+                std::stable_sort(extra.begin(), extra.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
+                const size_t room = keep.size() < (size_t)kBatchColumns ? kBatchColumns - keep.size() : 0;
+                if (extra.size() > room) extra.resize(room);
+                keep.insert(keep.end(), extra.begin(), extra.end());
+            }
+            drop_batch();
+            cands = keep;
+            // columns (mu nu | p1 p0) for all shell pairs (real: b >= a).  The
+            // quartet list, its plan and block offsets depend only on the
+            // pivot shell pair: built once per factorisation and reused.
+            const int sa = a, sb = c;
+            auto& cp = column_plans[{sa, sb}];
+            if (!cp) {
+                cp = std::make_unique<ColumnPlan>();
+                std::vector<QuartetRequest> req;
+                std::vector<long long> boff;
+                int64_t off = 0;
+                for (int x = 0; x < ns; ++x)
+                    for (int y = real ? x : 0; y < ns; ++y) {
+                        req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
+                        boff.push_back(off);
+                        off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
+                    }
+                build_plan(ctx, b, req, cp->plan);
+                upload(cp->boff, boff, st);
+                cp->nblocks = (int)req.size();
+                cp->entries = off;
+                cp->counters.reserve(std::max<size_t>(2 * cp->plan.classes.size(), 2) * sizeof(unsigned long long));
+                GX_CUDA(cudaMemsetAsync(cp->counters.ptr, 0, cp->counters.bytes, st));
+            }
+            if (column_info.ptr == nullptr) {
+                std::vector<int> info;
+                for (int x = 0; x < ns; ++x)
+                    for (int y = real ? x : 0; y < ns; ++y)
+                        info.insert(info.end(), {(int)b->ao_off[x], (int)b->ao_off[y], (int)b->nao_of(x),
+                                                 (int)b->nao_of(y), x == y ? 1 : 0});
+                upload(column_info, info, st);
+            }
+            std::vector<int> cl;
+            std::vector<void*> dst;
+            for (int64_t fl : cands) {
+                cl.push_back((int)(fl % n - b->ao_off[sb]));  // c: p1 within sb
+                cl.push_back((int)(fl / n - b->ao_off[sa]));  // d: p0 within sa
+                const int slot = pool.take();
+                cand_slot.push_back(slot);
+                dst.push_back(pool.ptr(slot));
+            }
+            upload(d_cand, cl, st);
+            upload(d_dst, dst, st);
+            GX_CUDA(cudaEventRecord(ev_col.a, st));
+            execute_plan(ctx, b, iB, iO, cp->plan, ctx->scratch_a.as<double2>(), GX_PRECISION_FP64, 0.0,
+                         cp->counters.as<unsigned long long>(), /*accumulate=*/true);
+            GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), cp->boff.as<long long>(),
+                                         column_info.as<int>(), cp->nblocks, d_cand.as<int>(), (int)cands.size(),
+                                         (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
+            GX_CUDA(cudaEventRecord(ev_col.b, st));
+            col_pending = true;
+            ++stats.block_evaluations;
+            stats.column_entries += (int64_t)cands.size() * N;
+            for (size_t k = 0; k < cands.size(); ++k) {
+                if (cands[k] == pivot) continue;
+                // assignment to an existing key keeps its position (OrderedDict semantics)
+                auto old = lru_pos.find(cands[k]);
+                pool.retain(cand_slot[k]);
+                if (old != lru_pos.end()) {
+                    pool.release(old->second->second);
+                    old->second->second = cand_slot[k];
+                } else {
+                    lru.push_back({cands[k], cand_slot[k]});
+                    lru_pos[cands[k]] = std::prev(lru.end());
+                }
+            }
+            while (lru.size() > (size_t)cache_cap) {
+                pool.release(lru.front().second);
+                lru_pos.erase(lru.front().first);
+                lru.pop_front();
+            }
+            it = std::find(cands.begin(), cands.end(), pivot);
+        }
+        {
+            auto c2it = lru_pos.find(pivot);
+            if (c2it != lru_pos.end()) {
+                pool.release(c2it->second->second);
+                lru.erase(c2it->second);
+                lru_pos.erase(c2it);
+            }
+        }
+        const int slot = cand_slot[it - cands.begin()];
+        void* Lrow = static_cast<char*>(f.L.ptr) + (size_t)rank * col_bytes;
+        GX_CUDA(cudaEventRecord(ev_upd.a, st));
+        GX_CUDA(gx::launch_chol_step(real, f.L.ptr, N, (int)rank, pivot, pool.ptr(slot), d_work.ptr, (int)n,
+                                     d_res.as<double>(), d_scale.as<double>(), Lrow, d_partial.ptr, d_red.ptr, st,
+                                     d_gemv.ptr, kGemvChunks, ctx->sm_count));
+        GX_CUDA(cudaEventRecord(ev_upd.b, st));
+        upd_pending = true;
+        // algorithmic work of the step: L read once (rank rows), the raw
+        // column read, the new row written, the residual read and written
+        stats.update_bytes += (double)col_bytes * (rank + 2) + 16.0 * N;
+        stats.update_flops += (real ? 2.0 : 8.0) * (double)rank * N;
+        fetch_red();
+        f.pivots.push_back(pivot / n);
+        f.pivots.push_back(pivot % n);
+        ++rank;
+        if (red.minv < -std::max(floor * 16, 1e-12))
+            raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
+    }
+    double final_max = std::max(red.maxv, 0.0);
+    if (!skipped.empty()) {
+        read_diagonal(skipped, d_D.as<double>());
+        GX_CUDA(gx::launch_chol_final_residual(real, d_D.as<double>(), f.L.ptr, (int)rank, N, d_res.as<double>(),
+                                               st));
+        GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
+        fetch_red();
+        final_max = std::max(red.maxv, 0.0);
+    }
+    // primitive quartets of the column evaluations and their FP64 FLOP model
+    for (const auto& kv : column_plans) {
+        const ColumnPlan& cp = *kv.second;
+        std::vector<unsigned long long> c(2 * cp.plan.classes.size());
+        if (c.empty()) continue;
+        GX_CUDA(cudaMemcpyAsync(c.data(), cp.counters.ptr, c.size() * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < cp.plan.classes.size(); ++i) {
+            stats.column_primitive_quartets += (int64_t)c[2 * i];
+            stats.column_model_flops += (double)c[2 * i] * cp.plan.classes[i].flops_per_primitive_quartet;
+        }
+    }
+    f.rank = rank;
+    f.max_residual = final_max;
+    stats.rank = rank;
+    stats.column_pool_bytes = (double)pool.capacity * col_bytes;
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+}
+
+// Factor rows [0, rank) as complex128 into host memory.
+void copy_factors(const gx_cholesky_factors& f, double* vectors) {
+    if (!f.rank) return;
+    cudaStream_t st = f.ctx->stream;
+    const int64_t N = f.n * f.n;
+    if (f.real) {
+        std::vector<double> tmp(f.rank * N);
+        GX_CUDA(cudaMemcpyAsync(tmp.data(), f.L.ptr, f.rank * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+        for (int64_t j = 0; j < f.rank * N; ++j) {
+            vectors[2 * j] = tmp[j];
+            vectors[2 * j + 1] = 0.0;
+        }
+    } else {
+        GX_CUDA(cudaMemcpyAsync(vectors, f.L.ptr, f.rank * N * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaStreamSynchronize(st));
+    }
+}
+
 }  // namespace
 
 extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const double* Of,
@@ -2302,354 +2879,89 @@ extern "C" int gx_cholesky(gx_context* ctx, gx_basis* b, const double* Bf, const
     return guarded([&] {
         if (!ctx || !b || !opt) raise(GX_EINVAL, "null context, basis or options");
         check_field(Bf, Of);
-        const double threshold = opt->threshold, screening = opt->screening_threshold;
-        if (!std::isfinite(threshold) || threshold < 0.0) raise(GX_EINVAL, "threshold must be finite and non-negative");
-        if (!std::isfinite(screening) || screening < 0.0)
-            raise(GX_EINVAL, "screening_threshold must be finite and non-negative");
-        if (opt->pivot_batch_size < 1) raise(GX_EINVAL, "pivot_batch_size must be a positive integer");
-        std::lock_guard<std::mutex> lock(ctx->mu);
-        GX_CUDA(cudaSetDevice(ctx->device));
-        cudaStream_t st = ctx->stream;
-        const int ns = b->ns;
-        const int64_t n = b->nao, N = n * n;
         *rank_out = 0;
         *max_residual = 0.0;
-        if (n == 0) return;
-        // single centre: the London phase cancels; use zero-field integrals (cholesky.py:130-133)
-        bool single = true;
-        for (int s = 1; s < ns; ++s)
-            for (int k = 0; k < 3; ++k) single = single && b->center[3 * s + k] == b->center[k];
-        const double zero3[3] = {0.0, 0.0, 0.0};
-        const double* iB = single ? zero3 : Bf;
-        const double* iO = single ? zero3 : Of;
-        const bool real = (Bf[0] == 0.0 && Bf[1] == 0.0 && Bf[2] == 0.0) || single;
-        const size_t esz = real ? sizeof(double) : sizeof(double2);
-        std::vector<int> owner(n);
-        for (int s = 0; s < ns; ++s)
-            for (int64_t i = b->ao_off[s]; i < b->ao_off[s] + b->nao_of(s); ++i) owner[i] = s;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        gx_cholesky_factors f;
+        try {
+            cholesky_core(ctx, b, Bf, Of, opt, f);
+        } catch (const ApiError&) {
+            *rank_out = f.rank;
+            ctx->last_cholesky = f.stats;
+            throw;
+        }
+        ctx->last_cholesky = f.stats;
+        copy_factors(f, vectors);
+        std::copy(f.pivots.begin(), f.pivots.end(), pivots_out);
+        *rank_out = f.rank;
+        *max_residual = f.max_residual;
+    });
+}
 
-        // ---- diagonal (with optional Schwarz skip of initial blocks) ----
-        DeviceBuffer d_D, d_res, d_partial, d_red, d_scale, d_work, d_L, d_boff, d_info, d_cand, d_dst;
-        d_D.reserve(N * sizeof(double));
-        d_res.reserve(N * sizeof(double));
-        d_partial.reserve(gx::chol_partial_bytes());
-        d_red.reserve(gx::chol_red_bytes());
-        d_scale.reserve(sizeof(double));
-        GX_CUDA(cudaMemsetAsync(d_D.ptr, 0, N * sizeof(double), st));
-        std::vector<double> q;
-        if (screening > 0.0) q = schwarz_values(ctx, b, iB, iO);
-        std::vector<std::pair<int, int>> measured, skipped;
-        std::vector<double> skip_fill;
-        for (int a = 0; a < ns; ++a)
-            for (int c = a; c < ns; ++c) {
-                const double qq = screening > 0.0 ? q[(size_t)a * ns + c] * q[(size_t)a * ns + c] : 0.0;
-                if (screening > 0.0 && qq <= std::min(threshold, screening)) {
-                    skipped.push_back({a, c});
-                    skip_fill.push_back(qq);
-                } else {
-                    measured.push_back({a, c});
-                }
-            }
-        auto read_diagonal = [&](const std::vector<std::pair<int, int>>& pairs, double* target) {
-            if (pairs.empty()) return;
-            std::vector<QuartetRequest> req;
-            std::vector<long long> boff;
-            std::vector<int> info;
-            int64_t off = 0;
-            for (const auto& pr : pairs) {
-                const uint32_t a = pr.first, c = pr.second;
-                req.push_back({a, c, c, a, off});
-                boff.push_back(off);
-                info.insert(info.end(), {(int)b->ao_off[a], (int)b->ao_off[c], (int)b->nao_of(a), (int)b->nao_of(c)});
-                off += b->nao_of(a) * b->nao_of(c) * b->nao_of(c) * b->nao_of(a);
-            }
-            ctx->scratch_a.reserve(off * sizeof(double2));
-            run_quartets(ctx, b, iB, iO, req, ctx->scratch_a.as<double2>(), nullptr);
-            upload(d_boff, boff, st);
-            upload(d_info, info, st);
-            GX_CUDA(gx::launch_chol_diag(ctx->scratch_a.as<double2>(), d_boff.as<long long>(), d_info.as<int>(),
-                                         (int)pairs.size(), (int)n, target, st));
-        };
-        read_diagonal(measured, d_D.as<double>());
-        if (!skipped.empty()) {
-            std::vector<double> D(N);
-            GX_CUDA(cudaMemcpyAsync(D.data(), d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, st));
-            GX_CUDA(cudaStreamSynchronize(st));
-            for (size_t k = 0; k < skipped.size(); ++k) {
-                const int a = skipped[k].first, c = skipped[k].second;
-                for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
-                    for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) {
-                        D[i * n + j] = skip_fill[k];
-                        D[j * n + i] = skip_fill[k];
-                    }
-            }
-            GX_CUDA(cudaMemcpyAsync(d_D.ptr, D.data(), N * sizeof(double), cudaMemcpyHostToDevice, st));
+extern "C" int gx_cholesky_factor(gx_context* ctx, gx_basis* b, const double* Bf, const double* Of,
+                                  const gx_cholesky_options* opt, gx_cholesky_factors** out) {
+    return guarded([&] {
+        if (!ctx || !b || !opt || !out) raise(GX_EINVAL, "null context, basis, options or output");
+        *out = nullptr;
+        check_field(Bf, Of);
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        auto f = std::make_unique<gx_cholesky_factors>();
+        try {
+            cholesky_core(ctx, b, Bf, Of, opt, *f);
+        } catch (const ApiError&) {
+            ctx->last_cholesky = f->stats;  // its rank: the rows reached when a capacity ran out
+            throw;
         }
-        GX_CUDA(cudaMemcpyAsync(d_res.ptr, d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        CholRed red;
-        int status_code = 0;
-        auto fetch_red = [&] {
-            // the reduction result and the kernels' status word in one wait (a
-            // failure in a column batch is reported before the next pivot)
-            GX_CUDA(cudaMemcpyAsync(&red, d_red.ptr, sizeof red, cudaMemcpyDeviceToHost, st));
-            GX_CUDA(cudaMemcpyAsync(&status_code, ctx->status.ptr, sizeof status_code, cudaMemcpyDeviceToHost, st));
-            GX_CUDA(cudaStreamSynchronize(st));
-            if (status_code) check_status(ctx);
-        };
-        GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
-        fetch_red();
-        const double floor = 64 * 2.220446049250313e-16 * std::max(red.maxv, 0.0);
-        const double tol = std::max(threshold, floor);
-        const int64_t limit = std::min<int64_t>(N, opt->max_rank);
+        ctx->last_cholesky = f->stats;
+        *out = f.release();
+    });
+}
 
-        // ---- pivot loop ----
-        bool reuse = !single;
-        for (int s = 0; s < ns; ++s) reuse = reuse || b->ncontr[s] > 1 || b->nprim[s] > 1;
-        // Columns kept per pivot-block evaluation.  The evaluation computes
-        // every column of the pivot's shell-pair block; without the
-        // contracted-variant rule the pivot is always the global argmax, so
-        // keeping more of them (and the raw-column cache below) changes only
-        // how often a block is evaluated, never a result.
-        const int candidate_count = reuse ? 32 : 256;
-        ColumnPool pool;
-        pool.init(256 + 1024 + 64, N * esz);
-        d_work.reserve(N * esz);
-        constexpr int kGemvChunks = 8;  // rank chunks of the factor update (partial sums)
-        DeviceBuffer d_gemv;
-        d_gemv.reserve((size_t)kGemvChunks * N * esz);
-        d_L.reserve(std::max<int64_t>(limit, 1) * N * esz);
-        std::vector<int64_t> cands;               // current batch candidates (flat indices)
-        std::vector<int> cand_slot;               // their column slots
-        std::vector<int64_t> block_cands;         // local block-pivot candidates
-        std::list<std::pair<int64_t, int>> lru;   // raw-column cache, oldest first
-        std::map<int64_t, std::list<std::pair<int64_t, int>>::iterator> lru_pos;
-        std::vector<double> hostblk;
-        // Column evaluation of one pivot shell pair: its plan and block offsets.
-        struct ColumnPlan {
-            PlanData plan;
-            DeviceBuffer boff;
-            int nblocks = 0;
-            int64_t entries = 0;
-        };
-        std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
-        DeviceBuffer column_info;
-        {
-            // largest column batch: all (x, y) blocks against the largest pivot pair
-            int64_t sum_xy = 0, max_ao = 0;
-            for (int x = 0; x < ns; ++x) {
-                max_ao = std::max<int64_t>(max_ao, b->nao_of(x));
-                for (int y = real ? x : 0; y < ns; ++y) sum_xy += b->nao_of(x) * b->nao_of(y);
-            }
-            ctx->scratch_a.reserve(std::max<int64_t>(sum_xy * max_ao * max_ao, 1) * sizeof(double2));
-        }
-        int64_t rank = 0;
-        auto residual_at = [&](const std::vector<int64_t>& idx, std::vector<double>& vals) {
-            vals.resize(idx.size());
-            for (size_t k = 0; k < idx.size(); ++k)
-                GX_CUDA(cudaMemcpyAsync(&vals[k], d_res.as<double>() + idx[k], sizeof(double), cudaMemcpyDeviceToHost,
-                                        st));
-            GX_CUDA(cudaStreamSynchronize(st));
-        };
-        auto drop_batch = [&] {
-            for (int s : cand_slot) pool.release(s);
-            cands.clear();
-            cand_slot.clear();
-        };
-        while (red.maxv > tol) {
-            int64_t pivot = red.idx;
-            if (reuse && !real && opt->pivot_batch_size > 1 && !block_cands.empty()) {
-                std::vector<double> v;
-                residual_at(block_cands, v);
-                size_t best = 0;
-                for (size_t k = 1; k < v.size(); ++k)
-                    if (v[k] > v[best]) best = k;
-                if (v[best] > tol && v[best] >= 0.01 * red.maxv) pivot = block_cands[best];
-            }
-            if (rank >= limit) {
-                *rank_out = rank;
-                raise(GX_ENOMEM, "Cholesky rank capacity exceeded");
-            }
-            auto cached = lru_pos.find(pivot);
-            if (cached != lru_pos.end()) {
-                const int slot = cached->second->second;
-                lru.erase(cached->second);
-                lru_pos.erase(cached);
-                drop_batch();
-                cands.push_back(pivot);
-                cand_slot.push_back(slot);  // cache reference moves to the batch
-            }
-            auto it = std::find(cands.begin(), cands.end(), pivot);
-            if (it == cands.end()) {
-                const int64_t mu = pivot / n, nu = pivot % n;
-                const int a = owner[mu], c = owner[nu];
-                std::vector<int64_t> idx;
-                if (reuse) {
-                    const int ca = b->ncart_of(a), cc = b->ncart_of(c);
-                    for (int xa = 0; xa < b->ncontr[a]; ++xa)
-                        for (int xc = 0; xc < b->ncontr[c]; ++xc)
-                            idx.push_back((b->ao_off[a] + (mu - b->ao_off[a]) % ca + (int64_t)ca * xa) * n +
-                                          b->ao_off[c] + (nu - b->ao_off[c]) % cc + (int64_t)cc * xc);
-                } else {
-                    for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + b->nao_of(a); ++i)
-                        for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + b->nao_of(c); ++j) idx.push_back(i * n + j);
-                }
-                // residual on the block: one strided 2-D copy
-                const int64_t na = b->nao_of(a), nc = b->nao_of(c);
-                hostblk.resize(na * nc);
-                GX_CUDA(cudaMemcpy2DAsync(hostblk.data(), nc * sizeof(double),
-                                          d_res.as<double>() + b->ao_off[a] * n + b->ao_off[c], n * sizeof(double),
-                                          nc * sizeof(double), na, cudaMemcpyDeviceToHost, st));
-                GX_CUDA(cudaStreamSynchronize(st));
-                auto rv = [&](int64_t f) {
-                    return hostblk[(f / n - b->ao_off[a]) * nc + (f % n - b->ao_off[c])];
-                };
-                std::vector<int64_t> keep;
-                for (int64_t f : idx)
-                    if (rv(f) > tol) keep.push_back(f);
-                std::stable_sort(keep.begin(), keep.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
-                if ((int)keep.size() > candidate_count) keep.resize(candidate_count);
-                if (std::find(keep.begin(), keep.end(), pivot) == keep.end()) {
-                    if (keep.empty())
-                        keep.push_back(pivot);
-                    else
-                        keep.back() = pivot;
-                }
-                block_cands.assign(keep.begin(), keep.begin() + std::min<size_t>(keep.size(),
-                                                                                 std::min(32, opt->pivot_batch_size)));
-                if (reuse) {
-                    // the evaluation below computes every column of the block:
-                    // keep the other entries above the threshold too (largest
-                    // residual first) for the raw-column cache; the pivot rule
-                    // above uses only the contraction variants
-                    std::vector<int64_t> extra;
-                    for (int64_t i = b->ao_off[a]; i < b->ao_off[a] + na; ++i)
-                        for (int64_t j = b->ao_off[c]; j < b->ao_off[c] + nc; ++j) {
-                            const int64_t f = i * n + j;
-                            if (rv(f) > tol && std::find(keep.begin(), keep.end(), f) == keep.end())
-                                extra.push_back(f);
-                        }
-                    std::stable_sort(extra.begin(), extra.end(), [&](int64_t x, int64_t y) { return rv(x) > rv(y); });
-                    const size_t room = keep.size() < 256 ? 256 - keep.size() : 0;
-                    if (extra.size() > room) extra.resize(room);
-                    keep.insert(keep.end(), extra.begin(), extra.end());
-                }
-                drop_batch();
-                cands = keep;
-                // columns (mu nu | p1 p0) for all shell pairs (real: b >= a).  The
-                // quartet list, its plan and block offsets depend only on the
-                // pivot shell pair: built once per factorisation and reused.
-                const int sa = a, sb = c;
-                auto& cp = column_plans[{sa, sb}];
-                if (!cp) {
-                    cp = std::make_unique<ColumnPlan>();
-                    std::vector<QuartetRequest> req;
-                    std::vector<long long> boff;
-                    int64_t off = 0;
-                    for (int x = 0; x < ns; ++x)
-                        for (int y = real ? x : 0; y < ns; ++y) {
-                            req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
-                            boff.push_back(off);
-                            off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
-                        }
-                    build_plan(ctx, b, req, cp->plan);
-                    upload(cp->boff, boff, st);
-                    cp->nblocks = (int)req.size();
-                    cp->entries = off;
-                }
-                if (column_info.ptr == nullptr) {
-                    std::vector<int> info;
-                    for (int x = 0; x < ns; ++x)
-                        for (int y = real ? x : 0; y < ns; ++y)
-                            info.insert(info.end(), {(int)b->ao_off[x], (int)b->ao_off[y], (int)b->nao_of(x),
-                                                     (int)b->nao_of(y), x == y ? 1 : 0});
-                    upload(column_info, info, st);
-                }
-                execute_plan(ctx, b, iB, iO, cp->plan, ctx->scratch_a.as<double2>(), GX_PRECISION_FP64, 0.0, nullptr);
-                std::vector<int> cl;
-                std::vector<void*> dst;
-                for (int64_t f : cands) {
-                    cl.push_back((int)(f % n - b->ao_off[sb]));  // c: p1 within sb
-                    cl.push_back((int)(f / n - b->ao_off[sa]));  // d: p0 within sa
-                    const int slot = pool.take();
-                    cand_slot.push_back(slot);
-                    dst.push_back(pool.ptr(slot));
-                }
-                upload(d_cand, cl, st);
-                upload(d_dst, dst, st);
-                GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), cp->boff.as<long long>(),
-                                             column_info.as<int>(), cp->nblocks, d_cand.as<int>(), (int)cands.size(),
-                                             (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
-                {
-                    for (size_t k = 0; k < cands.size(); ++k) {
-                        if (cands[k] == pivot) continue;
-                        // assignment to an existing key keeps its LRU position (OrderedDict semantics)
-                        auto old = lru_pos.find(cands[k]);
-                        pool.retain(cand_slot[k]);
-                        if (old != lru_pos.end()) {
-                            pool.release(old->second->second);
-                            old->second->second = cand_slot[k];
-                        } else {
-                            lru.push_back({cands[k], cand_slot[k]});
-                            lru_pos[cands[k]] = std::prev(lru.end());
-                        }
-                    }
-                    // raw columns are exact whenever they were computed, so the
-                    // cache size changes only how often a block is evaluated
-                    const size_t cap = 1024;
-                    while (lru.size() > cap) {
-                        pool.release(lru.front().second);
-                        lru_pos.erase(lru.front().first);
-                        lru.pop_front();
-                    }
-                }
-                it = std::find(cands.begin(), cands.end(), pivot);
-            }
-            {
-                auto c2it = lru_pos.find(pivot);
-                if (c2it != lru_pos.end()) {
-                    pool.release(c2it->second->second);
-                    lru.erase(c2it->second);
-                    lru_pos.erase(c2it);
-                }
-            }
-            const int slot = cand_slot[it - cands.begin()];
-            void* Lrow = static_cast<char*>(d_L.ptr) + (size_t)rank * N * esz;
-            GX_CUDA(gx::launch_chol_step(real, d_L.ptr, N, (int)rank, pivot, pool.ptr(slot), d_work.ptr, (int)n,
-                                         d_res.as<double>(), d_scale.as<double>(), Lrow, d_partial.ptr, d_red.ptr,
-                                         st, d_gemv.ptr, kGemvChunks, ctx->sm_count));
-            fetch_red();
-            pivots_out[2 * rank] = pivot / n;
-            pivots_out[2 * rank + 1] = pivot % n;
-            ++rank;
-            if (red.minv < -std::max(floor * 16, 1e-12))
-                raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
-        }
-        double final_max = std::max(red.maxv, 0.0);
-        if (!skipped.empty()) {
-            read_diagonal(skipped, d_D.as<double>());
-            GX_CUDA(gx::launch_chol_final_residual(real, d_D.as<double>(), d_L.ptr, (int)rank, N, d_res.as<double>(),
-                                                   st));
-            GX_CUDA(gx::launch_chol_scan(d_res.as<double>(), N, d_partial.ptr, d_red.ptr, st));
-            fetch_red();
-            final_max = std::max(red.maxv, 0.0);
-        }
-        // factors out as complex128
-        if (rank) {
-            if (real) {
-                std::vector<double> tmp(rank * N);
-                GX_CUDA(cudaMemcpyAsync(tmp.data(), d_L.ptr, rank * N * sizeof(double), cudaMemcpyDeviceToHost, st));
-                GX_CUDA(cudaStreamSynchronize(st));
-                for (int64_t j = 0; j < rank * N; ++j) {
-                    vectors[2 * j] = tmp[j];
-                    vectors[2 * j + 1] = 0.0;
-                }
-            } else {
-                GX_CUDA(cudaMemcpyAsync(vectors, d_L.ptr, rank * N * sizeof(double2), cudaMemcpyDeviceToHost, st));
-                GX_CUDA(cudaStreamSynchronize(st));
-            }
-        }
-        *rank_out = rank;
-        *max_residual = final_max;
+extern "C" int gx_cholesky_factors_info(const gx_cholesky_factors* f, int64_t* rank, int64_t* nao,
+                                        double* max_residual, int* real) {
+    return guarded([&] {
+        if (!f) raise(GX_EINVAL, "null factors");
+        if (rank) *rank = f->rank;
+        if (nao) *nao = f->n;
+        if (max_residual) *max_residual = f->max_residual;
+        if (real) *real = f->real ? 1 : 0;
+    });
+}
+
+extern "C" int gx_cholesky_factors_copy(const gx_cholesky_factors* f, double* vectors, int64_t* pivots) {
+    return guarded([&] {
+        if (!f) raise(GX_EINVAL, "null factors");
+        std::lock_guard<std::mutex> lock(f->ctx->mu);
+        GX_CUDA(cudaSetDevice(f->ctx->device));
+        if (vectors) copy_factors(*f, vectors);
+        if (pivots) std::copy(f->pivots.begin(), f->pivots.end(), pivots);
+    });
+}
+
+extern "C" const void* gx_cholesky_factors_device(const gx_cholesky_factors* f) { return f ? f->L.ptr : nullptr; }
+
+extern "C" int gx_cholesky_factors_stats(const gx_cholesky_factors* f, gx_cholesky_stats* out) {
+    return guarded([&] {
+        if (!f || !out) raise(GX_EINVAL, "null factors or output");
+        *out = f->stats;
+    });
+}
+
+extern "C" void gx_cholesky_factors_destroy(gx_cholesky_factors* f) {
+    if (!f) return;
+    if (f->ctx) {
+        std::lock_guard<std::mutex> lock(f->ctx->mu);
+        cudaSetDevice(f->ctx->device);
+        f->L.release();
+    }
+    delete f;
+}
+
+extern "C" int gx_cholesky_last_stats(gx_context* ctx, gx_cholesky_stats* out) {
+    return guarded([&] {
+        if (!ctx || !out) raise(GX_EINVAL, "null context or output");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        *out = ctx->last_cholesky;
     });
 }
 
@@ -2859,7 +3171,7 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
         for (size_t ci = 0; ci < nc; ++ci) {
             launch_class(ctx, dev, pd, ci, tuned.valid ? tuned.conf[ci] : ClassConf{},
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, &b1[ci],
-                         &wpb[ci], &tiles[3 * ci]);
+                         &wpb[ci], &tiles[3 * ci], gs.dev.as<int2>() + gs.lane[ci].first, (int)gs.lane[ci].second);
             GX_CUDA(cudaEventRecord(ev[ci + 1], s));
         }
         GX_CUDA(cudaEventSynchronize(ev[nc]));
@@ -2903,7 +3215,7 @@ int gx_eri_plan_get_config(gx_eri_plan* plan, int precision, gx_class_config* ou
         const auto& tuned = pd.tuned[precision];
         for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
             const ClassConf c = tuned.valid ? tuned.conf[ci] : ClassConf{};
-            out[ci] = gx_class_config{c.per_group, c.wpb, c.b1, c.kt, c.ct, c.minb, c.nostage, c.stream};
+            out[ci] = gx_class_config{c.per_group, c.wpb, c.b1, c.kt, c.ct, c.minb, c.nostage, c.stream, c.nolane};
         }
     });
 }
@@ -2922,10 +3234,10 @@ int gx_eri_plan_set_config(gx_eri_plan* plan, int precision, const gx_class_conf
             if (c.per_group < 0 || c.warps_per_block < 0 || c.warps_per_block > 4 || c.batch < 0 || c.batch > 32 ||
                 (c.kt != 0 && c.kt != 1 && c.kt != 2 && c.kt != 4) || c.ct < 0 || c.ct > 4 ||
                 (c.min_blocks != 0 && c.min_blocks != 2 && c.min_blocks != 4) || (c.nostage != 0 && c.nostage != 1) ||
-                (c.stream != 0 && c.stream != 1))
+                (c.stream != 0 && c.stream != 1) || (c.nolane != 0 && c.nolane != 1))
                 raise(GX_EINVAL, "class configuration out of range");
             conf[ci] = ClassConf{c.per_group, c.warps_per_block, c.batch, c.kt, c.ct, c.min_blocks, c.nostage,
-                                 c.stream};
+                                 c.stream, c.nolane};
         }
         auto& tuned = pd.tuned[precision];
         make_group_set(ctx, pd, conf, tuned.groups);
@@ -2974,12 +3286,20 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
             }
             double best_ms = 0.0, def_ms = 0.0;
             auto time_conf = [&](const ClassConf& cf) {
-                const auto groups = make_groups(ctx, pd, ci, cf);
+                auto groups = make_groups(ctx, pd, ci, cf);
+                const int ngroup = (int)groups.size();
+                int nlane = 0;
+                if (lane_class(pd.classes[ci])) {
+                    const auto lg = make_groups(ctx, pd, ci, cf, true);
+                    nlane = (int)lg.size();
+                    groups.insert(groups.end(), lg.begin(), lg.end());
+                }
                 upload(tmp, groups, s);
                 double t = 1e30;
                 for (int r = 0; r <= repeats; ++r) {  // first launch warms caches
                     GX_CUDA(cudaEventRecord(e0, s));
-                    launch_class(ctx, dev, pd, ci, cf, tmp.as<int2>(), (int)groups.size(), nullptr, s);
+                    launch_class(ctx, dev, pd, ci, cf, tmp.as<int2>(), ngroup, nullptr, s, nullptr, nullptr, nullptr,
+                                 tmp.as<int2>() + ngroup, nlane);
                     GX_CUDA(cudaEventRecord(e1, s));
                     GX_CUDA(cudaEventSynchronize(e1));
                     float ms = 0.0f;
@@ -3056,6 +3376,16 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
                             }
                         }
             }
+            if (precision == GX_PRECISION_MIXED && lane_class(pd.classes[ci])) {
+                // fifth stage: the FP32 entries in the generic kernel instead of the lane kernel
+                ClassConf cf = best[ci];
+                cf.nolane = 1;
+                const double t = time_conf(cf);
+                if (t < 0.97 * best_ms) {
+                    best_ms = t;
+                    best[ci] = cf;
+                }
+            }
             tot_default += def_ms;
             tot_best += best_ms;
         }
@@ -3111,6 +3441,18 @@ int gx_measure_fp64_peak(gx_context* ctx, double* tflops) {
         float ms = 0.f;
         double flops = 0.0;
         GX_CUDA(gx::run_fp64_probe(ctx->sm_count, ctx->stream, &ms, &flops));
+        *tflops = flops / (ms * 1e-3) / 1e12;
+    });
+}
+
+int gx_measure_fp32_peak(gx_context* ctx, double* tflops) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        float ms = 0.f;
+        double flops = 0.0;
+        GX_CUDA(gx::run_fp32_probe(ctx->sm_count, ctx->stream, &ms, &flops));
         *tflops = flops / (ms * 1e-3) / 1e12;
     });
 }

@@ -84,6 +84,7 @@ struct QuartetClass {
     int KT, CT;            // Hermite rows per lane in the ket transform, ket components per lane in the bra transform
     int stream;            // 1: phase 1 keeps only the seeds of the batch; each entry's R is built by the warp
                            //    into a two-column buffer right before its ket transform (small shared footprint)
+    int no32;              // 1: leave the FP32 entries of a mixed-precision pass to the FP32 lane kernel
     int ntask;
     const Task* tasks;
     int ngroup;
@@ -203,6 +204,12 @@ cudaError_t launch_deriv_contract(const DerivContractArgs& args, int sms, cudaSt
 cudaError_t launch_gather_abs(const double2* src, const long long* idx, double* dst, long long n, int sms,
                               cudaStream_t s);
 
+// FP32 lane kernel of the mixed-precision entries of 3 <= L <= 4 classes
+// (gx_lane*.cu, dispatched in gx_small.cu); runs after the class-generic
+// kernel of the same class on the same stream
+bool lane32_class(int la, int lb, int lc, int ld);
+cudaError_t launch_lane32(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s);
+
 // register-resident small classes (gx_small.cu)
 bool small_class(int la, int lb, int lc, int ld);
 cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s);
@@ -227,5 +234,6 @@ size_t chol_partial_bytes();
 int set_error(int code, const std::string& msg);
 
 cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops);
+cudaError_t run_fp32_probe(int sms, cudaStream_t s, float* ms, double* flops);
 
 }  // namespace gx

@@ -979,6 +979,9 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     const int wpb = blockDim.x >> 5;
     const int B1p = qc.B1 + 1;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
+    // with the FP32 lane kernel in charge of the FP32 entries, this kernel
+    // takes only the entries at or above the FP32 cutoff
+    const float skip64 = qc.no32 ? fmaxf(skip, cut32) : skip;
     const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e, qc.stream, qc.L);
     const size_t tab_bytes = (((size_t)qc.tab_words * 4 + 15) / 16) * 16;
     char* base = reinterpret_cast<char*>(sm) + tab_bytes + (size_t)wib * lay.total;
@@ -1053,7 +1056,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
                         const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
                         const float b = pp.sbound[op] * pp.sbound[oq];
-                        valid = b >= skip;
+                        valid = b >= skip64;
                     }
                     const unsigned mask = __ballot_sync(0xffffffffu, valid);
                     const int cnt = __popc(mask);
@@ -1342,13 +1345,13 @@ cudaError_t launch_scatter_full(const double2* packed, const long long* block_of
 }
 
 // ---------------------------------------------------------------------------
-// FP64 FMA throughput probe: 8 independent dependent-FMA chains per thread,
-// 8 resident blocks of 256 threads per SM.
+// FMA throughput probes (FP64 and FP32): 8 independent dependent-FMA chains
+// per thread, 8 resident blocks of 256 threads per SM.
 // ---------------------------------------------------------------------------
 
-__global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
-    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
-           x7 = x0 + 7;
+template <typename T>
+__global__ void fma_probe_kernel(T* out, int iters, T a, T b) {
+    T x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
@@ -1365,17 +1368,18 @@ __global__ void fp64_probe_kernel(double* out, int iters, double a, double b) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
-cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops) {
-    const int blocks = sms * 8, threads = 256, iters = 1000;
-    double* buf = nullptr;
-    cudaError_t e = cudaMalloc(&buf, sizeof(double) * blocks * threads);
+template <typename T>
+cudaError_t run_fma_probe(int sms, cudaStream_t s, int iters, float* ms, double* flops) {
+    const int blocks = sms * 8, threads = 256;
+    T* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, sizeof(T) * blocks * threads);
     if (e != cudaSuccess) return e;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    fp64_probe_kernel<<<blocks, threads, 0, s>>>(buf, 20, 1.0000001, 1e-9);
+    fma_probe_kernel<T><<<blocks, threads, 0, s>>>(buf, 20, (T)1.0000001, (T)1e-9);
     cudaEventRecord(a, s);
-    fp64_probe_kernel<<<blocks, threads, 0, s>>>(buf, iters, 1.0000001, 1e-9);
+    fma_probe_kernel<T><<<blocks, threads, 0, s>>>(buf, iters, (T)1.0000001, (T)1e-9);
     cudaEventRecord(b, s);
     e = cudaEventSynchronize(b);
     cudaEventElapsedTime(ms, a, b);
@@ -1384,6 +1388,14 @@ cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops) {
     cudaEventDestroy(b);
     cudaFree(buf);
     return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+cudaError_t run_fp64_probe(int sms, cudaStream_t s, float* ms, double* flops) {
+    return run_fma_probe<double>(sms, s, 1000, ms, flops);
+}
+
+cudaError_t run_fp32_probe(int sms, cudaStream_t s, float* ms, double* flops) {
+    return run_fma_probe<float>(sms, s, 20000, ms, flops);
 }
 
 }  // namespace gx

@@ -14,6 +14,11 @@
 // Limit: n * n <= GX_NOALLOC_MAX_ENTRIES (65,536 ordered AO pairs, i.e.
 // n <= 256); larger problems are rejected with GX_ELENGTH.
 //
+// Precondition, as in the allocating driver (which only pivots on entries
+// above its stopping threshold): residual[pivot] > 0.  A non-positive pivot
+// residual makes the scale 1/sqrt(residual) non-finite, and the new row,
+// the residual and result->min_residual then hold non-finite values.
+//
 // The kernels are the ones gx_cholesky runs for the same step
 // (launch_chol_step in gx_chol.cu); only the scratch pointers differ.
 #include <mutex>
@@ -46,21 +51,34 @@ std::mutex g_mu;
 
 int fail(int code, const std::string& m) { return gx::set_error(code, m); }
 
-// Device addresses of the scratch arrays, resolved once per device with that
-// device current (the first call on a device does this; make that first call
-// before any stream capture).
-int resolve(int device, Addresses& out) {
+// Device addresses of the scratch arrays on `device` (current).  Looked up
+// again on every call made outside stream capture, so that a context
+// re-created after cudaDeviceReset (which reloads this module and moves the
+// arrays) is followed; under capture the addresses recorded by the last
+// uncaptured call on the device are used, so the first call on a device must
+// come before any stream capture.
+int resolve(int device, cudaStream_t stream, Addresses& out) {
     std::lock_guard<std::mutex> lock(g_mu);
     Addresses& a = g_addr[device];
-    if (!a.ready) {
-        cudaError_t e = cudaGetSymbolAddress(&a.work, g_work);
-        if (e == cudaSuccess) e = cudaGetSymbolAddress(&a.partial, g_partial);
-        if (e == cudaSuccess) e = cudaGetSymbolAddress(&a.scale, g_scale);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GX_ECUDA, std::string("cudaStreamIsCapturing failed: ") + cudaGetErrorString(e));
+    }
+    if (cap == cudaStreamCaptureStatusNone) {
+        Addresses fresh;
+        e = cudaGetSymbolAddress(&fresh.work, g_work);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&fresh.partial, g_partial);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&fresh.scale, g_scale);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return fail(GX_ECUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
         }
-        a.ready = true;
+        fresh.ready = true;
+        a = fresh;
+    } else if (!a.ready) {
+        return fail(GX_EINVAL, "gx_cholesky_step_noalloc: the first call on a device must come before stream capture");
     }
     out = a;
     return GX_OK;
@@ -86,7 +104,7 @@ extern "C" int gx_cholesky_step_noalloc(const void* factors, int64_t rank, int64
     if (e != cudaSuccess) return fail(GX_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (device < 0 || device >= kMaxDevices) return fail(GX_EINVAL, "device index out of range");
     Addresses a;
-    if (int rc = resolve(device, a)) return rc;
+    if (int rc = resolve(device, static_cast<cudaStream_t>(stream), a)) return rc;
     e = gx::launch_chol_step(real != 0, factors, N, (int)rank, pivot, column, a.work, n, residual,
                              static_cast<double*>(a.scale), new_row, a.partial, result,
                              static_cast<cudaStream_t>(stream));

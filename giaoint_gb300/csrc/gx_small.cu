@@ -15,6 +15,27 @@ cudaError_t go(const EriDev& d, const QuartetClass& qc, cudaStream_t s) {
 
 bool small_class(int la, int lb, int lc, int ld) { return la + lb + lc + ld <= 2; }
 
+cudaError_t launch_lane32_a(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s,
+                            bool* found);
+cudaError_t launch_lane32_b(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s,
+                            bool* found);
+cudaError_t launch_lane32_c(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s,
+                            bool* found);
+
+bool lane32_class(int la, int lb, int lc, int ld) {
+    const int L = la + lb + lc + ld;
+    return L >= 3 && L <= 4 && la <= 2 && lb <= 2 && lc <= 2 && ld <= 2;
+}
+
+cudaError_t launch_lane32(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s) {
+    if (qc.ntask <= 0 || qc.ngroup <= 0) return cudaSuccess;
+    bool found = false;
+    cudaError_t e = launch_lane32_a(la, lb, lc, ld, d, qc, s, &found);
+    if (!found) e = launch_lane32_b(la, lb, lc, ld, d, qc, s, &found);
+    if (!found) e = launch_lane32_c(la, lb, lc, ld, d, qc, s, &found);
+    return found ? e : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s) {
     if (qc.ntask <= 0 || qc.ngroup <= 0) return cudaSuccess;
     const int key = ((la * 3 + lb) * 3 + lc) * 3 + ld;

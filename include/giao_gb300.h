@@ -254,6 +254,46 @@ int gx_cholesky(gx_context* ctx, gx_basis* basis, const double* B, const double*
                 const gx_cholesky_options* options, double* vectors, int64_t* pivots, int64_t* rank,
                 double* max_residual);
 
+/* Work and device time of one factorisation. */
+typedef struct gx_cholesky_stats {
+    int64_t rank;                        /* pivots taken (on failure: when it stopped)          */
+    int64_t block_evaluations;           /* pivot shell-pair column evaluations                 */
+    int64_t column_entries;              /* raw column entries extracted (candidates x n^2)     */
+    int64_t column_primitive_quartets;   /* FP64 primitive quartets of the column evaluations   */
+    int64_t diagonal_primitive_quartets; /* FP64 primitive quartets of the diagonal             */
+    int64_t column_cache_capacity;       /* raw columns the cache may hold (fitted to memory)   */
+    double column_model_flops;           /* FP64 FLOP model of the column primitive quartets    */
+    double column_ms;                    /* event-timed column evaluations + extraction         */
+    double update_ms;                    /* event-timed factor update, residual and argmax      */
+    double update_bytes;                 /* algorithmic bytes of the updates: L read once per
+                                            pivot (rank rows), raw column, new row, residual     */
+    double update_flops;                 /* 2 (real) or 8 (complex) x rank x n^2, summed        */
+    double column_pool_bytes;            /* device bytes of the column slots                    */
+    double seconds;                      /* wall time of the factorisation                      */
+} gx_cholesky_stats;
+
+/* The same factorisation with the factors kept on the device (the factor
+ * state a serving loop keeps resident): options->max_rank is the rank limit
+ * (the reference's max_bytes // row_bytes; MemoryError beyond it) and the
+ * factor rows grow on the device as the rank grows, so no output capacity
+ * has to be guessed.  Destroy with gx_cholesky_factors_destroy. */
+typedef struct gx_cholesky_factors gx_cholesky_factors;
+int gx_cholesky_factor(gx_context* ctx, gx_basis* basis, const double* B, const double* O,
+                       const gx_cholesky_options* options, gx_cholesky_factors** out);
+/* rank, n (AOs), max residual diagonal and 1 when the factors are real
+ * (zero field or a single centre: stored as float64 on the device). */
+int gx_cholesky_factors_info(const gx_cholesky_factors* factors, int64_t* rank, int64_t* nao,
+                             double* max_residual, int* real);
+/* vectors: host complex128[rank][n][n] (may be NULL); pivots: int64[rank][2] (may be NULL). */
+int gx_cholesky_factors_copy(const gx_cholesky_factors* factors, double* vectors, int64_t* pivots);
+/* Device address of the factor rows ([rank][n*n], float64 when real else
+ * complex128) for in-process GPU consumers; valid until destroyed. */
+const void* gx_cholesky_factors_device(const gx_cholesky_factors* factors);
+int gx_cholesky_factors_stats(const gx_cholesky_factors* factors, gx_cholesky_stats* out);
+void gx_cholesky_factors_destroy(gx_cholesky_factors* factors);
+/* Statistics of the last factorisation on the context (also after a failure). */
+int gx_cholesky_last_stats(gx_context* ctx, gx_cholesky_stats* out);
+
 
 /* GIAO nuclear-attraction matrix out[mu][nu] (complex128, n x n, AO order
  * of the basis) = sum_C -Z_C <mu|1/|r - C||nu> over nnuc point charges
@@ -334,10 +374,12 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
  * cap (<= 4), phase-1 batch cap (<= 32), ket-transform rows per lane (1, 2,
  * 4), bra-transform components per lane (1-4), register-budget variant (2
  * or 4 resident blocks), 1 = no shared staging, 1 = stream mode (per-entry
- * recurrences into a two-column buffer).  Fields other than per_group apply
- * to the generic kernel only. */
+ * recurrences into a two-column buffer), 1 = no FP32 lane kernel (mixed
+ * precision, classes with 3 <= L <= 4: the generic kernel then also takes
+ * the FP32 primitive quartets).  Fields other than per_group apply to the
+ * generic kernel only. */
 typedef struct gx_class_config {
-    int per_group, warps_per_block, batch, kt, ct, min_blocks, nostage, stream;
+    int per_group, warps_per_block, batch, kt, ct, min_blocks, nostage, stream, nolane;
 } gx_class_config;
 /* Read / replace the configuration of every class (gx_eri_plan_class_count
  * entries) for one precision mode; a set configuration is used by later
@@ -355,6 +397,9 @@ int64_t gx_canonical_quartets(int ns, uint32_t* out);
 /* Measured FP64 FMA throughput of the device (TFLOP/s) from a dependent-
  * chain probe kernel: the roofline denominator of the FP64-bound kernels. */
 int gx_measure_fp64_peak(gx_context* ctx, double* tflops);
+/* The same probe in FP32: the denominator of the FP32 term of the
+ * mixed-precision roofline. */
+int gx_measure_fp32_peak(gx_context* ctx, double* tflops);
 
 /* ---------------------------------------------------------------------- */
 /* allocation-free Cholesky step                                           */
@@ -386,9 +431,14 @@ typedef struct gx_cholesky_step_result {
  * plus a few KiB, held by every GPU that loads the library until process
  * exit; n*n above GX_NOALLOC_MAX_ENTRIES returns GX_ELENGTH.  All calls share
  * that scratch, so calls that overlap on the GPU (different streams or
- * threads without ordering) race.  The first call on a device resolves the
- * scratch address with that device current; make it before any stream
- * capture. */
+ * threads without ordering) race.  Every call outside stream capture looks
+ * the scratch address up with the calling thread's current device (so a
+ * context re-created after cudaDeviceReset is followed); a call under
+ * capture reuses the address of the last uncaptured call on that device, so
+ * the first call on a device must come before any stream capture.  The pivot
+ * must have a positive residual (residual[pivot] > 0), as the allocating
+ * driver guarantees; otherwise the row and result->min_residual are not
+ * finite. */
 int gx_cholesky_step_noalloc(const void* factors, int64_t rank, int64_t pivot, const void* column, int n, int real,
                              double* residual, void* new_row, void* result, void* stream);
 

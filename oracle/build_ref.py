@@ -19,7 +19,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: GIAO_REFERENCE_ROOT, else a "reference" directory beside the repository
+REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", str(HERE.parent.parent / "reference")))
 SOURCES = ["types.cpp", "overlap.cpp", "hermite.cpp", "boys.cpp", "eri.cpp", "cholesky.cpp", "nuclear.cpp",
            "derivatives.cpp", "property.cpp", "assembly.cpp"]
 FLAGS = ["-std=c++20", "-O3", "-fPIC", "-fopenmp", "-DGIAO_HAS_OPENMP"]

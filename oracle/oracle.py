@@ -520,8 +520,20 @@ class CholeskyResult:
 
 def cholesky_eri(backend: _Backend, shells, B=None, O=None, threshold: float = 1e-8,
                  screening_threshold: float = 0.0, threads: int = 1, max_bytes: int | None = None,
-                 pivot_batch_size: int = 32) -> CholeskyResult:
-    """Restatement of the reference driver with the given integral backend."""
+                 pivot_batch_size: int = 32, max_pivots: int | None = None, follow=None) -> CholeskyResult:
+    """Restatement of the reference driver with the given integral backend.
+
+    Checker-only options (not reference options):
+    ``max_pivots`` stops after that many pivots and returns the partial
+    factorisation, so that the pivot sequence and factors of a large system
+    can be compared on a prefix.
+    ``follow`` (pivots (M, 2) of another factorisation) replays the driver
+    along that sequence: at every step the driver makes its own choice by
+    the reference rules (global argmax, local block rule, raw-column cache
+    state), and where the followed pivot differs it records the residual gap
+    between the two and continues with the followed one.  The result's
+    ``forced_steps`` and ``max_forced_gap`` then say whether every choice of
+    the other factorisation was the reference's or tied with it."""
     specs = as_specs(shells)
     n = sum(s.nao for s in specs)
     offsets = []
@@ -572,12 +584,23 @@ def cholesky_eri(backend: _Backend, shells, B=None, O=None, threshold: float = 1
     block_candidates = np.empty(0, dtype=int)
     candidates = np.empty(0, dtype=int)
     columns = np.empty((0, n * n), dtype=dtype)
+    forced_steps, max_forced_gap = 0, 0.0
     while float(np.max(residual, initial=0.0)) > tolerance:
+        if max_pivots is not None and len(pivots) >= max_pivots:
+            break
+        if follow is not None and len(pivots) >= len(follow):
+            break
         pivot = int(np.argmax(residual))
         if reuse and not real and pivot_batch_size > 1 and len(block_candidates):
             local = int(block_candidates[np.argmax(residual[block_candidates])])
             if residual[local] > tolerance and residual[local] >= 0.01 * residual[pivot]:
                 pivot = local
+        if follow is not None:
+            other = int(follow[len(pivots)][0]) * n + int(follow[len(pivots)][1])
+            if other != pivot:
+                forced_steps += 1
+                max_forced_gap = max(max_forced_gap, abs(float(residual[pivot]) - float(residual[other])))
+                pivot = other
         rank = len(pivots)
         if rank >= limit:
             raise MemoryError(f"Cholesky ERI output requires at least {(rank + 1) * row_bytes} bytes, "
@@ -636,8 +659,12 @@ def cholesky_eri(backend: _Backend, shells, B=None, O=None, threshold: float = 1
         read_diagonal(skipped)
         residual = diagonal.ravel() - np.sum(np.abs(factors[: len(pivots)]) ** 2, axis=0)
     vectors = np.array(factors[: len(pivots)], dtype=np.complex128).reshape(len(pivots), n, n)
-    return CholeskyResult(vectors, np.asarray(pivots, dtype=np.int64).reshape(-1, 2), threshold,
-                          float(np.max(residual, initial=0.0)))
+    out = CholeskyResult(vectors, np.asarray(pivots, dtype=np.int64).reshape(-1, 2), threshold,
+                         float(np.max(residual, initial=0.0)))
+    out.forced_steps = forced_steps
+    out.max_forced_gap = max_forced_gap
+    out.stopped_by_threshold = float(np.max(residual, initial=0.0)) <= tolerance
+    return out
 
 
 # --------------------------------------------------------------------------

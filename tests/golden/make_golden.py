@@ -1,7 +1,8 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
-Run where the reference checkout exists (GIAO_REFERENCE_ROOT, default the
-read-only reference path used to build oracle/_ref):
+Run where the reference checkout exists (GIAO_REFERENCE_ROOT, default a
+``reference`` directory beside the repository; the same checkout oracle/_ref
+is built from):
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py nuclear    # one fixture (boys, m8, blocks, nuclear,
@@ -63,7 +64,8 @@ from giaoint_gb300 import synthetic as syn  # noqa: E402
 from oracle import build_ref  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: GIAO_REFERENCE_ROOT, else a "reference" directory beside the repository
+REFERENCE = Path(os.environ.get("GIAO_REFERENCE_ROOT", str(ROOT.parent / "reference")))
 
 BOYS_MAP = [0.0, 1.0e-14 + 1.0e-14j, 0.749999, 0.750001, 1.0 + 4.0j, 20.0 - 35.0j, -1.0 + 2.0j, -30.0 - 12.0j,
             -100.0 + 20.0j, 123.999, 124.001, 130.0 + 10.0j, 159.999j, 1000.0 - 25.0j]
@@ -213,8 +215,16 @@ def cholesky_fixture(ref):
     mod, Basis, MagneticField = reference_cholesky_module(ref)
     df = [O.ShellSpec((0.2, -0.1, 0.3), 2, [0.8], [[1.0]]), O.ShellSpec((-0.3, 0.4, -0.2), 3, [0.6], [[1.0]])]
     tri = O.as_specs(syn.random_molecule(11, natoms=3, box=4.0))
+    # generally contracted shells (two contraction rows each) on two centres:
+    # the complex local block rule and the raw-column cache of the reference
+    # decide pivots here
+    gen = [O.ShellSpec((0.0, 0.0, 0.0), 0, [9.0, 1.6, 0.35], [[0.15, 0.55, 0.45], [-0.1, -0.2, 1.0]]),
+           O.ShellSpec((0.0, 0.0, 0.0), 1, [2.2, 0.45], [[0.5, 0.6], [-0.3, 1.0]]),
+           O.ShellSpec((1.3, 0.4, -0.6), 0, [5.5, 0.9, 0.2], [[0.2, 0.6, 0.4], [0.05, -0.4, 1.0]]),
+           O.ShellSpec((1.3, 0.4, -0.6), 1, [1.4, 0.3], [[0.6, 0.5], [-0.2, 1.0]]),
+           O.ShellSpec((1.3, 0.4, -0.6), 2, [0.7], [[1.0]])]
     cases = []
-    for name, specs in (("df", df), ("molecule3", tri)):
+    for name, specs in (("df", df), ("molecule3", tri), ("contracted", gen)):
         for label, B, origin in (("zero", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0)),
                                  ("field", (0.05, -0.03, 0.2), (0.37, -0.29, 0.43))):
             for tau in (1e-4, 1e-8):
@@ -232,7 +242,8 @@ def cholesky_fixture(ref):
                         "vector_abs_sum": float(np.abs(v).sum()),
                         "first_vector": [[x.real, x.imag] for x in v[0].ravel()[:256]],
                     })
-    shells = {"df": [s.__dict__ for s in df], "molecule3": [s.__dict__ for s in tri]}
+    shells = {"df": [s.__dict__ for s in df], "molecule3": [s.__dict__ for s in tri],
+              "contracted": [s.__dict__ for s in gen]}
     return {"shells": shells, "cases": cases}
 
 

@@ -31,7 +31,7 @@ def test_noalloc_step_matches_allocating_driver(B):
     basis = two_shell_basis()
     field = gi.MagneticField(B, (0.37, -0.29, 0.43))
     real = all(x == 0 for x in B)
-    ref = gi.cholesky_eri(basis, field=field, threshold=1e-8, backend="device")
+    ref = gi.cholesky_eri(basis, field=field, threshold=1e-8)
     assert len(ref.pivots) > 3
     n = basis.ao_count
     N = n * n
