@@ -89,6 +89,8 @@ def parse():
     p.add_argument("--cholesky-only", action="store_true",
                    help="run only the Cholesky leg (no CPU port) and print its JSON (profiling)")
     p.add_argument("--serving-requests", type=int, default=32)
+    p.add_argument("--serving-request-gib", type=float, default=6.0,
+                   help="per-request device-memory limit of the serving leg (estimated footprint; GiB)")
     p.add_argument("--profile-step", default="", choices=["", "fp64", "mixed", "fp64_exact"],
                    help="run warm-up steps and one step of this mode inside an NVTX range, then exit (profiling)")
     p.add_argument("--sweep", type=int, default=64,
@@ -456,35 +458,124 @@ def derivative_leg(ctx, recs, B, quartets, run_cpu: bool, count: int = 200000, s
     return out
 
 
-def serving_leg(args):
-    """Serving mix: Poisson arrivals at 200 req/s of ERI-block requests (3-40
-    atom molecules of the 12-atom recipe, |B| <= 0.3, seeded canonical quartet
-    subsets of up to 2^24 complex entries) and Cholesky requests (3-6 atoms,
-    threshold 1e-6/1e-7/1e-8), served by four overlapping slots with
-    admission by device footprint."""
+def serving_cpu_baseline(reqs, budget_s: float = 20.0) -> dict:
+    """The same request list served sequentially by the CPU oracle port (all
+    host threads), bounded: requests are run in arrival order until
+    ``budget_s`` of CPU service time is spent (a Cholesky request only when
+    its molecule has at most 4 atoms: larger ones take minutes on the port).
+    The service time of every other request is modelled from the measured
+    rates (ERI requests: ERIs/s; Cholesky: seconds per pivot-block column
+    entry are not modelled, the request is reported as not run), and the
+    sequential schedule start = max(arrival, previous finish) gives the
+    latencies."""
+    from oracle import oracle as O
+
+    orc = O.Oracle()
+    threads = os.cpu_count() or 1
+    spent = 0.0
+    service = [None] * len(reqs)
+    entries = [0] * len(reqs)
+    measured = 0
+    for i, r in enumerate(reqs):
+        sizes = np.array([(s_.angular_momentum + 1) * (s_.angular_momentum + 2) // 2 * len(s_.raw_coefficients)
+                          for s_ in r.shells])
+        if r.kind == "eri":
+            q = np.asarray(r.quartets, dtype=np.uint32).reshape(-1, 4)
+            entries[i] = int(np.prod(sizes[q.astype(np.int64)], axis=1).sum()) if len(q) else 0
+            if spent < budget_s:
+                t0 = time.perf_counter()
+                orc.eri_batch(list(r.shells), q, tuple(r.field), None, threads)
+                service[i] = time.perf_counter() - t0
+                spent += service[i]
+                measured += 1
+        elif spent < budget_s and len(r.shells) <= 4 * len(syn_recipe()):
+            t0 = time.perf_counter()
+            O.cholesky_eri(orc, list(r.shells), tuple(r.field), None, threshold=float(r.threshold), threads=threads)
+            service[i] = time.perf_counter() - t0
+            spent += service[i]
+            measured += 1
+    eri_meas = [(service[i], entries[i]) for i, r in enumerate(reqs) if r.kind == "eri" and service[i] is not None]
+    rate = sum(e for _, e in eri_meas) / max(sum(t for t, _ in eri_meas), 1e-9) if eri_meas else None
+    modelled = 0
+    for i, r in enumerate(reqs):
+        if service[i] is None and r.kind == "eri" and rate:
+            service[i] = entries[i] / rate
+            modelled += 1
+    t = 0.0
+    lat, kinds = [], []
+    served = 0
+    for i, r in enumerate(reqs):
+        if service[i] is None:
+            continue
+        start = max(t, r.arrival)
+        t = start + service[i]
+        lat.append(t - r.arrival)
+        kinds.append(r.kind)
+        served += 1
+    lat_ms = np.array(lat) * 1e3
+    makespan = t - min(r.arrival for r in reqs) if served else 0.0
+    served_entries = sum(entries[i] for i in range(len(reqs)) if service[i] is not None)
+    return {"threads": threads, "kind": "port", "requests": len(reqs), "measured": measured,
+            "modelled_from_rate": modelled, "not_run": len(reqs) - served,
+            "cpu_seconds_measured": spent,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if served else None,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if served else None,
+            "eris_per_s": served_entries / makespan if makespan > 0 else None,
+            "requests_per_s": served / makespan if makespan > 0 else None,
+            "eri_rate_measured": rate,
+            "note": "sequential service on the host in arrival order; requests beyond the measured budget are "
+                    "modelled from the measured ERI rate; Cholesky requests above 4 atoms are not run"}
+
+
+def syn_recipe():
+    from giaoint_gb300 import synthetic as syn
+
+    return syn.MOLECULE_RECIPE
+
+
+def serving_leg(args, run_cpu: bool):
+    """Serving mix (config 5 as specified): Poisson arrivals at 200 req/s; each
+    request a seeded molecule of 3-40 atoms (the 12-atom recipe), |B| <= 0.3,
+    either an ERI block of up to 2^24 complex entries (seeded canonical
+    quartet subset) or Cholesky at threshold 1e-6/1e-7/1e-8.  Four
+    overlapping slots admit requests by estimated device footprint; a request
+    estimated above the per-request limit (--serving-request-gib) is refused
+    with MemoryError and counted.  Then the same list at a load the GPU
+    sustains, and the CPU port serving the list sequentially."""
     from giaoint_gb300 import synthetic as syn
     from giaoint_gb300.serving import Server, latency_summary
 
-    def trace(rate, count, seed):
-        reqs = syn.serving_requests(count=count, rate=rate, seed=seed, atoms=(3, 40), max_entries=1 << 24,
-                                    cholesky_fraction=0.25, cholesky_atoms=(3, 6))
-        with Server(slots=4, precision=args.precision, mixed_cutoff=args.mixed_cutoff) as srv:
+    limit = int(args.serving_request_gib * (1 << 30))
+
+    def requests(rate, count, seed):
+        return syn.serving_requests(count=count, rate=rate, seed=seed, atoms=(3, 40), max_entries=1 << 24,
+                                    cholesky_fraction=0.25, cholesky_atoms=(3, 40))
+
+    def trace(reqs, rate):
+        with Server(slots=4, precision=args.precision, mixed_cutoff=args.mixed_cutoff,
+                    max_request_bytes=limit) as srv:
             done = srv.run(reqs)
             summary = latency_summary(done)
             summary.update(load={"rate_req_s": rate, "requests": len(reqs), "slots": 4,
                                  "hbm_budget_bytes": srv.hbm_budget, "max_inflight": srv.max_inflight,
+                                 "per_request_limit_bytes": limit, "refused": srv.refused,
                                  "eri_requests": sum(r.kind == "eri" for r in reqs),
-                                 "cholesky_requests": sum(r.kind == "cholesky" for r in reqs)},
+                                 "cholesky_requests": sum(r.kind == "cholesky" for r in reqs),
+                                 "cholesky_atoms": sorted(len(r.shells) // len(syn.MOLECULE_RECIPE)
+                                                          for r in reqs if r.kind == "cholesky")},
                            precision=args.precision)
-            errors = [repr(c.error) for c in done if c.error is not None]
+            errors = [repr(c.error) for c in done if c.error is not None and not isinstance(c.error, MemoryError)]
             if errors:
                 summary["errors"] = errors[:3]
         return summary
 
     # the specified load (200 req/s offered: beyond one GPU, latency is mostly
     # queueing), then a load the GPU sustains (service latency)
-    out = trace(200.0, args.serving_requests, 2026)
-    out["sustained_load"] = trace(4.0, max(8, args.serving_requests // 2), 2027)
+    reqs = requests(200.0, args.serving_requests, 2026)
+    out = trace(reqs, 200.0)
+    out["sustained_load"] = trace(requests(4.0, max(8, args.serving_requests // 2), 2027), 4.0)
+    if run_cpu:
+        out["cpu_sequential"] = serving_cpu_baseline(reqs)
     return out
 
 
@@ -790,7 +881,7 @@ def run_gpu(args):
                # per warm call: the field (B, O); the quartet list is read and
                # hashed on the host, its plan is cached on the device
                "h2d_bytes_per_step": 48, "d2h_bytes_per_step": int(total * 16), "seconds_per_step": e2e_s,
-               "cold_call_seconds": cold_s, "cold_h2d_bytes": int(ntask.value * 40 + 48),
+               "cold_call_seconds": cold_s, "cold_h2d_bytes": int(ntask.value * 48 + 48),
                "d2h_copy_seconds": d2h_s, "d2h_gb_per_s": total * 16 / d2h_s / 1e9,
                "api": "gx_eri_batch (C ABI, pinned host buffers)", "max_abs_diff_vs_device_path": e2e_diff,
                "call_seconds": times, "call_seconds_median": float(statistics.median(times)),
@@ -830,7 +921,7 @@ def run_gpu(args):
                                      count=args.derivative_quartets)
     serving = None
     if rank == 0 and not args.no_serving:
-        serving = serving_leg(args)
+        serving = serving_leg(args, run_cpu=(world == 1 and not args.no_cpu))
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -175,6 +175,15 @@ std::vector<std::array<int, 3>> components(int l) {
 // context
 // ---------------------------------------------------------------------------
 
+// Immutable device tables shared by every context on a device: the Boys
+// table (132 MB, 93 ms to build), the Gauss-Legendre rules, the Hermite
+// index table and the recurrence plans.  Built by the first context on a
+// device and kept while any context on it lives.
+struct SharedTables {
+    DeviceBuffer boys_S, boys_E0, gl, herm, rec_plan, rec_plan_off;
+    double boys_table_agreement = 0.0;
+};
+
 struct gx_context {
     int device = 0;
     int sm_count = 0;
@@ -185,8 +194,8 @@ struct gx_context {
     std::vector<cudaStream_t> aux;
     std::vector<cudaEvent_t> aux_done;
     cudaEvent_t fork = nullptr;
-    double boys_table_agreement = 0.0;
-    DeviceBuffer boys_S, boys_E0, gl, herm, rec_plan, rec_plan_off, status;
+    std::shared_ptr<SharedTables> t;  // shared immutable tables of the device
+    DeviceBuffer status;
     std::mutex mu;
     std::map<std::pair<int, int>, std::unique_ptr<PairClassHost>> pair_classes;
     // scratch
@@ -224,7 +233,7 @@ struct gx_context {
     }
 
     gx::BoysTable boys() const {
-        return gx::BoysTable{boys_S.as<double2>(), boys_E0.as<double2>()};
+        return gx::BoysTable{t->boys_S.as<double2>(), t->boys_E0.as<double2>()};
     }
 
     void reset_status() { GX_CUDA(cudaMemsetAsync(status.ptr, 0, sizeof(gx::DevStatus), stream)); }
@@ -428,10 +437,10 @@ FieldPairs& field_pairs(gx_basis* b, const double* B, const double* O) {
     dev.basis = b->dev();
     dev.pairs = pair_view(b, fp);
     dev.boys = b->ctx->boys();
-    dev.gl = b->ctx->gl.as<gx::GLRules>();
-    dev.herm_xyz = b->ctx->herm.as<uint32_t>();
-    dev.rec_plan = b->ctx->rec_plan.as<int2>();
-    dev.rec_plan_off = b->ctx->rec_plan_off.as<int>();
+    dev.gl = b->ctx->t->gl.as<gx::GLRules>();
+    dev.herm_xyz = b->ctx->t->herm.as<uint32_t>();
+    dev.rec_plan = b->ctx->t->rec_plan.as<int2>();
+    dev.rec_plan_off = b->ctx->t->rec_plan_off.as<int>();
     GX_CUDA(gx::launch_pair_precompute(b->dev(), B, O, b->npp, b->d_pp_a.as<int>(), b->d_pp_b.as<int>(),
                                        b->d_pp_pa.as<int>(), b->d_pp_pb.as<int>(), b->d_pp_class.as<int>(),
                                        b->d_classes.as<gx::PairClassDev>(), fp.p.as<double>(), fp.Pr.as<double>(),
@@ -619,22 +628,23 @@ bool lane_class(const PlanClass& pc) { return gx::lane32_class(pc.key[0], pc.key
 // units (one lane per primitive quartet: up to 1024 primitive quartets and 128
 // tasks per warp), in one device array.
 void make_group_set(gx_context* ctx, const PlanData& plan, const std::vector<ClassConf>& conf, GroupSet& out) {
+    const size_t nc = plan.classes.size();
+    std::vector<std::vector<int2>> g(nc), lg(nc);
+#pragma omp parallel for schedule(dynamic)
+    for (long long ci = 0; ci < (long long)nc; ++ci) {
+        g[ci] = make_groups(ctx, plan, ci, conf[ci]);
+        if (lane_class(plan.classes[ci])) lg[ci] = make_groups(ctx, plan, ci, conf[ci], true);
+    }
     std::vector<int2> all;
     out.range.clear();
     out.lane.clear();
-    for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
-        const auto g = make_groups(ctx, plan, ci, conf[ci]);
-        out.range.push_back({all.size(), g.size()});
-        all.insert(all.end(), g.begin(), g.end());
+    for (size_t ci = 0; ci < nc; ++ci) {
+        out.range.push_back({all.size(), g[ci].size()});
+        all.insert(all.end(), g[ci].begin(), g[ci].end());
     }
-    for (size_t ci = 0; ci < plan.classes.size(); ++ci) {
-        if (!lane_class(plan.classes[ci])) {
-            out.lane.push_back({0, 0});
-            continue;
-        }
-        const auto g = make_groups(ctx, plan, ci, conf[ci], true);
-        out.lane.push_back({all.size(), g.size()});
-        all.insert(all.end(), g.begin(), g.end());
+    for (size_t ci = 0; ci < nc; ++ci) {
+        out.lane.push_back({all.size(), lg[ci].size()});
+        all.insert(all.end(), lg[ci].begin(), lg[ci].end());
     }
     upload(out.dev, all, ctx->stream);
 }
@@ -657,69 +667,147 @@ void apply_recorded_tuning(gx_context* ctx, const gx_basis* b, int precision, Pl
     plan.tuned[precision].valid = true;
 }
 
+// Class-sorted task list of `req`: one task per segmented shell quartet
+// (general contractions split), ordered by class (la, lb, lc, ld), then by
+// decreasing bra and ket primitive counts, then in request order -- a
+// parallel counting sort over (class, Kab, Kcd) buckets: per-chunk bucket
+// histograms, one prefix over (bucket, chunk), and a scatter pass.
 void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
-    std::map<std::array<int, 4>, std::vector<gx::Task>> by_class;
-    std::map<std::array<int, 4>, int64_t> prims;
-    for (const auto& r : req) {
-        const int sh[4] = {(int)r.a, (int)r.b, (int)r.c, (int)r.d};
-        int64_t N[4];
-        int nc[4];
-        for (int k = 0; k < 4; ++k) {
-            N[k] = b->nao_of(sh[k]);
-            nc[k] = b->ncart_of(sh[k]);
-        }
-        const std::array<int, 4> key{b->l[sh[0]], b->l[sh[1]], b->l[sh[2]], b->l[sh[3]]};
-        if (key[0] + key[1] + key[2] + key[3] > 32)
-            raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
-        const int st0 = (int)(N[1] * N[2] * N[3]), st1 = (int)(N[2] * N[3]), st2 = (int)N[3];
-        auto& vec = by_class[key];
-        auto& np = prims[key];
-        for (int xa = 0; xa < b->ncontr[sh[0]]; ++xa)
-            for (int xb = 0; xb < b->ncontr[sh[1]]; ++xb)
-                for (int xc = 0; xc < b->ncontr[sh[2]]; ++xc)
-                    for (int xd = 0; xd < b->ncontr[sh[3]]; ++xd) {
-                        gx::Task t;
-                        t.sa = b->seg_first[sh[0]] + xa;
-                        t.sb = b->seg_first[sh[1]] + xb;
-                        t.sc = b->seg_first[sh[2]] + xc;
-                        t.sd = b->seg_first[sh[3]] + xd;
-                        t.out_off = r.out_off + (int64_t)xa * nc[0] * st0 + (int64_t)xb * nc[1] * st1 +
-                                    (int64_t)xc * nc[2] * st2 + (int64_t)xd * nc[3];
-                        t.st[0] = st0;
-                        t.st[1] = st1;
-                        t.st[2] = st2;
-                        t.st[3] = 1;
-                        vec.push_back(t);
-                        np += (int64_t)b->seg_nprim[t.sa] * b->seg_nprim[t.sb] * b->seg_nprim[t.sc] *
-                              b->seg_nprim[t.sd];
-                    }
+    // shell codes: distinct (l, nprim) of the segmented shells
+    std::map<std::pair<int, int>, int> code_of;
+    for (int s = 0; s < b->nseg; ++s) code_of.emplace(std::make_pair(b->seg_l[s], b->seg_nprim[s]), 0);
+    std::vector<std::pair<int, int>> codes;
+    for (auto& kv : code_of) {
+        kv.second = (int)codes.size();
+        codes.push_back(kv.first);
     }
-    std::vector<gx::Task> all;
+    const int nsc = (int)codes.size();
+    std::vector<int> seg_code(b->nseg);
+    for (int s = 0; s < b->nseg; ++s) seg_code[s] = code_of[{b->seg_l[s], b->seg_nprim[s]}];
+    const int64_t ntuple = (int64_t)nsc * nsc * nsc * nsc;
+    if (ntuple > (int64_t)1 << 24) raise(GX_EINVAL, "too many distinct (l, primitive count) shells in one basis");
+    // buckets: distinct (la, lb, lc, ld, -Kab, -Kcd) in sorted order
+    using BKey = std::array<int, 6>;
+    std::vector<BKey> tkey(ntuple);
+    for (int64_t t = 0; t < ntuple; ++t) {
+        const int c0 = (int)(t / ((int64_t)nsc * nsc * nsc)), c1 = (int)(t / ((int64_t)nsc * nsc) % nsc);
+        const int c2 = (int)(t / nsc % nsc), c3 = (int)(t % nsc);
+        tkey[t] = BKey{codes[c0].first, codes[c1].first, codes[c2].first, codes[c3].first,
+                       -codes[c0].second * codes[c1].second, -codes[c2].second * codes[c3].second};
+    }
+    std::vector<BKey> bkeys(tkey);
+    std::sort(bkeys.begin(), bkeys.end());
+    bkeys.erase(std::unique(bkeys.begin(), bkeys.end()), bkeys.end());
+    const int nb = (int)bkeys.size();
+    std::vector<int> bucket_of(ntuple);
+    for (int64_t t = 0; t < ntuple; ++t)
+        bucket_of[t] = (int)(std::lower_bound(bkeys.begin(), bkeys.end(), tkey[t]) - bkeys.begin());
+    auto tuple_of = [&](int a, int bb, int c, int d) {
+        return ((int64_t)(seg_code[a] * nsc + seg_code[bb]) * nsc + seg_code[c]) * nsc + seg_code[d];
+    };
+    const int64_t nreq = (int64_t)req.size();
+    constexpr int64_t kChunk = 1 << 15;
+    const int64_t nchunk = std::max<int64_t>(1, (nreq + kChunk - 1) / kChunk);
+    std::vector<int64_t> hist((size_t)nchunk * nb, 0);
+    // pass 1: bucket histograms per chunk
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nchunk; ++c) {
+        int64_t* h = hist.data() + (size_t)c * nb;
+        for (int64_t i = c * kChunk; i < std::min(nreq, (c + 1) * kChunk); ++i) {
+            const auto& r = req[i];
+            for (int xa = 0; xa < b->ncontr[r.a]; ++xa)
+                for (int xb = 0; xb < b->ncontr[r.b]; ++xb)
+                    for (int xc = 0; xc < b->ncontr[r.c]; ++xc)
+                        for (int xd = 0; xd < b->ncontr[r.d]; ++xd)
+                            ++h[bucket_of[tuple_of(b->seg_first[r.a] + xa, b->seg_first[r.b] + xb,
+                                                   b->seg_first[r.c] + xc, b->seg_first[r.d] + xd)]];
+        }
+    }
+    // prefix over (bucket, chunk): the first position of each chunk's run
+    std::vector<int64_t> btotal(nb, 0);
+    int64_t T = 0;
+    for (int bk = 0; bk < nb; ++bk)
+        for (int64_t c = 0; c < nchunk; ++c) {
+            const int64_t n = hist[(size_t)c * nb + bk];
+            hist[(size_t)c * nb + bk] = T;
+            T += n;
+            btotal[bk] += n;
+        }
+    for (int bk = 0; bk < nb; ++bk)
+        if (btotal[bk] && bkeys[bk][0] + bkeys[bk][1] + bkeys[bk][2] + bkeys[bk][3] > 32)
+            raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
+    std::unique_ptr<gx::Task[]> all(new gx::Task[std::max<int64_t>(T, 1)]);
+    plan.task_kk.resize(T);
+    // pass 2: scatter
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nchunk; ++c) {
+        int64_t* cur = hist.data() + (size_t)c * nb;
+        for (int64_t i = c * kChunk; i < std::min(nreq, (c + 1) * kChunk); ++i) {
+            const auto& r = req[i];
+            const int sh[4] = {(int)r.a, (int)r.b, (int)r.c, (int)r.d};
+            int64_t N[4];
+            int nc[4];
+            for (int k = 0; k < 4; ++k) {
+                N[k] = b->nao_of(sh[k]);
+                nc[k] = b->ncart_of(sh[k]);
+            }
+            const int st0 = (int)(N[1] * N[2] * N[3]), st1 = (int)(N[2] * N[3]), st2 = (int)N[3];
+            for (int xa = 0; xa < b->ncontr[sh[0]]; ++xa)
+                for (int xb = 0; xb < b->ncontr[sh[1]]; ++xb)
+                    for (int xc = 0; xc < b->ncontr[sh[2]]; ++xc)
+                        for (int xd = 0; xd < b->ncontr[sh[3]]; ++xd) {
+                            gx::Task t;
+                            t.sa = b->seg_first[sh[0]] + xa;
+                            t.sb = b->seg_first[sh[1]] + xb;
+                            t.sc = b->seg_first[sh[2]] + xc;
+                            t.sd = b->seg_first[sh[3]] + xd;
+                            t.out_off = r.out_off + (int64_t)xa * nc[0] * st0 + (int64_t)xb * nc[1] * st1 +
+                                        (int64_t)xc * nc[2] * st2 + (int64_t)xd * nc[3];
+                            t.st[0] = st0;
+                            t.st[1] = st1;
+                            t.st[2] = st2;
+                            t.st[3] = 1;
+                            t.pab = b->sp_off[(size_t)t.sa * b->nseg + t.sb];
+                            t.pcd = b->sp_off[(size_t)t.sc * b->nseg + t.sd];
+                            const int64_t pos = cur[bucket_of[tuple_of(t.sa, t.sb, t.sc, t.sd)]]++;
+                            all[pos] = t;
+                            plan.task_kk[pos] = (b->seg_nprim[t.sa] * b->seg_nprim[t.sb]) << 16 |
+                                                (b->seg_nprim[t.sc] * b->seg_nprim[t.sd]);
+                        }
+        }
+    }
+    // classes: runs of buckets with the same (la, lb, lc, ld)
     plan.classes.clear();
     plan.primitive_quartets = 0;
     plan.model_flops = 0.0;
-    for (auto& kv : by_class) {
-        const auto& k = kv.first;
-        const int64_t np = prims[k];
-        // uniform warps: order by primitive counts (largest first)
-        std::stable_sort(kv.second.begin(), kv.second.end(), [&](const gx::Task& x, const gx::Task& y) {
-            const int kx = b->seg_nprim[x.sa] * b->seg_nprim[x.sb], ky = b->seg_nprim[y.sa] * b->seg_nprim[y.sb];
-            if (kx != ky) return kx > ky;
-            return b->seg_nprim[x.sc] * b->seg_nprim[x.sd] > b->seg_nprim[y.sc] * b->seg_nprim[y.sd];
-        });
-        plan.classes.push_back({k, all.size(), kv.second.size(), np, model_flops(k[0], k[1], k[2], k[3])});
-        plan.primitive_quartets += np;
-        plan.model_flops += (double)np * model_flops(k[0], k[1], k[2], k[3]);
-        all.insert(all.end(), kv.second.begin(), kv.second.end());
+    size_t first = 0;
+    for (int bk = 0; bk < nb;) {
+        const std::array<int, 4> key{bkeys[bk][0], bkeys[bk][1], bkeys[bk][2], bkeys[bk][3]};
+        size_t count = 0;
+        int64_t np = 0;
+        int e = bk;
+        for (; e < nb && bkeys[e][0] == key[0] && bkeys[e][1] == key[1] && bkeys[e][2] == key[2] &&
+               bkeys[e][3] == key[3];
+             ++e) {
+            count += btotal[e];
+            np += btotal[e] * (int64_t)bkeys[e][4] * bkeys[e][5];  // (-Kab)(-Kcd)
+        }
+        if (count) {
+            const double fl = model_flops(key[0], key[1], key[2], key[3]);
+            plan.classes.push_back({key, first, count, np, fl});
+            plan.primitive_quartets += np;
+            plan.model_flops += (double)np * fl;
+            first += count;
+        }
+        bk = e;
     }
-    plan.ntask = (int64_t)all.size();
-    upload(plan.tasks, all, ctx->stream);
-    plan.task_kk.resize(all.size());
-    for (size_t t = 0; t < all.size(); ++t)
-        plan.task_kk[t] = (b->seg_nprim[all[t].sa] * b->seg_nprim[all[t].sb]) << 16 |
-                          (b->seg_nprim[all[t].sc] * b->seg_nprim[all[t].sd]);
+    plan.ntask = T;
+    plan.tasks.reserve(sizeof(gx::Task) * std::max<int64_t>(T, 1));
+    if (T) GX_CUDA(cudaMemcpyAsync(plan.tasks.ptr, all.get(), sizeof(gx::Task) * T, cudaMemcpyHostToDevice, ctx->stream));
     std::vector<ClassConf> defaults(plan.classes.size());
     make_group_set(ctx, plan, defaults, plan.base);
+    // (a copy from pageable memory is staged before cudaMemcpyAsync returns,
+    // so the host task array may be freed now)
 }
 
 // Primitive screening thresholds on the Schwarz product B_P B_Q.  FP64: a
@@ -739,10 +827,10 @@ gx::EriDev make_dev(gx_context* ctx, gx_basis* b, FieldPairs& fp, double2* out, 
     dev.basis = b->dev();
     dev.pairs = pair_view(b, fp);
     dev.boys = ctx->boys();
-    dev.gl = ctx->gl.as<gx::GLRules>();
-    dev.herm_xyz = ctx->herm.as<uint32_t>();
-    dev.rec_plan = ctx->rec_plan.as<int2>();
-    dev.rec_plan_off = ctx->rec_plan_off.as<int>();
+    dev.gl = ctx->t->gl.as<gx::GLRules>();
+    dev.herm_xyz = ctx->t->herm.as<uint32_t>();
+    dev.rec_plan = ctx->t->rec_plan.as<int2>();
+    dev.rec_plan_off = ctx->t->rec_plan_off.as<int>();
     dev.out = out;
     dev.status = ctx->status.as<gx::DevStatus>();
     return dev;
@@ -1170,14 +1258,16 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         int64_t nprim = 0, evaluated[2] = {0, 0};
         if (count) {
             PlanData& plan = lookup_plan(ctx, b, h1, h2, count, off, [&] {
-                std::vector<QuartetRequest> req;
-                req.reserve((size_t)count);
-                int64_t o = 0;
-                for (int64_t i = 0; i < nq; ++i) {
-                    const uint32_t* x = quartets + 4 * i;
-                    if (!keep(x)) continue;
-                    req.push_back({x[0], x[1], x[2], x[3], o});
-                    o += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+                std::vector<QuartetRequest> req((size_t)count);
+#pragma omp parallel for schedule(static)
+                for (int64_t c = 0; c < nchunk; ++c) {
+                    int64_t k = ccount[c];
+                    for (int64_t i = c * kChunk; i < std::min(nq, (c + 1) * kChunk); ++i) {
+                        const uint32_t* x = quartets + 4 * i;
+                        if (!keep(x)) continue;
+                        req[k] = QuartetRequest{x[0], x[1], x[2], x[3], offsets[k]};
+                        ++k;
+                    }
                 }
                 return req;
             });
@@ -1724,6 +1814,84 @@ int gx_shell_normalize(int l, int nprim, int ncontr, const double* exps, const d
     });
 }
 
+}  // extern "C"
+
+namespace {
+
+std::mutex g_tables_mu;
+std::map<int, std::weak_ptr<SharedTables>> g_tables;
+
+// The shared tables of `device` (current), built on stream `st` by the first
+// caller and completed before they are published.
+std::shared_ptr<SharedTables> device_tables(int device, cudaStream_t st) {
+    std::lock_guard<std::mutex> lock(g_tables_mu);
+    if (auto live = g_tables[device].lock()) return live;
+    auto tb = std::make_shared<SharedTables>();
+    gx::GLRules gl;
+    gauss_legendre(16, gl.x16, gl.w16);
+    gauss_legendre(32, gl.x32, gl.w32);
+    tb->gl.reserve(sizeof gl);
+    GX_CUDA(cudaMemcpy(tb->gl.ptr, &gl, sizeof gl, cudaMemcpyHostToDevice));
+    std::vector<uint32_t> herm(gx::herm_count(32));
+    for (int s = 0; s <= 32; ++s)
+        for (int k = s; k >= 0; --k)
+            for (int l = s - k; l >= 0; --l) {
+                const int m = s - k - l;
+                herm[gx::herm_index(k, l, m)] = (uint32_t)(k | (l << 8) | (m << 16));
+            }
+    upload(tb->herm, herm, st);
+    {
+        std::vector<int2> plan;
+        std::vector<int> off{0, 0};  // L = 0 has no steps
+        for (int L = 1; L <= gx::REC_PLAN_MAX; ++L) {
+            for (int n = L - 1; n >= 0; --n) {
+                for (int dg = L - n; dg >= 1; --dg)
+                    for (int k = dg; k >= 0; --k)
+                        for (int l = dg - k; l >= 0; --l) {
+                            const int m = dg - k - l;
+                            int axis, pw, i1, i2;
+                            if (k > 0) {
+                                axis = 0, pw = k, i1 = gx::herm_index(k - 1, l, m);
+                                i2 = k > 1 ? gx::herm_index(k - 2, l, m) : 0;
+                            } else if (l > 0) {
+                                axis = 1, pw = l, i1 = gx::herm_index(0, l - 1, m);
+                                i2 = l > 1 ? gx::herm_index(0, l - 2, m) : 0;
+                            } else {
+                                axis = 2, pw = m, i1 = gx::herm_index(0, 0, m - 1);
+                                i2 = m > 1 ? gx::herm_index(0, 0, m - 2) : 0;
+                            }
+                            plan.push_back(make_int2(gx::herm_index(k, l, m) | (i1 << 16),
+                                                     i2 | (axis << 14) | ((pw - 1) << 16)));
+                        }
+                plan.push_back(make_int2(0, (1 << 22) | (n << 23)));
+            }
+            off.push_back((int)plan.size());
+        }
+        upload(tb->rec_plan, plan, st);
+        upload(tb->rec_plan_off, off, st);
+    }
+    const size_t npts = (size_t)gx::BOYS_NX * gx::BOYS_NY;
+    tb->boys_S.reserve(npts * gx::BOYS_TABLE_ORDERS * sizeof(double2));
+    tb->boys_E0.reserve(npts * sizeof(double2));
+    DeviceBuffer fails;  // [0]: points worse than 1e-13, [1]: worst relative agreement (double bits)
+    fails.reserve(2 * sizeof(unsigned long long));
+    GX_CUDA(cudaMemsetAsync(fails.ptr, 0, 2 * sizeof(unsigned long long), st));
+    GX_CUDA(gx::launch_boys_table(tb->boys_S.as<double2>(), tb->boys_E0.as<double2>(),
+                                  tb->gl.as<gx::GLRules>(), fails.as<int>(), st));
+    unsigned long long words[2] = {0, 0};
+    GX_CUDA(cudaMemcpyAsync(words, fails.ptr, sizeof words, cudaMemcpyDeviceToHost, st));
+    GX_CUDA(cudaStreamSynchronize(st));
+    double worst;
+    std::memcpy(&worst, &words[1], sizeof worst);
+    tb->boys_table_agreement = worst;
+    g_tables[device] = tb;
+    return tb;
+}
+
+}  // namespace
+
+extern "C" {
+
 int gx_context_create(int device, gx_context** out) {
     return guarded([&] {
         auto ctx = std::make_unique<gx_context>();
@@ -1732,65 +1900,8 @@ int gx_context_create(int device, gx_context** out) {
         GX_CUDA(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
         GX_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
         ctx->stream = ctx->own_stream;
-        gx::GLRules gl;
-        gauss_legendre(16, gl.x16, gl.w16);
-        gauss_legendre(32, gl.x32, gl.w32);
-        ctx->gl.reserve(sizeof gl);
-        GX_CUDA(cudaMemcpy(ctx->gl.ptr, &gl, sizeof gl, cudaMemcpyHostToDevice));
-        std::vector<uint32_t> herm(gx::herm_count(32));
-        for (int s = 0; s <= 32; ++s)
-            for (int k = s; k >= 0; --k)
-                for (int l = s - k; l >= 0; --l) {
-                    const int m = s - k - l;
-                    herm[gx::herm_index(k, l, m)] = (uint32_t)(k | (l << 8) | (m << 16));
-                }
-        upload(ctx->herm, herm, ctx->stream);
-        {
-            std::vector<int2> plan;
-            std::vector<int> off{0, 0};  // L = 0 has no steps
-            for (int L = 1; L <= gx::REC_PLAN_MAX; ++L) {
-                for (int n = L - 1; n >= 0; --n) {
-                    for (int dg = L - n; dg >= 1; --dg)
-                        for (int k = dg; k >= 0; --k)
-                            for (int l = dg - k; l >= 0; --l) {
-                                const int m = dg - k - l;
-                                int axis, pw, i1, i2;
-                                if (k > 0) {
-                                    axis = 0, pw = k, i1 = gx::herm_index(k - 1, l, m);
-                                    i2 = k > 1 ? gx::herm_index(k - 2, l, m) : 0;
-                                } else if (l > 0) {
-                                    axis = 1, pw = l, i1 = gx::herm_index(0, l - 1, m);
-                                    i2 = l > 1 ? gx::herm_index(0, l - 2, m) : 0;
-                                } else {
-                                    axis = 2, pw = m, i1 = gx::herm_index(0, 0, m - 1);
-                                    i2 = m > 1 ? gx::herm_index(0, 0, m - 2) : 0;
-                                }
-                                plan.push_back(make_int2(gx::herm_index(k, l, m) | (i1 << 16),
-                                                         i2 | (axis << 14) | ((pw - 1) << 16)));
-                            }
-                    plan.push_back(make_int2(0, (1 << 22) | (n << 23)));
-                }
-                off.push_back((int)plan.size());
-            }
-            upload(ctx->rec_plan, plan, ctx->stream);
-            upload(ctx->rec_plan_off, off, ctx->stream);
-        }
         ctx->status.reserve(sizeof(gx::DevStatus));
-        const size_t npts = (size_t)gx::BOYS_NX * gx::BOYS_NY;
-        ctx->boys_S.reserve(npts * gx::BOYS_TABLE_ORDERS * sizeof(double2));
-        ctx->boys_E0.reserve(npts * sizeof(double2));
-        DeviceBuffer fails;  // [0]: points worse than 1e-13, [1]: worst relative agreement (double bits)
-        fails.reserve(2 * sizeof(unsigned long long));
-        GX_CUDA(cudaMemsetAsync(fails.ptr, 0, 2 * sizeof(unsigned long long), ctx->stream));
-        GX_CUDA(gx::launch_boys_table(ctx->boys_S.as<double2>(), ctx->boys_E0.as<double2>(),
-                                      ctx->gl.as<gx::GLRules>(), fails.as<int>(), ctx->stream));
-        unsigned long long words[2] = {0, 0};
-        GX_CUDA(cudaMemcpyAsync(words, fails.ptr, sizeof words, cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(cudaStreamSynchronize(ctx->stream));
-        double worst;
-        std::memcpy(&worst, &words[1], sizeof worst);
-        ctx->boys_table_agreement = worst;
-        (void)worst;
+        ctx->t = device_tables(device, ctx->stream);
         *out = ctx.release();
     });
 }
@@ -1855,7 +1966,7 @@ int gx_boys(gx_context* ctx, const double* z, int64_t count, int nmax, int scale
         GX_CUDA(cudaMemcpyAsync(ctx->scratch_a.ptr, z, nz, cudaMemcpyHostToDevice, ctx->stream));
         ctx->reset_status();
         GX_CUDA(gx::launch_boys_values(ctx->scratch_a.as<double2>(), count, nmax, scaled, ctx->boys(),
-                                       ctx->gl.as<gx::GLRules>(), ctx->scratch_b.as<double2>(),
+                                       ctx->t->gl.as<gx::GLRules>(), ctx->scratch_b.as<double2>(),
                                        region ? ctx->scratch_c.as<int>() : nullptr,
                                        ctx->status.as<gx::DevStatus>(), ctx->stream));
         check_status(ctx);
@@ -2182,8 +2293,8 @@ int gx_nuclear_attraction(gx_context* ctx, gx_basis* b, const double* B, const d
         upload(d_seg, seg_ao, st);
         ctx->scratch_b.reserve((size_t)n * n * sizeof(double2));
         ctx->reset_status();
-        GX_CUDA(gx::launch_nuclear(b->dev(), pair_view(b, fp), ctx->boys(), ctx->gl.as<gx::GLRules>(),
-                                   ctx->herm.as<uint32_t>(), b->d_classes.as<gx::PairClassDev>(),
+        GX_CUDA(gx::launch_nuclear(b->dev(), pair_view(b, fp), ctx->boys(), ctx->t->gl.as<gx::GLRules>(),
+                                   ctx->t->herm.as<uint32_t>(), b->d_classes.as<gx::PairClassDev>(),
                                    b->d_pp_class.as<int>(), nnuc, ctx->scratch_c.as<double>(),
                                    ctx->scratch_c.as<double>() + nnuc, d_seg.as<long long>(), n, 2 * lmax, nab_max,
                                    ctx->scratch_b.as<double2>(), ctx->status.as<gx::DevStatus>(), st));

@@ -27,6 +27,7 @@ struct Task {
     int sa, sb, sc, sd;
     long long out_off;  // complex-element offset of element (0,0,0,0)
     int st[4];          // complex-element strides of the component indices
+    int pab, pcd;       // first primitive-pair record (sorted order) of the bra pair (sa, sb) and ket pair (sc, sd)
 };
 
 // Per-(basis, field) primitive-pair data, structure of arrays.

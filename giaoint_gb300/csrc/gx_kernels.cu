@@ -996,7 +996,6 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     double2* stg = qc.stage_e > 0 ? reinterpret_cast<double2*>(base + lay.stage) : nullptr;  // E~ staging
     const int nab = qc.bra.nab, ncd = qc.ket.nab;
     const int ncb = ncart(qc.bra.lb), ncdd = ncart(qc.ket.lb);
-    const int ns = d.basis.ns;
     const PairData& pp = d.pairs;
     // Mixed precision runs in the same batches as FP64: every entry carries its
     // own precision (FP32 below cut32), FP32 R columns share the slots of the
@@ -1053,8 +1052,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         const int g = idx / KK, r = idx - g * KK;
                         const int P = r / Kcd, Q = r - P * Kcd;
                         const Task tg = qc.tasks[gi.x + g];
-                        const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
-                        const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
+                        const int op = tg.pab + P;
+                        const int oq = tg.pcd + Q;
                         const float b = pp.sbound[op] * pp.sbound[oq];
                         valid = b >= skip64;
                     }
@@ -1081,13 +1080,13 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                         const int g = idx / KK, r = idx - g * KK;
                         const int P = r / Kcd, Q = r - P * Kcd;
                         const Task tg = qc.tasks[gi.x + g];
-                        const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                        const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                        const int ip = pp.order[tg.pab + P];
+                        const int iq = pp.order[tg.pcd + Q];
                         const QuartetArgs qa = quartet_args(pp, ip, iq);
                         double2 Sh[BOYS_MAX_ORDER + 1];
                         float2 S32[BOYS_MAX_ORDER + 1];
-                        const bool want32 = mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
-                                                             pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] <
+                        const bool want32 = mixed && pp.sbound[tg.pab + P] *
+                                                             pp.sbound[tg.pcd + Q] <
                                                          cut32;
                         int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
                         if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
@@ -1115,14 +1114,14 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                             const int g = idx / KK, r = idx - g * KK;
                             const int P = r / Kcd, Q = r - P * Kcd;
                             const Task tg = qc.tasks[gi.x + g];
-                            const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                            const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                            const int ip = pp.order[tg.pab + P];
+                            const int iq = pp.order[tg.pcd + Q];
                             const QuartetArgs qa = quartet_args(pp, ip, iq);
                             double2 Sh[BOYS_MAX_ORDER + 1];
                             float2 S32[BOYS_MAX_ORDER + 1];
                             const bool want32 =
-                                mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
-                                                 pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] < cut32;
+                                mixed && pp.sbound[tg.pab + P] *
+                                                 pp.sbound[tg.pcd + Q] < cut32;
                             int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
                             if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
                             if (f == 1) {
@@ -1153,13 +1152,13 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                     const int g = idx / KK, r = idx - g * KK;
                     const int P = r / Kcd, Q = r - P * Kcd;
                     const Task tg = qc.tasks[gi.x + g];
-                    const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                    const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                    const int ip = pp.order[tg.pab + P];
+                    const int iq = pp.order[tg.pcd + Q];
                     const QuartetArgs qa = quartet_args(pp, ip, iq);
                     double2 Sh[BOYS_MAX_ORDER + 1];
                     float2 S32[BOYS_MAX_ORDER + 1];
-                    const bool want32 = mixed && pp.sbound[d.basis.sp_off[tg.sa * ns + tg.sb] + P] *
-                                                         pp.sbound[d.basis.sp_off[tg.sc * ns + tg.sd] + Q] <
+                    const bool want32 = mixed && pp.sbound[tg.pab + P] *
+                                                         pp.sbound[tg.pcd + Q] <
                                                      cut32;
                     int f = entry_seeds(d, qc.L, want32 ? 1 : 0, qa, Sh, S32, gi.x + g);
                     if (f == 2) f = 1;  // FP32 seeds out of range: this entry runs in FP64
@@ -1187,7 +1186,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                             __syncwarp();
                             const int cg = cur / Kab, cP = cur - cg * Kab;
                             const Task tc = qc.tasks[gi.x + cg];
-                            step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64,
+                            step_b_any(d, qc, tabs, tc, pp.order[tc.pab + cP], W, W32, any64,
                                        any32, stg, c0, chn, lane);
                             __syncwarp();
                             for (int it = lane; it < qc.Nab * qc.CH; it += 32) {
@@ -1233,7 +1232,7 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
                 __syncwarp();
                 const int cg = cur / Kab, cP = cur - cg * Kab;
                 const Task tc = qc.tasks[gi.x + cg];
-                step_b_any(d, qc, tabs, tc, pp.order[d.basis.sp_off[tc.sa * ns + tc.sb] + cP], W, W32, any64, any32, stg,
+                step_b_any(d, qc, tabs, tc, pp.order[tc.pab + cP], W, W32, any64, any32, stg,
                            c0, chn, lane);
             }
             __syncwarp();

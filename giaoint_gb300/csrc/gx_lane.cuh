@@ -181,7 +181,6 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
     int* queue = s_queue[wib];
     const int nwarp = gridDim.x * (blockDim.x >> 5);
     const PairData& pp = d.pairs;
-    const int ns = d.basis.ns;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
     unsigned n32 = 0;
     for (int grp = blockIdx.x * (blockDim.x >> 5) + wib; grp < qc.ngroup; grp += nwarp) {
@@ -203,8 +202,8 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                         const int g = idx / KK, r = idx - g * KK;
                         const int P = r / Kcd, Q = r - P * Kcd;
                         const Task tg = qc.tasks[gi.x + g];
-                        const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
-                        const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
+                        const int op = tg.pab + P;
+                        const int oq = tg.pcd + Q;
                         const float b = pp.sbound[op] * pp.sbound[oq];
                         valid = b >= skip && b < cut32 &&
                                 (pass == 0) == boys_asymptotic32(pp, pp.order[op], pp.order[oq], L);
@@ -237,8 +236,8 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                     const int P = r / Kcd, Q = r - P * Kcd;
                     key = g;
                     tg = qc.tasks[gi.x + g];
-                    ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                    iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                    ip = pp.order[tg.pab + P];
+                    iq = pp.order[tg.pcd + Q];
                     const double p = pp.p[ip], q = pp.p[iq];
 #pragma unroll
                     for (int x = 0; x < 3; ++x)
@@ -262,10 +261,15 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                     } else {
                         small::quartet_seeds<L>(d, gi.x + g, C, rho, tre, tim, Sh);
                     }
-                    double m = 0.0;
+                    // largest binary exponent of the seeds, read from the bits
+                    // (integer work: no FP64 instruction)
 #pragma unroll
-                    for (int n = 0; n <= L; ++n) m = fmax(m, fabs(Sh[n].x) + fabs(Sh[n].y));
-                    if (m > 0.0 && m <= 1.0e300) e_lane = ilogb(m);
+                    for (int n = 0; n <= L; ++n) {
+                        const int ex = (__double2hiint(Sh[n].x) >> 20) & 0x7ff;
+                        const int ey = (__double2hiint(Sh[n].y) >> 20) & 0x7ff;
+                        const int e = max(ex, ey);
+                        if (e > 0 && e < 0x7ff) e_lane = max(e_lane, e - 1023);
+                    }
                 }
                 // segment structure: heads, the take masks of the reduction and
                 // the largest seed exponent of each segment, broadcast to it

@@ -297,7 +297,6 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, QuartetClass qc) {
     int* queue = s_queue[wib];
     const int nwarp = gridDim.x * (blockDim.x >> 5);
     const PairData& pp = d.pairs;
-    const int ns = d.basis.ns;
     const float skip = d.skip_cut, cut32 = d.fp32_cut;
     const float cut64 = fmaxf(cut32, skip);
     // Mixed precision: pass 0 evaluates the FP64 quartets, pass 1 the FP32
@@ -336,8 +335,8 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, QuartetClass qc) {
                         const int g = idx / KK, r = idx - g * KK;
                         const int P = r / Kcd, Q = r - P * Kcd;
                         const Task tg = qc.tasks[gi.x + g];
-                        const int op = d.basis.sp_off[tg.sa * ns + tg.sb] + P;
-                        const int oq = d.basis.sp_off[tg.sc * ns + tg.sd] + Q;
+                        const int op = tg.pab + P;
+                        const int oq = tg.pcd + Q;
                         const float b = pp.sbound[op] * pp.sbound[oq];
                         valid = pass == 0 ? b >= cut64 : (b >= skip && b < cut32);
                         if (valid && pass > 0)
@@ -374,8 +373,8 @@ __global__ void __launch_bounds__(128) small_kernel(EriDev d, QuartetClass qc) {
                     const int P = r / Kcd, Q = r - P * Kcd;
                     key = g;
                     const Task tg = qc.tasks[gi.x + g];
-                    const int ip = pp.order[d.basis.sp_off[tg.sa * ns + tg.sb] + P];
-                    const int iq = pp.order[d.basis.sp_off[tg.sc * ns + tg.sd] + Q];
+                    const int ip = pp.order[tg.pab + P];
+                    const int iq = pp.order[tg.pcd + Q];
                     const double p = pp.p[ip], q = pp.p[iq];
                     const double2 X[3] = {c2(pp.Pr[3 * ip] - pp.Pr[3 * iq], pp.Pi[3 * ip] - pp.Pi[3 * iq]),
                                           c2(pp.Pr[3 * ip + 1] - pp.Pr[3 * iq + 1], pp.Pi[3 * ip + 1] - pp.Pi[3 * iq + 1]),

@@ -56,8 +56,10 @@ def footprint_bytes(request) -> int:
     n = int(sizes.sum())
     N = n * n
     rank_guess = min(N, max(64, 8 * n))
-    # factors, column pool (1344 columns), residual/diagonal/work vectors
-    return _BASE_BYTES + (rank_guess + 1344 + 4) * N * 16
+    # factor rows (the first allocation; they grow on the device when the
+    # rank passes it), column slots (256 batch + at most 1024 cached + 64),
+    # the rank-chunk partial sums (8 columns) and residual/diagonal/work vectors
+    return _BASE_BYTES + (rank_guess + 1344 + 8 + 4) * N * 16
 
 
 @dataclass
@@ -102,9 +104,14 @@ class Server:
     half of the device's free memory at start-up."""
 
     def __init__(self, slots: int = 4, *, hbm_budget: int | None = None, precision: str = "fp64",
-                 mixed_cutoff: float = 1e-6, device: int = 0, runner=None, bases_per_slot: int = 32):
+                 mixed_cutoff: float = 1e-6, device: int = 0, runner=None, bases_per_slot: int = 32,
+                 max_request_bytes: int | None = None):
         if slots < 1:
             raise ValueError("slots must be a positive integer")
+        # per-request device-memory limit (None: the whole budget); a request
+        # estimated above it is refused with MemoryError at submission
+        self.max_request_bytes = None if max_request_bytes is None else int(max_request_bytes)
+        self.refused = 0
         self.slots = int(slots)
         self.precision = precision
         self.mixed_cutoff = float(mixed_cutoff)
@@ -136,9 +143,12 @@ class Server:
         """Queue a request; the future resolves to its ``Completion``."""
         fp = footprint_bytes(request)
         p = _Pending(index, request, self.now() if arrival is None else arrival, fp)
-        if fp > self.hbm_budget:
+        limit = self.hbm_budget if self.max_request_bytes is None else min(self.hbm_budget, self.max_request_bytes)
+        if fp > limit:
+            self.refused += 1
+            which = "serving budget" if limit == self.hbm_budget else "per-request limit"
             p.future.set_exception(MemoryError(
-                f"request needs about {fp} bytes of device memory; the serving budget is {self.hbm_budget} bytes"))
+                f"request needs about {fp} bytes of device memory; the {which} is {limit} bytes"))
             return p.future
         with self._cv:
             if self._closing:
@@ -158,11 +168,12 @@ class Server:
                     time.sleep(delay)
             futures.append(self.submit(r, i, arrival=r.arrival if realtime else self.now()))
         out = []
-        for f in futures:
+        for i, f in enumerate(futures):
             try:
                 out.append(f.result())
             except BaseException as e:  # noqa: BLE001 - reported per request
-                out.append(Completion(-1, "error", 0.0, error=e))
+                r = requests[i]
+                out.append(Completion(i, getattr(r, "kind", "error"), getattr(r, "arrival", 0.0), error=e))
         return out
 
     def close(self) -> None:
@@ -273,8 +284,9 @@ class Server:
 def latency_summary(done: list[Completion]) -> dict:
     """p50 / p99 latency, queue wait and throughput of a served trace."""
     ok = [c for c in done if c.error is None]
+    refused = sum(isinstance(c.error, MemoryError) for c in done)
     if not ok:
-        return {"requests": len(done), "completed": 0}
+        return {"requests": len(done), "completed": 0, "refused_memory": refused}
     lat = np.array([c.latency for c in ok]) * 1e3
     wait = np.array([c.queue_wait for c in ok]) * 1e3
     start = min(c.arrival for c in ok)
@@ -283,6 +295,7 @@ def latency_summary(done: list[Completion]) -> dict:
     out = {
         "requests": len(done),
         "completed": len(ok),
+        "refused_memory": refused,
         "p50_ms": float(np.percentile(lat, 50)),
         "p99_ms": float(np.percentile(lat, 99)),
         "mean_ms": float(lat.mean()),

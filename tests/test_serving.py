@@ -91,3 +91,21 @@ def test_runner_errors_reach_the_caller():
         fut = srv.submit(reqs[0])
         with pytest.raises(ValueError, match="bad request"):
             fut.result(timeout=5)
+
+
+def test_per_request_limit_refuses_and_counts():
+    """A request estimated above the per-request device-memory limit is
+    refused with MemoryError at submission; the rest of the trace is served
+    and the summary counts the refusals."""
+    reqs = _trace(12)
+    fps = sorted(footprint_bytes(r) for r in reqs)
+    limit = fps[len(fps) // 2]
+    with Server(slots=2, hbm_budget=1 << 50, max_request_bytes=limit, runner=lambda s, r: (None, 1)) as srv:
+        done = srv.run(reqs, realtime=False)
+    over = sum(footprint_bytes(r) > limit for r in reqs)
+    assert over > 0 and srv.refused == over
+    refused = [c for c in done if c.error is not None]
+    assert len(refused) == over and all(isinstance(c.error, MemoryError) for c in refused)
+    assert all("per-request limit" in str(c.error) for c in refused)
+    s = latency_summary(done)
+    assert s["refused_memory"] == over and s["completed"] == len(reqs) - over
