@@ -138,6 +138,10 @@ SIGNATURES = {
     "gx_cholesky_factors_stats": (ctypes.c_int, [_vp, ctypes.POINTER(GxCholeskyStats)]),
     "gx_cholesky_factors_destroy": (None, [_vp]),
     "gx_cholesky_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(GxCholeskyStats)]),
+    "gx_eri_batch_packed": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp), _d, _d, ctypes.POINTER(_u32), _i64,
+                                           ctypes.c_int, ctypes.c_double, ctypes.POINTER(_i64), ctypes.POINTER(_d),
+                                           _i64, _d]),
+    "gx_context_set_stable_launch": (ctypes.c_int, [_vp, ctypes.c_int]),
     "gx_context_set_stream": (ctypes.c_int, [_vp, _vp]),
     "gx_context_synchronize": (ctypes.c_int, [_vp]),
     "gx_eri_plan_create": (ctypes.c_int, [_vp, _vp, _u32, ctypes.c_int64, _i64, ctypes.POINTER(_vp)]),

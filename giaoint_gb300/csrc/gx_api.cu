@@ -202,6 +202,7 @@ struct gx_context {
     DeviceBuffer out, tasks, scratch_a, scratch_b, scratch_c;
     DeviceBuffer deriv_vals, deriv_meta;
     gx_cholesky_stats last_cholesky{};  // of the last factorisation on this context
+    bool stable_launch = false;         // plans built here use size-independent launch configurations
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -517,6 +518,8 @@ struct PlanData {
     GroupSet base;                  // default configuration
     std::vector<PlanClass> classes;
     std::vector<int> task_kk;       // per task (class order): Kab << 16 | Kcd, for regrouping
+    std::vector<int> task_part;     // per task: its part (request) of a packed plan; empty for one part
+    bool stable = false;            // launch configuration independent of the plan's size (see launch_class)
     int64_t ntask = 0, primitive_quartets = 0;
     double model_flops = 0.0;
     // autotuned configuration per precision mode (GX_PRECISION_*)
@@ -615,7 +618,15 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
         const int want = small ? std::max(1, std::min(128, per / kk))
                                : std::max(1, std::min({1024, (per + kk - 1) / kk, spread}));
         size_t j = i + 1;
-        while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
+        if (plan.task_part.empty()) {
+            while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
+        } else {
+            // a packed plan: units never mix requests, so that every request's
+            // units (and its results, bit for bit) are those of its plan alone
+            while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code &&
+                   plan.task_part[j] == plan.task_part[i])
+                ++j;
+        }
         groups.push_back(make_int2((int)(i - pc.first), (int)(j - i)));
         i = j;
     }
@@ -667,25 +678,40 @@ void apply_recorded_tuning(gx_context* ctx, const gx_basis* b, int precision, Pl
     plan.tuned[precision].valid = true;
 }
 
-// Class-sorted task list of `req`: one task per segmented shell quartet
-// (general contractions split), ordered by class (la, lb, lc, ld), then by
-// decreasing bra and ket primitive counts, then in request order -- a
-// parallel counting sort over (class, Kab, Kcd) buckets: per-chunk bucket
-// histograms, one prefix over (bucket, chunk), and a scatter pass.
-void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
-    // shell codes: distinct (l, nprim) of the segmented shells
+// One request of a plan: its basis, its blocks, and where its segmented
+// shells, primitive-pair records and output start in the packed numbering
+// (all zero for a plan of one basis).
+struct PlanPart {
+    const gx_basis* b;
+    const std::vector<QuartetRequest>* req;
+    int seg_base = 0, pair_base = 0;
+    int64_t out_base = 0;
+};
+
+// Class-sorted task list of the parts' blocks: one task per segmented shell
+// quartet (general contractions split), ordered by class (la, lb, lc, ld),
+// then by decreasing bra and ket primitive counts, then by part and request
+// order -- a parallel counting sort over (class, Kab, Kcd) buckets: per-chunk
+// bucket histograms, one prefix over (bucket, chunk), and a scatter pass.
+void build_plan_parts(gx_context* ctx, const std::vector<PlanPart>& parts, PlanData& plan) {
+    // shell codes: distinct (l, nprim) of the segmented shells of all parts
     std::map<std::pair<int, int>, int> code_of;
-    for (int s = 0; s < b->nseg; ++s) code_of.emplace(std::make_pair(b->seg_l[s], b->seg_nprim[s]), 0);
+    for (const auto& pt : parts)
+        for (int s = 0; s < pt.b->nseg; ++s) code_of.emplace(std::make_pair(pt.b->seg_l[s], pt.b->seg_nprim[s]), 0);
     std::vector<std::pair<int, int>> codes;
     for (auto& kv : code_of) {
         kv.second = (int)codes.size();
         codes.push_back(kv.first);
     }
     const int nsc = (int)codes.size();
-    std::vector<int> seg_code(b->nseg);
-    for (int s = 0; s < b->nseg; ++s) seg_code[s] = code_of[{b->seg_l[s], b->seg_nprim[s]}];
+    std::vector<std::vector<int>> part_code(parts.size());
+    for (size_t pi = 0; pi < parts.size(); ++pi) {
+        const gx_basis* b = parts[pi].b;
+        part_code[pi].resize(b->nseg);
+        for (int s = 0; s < b->nseg; ++s) part_code[pi][s] = code_of[{b->seg_l[s], b->seg_nprim[s]}];
+    }
     const int64_t ntuple = (int64_t)nsc * nsc * nsc * nsc;
-    if (ntuple > (int64_t)1 << 24) raise(GX_EINVAL, "too many distinct (l, primitive count) shells in one basis");
+    if (ntuple > (int64_t)1 << 24) raise(GX_EINVAL, "too many distinct (l, primitive count) shells in one plan");
     // buckets: distinct (la, lb, lc, ld, -Kab, -Kcd) in sorted order
     using BKey = std::array<int, 6>;
     std::vector<BKey> tkey(ntuple);
@@ -702,19 +728,33 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
     std::vector<int> bucket_of(ntuple);
     for (int64_t t = 0; t < ntuple; ++t)
         bucket_of[t] = (int)(std::lower_bound(bkeys.begin(), bkeys.end(), tkey[t]) - bkeys.begin());
-    auto tuple_of = [&](int a, int bb, int c, int d) {
-        return ((int64_t)(seg_code[a] * nsc + seg_code[bb]) * nsc + seg_code[c]) * nsc + seg_code[d];
-    };
-    const int64_t nreq = (int64_t)req.size();
+    // chunks of requests, never across parts: (part, first, end)
     constexpr int64_t kChunk = 1 << 15;
-    const int64_t nchunk = std::max<int64_t>(1, (nreq + kChunk - 1) / kChunk);
+    struct Chunk {
+        int part;
+        int64_t first, end;
+    };
+    std::vector<Chunk> chunks;
+    for (size_t pi = 0; pi < parts.size(); ++pi) {
+        const int64_t n = (int64_t)parts[pi].req->size();
+        for (int64_t f = 0; f < n; f += kChunk) chunks.push_back({(int)pi, f, std::min(n, f + kChunk)});
+    }
+    if (chunks.empty()) chunks.push_back({0, 0, 0});
+    const int64_t nchunk = (int64_t)chunks.size();
     std::vector<int64_t> hist((size_t)nchunk * nb, 0);
     // pass 1: bucket histograms per chunk
 #pragma omp parallel for schedule(static)
     for (int64_t c = 0; c < nchunk; ++c) {
         int64_t* h = hist.data() + (size_t)c * nb;
-        for (int64_t i = c * kChunk; i < std::min(nreq, (c + 1) * kChunk); ++i) {
-            const auto& r = req[i];
+        if (parts.empty()) continue;
+        const PlanPart& pt = parts[chunks[c].part];
+        const gx_basis* b = pt.b;
+        const std::vector<int>& seg_code = part_code[chunks[c].part];
+        auto tuple_of = [&](int a, int bb, int cc, int d) {
+            return ((int64_t)(seg_code[a] * nsc + seg_code[bb]) * nsc + seg_code[cc]) * nsc + seg_code[d];
+        };
+        for (int64_t i = chunks[c].first; i < chunks[c].end; ++i) {
+            const auto& r = (*pt.req)[i];
             for (int xa = 0; xa < b->ncontr[r.a]; ++xa)
                 for (int xb = 0; xb < b->ncontr[r.b]; ++xb)
                     for (int xc = 0; xc < b->ncontr[r.c]; ++xc)
@@ -738,12 +778,21 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
             raise(GX_EINVAL, "electron repulsion supports combined angular order through 32");
     std::unique_ptr<gx::Task[]> all(new gx::Task[std::max<int64_t>(T, 1)]);
     plan.task_kk.resize(T);
+    plan.task_part.assign(parts.size() > 1 ? T : 0, 0);
     // pass 2: scatter
 #pragma omp parallel for schedule(static)
     for (int64_t c = 0; c < nchunk; ++c) {
         int64_t* cur = hist.data() + (size_t)c * nb;
-        for (int64_t i = c * kChunk; i < std::min(nreq, (c + 1) * kChunk); ++i) {
-            const auto& r = req[i];
+        if (parts.empty()) continue;
+        const int pidx = chunks[c].part;
+        const PlanPart& pt = parts[pidx];
+        const gx_basis* b = pt.b;
+        const std::vector<int>& seg_code = part_code[pidx];
+        auto tuple_of = [&](int a, int bb, int cc, int d) {
+            return ((int64_t)(seg_code[a] * nsc + seg_code[bb]) * nsc + seg_code[cc]) * nsc + seg_code[d];
+        };
+        for (int64_t i = chunks[c].first; i < chunks[c].end; ++i) {
+            const auto& r = (*pt.req)[i];
             const int sh[4] = {(int)r.a, (int)r.b, (int)r.c, (int)r.d};
             int64_t N[4];
             int nc[4];
@@ -757,22 +806,25 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
                     for (int xc = 0; xc < b->ncontr[sh[2]]; ++xc)
                         for (int xd = 0; xd < b->ncontr[sh[3]]; ++xd) {
                             gx::Task t;
-                            t.sa = b->seg_first[sh[0]] + xa;
-                            t.sb = b->seg_first[sh[1]] + xb;
-                            t.sc = b->seg_first[sh[2]] + xc;
-                            t.sd = b->seg_first[sh[3]] + xd;
-                            t.out_off = r.out_off + (int64_t)xa * nc[0] * st0 + (int64_t)xb * nc[1] * st1 +
-                                        (int64_t)xc * nc[2] * st2 + (int64_t)xd * nc[3];
+                            const int ga = b->seg_first[sh[0]] + xa, gb = b->seg_first[sh[1]] + xb;
+                            const int gc = b->seg_first[sh[2]] + xc, gd = b->seg_first[sh[3]] + xd;
+                            t.sa = pt.seg_base + ga;
+                            t.sb = pt.seg_base + gb;
+                            t.sc = pt.seg_base + gc;
+                            t.sd = pt.seg_base + gd;
+                            t.out_off = pt.out_base + r.out_off + (int64_t)xa * nc[0] * st0 +
+                                        (int64_t)xb * nc[1] * st1 + (int64_t)xc * nc[2] * st2 + (int64_t)xd * nc[3];
                             t.st[0] = st0;
                             t.st[1] = st1;
                             t.st[2] = st2;
                             t.st[3] = 1;
-                            t.pab = b->sp_off[(size_t)t.sa * b->nseg + t.sb];
-                            t.pcd = b->sp_off[(size_t)t.sc * b->nseg + t.sd];
-                            const int64_t pos = cur[bucket_of[tuple_of(t.sa, t.sb, t.sc, t.sd)]]++;
+                            t.pab = pt.pair_base + b->sp_off[(size_t)ga * b->nseg + gb];
+                            t.pcd = pt.pair_base + b->sp_off[(size_t)gc * b->nseg + gd];
+                            const int64_t pos = cur[bucket_of[tuple_of(ga, gb, gc, gd)]]++;
                             all[pos] = t;
-                            plan.task_kk[pos] = (b->seg_nprim[t.sa] * b->seg_nprim[t.sb]) << 16 |
-                                                (b->seg_nprim[t.sc] * b->seg_nprim[t.sd]);
+                            plan.task_kk[pos] = (b->seg_nprim[ga] * b->seg_nprim[gb]) << 16 |
+                                                (b->seg_nprim[gc] * b->seg_nprim[gd]);
+                            if (!plan.task_part.empty()) plan.task_part[pos] = pidx;
                         }
         }
     }
@@ -802,12 +854,17 @@ void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>&
         bk = e;
     }
     plan.ntask = T;
+    plan.stable = ctx->stable_launch;
     plan.tasks.reserve(sizeof(gx::Task) * std::max<int64_t>(T, 1));
     if (T) GX_CUDA(cudaMemcpyAsync(plan.tasks.ptr, all.get(), sizeof(gx::Task) * T, cudaMemcpyHostToDevice, ctx->stream));
     std::vector<ClassConf> defaults(plan.classes.size());
     make_group_set(ctx, plan, defaults, plan.base);
     // (a copy from pageable memory is staged before cudaMemcpyAsync returns,
     // so the host task array may be freed now)
+}
+
+void build_plan(gx_context* ctx, gx_basis* b, const std::vector<QuartetRequest>& req, PlanData& plan) {
+    build_plan_parts(ctx, {PlanPart{b, &req}}, plan);
 }
 
 // Primitive screening thresholds on the Schwarz product B_P B_Q.  FP64: a
@@ -868,8 +925,10 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
     qc.CH = std::max(1, std::min(ncd, 2048 / qc.Nab));
     // Few work units: split the ket components of a group over several
     // warps (each chunk keeps at least 32 ket-transform rows per warp).
+    // (not in a stable plan: there the configuration of a class does not depend
+    // on how many tasks it holds, so a request gives the same bits in any pack)
     const int target_units = 8 * std::max(ctx->sm_count, 1);
-    if (ngroup > 0 && ngroup * ((ncd + qc.CH - 1) / qc.CH) < target_units) {
+    if (!plan.stable && ngroup > 0 && ngroup * ((ncd + qc.CH - 1) / qc.CH) < target_units) {
         const int want = (target_units + ngroup - 1) / ngroup;
         const int ch = std::max((ncd + want - 1) / want, (32 + qc.Nab - 1) / qc.Nab);
         qc.CH = std::max(1, std::min(qc.CH, ch));
@@ -973,12 +1032,21 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
 // the autotuned configuration of the precision mode when there is one.
 // counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null;
 // zeroed first unless `accumulate`.
+int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, int precision,
+                 unsigned long long* counters, bool accumulate);
+
 int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
                  double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
                  unsigned long long* counters = nullptr, bool accumulate = false) {
-    cudaStream_t s = ctx->stream;
     FieldPairs& fp = field_pairs(b, B, O);
     const gx::EriDev dev = make_dev(ctx, b, fp, out, precision, mixed_cutoff);
+    return enqueue_plan(ctx, dev, plan, precision, counters, accumulate);
+}
+
+// Enqueue every class launch of `plan` for the evaluation view `dev`.
+int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, int precision,
+                 unsigned long long* counters, bool accumulate) {
+    cudaStream_t s = ctx->stream;
     if (counters && !accumulate) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
     ctx->reset_status();
     const auto& tuned = plan.tuned[precision];
@@ -1288,6 +1356,183 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         }
     });
 }
+
+// ---------------------------------------------------------------------------
+// packed requests: several (basis, field, quartet list) in one execution
+// ---------------------------------------------------------------------------
+
+// Primitive-pair records of several (basis, field) requests side by side:
+// each request's records keep their layout at a pair base and an E~ base,
+// with the record indices (order) and E~ offsets (Eoff) shifted by them, and
+// the primitive counts of their segmented shells at a segment base.
+struct PackedPairs {
+    DeviceBuffer nprim, p, Pr, Pi, F, Eoff, Epool, bound, Epool32, order, sbound, g32;
+    int npp = 0, nseg = 0;
+};
+
+void pack_pairs(gx_context* ctx, const std::vector<gx_basis*>& bases, const double* B, const double* O,
+                PackedPairs& pk, std::vector<int>& seg_base, std::vector<int>& pair_base) {
+    cudaStream_t st = ctx->stream;
+    int64_t npp = 0, nseg = 0, E = 0;
+    for (gx_basis* b : bases) {
+        npp += b->npp;
+        nseg += b->nseg;
+        E += b->Etotal;
+    }
+    if (npp > (int64_t)INT32_MAX || nseg > (int64_t)INT32_MAX) raise(GX_ELENGTH, "packed requests are too large");
+    const size_t n = std::max<int64_t>(npp, 1), e = std::max<int64_t>(E, 1);
+    pk.p.reserve(n * sizeof(double));
+    pk.Pr.reserve(3 * n * sizeof(double));
+    pk.Pi.reserve(3 * n * sizeof(double));
+    pk.F.reserve(n * sizeof(double2));
+    pk.Eoff.reserve(n * sizeof(long long));
+    pk.bound.reserve(n * sizeof(double));
+    pk.order.reserve(n * sizeof(int));
+    pk.sbound.reserve(n * sizeof(float));
+    pk.g32.reserve(2 * n * sizeof(float4));
+    pk.Epool.reserve(e * sizeof(double2));
+    pk.Epool32.reserve(e * sizeof(float2));
+    std::vector<int> nprim;
+    seg_base.clear();
+    pair_base.clear();
+    int64_t pb = 0, eb = 0;
+    for (size_t r = 0; r < bases.size(); ++r) {
+        gx_basis* b = bases[r];
+        seg_base.push_back((int)nprim.size());
+        pair_base.push_back((int)pb);
+        nprim.insert(nprim.end(), b->seg_nprim.begin(), b->seg_nprim.end());
+        FieldPairs& fp = field_pairs(b, B + 3 * r, O + 3 * r);
+        const int64_t m = b->npp;
+        auto cp = [&](DeviceBuffer& dst, const DeviceBuffer& src, size_t elem, int64_t first, int64_t count) {
+            if (count > 0)
+                GX_CUDA(cudaMemcpyAsync(static_cast<char*>(dst.ptr) + first * elem, src.ptr, count * elem,
+                                        cudaMemcpyDeviceToDevice, st));
+        };
+        cp(pk.p, fp.p, sizeof(double), pb, m);
+        cp(pk.Pr, fp.Pr, 3 * sizeof(double), pb, m);
+        cp(pk.Pi, fp.Pi, 3 * sizeof(double), pb, m);
+        cp(pk.F, fp.F, sizeof(double2), pb, m);
+        cp(pk.bound, fp.bound, sizeof(double), pb, m);
+        cp(pk.sbound, fp.sbound, sizeof(float), pb, m);
+        cp(pk.g32, fp.g32, 2 * sizeof(float4), pb, m);
+        cp(pk.Epool, fp.Epool, sizeof(double2), eb, b->Etotal);
+        cp(pk.Epool32, fp.Epool32, sizeof(float2), eb, b->Etotal);
+        GX_CUDA(gx::launch_offset_copy(pk.order.as<int>() + pb, fp.order.as<int>(), m, (int)pb, st));
+        GX_CUDA(gx::launch_offset_copy(pk.Eoff.as<long long>() + pb, b->d_Eoff.as<long long>(), m, (long long)eb,
+                                       st));
+        // the next request's field_pairs may rewrite this basis's records
+        // (same basis, other field): the copies above come first on the stream
+        pb += m;
+        eb += b->Etotal;
+    }
+    upload(pk.nprim, nprim, st);
+    pk.npp = (int)npp;
+    pk.nseg = (int)nseg;
+}
+
+}  // namespace
+
+extern "C" int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* bases, const double* B,
+                                   const double* O, const uint32_t* const* quartets, const int64_t* nq, int precision,
+                                   double mixed_cutoff, int64_t* const* offsets, double* const* values,
+                                   const int64_t* capacity, double* kernel_ms) {
+    return guarded([&] {
+        if (!ctx || nreq < 0 || (nreq > 0 && (!bases || !B || !O || !quartets || !nq || !offsets || !values ||
+                                               !capacity)))
+            raise(GX_EINVAL, "null argument");
+        if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
+            raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
+        if (precision == GX_PRECISION_MIXED && !(std::isfinite(mixed_cutoff) && mixed_cutoff >= 0.0))
+            raise(GX_EINVAL, "mixed_cutoff must be finite and non-negative");
+        for (int r = 0; r < nreq; ++r) {
+            if (!bases[r] || bases[r]->ctx != ctx) raise(GX_EINVAL, "every basis must belong to the context");
+            check_field(B + 3 * r, O + 3 * r);
+            if (nq[r] < 0 || (nq[r] > 0 && !quartets[r])) raise(GX_EINVAL, "null quartet list");
+            validate_quartets(bases[r], quartets[r], nq[r]);
+        }
+        if (kernel_ms) *kernel_ms = 0.0;
+        if (nreq == 0) return;
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        GX_CUDA(cudaSetDevice(ctx->device));
+        // blocks of every request at its own output base, offsets relative to it
+        std::vector<std::vector<QuartetRequest>> reqs(nreq);
+        std::vector<int64_t> base(nreq + 1, 0);
+        for (int r = 0; r < nreq; ++r) {
+            const gx_basis* b = bases[r];
+            int64_t o = 0;
+            reqs[r].reserve((size_t)nq[r]);
+            for (int64_t i = 0; i < nq[r]; ++i) {
+                const uint32_t* x = quartets[r] + 4 * i;
+                offsets[r][i] = o;
+                reqs[r].push_back({x[0], x[1], x[2], x[3], o});
+                o += b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+            }
+            offsets[r][nq[r]] = o;
+            if (o > capacity[r]) raise(GX_ELENGTH, "ERI output buffer is too small");
+            base[r + 1] = base[r] + o;
+        }
+        std::vector<gx_basis*> bv(bases, bases + nreq);
+        PackedPairs pk;
+        std::vector<int> seg_base, pair_base;
+        pack_pairs(ctx, bv, B, O, pk, seg_base, pair_base);
+        std::vector<PlanPart> parts;
+        for (int r = 0; r < nreq; ++r) parts.push_back({bases[r], &reqs[r], seg_base[r], pair_base[r], base[r]});
+        PlanData plan;
+        build_plan_parts(ctx, parts, plan);
+        const int64_t total = base[nreq];
+        ctx->out.reserve(std::max<int64_t>(total, 1) * sizeof(double2));
+        gx::EriDev dev = make_dev(ctx, bases[0], field_pairs(bases[0], B, O), ctx->out.as<double2>(), precision,
+                                  mixed_cutoff);
+        dev.basis = gx::BasisDev{};
+        dev.basis.ns = pk.nseg;
+        dev.basis.nprim = pk.nprim.as<int>();
+        dev.pairs = gx::PairData{pk.npp,
+                                 pk.p.as<double>(),
+                                 pk.Pr.as<double>(),
+                                 pk.Pi.as<double>(),
+                                 pk.F.as<double2>(),
+                                 pk.Eoff.as<long long>(),
+                                 pk.Epool.as<double2>(),
+                                 pk.bound.as<double>(),
+                                 pk.Epool32.as<float2>(),
+                                 pk.order.as<int>(),
+                                 pk.sbound.as<float>(),
+                                 pk.g32.as<float4>()};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (kernel_ms) {
+            GX_CUDA(cudaEventCreate(&e0));
+            GX_CUDA(cudaEventCreate(&e1));
+            GX_CUDA(cudaEventRecord(e0, ctx->stream));
+        }
+        if (plan.ntask) enqueue_plan(ctx, dev, plan, precision, nullptr, false);
+        if (kernel_ms) GX_CUDA(cudaEventRecord(e1, ctx->stream));
+        for (int r = 0; r < nreq; ++r)
+            if (base[r + 1] > base[r])
+                GX_CUDA(cudaMemcpyAsync(values[r], ctx->out.as<double2>() + base[r],
+                                        (base[r + 1] - base[r]) * sizeof(double2), cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+        GX_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (kernel_ms) {
+            float ms = 0.0f;
+            GX_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            *kernel_ms = ms;
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        check_status(ctx);
+    });
+}
+
+extern "C" int gx_context_set_stable_launch(gx_context* ctx, int stable) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        ctx->stable_launch = stable != 0;
+        drop_cached_plans(ctx, nullptr);  // cached plans were built under the other setting
+    });
+}
+
+namespace {
 
 // ---------------------------------------------------------------------------
 // ERI centre derivatives

@@ -131,6 +131,8 @@ cudaError_t launch_pair_precompute(const BasisDev& basis, const double* B, const
 size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed);
 cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps_per_block, int grid,
                             cudaStream_t s);
+cudaError_t launch_offset_copy(int* dst, const int* src, long long n, int off, cudaStream_t s);
+cudaError_t launch_offset_copy(long long* dst, const long long* src, long long n, long long off, cudaStream_t s);
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
                                 long long n, double2* full, cudaStream_t s);
 

@@ -20,6 +20,7 @@
 // on the primitive pair, so it is computed once per (basis, field) by
 // pair_kernel; per primitive quartet only Rh (C(L+3,3) entries) and the two
 // contractions remain.
+#include <algorithm>
 #include <cstdio>
 
 #include "gx_internal.h"
@@ -1340,6 +1341,28 @@ cudaError_t launch_scatter_full(const double2* packed, const long long* block_of
     const int gx = nblocks < 65535 ? nblocks : 65535;
     const int gy = (nblocks + gx - 1) / gx;
     scatter_full_kernel<<<dim3(gx, gy), 128, 0, s>>>(packed, block_off, block_info, nblocks, n, full);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Index arrays of packed pair records: dst[i] = src[i] + off.
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void offset_copy_kernel(T* dst, const T* src, long long n, T off) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i] + off;
+}
+
+cudaError_t launch_offset_copy(int* dst, const int* src, long long n, int off, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    offset_copy_kernel<int><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(dst, src, n, off);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_offset_copy(long long* dst, const long long* src, long long n, long long off, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    offset_copy_kernel<long long><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(dst, src, n, off);
     return cudaGetLastError();
 }
 

@@ -176,6 +176,46 @@ def eri_batches(basis: Basis, *, field: MagneticField | None = None, quartets: I
         yield emit()
 
 
+def _eri_batch_packed(items, *, precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF, context=None,
+                      stats: dict | None = None):
+    """Several requests in one class-sorted execution (gx_eri_batch_packed).
+
+    ``items`` is a sequence of (basis, quartets, field); returns one
+    (offsets int64[k+1], values complex128) pair per item, in the packed
+    block layout that ``_eri_batch`` gives the item alone (no screening)."""
+    ctx = context or nat.default_context()
+    n = len(items)
+    qs, offs, vals, caps = [], [], [], []
+    Bs = np.zeros((max(n, 1), 3))
+    Os = np.zeros((max(n, 1), 3))
+    for r, (basis, quartets, field) in enumerate(items):
+        q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+        if len(q) and (q.min() < 0 or q.max() >= len(basis.shells)):
+            raise IndexError("ERI shell-quartet index is out of range")
+        q = q.astype(np.uint32)
+        sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+        total = int(np.prod(sizes[q.astype(np.int64)], axis=1).sum()) if len(q) else 0
+        qs.append(q)
+        offs.append(np.zeros(len(q) + 1, dtype=np.int64))
+        vals.append(np.empty(max(total, 1), dtype=np.complex128))
+        caps.append(total)
+        Bs[r], Os[r] = field_arrays(field)
+    lib = nat.lib()
+    handles = (ctypes.c_void_p * max(n, 1))(*[b._device(ctx).value for b, _, _ in items])
+    qptr = (nat._u32 * max(n, 1))(*[nat.u32ptr(q) for q in qs])
+    optr = (nat._i64 * max(n, 1))(*[nat.i64ptr(o) for o in offs])
+    vptr = (nat._d * max(n, 1))(*[nat.dptr(v.view(np.float64)) for v in vals])
+    nq = np.array([len(q) for q in qs] or [0], dtype=np.int64)
+    cap = np.array(caps or [0], dtype=np.int64)
+    ms = ctypes.c_double()
+    nat.check(lib.gx_eri_batch_packed(ctx.handle, n, handles, nat.dptr(Bs.reshape(-1)), nat.dptr(Os.reshape(-1)), qptr,
+                                      nat.i64ptr(nq), _precision(precision), float(mixed_cutoff), optr, vptr,
+                                      nat.i64ptr(cap), ctypes.byref(ms)))
+    if stats is not None:
+        stats["kernel_ms"] = ms.value
+    return [(o, v[: int(o[-1])]) for o, v in zip(offs, vals)]
+
+
 def _eri_full(basis: Basis, *, field: MagneticField | None = None, screening_threshold: float = 0.0, threads=None,
               precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF, context=None):
     """Native full tensor (src/bindings.cpp:640-671)."""

@@ -13,13 +13,20 @@ fields of different sizes with continuous batching:
   requests that arrive while others run are admitted the moment a slot and
   memory free up, in arrival order (a request that cannot fit even an empty
   budget fails with ``MemoryError``);
+* ERI requests waiting together are packed: the slot that takes an ERI
+  request also takes the ERI requests queued right behind it (up to ``pack``
+  requests and ``pack_entries`` entries, each fitting the budget) and runs
+  them as one class-sorted execution (``gx_eri_batch_packed``), so quartets
+  of uneven classes and contraction depths from several molecules and fields
+  share each class launch;
 * each context keeps the bases it has served resident (basis upload,
   primitive-pair records for the last field), so repeated molecules skip the
   upload, and Cholesky factors stay on the device for the whole pivot loop.
 
-Every request computes exactly what the same call computes alone: contexts
-share no device state, and every kernel's summation order depends only on the
-request itself.
+Every request computes exactly what it computes alone: the slots' contexts
+use launch configurations that do not depend on a plan's size, work units
+never mix requests, and every kernel's summation order depends only on the
+request itself, so an ERI request gives the same bits alone and in any pack.
 
 ``Server.run(requests)`` replays a trace (``synthetic.serving_requests``:
 Poisson arrivals) in real time and reports p50 / p99 latency beside
@@ -105,9 +112,18 @@ class Server:
 
     def __init__(self, slots: int = 4, *, hbm_budget: int | None = None, precision: str = "fp64",
                  mixed_cutoff: float = 1e-6, device: int = 0, runner=None, bases_per_slot: int = 32,
-                 max_request_bytes: int | None = None):
+                 max_request_bytes: int | None = None, pack: int = 8, pack_entries: int = 1 << 26,
+                 pack_runner=None):
         if slots < 1:
             raise ValueError("slots must be a positive integer")
+        if pack < 1:
+            raise ValueError("pack must be a positive integer")
+        # ERI requests waiting together are packed into one class-sorted
+        # execution: up to `pack` requests and `pack_entries` complex entries
+        self.pack = int(pack)
+        self.pack_entries = int(pack_entries)
+        self.max_pack = 0
+        self.packs = 0
         # per-request device-memory limit (None: the whole budget); a request
         # estimated above it is refused with MemoryError at submission
         self.max_request_bytes = None if max_request_bytes is None else int(max_request_bytes)
@@ -117,6 +133,11 @@ class Server:
         self.mixed_cutoff = float(mixed_cutoff)
         self.device = int(device)
         self._runner = runner or self._run_on_device
+        # packs run through pack_runner(slot, requests) -> [(result, entries)];
+        # with a custom runner and no pack runner, requests are not packed
+        if pack_runner is None and runner is not None:
+            self.pack = 1
+        self._pack_runner = pack_runner or self._run_pack_on_device
         self._contexts: list = [None] * self.slots
         self._bases: list[OrderedDict] = [OrderedDict() for _ in range(self.slots)]
         self._bases_per_slot = int(bases_per_slot)
@@ -196,17 +217,31 @@ class Server:
         self.close()
 
     # ---- scheduling -----------------------------------------------------------
-    def _take(self) -> _Pending | None:
-        """Admit the oldest request once it fits (called with the lock held)."""
+    def _take(self) -> list[_Pending] | None:
+        """Admit the oldest request once it fits, and with an ERI request the
+        ERI requests queued right behind it that fit too, up to the pack
+        limits (called with the lock held)."""
         while True:
             if self._queue and self._reserved + self._queue[0].footprint <= self.hbm_budget:
-                p = self._queue.popleft()
-                p.admitted = self.now()
-                self._reserved += p.footprint
-                self._inflight += 1
+                batch = [self._queue.popleft()]
+                entries = _entries(batch[0].request)
+                while (batch[0].request.kind == "eri" and len(batch) < self.pack and self._queue
+                       and self._queue[0].request.kind == "eri"
+                       and entries + _entries(self._queue[0].request) <= self.pack_entries
+                       and self._reserved + sum(b.footprint for b in batch) + self._queue[0].footprint
+                       <= self.hbm_budget):
+                    entries += _entries(self._queue[0].request)
+                    batch.append(self._queue.popleft())
+                now = self.now()
+                for p in batch:
+                    p.admitted = now
+                    self._reserved += p.footprint
+                    self._inflight += 1
                 self.max_inflight = max(self.max_inflight, self._inflight)
                 self.max_reserved = max(self.max_reserved, self._reserved)
-                return p
+                self.max_pack = max(self.max_pack, len(batch))
+                self.packs += len(batch) > 1
+                return batch
             if self._closing and not self._queue:
                 return None
             self._cv.wait()
@@ -214,23 +249,33 @@ class Server:
     def _worker(self, slot: int) -> None:
         while True:
             with self._cv:
-                p = self._take()
-            if p is None:
+                batch = self._take()
+            if batch is None:
                 return
-            c = Completion(p.index, p.request.kind, p.arrival, admitted=p.admitted, slot=slot, footprint=p.footprint)
+            cs = [Completion(p.index, p.request.kind, p.arrival, admitted=p.admitted, slot=slot,
+                             footprint=p.footprint) for p in batch]
             try:
-                c.result, c.entries = self._runner(slot, p.request)
-            except BaseException as e:  # noqa: BLE001 - delivered through the future
-                c.error = e
-            c.finished = self.now()
+                if len(batch) == 1:
+                    outs = [self._runner(slot, batch[0].request)]
+                else:
+                    outs = self._pack_runner(slot, [p.request for p in batch])
+                for c, (res, n) in zip(cs, outs):
+                    c.result, c.entries = res, n
+            except BaseException as e:  # noqa: BLE001 - delivered through the futures
+                for c in cs:
+                    c.error = e
+            finished = self.now()
             with self._cv:
-                self._reserved -= p.footprint
-                self._inflight -= 1
+                for c, p in zip(cs, batch):
+                    c.finished = finished
+                    self._reserved -= p.footprint
+                    self._inflight -= 1
                 self._cv.notify_all()
-            if c.error is not None:
-                p.future.set_exception(c.error)
-            else:
-                p.future.set_result(c)
+            for c, p in zip(cs, batch):
+                if c.error is not None:
+                    p.future.set_exception(c.error)
+                else:
+                    p.future.set_result(c)
 
     # ---- device execution -----------------------------------------------------
     def _default_budget(self) -> int:
@@ -246,7 +291,11 @@ class Server:
         from . import _native as nat
 
         if self._contexts[slot] is None:
-            self._contexts[slot] = nat.Context(self.device)
+            ctx = nat.Context(self.device)
+            # launch configurations independent of the pack a request lands in,
+            # so that every request gives the same bits alone and packed
+            nat.check(nat.lib().gx_context_set_stable_launch(ctx.handle, 1))
+            self._contexts[slot] = ctx
         return self._contexts[slot]
 
     def _basis(self, slot: int, shells):
@@ -267,18 +316,47 @@ class Server:
     def _run_on_device(self, slot: int, request):
         from ._types import MagneticField
         from .cholesky import _cholesky_device
-        from .eri import _eri_batch
 
         ctx = self._context(slot)
         basis = self._basis(slot, request.shells)
         field = MagneticField(request.field)
         if request.kind == "eri":
-            res = _eri_batch(basis, request.quartets, field=field, precision=self.precision,
-                             mixed_cutoff=self.mixed_cutoff, context=ctx)
-            return res, int(res[2][-1])
+            return self._run_pack_on_device(slot, [request])[0]
         if request.kind == "cholesky":
             return _cholesky_device(basis, field, float(request.threshold), 0.0, None, 32, context=ctx), 0
         raise ValueError("request kind must be 'eri' or 'cholesky'")
+
+    def _run_pack_on_device(self, slot: int, requests):
+        """ERI requests of different molecules and fields in one class-sorted
+        execution (gx_eri_batch_packed); each result is the tuple
+        (quartets, shapes, offsets, values, requested, screened) that
+        ``_eri_batch`` gives the request alone."""
+        from ._types import MagneticField
+        from .eri import _eri_batch_packed
+
+        ctx = self._context(slot)
+        items = []
+        for r in requests:
+            if r.kind != "eri":
+                raise ValueError("only ERI requests are packed")
+            items.append((self._basis(slot, r.shells), r.quartets, MagneticField(r.field)))
+        outs = _eri_batch_packed(items, precision=self.precision, mixed_cutoff=self.mixed_cutoff, context=ctx)
+        results = []
+        for (basis, quartets, _), (offsets, values) in zip(items, outs):
+            q = np.ascontiguousarray(np.asarray(quartets, dtype=np.uint32).reshape(-1, 4))
+            sizes = np.array([s.ao_count for s in basis.shells], dtype=np.int64)
+            shapes = sizes[q.astype(np.int64)] if len(q) else np.zeros((0, 4), dtype=np.int64)
+            results.append(((q, shapes, offsets, values, len(q), 0), int(offsets[-1])))
+        return results
+
+
+def _entries(request) -> int:
+    """Complex ERI entries of an ERI request (0 for other kinds)."""
+    if request.kind != "eri":
+        return 0
+    sizes = np.array([_ncart(s.angular_momentum) * len(s.raw_coefficients) for s in request.shells], dtype=np.int64)
+    q = np.asarray(request.quartets, dtype=np.int64).reshape(-1, 4)
+    return int(np.prod(sizes[q], axis=1).sum()) if len(q) else 0
 
 
 def latency_summary(done: list[Completion]) -> dict:

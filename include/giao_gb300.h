@@ -314,6 +314,29 @@ int gx_context_set_stream(gx_context* ctx, void* stream);
 /* Wait for the context's stream and report any device status word. */
 int gx_context_synchronize(gx_context* ctx);
 
+/* Several requests -- each its own basis, field (B[3 r], O[3 r]) and
+ * quartet list -- packed into one class-sorted execution: quartets of
+ * uneven classes and contraction depths from all requests share each class
+ * launch (evaluate_eri_shell_quartets, src/eri.cpp:644-767, called once per
+ * request in the reference).  Every basis must belong to ctx.  For request
+ * r, offsets[r] (nq[r] + 1) receives the packed offsets of its blocks and
+ * values[r] (host, capacity[r] complex elements) its blocks, in the layout
+ * gx_eri_batch gives that request alone (no screening).  Work units never
+ * mix requests, so on a context with stable launch configurations (below)
+ * each request's values are bit for bit those of the request packed alone.
+ * kernel_ms (may be NULL): device time of the class launches. */
+int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* bases, const double* B, const double* O,
+                        const uint32_t* const* quartets, const int64_t* nq, int precision, double mixed_cutoff,
+                        int64_t* const* offsets, double* const* values, const int64_t* capacity,
+                        double* kernel_ms);
+/* 1: plans built on ctx from now on choose launch configurations that do
+ * not depend on how many tasks a class holds (no splitting of ket
+ * components over extra warps for small classes), so a request gives the
+ * same bits alone and in any pack; 0 (default): configurations sized to the
+ * plan.  No reference counterpart (the reference has no batching across
+ * requests). */
+int gx_context_set_stable_launch(gx_context* ctx, int stable);
+
 /* A plan fixes a quartet list (its class-sorted task list and packed
  * offsets, offsets[nq+1]) so that it can be evaluated for many fields
  * without host work: the persistent batched form of

@@ -30,6 +30,11 @@ def test_results_alone_equal_results_in_the_mix():
     with Server(slots=4) as mix:
         done = mix.run(reqs)
     assert mix.max_inflight >= 2  # the requests really overlapped
+    with Server(slots=1, precision="fp64") as packed:
+        done_packed = packed.run(reqs, realtime=False)  # a queue forms behind one slot: ERI requests are packed
+    for r, c0, c1 in zip(reqs, ref, done_packed):
+        assert c1.error is None
+        _compare(r.kind, c0.result, c1.result)
     for r, c0, c1 in zip(reqs, ref, done):
         assert c1.error is None
         _compare(r.kind, c0.result, c1.result)

@@ -109,3 +109,33 @@ def test_per_request_limit_refuses_and_counts():
     assert all("per-request limit" in str(c.error) for c in refused)
     s = latency_summary(done)
     assert s["refused_memory"] == over and s["completed"] == len(reqs) - over
+
+
+def test_waiting_eri_requests_are_packed_cholesky_never():
+    """ERI requests queued behind an admitted ERI request join its pack (up to
+    the pack size); a Cholesky request is never packed and ends a pack."""
+    reqs = _trace(16)
+    packs = []
+
+    def pack_runner(slot, rs):
+        packs.append([r.kind for r in rs])
+        return [(None, 1) for _ in rs]
+
+    def runner(slot, r):
+        packs.append([r.kind])
+        if len(packs) == 1:
+            time.sleep(0.2)  # the rest of the trace queues up behind the first request
+        return None, 1
+
+    with Server(slots=1, hbm_budget=1 << 50, runner=runner, pack_runner=pack_runner, pack=4) as srv:
+        done = srv.run(reqs, realtime=False)
+    assert all(c.error is None for c in done)
+    assert sum(len(p) for p in packs) == len(reqs)
+    assert max(len(p) for p in packs) <= 4
+    assert srv.max_pack == max(len(p) for p in packs) >= 2
+    for p in packs:
+        if len(p) > 1:
+            assert all(k == "eri" for k in p)
+    # arrival order is kept across packs
+    kinds = [k for p in packs for k in p]
+    assert kinds == [r.kind for r in reqs]
