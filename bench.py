@@ -44,11 +44,17 @@ WORKLOAD = "12-atom s6 s1 s1 p3 p1 d1 molecule, seed 2026, |B|<=0.2, all 6722352
 DTYPE = "f64+f32 (mixed: FP32 primitive quartets under the cutoff, FP64 elsewhere and for every sum)"
 
 
-# DRAM bytes (read + write) of one plan execution, from an ncu capture of
-# every class launch of one step (dram__bytes_read.sum + dram__bytes_write.sum
-# summed over the launches; see the traffic basis); None until captured.
-TRAFFIC_PER_STEP: dict = {}
-TRAFFIC_BASIS = "not captured"
+# DRAM bytes (read + write) of one plan execution of this workload, from one
+# ncu capture of every launch of one step (dram__bytes_read.sum +
+# dram__bytes_write.sum summed over the 116 (mixed) / 81 (FP64) class
+# launches, L2 kept across launches; pair-record kernels excluded: they run
+# once per field):
+#   ncu --nvtx --nvtx-include "step/" --cache-control none --clock-control none
+#       --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+#       python bench.py --profile-step {mixed,fp64} --no-autotune --warmup 0 --no-cpu
+TRAFFIC_PER_STEP: dict = {"mixed": 649.9e6 + 4578.7e6, "fp64": 580.9e6 + 4367.9e6}
+TRAFFIC_BASIS = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every class launch of one step "
+                 "(default launch configurations, L2 kept across launches); algorithmic output 4.20 GB per step")
 
 
 def _measured_peaks() -> dict:
@@ -955,7 +961,7 @@ def run_gpu(args):
                                             "frac": mx_tf32 / peak32.value, "flops": cnt_mx[3]}},
                          "fp64_mode": {"achieved": achieved64, "frac": achieved64 / peak.value,
                                        "ms_per_step": ms64},
-                         "traffic": TRAFFIC_PER_STEP.get(args.precision),
+                         "traffic": TRAFFIC_PER_STEP.get(args.precision) if args.natoms == 12 else None,
                          "traffic_basis": TRAFFIC_BASIS,
                          "kernel": "one plan execution: quartet_kernel + small_kernel launches of the 81 classes",
                          "achieved_basis": "FLOP model per primitive quartet (reference-structured MD count) x "

@@ -55,6 +55,7 @@ class GxCholeskyStats(ctypes.Structure):
         ("column_primitive_quartets", ctypes.c_int64),
         ("diagonal_primitive_quartets", ctypes.c_int64),
         ("column_cache_capacity", ctypes.c_int64),
+        ("chained_steps", ctypes.c_int64),
         ("column_model_flops", ctypes.c_double),
         ("column_ms", ctypes.c_double),
         ("update_ms", ctypes.c_double),

@@ -2900,6 +2900,24 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     ColumnPool pool;
     pool.init(kBatchColumns + cache_cap + 64, col_bytes);
     stats.column_cache_capacity = cache_cap;
+    // Chained steps (no local block rule): the device takes the next pivots
+    // itself while their raw columns are cached; slot_of mirrors the cache.
+    const bool chain_ok = !local_rule;
+    DeviceBuffer d_slot_of, d_state, d_log;
+    std::vector<int> slot_of_h;
+    bool slot_dirty = true;
+    int chain_k = 8;
+    if (chain_ok) {
+        slot_of_h.assign(N, -1);
+        d_slot_of.reserve(N * sizeof(int));
+        d_state.reserve(sizeof(gx::ChainState));
+        d_log.reserve(std::max<int64_t>(limit, 1) * sizeof(long long));
+    }
+    auto set_slot = [&](int64_t fl, int v) {
+        if (!chain_ok) return;
+        slot_of_h[fl] = v;
+        slot_dirty = true;
+    };
     d_work.reserve(col_bytes);
     constexpr int kGemvChunks = 8;  // rank chunks of the factor update (partial sums)
     DeviceBuffer d_gemv;
@@ -3013,9 +3031,9 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             stats.rank = rank;
             raise(GX_ENOMEM, "Cholesky rank capacity exceeded");
         }
-        if (rank >= f.cap_rows) {
+        if (rank >= f.cap_rows || (chain_ok && rank + 1 + chain_k > f.cap_rows && f.cap_rows < limit)) {
             // grow the factor rows (doubling, at most `limit`)
-            const int64_t cap2 = std::min<int64_t>(limit, 2 * f.cap_rows);
+            const int64_t cap2 = std::min<int64_t>(limit, std::max<int64_t>(2 * f.cap_rows, rank + 1 + chain_k));
             DeviceBuffer grown;
             grown.reserve((size_t)cap2 * col_bytes);
             GX_CUDA(cudaMemcpyAsync(grown.ptr, f.L.ptr, (size_t)rank * col_bytes, cudaMemcpyDeviceToDevice, st));
@@ -3053,6 +3071,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             const int slot = cached->second->second;
             lru.erase(cached->second);
             lru_pos.erase(cached);
+            set_slot(pivot, -1);
             drop_batch();
             cands.push_back(pivot);
             cand_slot.push_back(slot);  // cache reference moves to the batch
@@ -3144,9 +3163,11 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                     lru.push_back({cands[k], cand_slot[k]});
                     lru_pos[cands[k]] = std::prev(lru.end());
                 }
+                set_slot(cands[k], cand_slot[k]);
             }
             while (lru.size() > (size_t)cache_cap) {
                 pool.release(lru.front().second);
+                set_slot(lru.front().first, -1);
                 lru_pos.erase(lru.front().first);
                 lru.pop_front();
             }
@@ -3158,6 +3179,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                 pool.release(c2it->second->second);
                 lru.erase(c2it->second);
                 lru_pos.erase(c2it);
+                set_slot(pivot, -1);
             }
         }
         const int slot = cand_slot[it - cands.begin()];
@@ -3166,6 +3188,35 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         GX_CUDA(gx::launch_chol_step(real, f.L.ptr, N, (int)rank, pivot, pool.ptr(slot), d_work.ptr, (int)n,
                                      d_res.as<double>(), d_scale.as<double>(), Lrow, d_partial.ptr, d_red.ptr, st,
                                      d_gemv.ptr, kGemvChunks, ctx->sm_count));
+        const double psd = std::max(floor * 16, 1e-12);
+        // then up to chain_k steps the device takes on its own while the next
+        // pivot's raw column is cached (one host synchronisation for all)
+        const bool chained = chain_ok && !lru.empty() && rank + 1 < std::min<int64_t>(limit, f.cap_rows);
+        gx::ChainState cs_out{};
+        std::vector<long long> chain_log;
+        if (chained) {
+            if (slot_dirty) {
+                GX_CUDA(cudaMemcpyAsync(d_slot_of.ptr, slot_of_h.data(), N * sizeof(int), cudaMemcpyHostToDevice, st));
+                slot_dirty = false;
+            }
+            gx::ChainState cs{};
+            cs.slot = -1;
+            cs.rank = (int)rank + 1;
+            cs.active = 1;
+            cs.rank_limit = (int)std::min<int64_t>(limit, f.cap_rows);
+            GX_CUDA(cudaMemcpyAsync(d_state.ptr, &cs, sizeof cs, cudaMemcpyHostToDevice, st));
+            GX_CUDA(gx::launch_chol_chain(real, f.L.ptr, N, (int)n, (int)rank + 1 + chain_k, chain_k,
+                                          d_state.as<gx::ChainState>(), d_slot_of.as<int>(), d_log.as<long long>(),
+                                          pool.buf.ptr, d_work.ptr, d_res.as<double>(), d_scale.as<double>(),
+                                          d_partial.ptr, d_red.ptr, d_gemv.ptr, kGemvChunks, ctx->sm_count, tol, psd,
+                                          st));
+            GX_CUDA(cudaMemcpyAsync(&cs_out, d_state.ptr, sizeof cs_out, cudaMemcpyDeviceToHost, st));
+            // the log holds `limit` entries; the chain writes at most up to rank_limit <= limit
+            const int64_t nlog = std::min<int64_t>(chain_k, limit - (rank + 1));
+            chain_log.resize(nlog);
+            GX_CUDA(cudaMemcpyAsync(chain_log.data(), d_log.as<long long>() + rank + 1, nlog * sizeof(long long),
+                                    cudaMemcpyDeviceToHost, st));
+        }
         GX_CUDA(cudaEventRecord(ev_upd.b, st));
         upd_pending = true;
         // algorithmic work of the step: L read once (rank rows), the raw
@@ -3176,8 +3227,28 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         f.pivots.push_back(pivot / n);
         f.pivots.push_back(pivot % n);
         ++rank;
-        if (red.minv < -std::max(floor * 16, 1e-12))
-            raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
+        if (chained) {
+            if (cs_out.stop == 4) raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
+            for (int k = 0; k < cs_out.steps; ++k) {
+                const int64_t p = chain_log[k];
+                stats.update_bytes += (double)col_bytes * (rank + 2) + 16.0 * N;
+                stats.update_flops += (real ? 2.0 : 8.0) * (double)rank * N;
+                f.pivots.push_back(p / n);
+                f.pivots.push_back(p % n);
+                ++rank;
+                auto e = lru_pos.find(p);  // the device consumed its cached column
+                if (e != lru_pos.end()) {
+                    pool.release(e->second->second);
+                    lru.erase(e->second);
+                    lru_pos.erase(e);
+                }
+                slot_of_h[p] = -1;  // already -1 on the device
+                ++stats.chained_steps;
+            }
+            // chain length: grow while chains run to their end, else follow them
+            chain_k = cs_out.active ? std::min(64, 2 * chain_k) : std::max(1, std::min(64, cs_out.steps + 2));
+        }
+        if (red.minv < -psd) raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
     }
     double final_max = std::max(red.maxv, 0.0);
     if (!skipped.empty()) {

@@ -325,6 +325,183 @@ cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, l
     return cudaGetLastError();
 }
 
+// ---- chained steps: pivots taken on the device while their columns are cached ----
+//
+// After a step the next pivot is the argmax of the residual.  When its raw
+// column is already in the column cache (slot_of[pivot] >= 0), the next step
+// needs no host decision, so the host enqueues up to K steps at once and
+// synchronises once: chain_select_kernel takes the argmax of the previous
+// step, stops the chain (active = 0, with the reason) when the residual has
+// converged, the rank limit is reached, the PSD check failed or the column is
+// not cached, and otherwise records the pivot and its slot; the step kernels
+// below read the pivot, rank and column from that state and return at once
+// when the chain has stopped.
+
+__global__ void chain_select_kernel(ChainState* st, const Red* red, int* slot_of, long long* log, double tol,
+                                    double psd) {
+    if (!st->active) return;
+    const Red r = *red;
+    int stop = 0;
+    int slot = -1;
+    if (r.minv < -psd)
+        stop = 4;
+    else if (!(r.maxv > tol))
+        stop = 2;
+    else if (st->rank >= st->rank_limit)
+        stop = 3;
+    else if ((slot = slot_of[r.idx]) < 0)
+        stop = 1;
+    if (stop) {
+        st->active = 0;
+        st->stop = stop;
+        return;
+    }
+    st->pivot = r.idx;
+    st->slot = slot;
+    slot_of[r.idx] = -1;
+    log[st->rank] = r.idx;
+}
+
+template <typename T>
+__global__ void chain_gemv_split_kernel(const T* L, long long ld, const ChainState* st, int nchunks, T* partials,
+                                        long long N) {
+    if (!st->active) return;
+    __shared__ T coef[256];
+    const int rank = st->rank;
+    const long long piv = st->pivot;
+    const int chunk = (rank + nchunks - 1) / nchunks;
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int rbeg = blockIdx.y * chunk, rend = min(rank, rbeg + chunk);
+    T acc;
+    if constexpr (sizeof(T) == 8) {
+        acc = T(0);
+    } else {
+        acc = c2(0.0, 0.0);
+    }
+    for (int r0 = rbeg; r0 < rend; r0 += 256) {
+        const int nr = min(256, rend - r0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nr; i += blockDim.x) coef[i] = L[(long long)(r0 + i) * ld + piv];
+        __syncthreads();
+        if (j < N) {
+#pragma unroll 8
+            for (int r = 0; r < nr; ++r) {
+                const T lv = __ldg(&L[(long long)(r0 + r) * ld + j]);
+                if constexpr (sizeof(T) == 8) {
+                    acc += coef[r] * lv;
+                } else {
+                    acc = conj_mul_add(acc, coef[r], lv);
+                }
+            }
+        }
+    }
+    if (j < N) partials[(long long)blockIdx.y * N + j] = acc;
+}
+
+template <typename T>
+__global__ void chain_gemv_sum_kernel(const T* pool, const ChainState* st, const T* partials, int nchunks, long long N,
+                                      T* col_out) {
+    if (!st->active) return;
+    const T* col_in = pool + (long long)st->slot * N;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        T acc = col_in[j];
+        for (int y = 0; y < nchunks; ++y) {
+            if constexpr (sizeof(T) == 8) {
+                acc -= partials[(long long)y * N + j];
+            } else {
+                acc = csub(acc, partials[(long long)y * N + j]);
+            }
+        }
+        col_out[j] = acc;
+    }
+}
+
+__global__ void chain_scale_kernel(const ChainState* st, const double* res, double* scale) {
+    if (st->active) *scale = rsqrt(res[st->pivot]);
+}
+
+template <typename T>
+__global__ void chain_update_kernel(const ChainState* st, const T* col, int n, const double* scale, T* L, double* res,
+                                    Red* partial) {
+    if (!st->active) return;
+    const long long N = (long long)n * n;
+    const long long piv = st->pivot;
+    T* Lrow = L + (long long)st->rank * N;
+    const double sc = *scale;
+    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
+        double mag2;
+        if constexpr (sizeof(T) == 8) {
+            const long long mu = j / n, nu = j - mu * n;
+            const double c = (col[j] + col[nu * n + mu]) * 0.5 * sc;
+            Lrow[j] = c;
+            mag2 = c * c;
+        } else {
+            const double2 c = cscale(col[j], sc);
+            Lrow[j] = c;
+            mag2 = c.x * c.x + c.y * c.y;
+        }
+        const double nr = res[j] - mag2;
+        const double kept = j == piv ? 0.0 : fmax(nr, 0.0);
+        res[j] = kept;
+        red_merge(r, Red{kept, j, nr});
+    }
+    r = block_reduce(r);
+    if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+__global__ void chain_final_kernel(ChainState* st, const Red* partial, int np, Red* out) {
+    if (!st->active) return;
+    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    for (int i = threadIdx.x; i < np; i += blockDim.x) red_merge(r, partial[i]);
+    r = block_reduce(r);
+    if (threadIdx.x == 0) {
+        *out = r;
+        st->rank += 1;
+        st->steps += 1;
+    }
+}
+
+cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_hi, int steps, ChainState* st,
+                              int* slot_of, long long* log, const void* pool, void* work, double* res, double* scale,
+                              void* partial, void* out, void* gemv_partials, int max_chunks, int sms, double tol,
+                              double psd, cudaStream_t s) {
+    const int blocks = (int)((N + 127) / 128);
+    int nchunks = 1;
+    if (gemv_partials && max_chunks > 1 && rank_hi >= 64 && sms > 0)
+        nchunks = std::max(1, std::min({max_chunks, (8 * sms) / std::max(blocks, 1), (rank_hi + 31) / 32}));
+    const dim3 grid(blocks, nchunks);
+    const int sblocks = (int)std::min<long long>((N + 255) / 256, 8LL * sms);
+    Red* red = static_cast<Red*>(out);
+    for (int k = 0; k < steps; ++k) {
+        chain_select_kernel<<<1, 1, 0, s>>>(st, red, slot_of, log, tol, psd);
+        if (real) {
+            chain_gemv_split_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(L), N, st, nchunks,
+                                                                 static_cast<double*>(gemv_partials), N);
+            chain_gemv_sum_kernel<double><<<sblocks, 256, 0, s>>>(static_cast<const double*>(pool), st,
+                                                                  static_cast<const double*>(gemv_partials), nchunks,
+                                                                  N, static_cast<double*>(work));
+        } else {
+            chain_gemv_split_kernel<double2><<<grid, 128, 0, s>>>(static_cast<const double2*>(L), N, st, nchunks,
+                                                                  static_cast<double2*>(gemv_partials), N);
+            chain_gemv_sum_kernel<double2><<<sblocks, 256, 0, s>>>(static_cast<const double2*>(pool), st,
+                                                                   static_cast<const double2*>(gemv_partials),
+                                                                   nchunks, N, static_cast<double2*>(work));
+        }
+        chain_scale_kernel<<<1, 1, 0, s>>>(st, res, scale);
+        if (real)
+            chain_update_kernel<double><<<RED_BLOCKS, 256, 0, s>>>(st, static_cast<const double*>(work), n, scale,
+                                                                   static_cast<double*>(L), res,
+                                                                   static_cast<Red*>(partial));
+        else
+            chain_update_kernel<double2><<<RED_BLOCKS, 256, 0, s>>>(st, static_cast<const double2*>(work), n, scale,
+                                                                    static_cast<double2*>(L), res,
+                                                                    static_cast<Red*>(partial));
+        chain_final_kernel<<<1, 256, 0, s>>>(st, static_cast<const Red*>(partial), RED_BLOCKS, red);
+    }
+    return cudaGetLastError();
+}
+
 // residual = D - sum_P |L_P|^2 (used when screened diagonal blocks are measured at the end)
 template <typename T>
 __global__ void chol_final_residual_kernel(const double* D, const T* L, int rank, long long N, double* res) {

@@ -230,6 +230,23 @@ cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, l
                              cudaStream_t s, void* gemv_partials = nullptr, int max_chunks = 0, int sms = 0);
 cudaError_t launch_chol_final_residual(bool real, const double* D, const void* L, int rank, long long N, double* res,
                                        cudaStream_t s);
+// State of a chain of pivot steps taken on the device (launch_chol_chain).
+struct ChainState {
+    long long pivot;  // pivot of the current step
+    int slot;         // its column slot in the cache
+    int rank;         // factor rows so far
+    int active;       // 1 while the chain runs
+    int steps;        // steps taken by this chain
+    int stop;         // why it stopped: 1 column not cached, 2 converged, 3 rank limit, 4 PSD check
+    int rank_limit;   // rows the factor buffer (and the caller's limit) allows
+};
+// Enqueue `steps` chained pivot steps (each returns at once after the chain
+// stopped): pool holds the cached raw columns (slot_of[flat index] = slot,
+// -1 if absent), log receives the pivot of every step at its rank.
+cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_hi, int steps, ChainState* st,
+                              int* slot_of, long long* log, const void* pool, void* work, double* res, double* scale,
+                              void* partial, void* out, void* gemv_partials, int max_chunks, int sms, double tol,
+                              double psd, cudaStream_t s);
 size_t chol_red_bytes();
 size_t chol_partial_bytes();
 

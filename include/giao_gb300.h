@@ -262,6 +262,8 @@ typedef struct gx_cholesky_stats {
     int64_t column_primitive_quartets;   /* FP64 primitive quartets of the column evaluations   */
     int64_t diagonal_primitive_quartets; /* FP64 primitive quartets of the diagonal             */
     int64_t column_cache_capacity;       /* raw columns the cache may hold (fitted to memory)   */
+    int64_t chained_steps;               /* pivot steps taken on the device without a host round
+                                            trip (their columns were cached)                    */
     double column_model_flops;           /* FP64 FLOP model of the column primitive quartets    */
     double column_ms;                    /* event-timed column evaluations + extraction         */
     double update_ms;                    /* event-timed factor update, residual and argmax      */
