@@ -1090,6 +1090,43 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
     return 1 + (int)nc;
 }
 
+// Enqueue several plans (each with its own evaluation view and counters,
+// accumulated) under one fork/join over the auxiliary streams, their class
+// launches interleaved round robin.
+void enqueue_plans(gx_context* ctx, const std::vector<std::pair<const PlanData*, gx::EriDev>>& runs, int precision,
+                   const std::vector<unsigned long long*>& counters) {
+    cudaStream_t s = ctx->stream;
+    ctx->reset_status();
+    constexpr int kAux = 32;
+    if (ctx->aux.empty()) {
+        ctx->aux.resize(kAux);
+        ctx->aux_done.resize(kAux);
+        for (int k = 0; k < kAux; ++k) {
+            GX_CUDA(cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking));
+            GX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done[k], cudaEventDisableTiming));
+        }
+        GX_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    }
+    GX_CUDA(cudaEventRecord(ctx->fork, s));
+    for (int k = 0; k < kAux; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
+    static const ClassConf kDefault{};
+    int next = 0;
+    for (size_t r = 0; r < runs.size(); ++r) {
+        const PlanData& plan = *runs[r].first;
+        const auto& tuned = plan.tuned[precision];
+        const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
+        for (size_t ci = 0; ci < plan.classes.size(); ++ci, ++next)
+            launch_class(ctx, runs[r].second, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters[r],
+                         ctx->aux[next % kAux], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
+                         (int)gs.lane[ci].second);
+    }
+    for (int k = 0; k < kAux; ++k) {
+        GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
+        GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
+    }
+}
+
 // Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
 // index = contraction * ncart + component) and wait for them.
 void run_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, PlanData& plan, double2* out,
@@ -2877,7 +2914,12 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     bool reuse = !single;
     for (int s = 0; s < ns; ++s) reuse = reuse || b->ncontr[s] > 1 || b->nprim[s] > 1;
     // The local block rule of complex contracted systems (cholesky.py:195-206).
-    const bool local_rule = reuse && !real && opt->pivot_batch_size > 1;
+    // Its candidates are the contraction variants of an evaluated pivot; with
+    // one contraction per shell that is the pivot alone, whose residual is
+    // zero once taken, so the rule never overrides the global argmax.
+    bool general = false;
+    for (int s = 0; s < ns; ++s) general = general || b->ncontr[s] > 1;
+    const bool local_rule = reuse && !real && opt->pivot_batch_size > 1 && general;
     // Columns kept per pivot-block evaluation: the evaluation computes every
     // column of the pivot's shell-pair block, and raw columns are exact
     // whenever they are computed, so keeping more of them (and the raw-column
@@ -2895,7 +2937,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         const int64_t first_rows = std::min<int64_t>(std::max<int64_t>(limit, 1), std::max<int64_t>(64, 8 * n));
         const double room = (double)free_b * 0.5 - (double)first_rows * col_bytes - 8.0 * col_bytes;
         const int64_t fit = (int64_t)(room / (double)col_bytes) - kBatchColumns - 64;
-        cache_cap = (int)std::max<int64_t>(0, std::min<int64_t>(1024, fit));
+        cache_cap = (int)std::max<int64_t>(0, std::min<int64_t>(2048, fit));
     }
     ColumnPool pool;
     pool.init(kBatchColumns + cache_cap + 64, col_bytes);
@@ -2907,14 +2949,20 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     std::vector<int> slot_of_h;
     bool slot_dirty = true;
     int chain_k = 8;
+    slot_of_h.assign(N, -1);  // cache slot of every flat index (-1: not cached)
     if (chain_ok) {
-        slot_of_h.assign(N, -1);
         d_slot_of.reserve(N * sizeof(int));
         d_state.reserve(sizeof(gx::ChainState));
         d_log.reserve(std::max<int64_t>(limit, 1) * sizeof(long long));
     }
+    struct GraphSet {  // instantiated chain graphs, destroyed with the factorisation
+        std::map<std::tuple<int, void*, int>, cudaGraphExec_t> m;
+        ~GraphSet() {
+            for (auto& kv : m) cudaGraphExecDestroy(kv.second);
+        }
+    } chain_graph_set;
+    auto& chain_graphs = chain_graph_set.m;
     auto set_slot = [&](int64_t fl, int v) {
-        if (!chain_ok) return;
         slot_of_h[fl] = v;
         slot_dirty = true;
     };
@@ -3099,29 +3147,49 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             }
             drop_batch();
             cands = keep;
+            // The pivot's block.  (Evaluating the blocks of the next largest
+            // uncached residual entries in the same launches was measured:
+            // 2-4 blocks per evaluation cost more column time than they saved
+            // on both the 140-AO atom and the 12-atom molecule.)
+            struct EvalBlock {
+                int sa, sb;
+                std::vector<int64_t> cols;
+            };
+            std::vector<EvalBlock> blocks{{a, c, {}}};
+            blocks[0].cols = cands;
             // columns (mu nu | p1 p0) for all shell pairs (real: b >= a).  The
             // quartet list, its plan and block offsets depend only on the
             // pivot shell pair: built once per factorisation and reused.
-            const int sa = a, sb = c;
-            auto& cp = column_plans[{sa, sb}];
-            if (!cp) {
-                cp = std::make_unique<ColumnPlan>();
-                std::vector<QuartetRequest> req;
-                std::vector<long long> boff;
-                int64_t off = 0;
-                for (int x = 0; x < ns; ++x)
-                    for (int y = real ? x : 0; y < ns; ++y) {
-                        req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
-                        boff.push_back(off);
-                        off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
-                    }
-                build_plan(ctx, b, req, cp->plan);
-                upload(cp->boff, boff, st);
-                cp->nblocks = (int)req.size();
-                cp->entries = off;
-                cp->counters.reserve(std::max<size_t>(2 * cp->plan.classes.size(), 2) * sizeof(unsigned long long));
-                GX_CUDA(cudaMemsetAsync(cp->counters.ptr, 0, cp->counters.bytes, st));
+            std::vector<ColumnPlan*> cps;
+            std::vector<int64_t> sbase;
+            int64_t stot = 0;
+            for (const auto& bl : blocks) {
+                const int sa = bl.sa, sb = bl.sb;
+                auto& cp = column_plans[{sa, sb}];
+                if (!cp) {
+                    cp = std::make_unique<ColumnPlan>();
+                    std::vector<QuartetRequest> req;
+                    std::vector<long long> boff;
+                    int64_t off = 0;
+                    for (int x = 0; x < ns; ++x)
+                        for (int y = real ? x : 0; y < ns; ++y) {
+                            req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
+                            boff.push_back(off);
+                            off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
+                        }
+                    build_plan(ctx, b, req, cp->plan);
+                    upload(cp->boff, boff, st);
+                    cp->nblocks = (int)req.size();
+                    cp->entries = off;
+                    cp->counters.reserve(std::max<size_t>(2 * cp->plan.classes.size(), 2) *
+                                         sizeof(unsigned long long));
+                    GX_CUDA(cudaMemsetAsync(cp->counters.ptr, 0, cp->counters.bytes, st));
+                }
+                cps.push_back(cp.get());
+                sbase.push_back(stot);
+                stot += cp->entries;
             }
+            ctx->scratch_a.reserve(std::max<int64_t>(stot, 1) * sizeof(double2));
             if (column_info.ptr == nullptr) {
                 std::vector<int> info;
                 for (int x = 0; x < ns; ++x)
@@ -3132,39 +3200,62 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             }
             std::vector<int> cl;
             std::vector<void*> dst;
-            for (int64_t fl : cands) {
-                cl.push_back((int)(fl % n - b->ao_off[sb]));  // c: p1 within sb
-                cl.push_back((int)(fl / n - b->ao_off[sa]));  // d: p0 within sa
-                const int slot = pool.take();
-                cand_slot.push_back(slot);
-                dst.push_back(pool.ptr(slot));
-            }
+            std::vector<std::vector<int>> bslots(blocks.size());
+            for (size_t k = 0; k < blocks.size(); ++k)
+                for (int64_t fl : blocks[k].cols) {
+                    cl.push_back((int)(fl % n - b->ao_off[blocks[k].sb]));  // c: p1 within sb
+                    cl.push_back((int)(fl / n - b->ao_off[blocks[k].sa]));  // d: p0 within sa
+                    const int slot = pool.take();
+                    bslots[k].push_back(slot);
+                    dst.push_back(pool.ptr(slot));
+                }
+            cand_slot = bslots[0];
             upload(d_cand, cl, st);
             upload(d_dst, dst, st);
             GX_CUDA(cudaEventRecord(ev_col.a, st));
-            execute_plan(ctx, b, iB, iO, cp->plan, ctx->scratch_a.as<double2>(), GX_PRECISION_FP64, 0.0,
-                         cp->counters.as<unsigned long long>(), /*accumulate=*/true);
-            GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>(), cp->boff.as<long long>(),
-                                         column_info.as<int>(), cp->nblocks, d_cand.as<int>(), (int)cands.size(),
-                                         (int)b->nao_of(sb), (int)b->nao_of(sa), (int)n, d_dst.as<void*>(), st));
+            {
+                // the blocks' class launches share one fork/join over the
+                // auxiliary streams, so they fill the GPU together
+                std::vector<std::pair<const PlanData*, gx::EriDev>> runs;
+                FieldPairs& fpairs = field_pairs(b, iB, iO);
+                for (size_t k = 0; k < blocks.size(); ++k)
+                    runs.push_back({&cps[k]->plan, make_dev(ctx, b, fpairs, ctx->scratch_a.as<double2>() + sbase[k],
+                                                            GX_PRECISION_FP64, 0.0)});
+                std::vector<unsigned long long*> ctr;
+                for (auto* cp : cps) ctr.push_back(cp->counters.as<unsigned long long>());
+                enqueue_plans(ctx, runs, GX_PRECISION_FP64, ctr);
+            }
+            int64_t coff = 0;
+            for (size_t k = 0; k < blocks.size(); ++k) {
+                const int ncand = (int)blocks[k].cols.size();
+                if (ncand)
+                    GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>() + sbase[k], cps[k]->boff.as<long long>(),
+                                                 column_info.as<int>(), cps[k]->nblocks, d_cand.as<int>() + 2 * coff,
+                                                 ncand, (int)b->nao_of(blocks[k].sb), (int)b->nao_of(blocks[k].sa),
+                                                 (int)n, d_dst.as<void*>() + coff, st));
+                coff += ncand;
+            }
             GX_CUDA(cudaEventRecord(ev_col.b, st));
             col_pending = true;
             ++stats.block_evaluations;
-            stats.column_entries += (int64_t)cands.size() * N;
-            for (size_t k = 0; k < cands.size(); ++k) {
-                if (cands[k] == pivot) continue;
-                // assignment to an existing key keeps its position (OrderedDict semantics)
-                auto old = lru_pos.find(cands[k]);
-                pool.retain(cand_slot[k]);
-                if (old != lru_pos.end()) {
-                    pool.release(old->second->second);
-                    old->second->second = cand_slot[k];
-                } else {
-                    lru.push_back({cands[k], cand_slot[k]});
-                    lru_pos[cands[k]] = std::prev(lru.end());
+            stats.column_entries += (int64_t)coff * N;
+            for (size_t k = 0; k < blocks.size(); ++k)
+                for (size_t t = 0; t < blocks[k].cols.size(); ++t) {
+                    const int64_t fl = blocks[k].cols[t];
+                    const int sl = bslots[k][t];
+                    if (k == 0 && fl == pivot) continue;
+                    // assignment to an existing key keeps its position (OrderedDict semantics)
+                    auto old = lru_pos.find(fl);
+                    pool.retain(sl);
+                    if (old != lru_pos.end()) {
+                        pool.release(old->second->second);
+                        old->second->second = sl;
+                    } else {
+                        lru.push_back({fl, sl});
+                        lru_pos[fl] = std::prev(lru.end());
+                    }
+                    set_slot(fl, sl);
                 }
-                set_slot(cands[k], cand_slot[k]);
-            }
             while (lru.size() > (size_t)cache_cap) {
                 pool.release(lru.front().second);
                 set_slot(lru.front().first, -1);
@@ -3205,11 +3296,41 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             cs.active = 1;
             cs.rank_limit = (int)std::min<int64_t>(limit, f.cap_rows);
             GX_CUDA(cudaMemcpyAsync(d_state.ptr, &cs, sizeof cs, cudaMemcpyHostToDevice, st));
-            GX_CUDA(gx::launch_chol_chain(real, f.L.ptr, N, (int)n, (int)rank + 1 + chain_k, chain_k,
-                                          d_state.as<gx::ChainState>(), d_slot_of.as<int>(), d_log.as<long long>(),
-                                          pool.buf.ptr, d_work.ptr, d_res.as<double>(), d_scale.as<double>(),
-                                          d_partial.ptr, d_red.ptr, d_gemv.ptr, kGemvChunks, ctx->sm_count, tol, psd,
-                                          st));
+            // the chain's launches replayed as one CUDA graph per (length,
+            // factor buffer, rank-chunk count): one launch instead of six per step
+            const int rank_hi = (int)rank + 1 + chain_k;
+            const int nblk = (int)((N + 127) / 128);
+            const int nchunks = rank_hi >= 64 ? std::max(1, std::min({kGemvChunks, (8 * ctx->sm_count) /
+                                                                                       std::max(nblk, 1),
+                                                                      (rank_hi + 31) / 32}))
+                                              : 1;
+            const auto gkey = std::make_tuple(chain_k, f.L.ptr, nchunks);
+            // (the legacy default stream cannot be captured: launch directly there)
+            const bool capturable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+            auto git = chain_graphs.find(gkey);
+            if (!capturable) {
+                GX_CUDA(gx::launch_chol_chain(real, f.L.ptr, N, (int)n, rank_hi, chain_k,
+                                              d_state.as<gx::ChainState>(), d_slot_of.as<int>(),
+                                              d_log.as<long long>(), pool.buf.ptr, d_work.ptr, d_res.as<double>(),
+                                              d_scale.as<double>(), d_partial.ptr, d_red.ptr, d_gemv.ptr,
+                                              kGemvChunks, ctx->sm_count, tol, psd, st));
+            } else if (git == chain_graphs.end()) {
+                cudaGraph_t graph = nullptr;
+                GX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const cudaError_t le = gx::launch_chol_chain(
+                    real, f.L.ptr, N, (int)n, rank_hi, chain_k, d_state.as<gx::ChainState>(), d_slot_of.as<int>(),
+                    d_log.as<long long>(), pool.buf.ptr, d_work.ptr, d_res.as<double>(), d_scale.as<double>(),
+                    d_partial.ptr, d_red.ptr, d_gemv.ptr, kGemvChunks, ctx->sm_count, tol, psd, st);
+                const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+                GX_CUDA(le);
+                GX_CUDA(ce);
+                cudaGraphExec_t exec = nullptr;
+                const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                GX_CUDA(ie);
+                git = chain_graphs.emplace(gkey, exec).first;
+            }
+            if (capturable) GX_CUDA(cudaGraphLaunch(git->second, st));
             GX_CUDA(cudaMemcpyAsync(&cs_out, d_state.ptr, sizeof cs_out, cudaMemcpyDeviceToHost, st));
             // the log holds `limit` entries; the chain writes at most up to rank_limit <= limit
             const int64_t nlog = std::min<int64_t>(chain_k, limit - (rank + 1));
@@ -3245,8 +3366,11 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                 slot_of_h[p] = -1;  // already -1 on the device
                 ++stats.chained_steps;
             }
-            // chain length: grow while chains run to their end, else follow them
-            chain_k = cs_out.active ? std::min(64, 2 * chain_k) : std::max(1, std::min(64, cs_out.steps + 2));
+            // chain length (a power of two, for few graphs): grow while chains
+            // run to their end, else follow them
+            int want = cs_out.active ? 2 * chain_k : cs_out.steps + 2;
+            chain_k = 1;
+            while (chain_k < want && chain_k < 64) chain_k *= 2;
         }
         if (red.minv < -psd) raise(GX_EPSD, "Coulomb Cholesky residual lost positive semidefiniteness");
     }

@@ -27,9 +27,12 @@
 //
 // Two passes over a warp's primitive quartets keep each batch on one Boys
 // path: pass 0 the entries whose argument the FP32 pair geometry places in
-// the asymptotic sector (FP32 Boys after an FP64 recheck of T; a lane that
-// fails the recheck takes the FP64 Boys function), pass 1 the others (FP64
-// Boys).
+// the asymptotic sector, pass 1 the others (FP64 Boys and seeds).  In pass 0
+// T is recomputed in FP32 from the FP64 separation X' (a lane outside the
+// sector takes the FP64 path), F_0 = sqrt(pi)/(2 sqrt T) in FP32, and the
+// seeds follow in FP32 from the scaled C F_0 by S_{n+1} = -(2n+1) S_n / X'.X'
+// (the asymptotic recurrence F_{n+1} = F_n (n + 1/2)/T with T = rho X'.X'):
+// only X', the prefactor C and its power-of-two scale stay in FP64.
 #pragma once
 
 #include <utility>
@@ -228,6 +231,9 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                 int ip = 0, iq = 0;
                 double2 Sh[L + 1];
                 double2 X[3];
+                double2 C = c2(0.0, 0.0);
+                float2 F0 = make_float2(0.0f, 0.0f), iXX = make_float2(0.0f, 0.0f);
+                int mode = 1;  // 0: FP32 seeds from the asymptotic recurrence; 1: FP64 seeds in Sh
                 int e_lane = -1000;
                 Task tg{};
                 if (active) {
@@ -243,32 +249,61 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                     for (int x = 0; x < 3; ++x)
                         X[x] = c2(pp.Pr[3 * ip + x] - pp.Pr[3 * iq + x], pp.Pi[3 * ip + x] - pp.Pi[3 * iq + x]);
                     const double rs = rsqrt(p + q);
-                    const double rho = p * q * rs * rs;
-                    const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
-                                              fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
-                    const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
-                    double2 C = cscale(cmul(pp.F[ip], pp.F[iq]), rs);
-                    float2 F32[L + 1];
-                    if (pass == 0 && boys_eval32(tre, tim, L, F32)) {
-                        // FP32 Boys values, FP64 seeds C (-2 rho)^n F_n
-                        const double m2r = -2.0 * rho;
+                    C = cscale(cmul(pp.F[ip], pp.F[iq]), rs);
+                    if (pass == 0) {
+                        // T in FP32 from the FP64 separation (the asymptotic
+                        // sector is far from T = 0, where FP32 would not do)
+                        const float2 x0 = make_float2((float)X[0].x, (float)X[0].y);
+                        const float2 x1 = make_float2((float)X[1].x, (float)X[1].y);
+                        const float2 x2 = make_float2((float)X[2].x, (float)X[2].y);
+                        const float pf = (float)p, qf = (float)q;
+                        const float rho32 = __fdividef(pf * qf, pf + qf);
+                        const float2 XX = make_float2(fmaf(x0.x, x0.x, fmaf(x1.x, x1.x, x2.x * x2.x)) -
+                                                          fmaf(x0.y, x0.y, fmaf(x1.y, x1.y, x2.y * x2.y)),
+                                                      2.0f * fmaf(x0.x, x0.y, fmaf(x1.x, x1.y, x2.x * x2.y)));
+                        const float tr = rho32 * XX.x, ti = rho32 * XX.y;
+                        const float r2 = fmaf(tr, tr, ti * ti);
+                        if (tr >= 2.0f * L + 24.0f && fabsf(ti) <= 0.5f * tr &&
+                            (r2 <= 160.0f * 160.0f || tr >= 2.0f * L + 60.0f)) {
+                            // F_0 = sqrt(pi) / (2 sqrt(T)); seeds later by
+                            // S_{n+1} = S_n (-(2n + 1)) / (X'.X'), from
+                            // F_{n+1} = F_n (n + 1/2) / T and T = rho X'.X'
+                            const float ir = rsqrtf(r2);
+                            const float sq = sqrtf(0.5f * (r2 * ir + tr));
+                            const float k0 = 0.886226925452758f * ir;
+                            F0 = make_float2(k0 * sq, -k0 * (0.5f * ti / sq));
+                            const float m2 = fmaf(XX.x, XX.x, XX.y * XX.y);
+                            iXX = make_float2(__fdividef(XX.x, m2), -__fdividef(XX.y, m2));
+                            const float ixx = rsqrtf(m2);
+                            float gm = 1.0f, gmax = 1.0f;
+#pragma unroll
+                            for (int n = 0; n < L; ++n) {
+                                gm *= (2.0f * n + 1.0f) * ixx;
+                                gmax = fmaxf(gmax, gm);
+                            }
+                            // binary exponents from the bits (integer work)
+                            const int ec = max((__double2hiint(C.x) >> 20) & 0x7ff, (__double2hiint(C.y) >> 20) & 0x7ff);
+                            const int ef = (__float_as_int(fmaxf(fabsf(F0.x), fabsf(F0.y))) >> 23) & 0xff;
+                            const int eg = (__float_as_int(gmax) >> 23) & 0xff;
+                            if (ec > 0 && ec < 0x7ff && ef > 0 && ef < 0xff && eg < 0xff)
+                                e_lane = (ec - 1023) + (ef - 127) + (eg - 127) + 2;
+                            mode = 0;
+                        }
+                    }
+                    if (mode == 1) {
+                        const double rho = p * q * rs * rs;
+                        const double tre = rho * (fma(X[0].x, X[0].x, fma(X[1].x, X[1].x, X[2].x * X[2].x)) -
+                                                  fma(X[0].y, X[0].y, fma(X[1].y, X[1].y, X[2].y * X[2].y)));
+                        const double tim = 2.0 * rho * fma(X[0].x, X[0].y, fma(X[1].x, X[1].y, X[2].x * X[2].y));
+                        small::quartet_seeds<L>(d, gi.x + g, C, rho, tre, tim, Sh);
+                        // largest binary exponent of the seeds, read from the bits
 #pragma unroll
                         for (int n = 0; n <= L; ++n) {
-                            Sh[n] = c2(C.x * (double)F32[n].x - C.y * (double)F32[n].y,
-                                       C.x * (double)F32[n].y + C.y * (double)F32[n].x);
-                            C = cscale(C, m2r);
+                            const int ex = (__double2hiint(Sh[n].x) >> 20) & 0x7ff;
+                            const int ey = (__double2hiint(Sh[n].y) >> 20) & 0x7ff;
+                            const int e = max(ex, ey);
+                            if (e > 0 && e < 0x7ff) e_lane = max(e_lane, e - 1023);
                         }
-                    } else {
-                        small::quartet_seeds<L>(d, gi.x + g, C, rho, tre, tim, Sh);
-                    }
-                    // largest binary exponent of the seeds, read from the bits
-                    // (integer work: no FP64 instruction)
-#pragma unroll
-                    for (int n = 0; n <= L; ++n) {
-                        const int ex = (__double2hiint(Sh[n].x) >> 20) & 0x7ff;
-                        const int ey = (__double2hiint(Sh[n].y) >> 20) & 0x7ff;
-                        const int e = max(ex, ey);
-                        if (e > 0 && e < 0x7ff) e_lane = max(e_lane, e - 1023);
                     }
                 }
                 // segment structure: heads, the take masks of the reduction and
@@ -299,8 +334,18 @@ __global__ void __launch_bounds__(128) lane32_kernel(EriDev d, QuartetClass qc) 
                 if (active) {
                     const double sc = pow2(-shift);
                     float2 S32[L + 1];
+                    if (mode == 0) {
+                        S32[0] = small::fmul2(make_float2((float)(C.x * sc), (float)(C.y * sc)), F0);
 #pragma unroll
-                    for (int n = 0; n <= L; ++n) S32[n] = make_float2((float)(Sh[n].x * sc), (float)(Sh[n].y * sc));
+                        for (int n = 0; n < L; ++n) {
+                            const float2 t = small::fmul2(S32[n], iXX);
+                            S32[n + 1] = make_float2(-(2.0f * n + 1.0f) * t.x, -(2.0f * n + 1.0f) * t.y);
+                        }
+                    } else {
+#pragma unroll
+                        for (int n = 0; n <= L; ++n)
+                            S32[n] = make_float2((float)(Sh[n].x * sc), (float)(Sh[n].y * sc));
+                    }
                     const float2 X32[3] = {make_float2((float)X[0].x, (float)X[0].y),
                                            make_float2((float)X[1].x, (float)X[1].y),
                                            make_float2((float)X[2].x, (float)X[2].y)};

@@ -22,6 +22,8 @@ cudaError_t launch_lane32_b(int la, int lb, int lc, int ld, const EriDev& d, con
 cudaError_t launch_lane32_c(int la, int lb, int lc, int ld, const EriDev& d, const QuartetClass& qc, cudaStream_t s,
                             bool* found);
 
+// (L = 5 classes were measured too: at 235-255 registers with spills the
+// lane kernel lost to the generic kernel on every one of them)
 bool lane32_class(int la, int lb, int lc, int ld) {
     const int L = la + lb + lc + ld;
     return L >= 3 && L <= 4 && la <= 2 && lb <= 2 && lc <= 2 && ld <= 2;
