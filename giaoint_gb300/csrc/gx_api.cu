@@ -615,8 +615,14 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
     while (i < end) {
         const int kk_code = plan.task_kk[i];
         const int kk = (kk_code >> 16) * (kk_code & 0xffff);
-        const int want = small ? std::max(1, std::min(128, per / kk))
-                               : std::max(1, std::min({1024, (per + kk - 1) / kk, spread}));
+        // one lane per primitive quartet: up to `per` of them and 128 tasks per
+        // unit, but at least ~4 units per SM when the class is small (a
+        // Cholesky column plan holds a few dozen tasks per class); a stable
+        // plan keeps its units independent of the class size
+        int want = small ? std::max(1, std::min(128, per / kk))
+                         : std::max(1, std::min({1024, (per + kk - 1) / kk, spread}));
+        if (small && !plan.stable)
+            want = std::max(1, std::min<int>(want, (int)(pc.count / (size_t)(4 * std::max(ctx->sm_count, 1)))));
         size_t j = i + 1;
         if (plan.task_part.empty()) {
             while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
@@ -1337,19 +1343,26 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             centries[c + 1] += centries[c];
         }
         const int64_t count = ccount[nchunk], off = centries[nchunk];
+        // pass 2 (parallel): kept quartets and packed offsets.  With a cached
+        // plan it runs on the host while the device evaluates.
+        bool pass2_done = false;
+        auto pass2 = [&] {
+            if (pass2_done) return;
 #pragma omp parallel for schedule(static)
-        for (int64_t c = 0; c < nchunk; ++c) {
-            int64_t k = ccount[c], o = centries[c];
-            for (int64_t i = c * kChunk; i < std::min(nq, (c + 1) * kChunk); ++i) {
-                const uint32_t* x = quartets + 4 * i;
-                if (!keep(x)) continue;
-                if (kept) std::memcpy(kept + 4 * k, x, 4 * sizeof(uint32_t));
-                offsets[k] = o;
-                o += nao[x[0]] * nao[x[1]] * nao[x[2]] * nao[x[3]];
-                ++k;
+            for (int64_t c = 0; c < nchunk; ++c) {
+                int64_t k = ccount[c], o = centries[c];
+                for (int64_t i = c * kChunk; i < std::min(nq, (c + 1) * kChunk); ++i) {
+                    const uint32_t* x = quartets + 4 * i;
+                    if (!keep(x)) continue;
+                    if (kept) std::memcpy(kept + 4 * k, x, 4 * sizeof(uint32_t));
+                    offsets[k] = o;
+                    o += nao[x[0]] * nao[x[1]] * nao[x[2]] * nao[x[3]];
+                    ++k;
+                }
             }
-        }
-        offsets[count] = off;
+            offsets[count] = off;
+            pass2_done = true;
+        };
         const int64_t screened = nq - count;
         if (off > capacity) raise(GX_ELENGTH, "ERI output buffer is too small");
         double2* dout;
@@ -1363,6 +1376,7 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         int64_t nprim = 0, evaluated[2] = {0, 0};
         if (count) {
             PlanData& plan = lookup_plan(ctx, b, h1, h2, count, off, [&] {
+                pass2();
                 std::vector<QuartetRequest> req((size_t)count);
 #pragma omp parallel for schedule(static)
                 for (int64_t c = 0; c < nchunk; ++c) {
@@ -1377,10 +1391,44 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                 return req;
             });
             apply_recorded_tuning(ctx, b, precision, plan);
-            run_plan(ctx, b, B, O, plan, dout, &ms, &nprim, precision, mixed_cutoff, stats ? evaluated : nullptr);
+            cudaStream_t s = ctx->stream;
+            nprim = plan.primitive_quartets;
+            unsigned long long* counters = nullptr;
+            if (stats) {
+                plan.counters.reserve(std::max<size_t>(2 * plan.classes.size(), 2) * sizeof(unsigned long long));
+                counters = plan.counters.as<unsigned long long>();
+            }
+            struct Ev {
+                cudaEvent_t a = nullptr, b = nullptr;
+                ~Ev() {
+                    if (a) cudaEventDestroy(a);
+                    if (b) cudaEventDestroy(b);
+                }
+            } ev;
+            GX_CUDA(cudaEventCreate(&ev.a));
+            GX_CUDA(cudaEventCreate(&ev.b));
+            GX_CUDA(cudaEventRecord(ev.a, s));
+            execute_plan(ctx, b, B, O, plan, dout, precision, mixed_cutoff, counters);
+            GX_CUDA(cudaEventRecord(ev.b, s));
+            if (!out_is_device && off)
+                GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            pass2();  // overlaps the device work
+            GX_CUDA(cudaEventSynchronize(ev.b));
+            GX_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            check_status(ctx);
+            if (stats) {
+                std::vector<unsigned long long> c(2 * plan.classes.size());
+                if (!c.empty())
+                    GX_CUDA(cudaMemcpy(c.data(), counters, c.size() * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < plan.classes.size(); ++i) {
+                    evaluated[0] += (int64_t)c[2 * i];
+                    evaluated[1] += (int64_t)c[2 * i + 1];
+                }
+            }
+        } else {
+            pass2();
         }
-        if (!out_is_device && off)
-            GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(cudaStreamSynchronize(ctx->stream));
         if (stats) {
             stats->requested = nq;
