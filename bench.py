@@ -839,7 +839,7 @@ def run_gpu(args):
         kept = np.empty((nq, 4), dtype=np.uint32)
         off2 = np.zeros(nq + 1, dtype=np.int64)
         stats = nat.GxStats()
-        times, kernel_ms = [], []
+        times, kernel_ms, prepare_ms, copy_ms = [], [], [], []
         reps = max(1, min(args.steps, 5))
         warm = max(3, args.warmup)  # the first call is the cold one, reported separately
         for i in range(warm + reps):
@@ -853,6 +853,8 @@ def run_gpu(args):
             if i >= warm:
                 times.append(dt)
                 kernel_ms.append(stats.kernel_ms)
+                prepare_ms.append(round(stats.prepare_ms, 2))
+                copy_ms.append(round(stats.copy_ms, 2))
             elif i == 0:
                 cold_s = dt  # builds and caches the class-sorted plan on the host
         # breakdown: the same call with device output (no host copy)
@@ -893,6 +895,8 @@ def run_gpu(args):
                "api": "gx_eri_batch (C ABI, pinned host buffers)", "max_abs_diff_vs_device_path": e2e_diff,
                "call_seconds": times, "call_seconds_median": float(statistics.median(times)),
                "call_kernel_ms": kernel_ms,
+               "call_prepare_ms": prepare_ms,
+               "call_copy_ms": copy_ms,
                "device_output_call_seconds": dev_times}
     cpu = None
     parity = {"bar": {"fp64": 1e-12, "fp64_exact": 1e-12, "mixed": 1e-10}}

@@ -35,7 +35,23 @@ class GxStats(ctypes.Structure):
         ("fp32_primitive_quartets", ctypes.c_int64),
         ("skipped_primitive_quartets", ctypes.c_int64),
         ("kernel_ms", ctypes.c_double),
+        ("prepare_ms", ctypes.c_double),
+        ("copy_ms", ctypes.c_double),
+        ("call_ms", ctypes.c_double),
     ]
+
+
+class GxQuartetBlock(ctypes.Structure):
+    _fields_ = [
+        ("shells", ctypes.c_uint32 * 4),
+        ("shape", ctypes.c_int64 * 4),
+        ("values", ctypes.POINTER(ctypes.c_double)),
+        ("count", ctypes.c_int64),
+    ]
+
+
+# int (*gx_quartet_consumer)(const gx_quartet_block*, void*)
+QUARTET_CONSUMER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(GxQuartetBlock), ctypes.c_void_p)
 
 
 class GxCholeskyOptions(ctypes.Structure):
@@ -112,6 +128,8 @@ SIGNATURES = {
     "gx_eri_batch_device": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_double, _u32, _i64, _vp, ctypes.c_int64,
                                            ctypes.POINTER(GxStats)]),
+    "gx_eri_for_each": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, QUARTET_CONSUMER, _vp, ctypes.POINTER(GxStats)]),
     "gx_eri_center_derivatives": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _d, ctypes.c_int64,
                                                  ctypes.POINTER(ctypes.c_float)]),
     "gx_eri_center_derivatives_device": (ctypes.c_int, [_vp, _vp, _d, _d, _u32, ctypes.c_int64, _i64, _vp,

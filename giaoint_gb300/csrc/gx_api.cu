@@ -11,6 +11,7 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <future>
 #include <list>
 #include <map>
 #include <memory>
@@ -184,6 +185,26 @@ struct SharedTables {
     double boys_table_agreement = 0.0;
 };
 
+// Page-locked host memory that grows on demand.
+struct PinnedHost {
+    void* p = nullptr;
+    size_t n = 0;
+    PinnedHost() = default;
+    PinnedHost(const PinnedHost&) = delete;
+    PinnedHost& operator=(const PinnedHost&) = delete;
+    ~PinnedHost() {
+        if (p) cudaFreeHost(p);
+    }
+    void reserve(size_t bytes) {
+        if (bytes <= n) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        GX_CUDA(cudaHostAlloc(&p, bytes, cudaHostAllocDefault));
+        n = bytes;
+    }
+};
+
 struct gx_context {
     int device = 0;
     int sm_count = 0;
@@ -203,6 +224,10 @@ struct gx_context {
     DeviceBuffer deriv_vals, deriv_meta;
     gx_cholesky_stats last_cholesky{};  // of the last factorisation on this context
     bool stable_launch = false;         // plans built here use size-independent launch configurations
+    // page-locked chunk buffers of gx_eri_for_each (held by stream_mu for a
+    // whole call)
+    PinnedHost stream_host[2];
+    std::mutex stream_mu;
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -1299,6 +1324,7 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             raise(GX_EINVAL, "ERI screening threshold must be finite and non-negative");
         validate_quartets(b, quartets, nq);
         std::lock_guard<std::mutex> lock(ctx->mu);
+        const auto t0 = std::chrono::steady_clock::now();
         GX_CUDA(cudaSetDevice(ctx->device));
         std::vector<double> q;
         if (screening > 0.0) q = schwarz_values(ctx, b, B, O);
@@ -1372,7 +1398,8 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             ctx->out.reserve(std::max<int64_t>(off, 1) * sizeof(double2));
             dout = ctx->out.as<double2>();
         }
-        float ms = 0.f;
+        float ms = 0.f, copy_ms = 0.f;
+        double prepare_ms = 0.0;
         int64_t nprim = 0, evaluated[2] = {0, 0};
         if (count) {
             PlanData& plan = lookup_plan(ctx, b, h1, h2, count, off, [&] {
@@ -1399,22 +1426,27 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                 counters = plan.counters.as<unsigned long long>();
             }
             struct Ev {
-                cudaEvent_t a = nullptr, b = nullptr;
+                cudaEvent_t a = nullptr, b = nullptr, c = nullptr;
                 ~Ev() {
                     if (a) cudaEventDestroy(a);
                     if (b) cudaEventDestroy(b);
+                    if (c) cudaEventDestroy(c);
                 }
             } ev;
             GX_CUDA(cudaEventCreate(&ev.a));
             GX_CUDA(cudaEventCreate(&ev.b));
+            GX_CUDA(cudaEventCreate(&ev.c));
+            prepare_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             GX_CUDA(cudaEventRecord(ev.a, s));
             execute_plan(ctx, b, B, O, plan, dout, precision, mixed_cutoff, counters);
             GX_CUDA(cudaEventRecord(ev.b, s));
             if (!out_is_device && off)
                 GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            GX_CUDA(cudaEventRecord(ev.c, s));
             pass2();  // overlaps the device work
-            GX_CUDA(cudaEventSynchronize(ev.b));
+            GX_CUDA(cudaEventSynchronize(ev.c));
             GX_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            GX_CUDA(cudaEventElapsedTime(&copy_ms, ev.b, ev.c));
             check_status(ctx);
             if (stats) {
                 std::vector<unsigned long long> c(2 * plan.classes.size());
@@ -1438,6 +1470,9 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             stats->fp32_primitive_quartets = evaluated[1];
             stats->skipped_primitive_quartets = nprim - evaluated[0] - evaluated[1];
             stats->kernel_ms = ms;
+            stats->prepare_ms = prepare_ms;
+            stats->copy_ms = copy_ms;
+            stats->call_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         }
     });
 }
@@ -2321,6 +2356,117 @@ int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const
                         int64_t out_capacity, gx_eri_stats* stats) {
     return eri_batch_impl(ctx, basis, B, O, quartets, nq, precision, mixed_cutoff, screening_threshold, kept, offsets,
                           out_device, true, out_capacity, stats);
+}
+
+int gx_eri_for_each(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
+                    int64_t nq, int precision, double mixed_cutoff, double screening, gx_quartet_consumer consumer,
+                    void* user_data, gx_eri_stats* stats) {
+    return guarded([&] {
+        if (!consumer) raise(GX_EINVAL, "ERI quartet consumer must not be null");
+        if (!ctx || !b) raise(GX_EINVAL, "null context or basis");
+        if (nq < 0) raise(GX_EINVAL, "negative quartet count");
+        check_field(B, O);
+        if (!std::isfinite(screening) || screening < 0.0)
+            raise(GX_EINVAL, "ERI screening threshold must be finite and non-negative");
+        validate_quartets(b, quartets, nq);
+        std::lock_guard<std::mutex> stream_lock(ctx->stream_mu);
+        const auto t0 = std::chrono::steady_clock::now();
+        // screening once for the whole call (src/eri.cpp:674-685)
+        std::vector<uint32_t> active;
+        const uint32_t* q = quartets;
+        int64_t n = nq;
+        if (screening > 0.0) {
+            std::vector<double> bound;
+            {
+                std::lock_guard<std::mutex> lock(ctx->mu);
+                GX_CUDA(cudaSetDevice(ctx->device));
+                bound = schwarz_values(ctx, b, B, O);
+            }
+            const size_t ns = (size_t)b->ns;
+            active.reserve((size_t)4 * nq);
+            for (int64_t i = 0; i < nq; ++i) {
+                const uint32_t* x = quartets + 4 * i;
+                if (bound[x[0] * ns + x[1]] * bound[x[2] * ns + x[3]] < screening) continue;
+                active.insert(active.end(), x, x + 4);
+            }
+            q = active.data();
+            n = (int64_t)(active.size() / 4);
+        }
+        // chunks of at most kStreamChunk complex elements (a larger block alone)
+        constexpr int64_t kStreamChunk = int64_t(1) << 23;
+        auto elems = [&](int64_t i) {
+            const uint32_t* x = q + 4 * i;
+            return b->nao_of(x[0]) * b->nao_of(x[1]) * b->nao_of(x[2]) * b->nao_of(x[3]);
+        };
+        std::vector<int64_t> first{0};
+        int64_t acc = 0, widest = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t e = elems(i);
+            if (acc && acc + e > kStreamChunk) {
+                first.push_back(i);
+                widest = std::max(widest, acc);
+                acc = 0;
+            }
+            acc += e;
+        }
+        widest = std::max(widest, acc);
+        if (n) first.push_back(n);
+        const int64_t nchunk = (int64_t)first.size() - 1;
+        for (int k = 0; k < std::min<int64_t>(nchunk, 2); ++k)
+            ctx->stream_host[k].reserve((size_t)std::max<int64_t>(widest, 1) * sizeof(double2));
+        struct Chunk {
+            std::vector<int64_t> offsets;
+            gx_eri_stats st{};
+            int rc = 0;
+            std::string msg;
+        };
+        auto run = [&](int64_t k, Chunk& c) {
+            const int slot = (int)(k & 1);
+            const int64_t cnt = first[k + 1] - first[k];
+            c.offsets.assign((size_t)cnt + 1, 0);
+            c.st = gx_eri_stats{};
+            c.rc = eri_batch_impl(ctx, b, B, O, q + 4 * first[k], cnt, precision, mixed_cutoff, 0.0, nullptr,
+                                  c.offsets.data(), ctx->stream_host[slot].p, false,
+                                  (int64_t)(ctx->stream_host[slot].n / sizeof(double2)), &c.st);
+            if (c.rc) c.msg = g_error;
+        };
+        gx_eri_stats total{};
+        total.requested = nq;
+        total.screened = nq - n;
+        total.computed = n;
+        Chunk cur, next;
+        if (nchunk) run(0, cur);
+        for (int64_t k = 0; k < nchunk; ++k) {
+            if (cur.rc) raise(cur.rc, cur.msg);
+            total.primitive_quartets += cur.st.primitive_quartets;
+            total.fp32_primitive_quartets += cur.st.fp32_primitive_quartets;
+            total.skipped_primitive_quartets += cur.st.skipped_primitive_quartets;
+            total.kernel_ms += cur.st.kernel_ms;
+            total.prepare_ms += cur.st.prepare_ms;
+            total.copy_ms += cur.st.copy_ms;
+            std::future<void> ahead;
+            if (k + 1 < nchunk) ahead = std::async(std::launch::async, [&, k] { run(k + 1, next); });
+            const double* base = static_cast<const double*>(ctx->stream_host[k & 1].p);
+            int crc = 0;
+            for (int64_t i = first[k]; i < first[k + 1] && !crc; ++i) {
+                const uint32_t* x = q + 4 * i;
+                gx_quartet_block blk;
+                for (int j = 0; j < 4; ++j) {
+                    blk.shells[j] = x[j];
+                    blk.shape[j] = b->nao_of(x[j]);
+                }
+                const int64_t o = cur.offsets[(size_t)(i - first[k])];
+                blk.values = base + 2 * o;
+                blk.count = cur.offsets[(size_t)(i - first[k]) + 1] - o;
+                crc = consumer(&blk, user_data);
+            }
+            if (ahead.valid()) ahead.wait();
+            if (crc) raise(GX_ECONSUMER, "ERI quartet consumer returned " + std::to_string(crc));
+            std::swap(cur, next);
+        }
+        total.call_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (stats) *stats = total;
+    });
 }
 
 int gx_eri_center_derivatives(gx_context* ctx, gx_basis* basis, const double* B, const double* O,

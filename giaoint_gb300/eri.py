@@ -176,6 +176,53 @@ def eri_batches(basis: Basis, *, field: MagneticField | None = None, quartets: I
         yield emit()
 
 
+def evaluate_eri_shell_quartets(basis: Basis, quartets, consumer, *, field: MagneticField | None = None,
+                                screening_threshold: float = 0.0, precision: str = "fp64",
+                                mixed_cutoff: float = DEFAULT_MIXED_CUTOFF, context=None) -> dict:
+    """Stream the blocks of ``quartets`` to ``consumer(quartet, block)`` in
+    input order, as the reference's C++ ``evaluate_eri_shell_quartets``
+    (include/giao_integrals/eri.hpp:127-135, src/eri.cpp:644-767), through
+    ``gx_eri_for_each``.  ``block`` is a C-order complex128 view of shape
+    (na, nb, nc, nd) into a host buffer of the call, valid only while the
+    consumer runs (copy it to keep it).  Quartets below the Schwarz
+    ``screening_threshold`` are skipped.  An exception raised by the consumer
+    stops the evaluation and propagates.  Returns the counts of the call
+    (requested, computed, screened) and its timings."""
+    if consumer is None:
+        raise ValueError("ERI quartet consumer must not be null")
+    ctx = context or nat.default_context()
+    q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int64).reshape(-1, 4))
+    ns = len(basis.shells)
+    if len(q) and (q.min() < 0 or q.max() >= ns):
+        raise IndexError("ERI shell-quartet index is out of range")
+    q = q.astype(np.uint32)
+    failure: list[BaseException] = []
+
+    def trampoline(blk_ptr, _user):
+        try:
+            blk = blk_ptr.contents
+            shape = tuple(int(x) for x in blk.shape)
+            flat = np.ctypeslib.as_array(blk.values, shape=(2 * int(blk.count),))
+            consumer(tuple(int(x) for x in blk.shells), flat.view(np.complex128).reshape(shape))
+            return 0
+        except BaseException as exc:  # handed back to the caller after the call returns
+            failure.append(exc)
+            return 1
+
+    callback = nat.QUARTET_CONSUMER(trampoline)
+    st = nat.GxStats()
+    B, O = field_arrays(field)
+    rc = nat.lib().gx_eri_for_each(ctx.handle, basis._device(ctx), nat.dptr(B), nat.dptr(O), nat.u32ptr(q), len(q),
+                                   _precision(precision), float(mixed_cutoff), float(screening_threshold), callback,
+                                   None, ctypes.byref(st))
+    if failure:
+        raise failure[0]
+    nat.check(rc)
+    return {"requested": int(st.requested), "computed": int(st.computed), "screened": int(st.screened),
+            "primitive_quartets": int(st.primitive_quartets), "kernel_ms": float(st.kernel_ms),
+            "call_ms": float(st.call_ms)}
+
+
 def _eri_batch_packed(items, *, precision: str = "fp64", mixed_cutoff: float = DEFAULT_MIXED_CUTOFF, context=None,
                       stats: dict | None = None):
     """Several requests in one class-sorted execution (gx_eri_batch_packed).

@@ -33,7 +33,8 @@ enum gx_status {
     GX_ECUDA = -5,    /* CUDA runtime failure   -> RuntimeError            */
     GX_ENOMEM = -6,   /* device memory budget   -> MemoryError             */
     GX_EPSD = -7,     /* Cholesky residual lost positive semidefiniteness  */
-    GX_ETIMEOUT = -8  /* a bounded device wait gave up                     */
+    GX_ETIMEOUT = -8, /* a bounded device wait gave up                     */
+    GX_ECONSUMER = -9 /* a quartet consumer returned non-zero              */
 };
 
 /* Arithmetic of the quartet kernels. */
@@ -59,6 +60,10 @@ typedef struct gx_eri_stats {
     int64_t fp32_primitive_quartets; /* of which in FP32 (mixed precision)       */
     int64_t skipped_primitive_quartets; /* dropped under the mixed-mode floor    */
     double kernel_ms;   /* device time of the quartet kernels                  */
+    double prepare_ms;  /* host time from entry to the first launch (hashing,
+                           screening, plan lookup or build)                     */
+    double copy_ms;     /* device time of the output copy to host memory       */
+    double call_ms;     /* wall time of the call                               */
 } gx_eri_stats;
 
 /* ---------------------------------------------------------------------- */
@@ -139,6 +144,38 @@ int gx_eri_batch_device(gx_context* ctx, gx_basis* basis, const double* B, const
                         const uint32_t* quartets, int64_t nq, int precision, double mixed_cutoff,
                         double screening_threshold, uint32_t* kept, int64_t* offsets, void* out_device,
                         int64_t out_capacity, gx_eri_stats* stats);
+
+/* One evaluated shell quartet, as the reference's ShellQuartetBlockView
+ * (include/giao_integrals/eri.hpp:64-68): the shells as given, the AO counts
+ * (na, nb, nc, nd) and `count` = na*nb*nc*nd interleaved complex128 values
+ * in C order.  `values` points into a host buffer of the call and is valid
+ * only while the consumer runs. */
+typedef struct gx_quartet_block {
+    uint32_t shells[4];
+    int64_t shape[4];
+    const double* values;
+    int64_t count;
+} gx_quartet_block;
+
+/* Consumer of evaluated quartets (eri.hpp:70).  A non-zero return stops the
+ * evaluation: the call then returns GX_ECONSUMER after the device work in
+ * flight has finished. */
+typedef int (*gx_quartet_consumer)(const gx_quartet_block* block, void* user_data);
+
+/* Streams the blocks of nq shell quartets to `consumer`, replacing
+ * evaluate_eri_shell_quartets / for_each_eri_shell_quartet
+ * (include/giao_integrals/eri.hpp:127-135, src/eri.cpp:637-767): quartets
+ * whose Schwarz product is below screening_threshold are dropped, every other
+ * quartet is passed to the consumer once, in input order, on the calling
+ * thread.  The quartets are evaluated in chunks of about 2^23 complex
+ * elements into two page-locked host buffers kept by the context: the device
+ * evaluates chunk k + 1 while the consumer reads chunk k, so host memory
+ * stays bounded for any nq.  A null consumer is GX_EINVAL ("ERI quartet
+ * consumer must not be null", as the reference).  stats (may be NULL)
+ * receives the counts of the whole call. */
+int gx_eri_for_each(gx_context* ctx, gx_basis* basis, const double* B, const double* O, const uint32_t* quartets,
+                    int64_t nq, int precision, double mixed_cutoff, double screening_threshold,
+                    gx_quartet_consumer consumer, void* user_data, gx_eri_stats* stats);
 
 /* ERI centre derivatives of nq shell quartets, replacing
  * compute_eri_derivative_blocks behind _eri_derivative_batch

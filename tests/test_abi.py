@@ -83,6 +83,9 @@ def test_api_validation_before_device_work():
         gi.cholesky_eri(b, threshold=-1.0)
     with pytest.raises(ValueError, match="through 32"):
         gi.boys(1.0, 33)
+    # the streaming entry point refuses a null consumer before it needs a device
+    rc = nat.lib().gx_eri_for_each(None, None, None, None, None, 0, 0, 0.0, 0.0, nat.QUARTET_CONSUMER(), None, None)
+    assert rc == -1 and "must not be null" in nat.last_error()
 
 
 def test_no_cpu_fallback_without_a_device():
