@@ -228,6 +228,11 @@ struct gx_context {
     // whole call)
     PinnedHost stream_host[2];
     std::mutex stream_mu;
+    // host-output calls: the output ranges' copies run on copy_stream while
+    // later ranges are evaluated; copy_parts = ranges per call (0: by size)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_done = nullptr;
+    int copy_parts = 0;
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -531,6 +536,28 @@ struct ClassConf {
     int nolane = 0;     // 1 = the generic kernel also takes the FP32 entries (no FP32 lane kernel)
 };
 
+// Configuration of a class before any tuning, from the autotuner's choices on
+// s/p/d molecules in both precision modes: two-warp blocks under the
+// four-resident-block register budget for every generic class; from L = 5
+// on, stream mode with 16-primitive-quartet units; below, 64-quartet units,
+// tables read from global memory at L = 3.  Small classes keep their own.
+ClassConf default_conf(const std::array<int, 4>& k) {
+    ClassConf c{};
+    if (gx::small_class(k[0], k[1], k[2], k[3])) return c;
+    const int L = k[0] + k[1] + k[2] + k[3];
+    c.wpb = 2;
+    c.minb = 4;
+    if (L >= 5) {
+        c.stream = 1;
+        c.per_group = 16;
+        c.b1 = 32;
+    } else {
+        c.per_group = 64;
+        c.nostage = L == 3 ? 1 : 0;
+    }
+    return c;
+}
+
 // Warp work units of every class: (first task within the class, task count).
 struct GroupSet {
     DeviceBuffer dev;
@@ -545,6 +572,9 @@ struct PlanData {
     std::vector<int> task_kk;       // per task (class order): Kab << 16 | Kcd, for regrouping
     std::vector<int> task_part;     // per task: its part (request) of a packed plan; empty for one part
     bool stable = false;            // launch configuration independent of the plan's size (see launch_class)
+    std::vector<ClassConf> defconf; // per class: the configuration used before any tuning
+    int spread_parts = 1;           // one of this many input ranges run back to back: work units are
+                                    // sized for the classes of the whole list
     int64_t ntask = 0, primitive_quartets = 0;
     double model_flops = 0.0;
     // autotuned configuration per precision mode (GX_PRECISION_*)
@@ -581,7 +611,11 @@ struct CachedPlan {
     const gx_basis* basis;
     uint64_t h1, h2;
     int64_t count, entries;
-    std::unique_ptr<PlanData> plan;
+    int nparts;
+    // the plan of each contiguous input range (one part: the whole list) and
+    // the output element at which each part's blocks end
+    std::vector<std::unique_ptr<PlanData>> parts;
+    std::vector<int64_t> part_end;
 };
 std::mutex g_plan_cache_mu;
 std::map<const gx_context*, std::list<CachedPlan>> g_plan_cache;
@@ -633,7 +667,8 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
     const PlanClass& pc = plan.classes[ci];
     const bool small = lane_units || gx::small_class(pc.key[0], pc.key[1], pc.key[2], pc.key[3]);
     const int per = lane_units ? 1024 : (conf.per_group > 0 ? conf.per_group : (small ? 1024 : 32));
-    const int spread = std::max<int>(1, (int)(pc.count / (size_t)(8 * std::max(ctx->sm_count, 1))));
+    const size_t count = pc.count * (size_t)std::max(plan.spread_parts, 1);
+    const int spread = std::max<int>(1, (int)(count / (size_t)(8 * std::max(ctx->sm_count, 1))));
     std::vector<int2> groups;
     size_t i = pc.first;
     const size_t end = pc.first + pc.count;
@@ -647,7 +682,7 @@ std::vector<int2> make_groups(const gx_context* ctx, const PlanData& plan, size_
         int want = small ? std::max(1, std::min(128, per / kk))
                          : std::max(1, std::min({1024, (per + kk - 1) / kk, spread}));
         if (small && !plan.stable)
-            want = std::max(1, std::min<int>(want, (int)(pc.count / (size_t)(4 * std::max(ctx->sm_count, 1)))));
+            want = std::max(1, std::min<int>(want, (int)(count / (size_t)(4 * std::max(ctx->sm_count, 1)))));
         size_t j = i + 1;
         if (plan.task_part.empty()) {
             while (j < end && (int)(j - i) < want && plan.task_kk[j] == kk_code) ++j;
@@ -694,7 +729,7 @@ void make_group_set(gx_context* ctx, const PlanData& plan, const std::vector<Cla
 // Give `plan` the recorded tuning of (basis, precision), when there is one.
 void apply_recorded_tuning(gx_context* ctx, const gx_basis* b, int precision, PlanData& plan) {
     if (plan.tuned[precision].valid) return;
-    std::vector<ClassConf> conf(plan.classes.size());
+    std::vector<ClassConf> conf = plan.defconf;
     {
         std::lock_guard<std::mutex> lock(g_plan_cache_mu);
         auto it = g_tune_db.find(TuneKey{ctx, b, precision});
@@ -888,8 +923,9 @@ void build_plan_parts(gx_context* ctx, const std::vector<PlanPart>& parts, PlanD
     plan.stable = ctx->stable_launch;
     plan.tasks.reserve(sizeof(gx::Task) * std::max<int64_t>(T, 1));
     if (T) GX_CUDA(cudaMemcpyAsync(plan.tasks.ptr, all.get(), sizeof(gx::Task) * T, cudaMemcpyHostToDevice, ctx->stream));
-    std::vector<ClassConf> defaults(plan.classes.size());
-    make_group_set(ctx, plan, defaults, plan.base);
+    plan.defconf.resize(plan.classes.size());
+    for (size_t ci = 0; ci < plan.classes.size(); ++ci) plan.defconf[ci] = default_conf(plan.classes[ci].key);
+    make_group_set(ctx, plan, plan.defconf, plan.base);
     // (a copy from pageable memory is staged before cudaMemcpyAsync returns,
     // so the host task array may be freed now)
 }
@@ -1082,7 +1118,6 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
     ctx->reset_status();
     const auto& tuned = plan.tuned[precision];
     const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
-    static const ClassConf kDefault{};
     const size_t nc = plan.classes.size();
     // The classes write disjoint output blocks, so they run concurrently on
     // the auxiliary streams: a plan of many small classes (a Cholesky column
@@ -1104,7 +1139,7 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
         GX_CUDA(cudaEventRecord(ctx->fork, s));
         for (int k = 0; k < K; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
         for (size_t ci = 0; ci < nc; ++ci)
-            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters,
                          ctx->aux[ci % K], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
@@ -1114,7 +1149,7 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
         }
     } else {
         for (size_t ci = 0; ci < nc; ++ci)
-            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, nullptr,
                          nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first, (int)gs.lane[ci].second);
     }
@@ -1140,14 +1175,13 @@ void enqueue_plans(gx_context* ctx, const std::vector<std::pair<const PlanData*,
     }
     GX_CUDA(cudaEventRecord(ctx->fork, s));
     for (int k = 0; k < kAux; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
-    static const ClassConf kDefault{};
     int next = 0;
     for (size_t r = 0; r < runs.size(); ++r) {
         const PlanData& plan = *runs[r].first;
         const auto& tuned = plan.tuned[precision];
         const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
         for (size_t ci = 0; ci < plan.classes.size(); ++ci, ++next)
-            launch_class(ctx, runs[r].second, plan, ci, tuned.valid ? tuned.conf[ci] : kDefault,
+            launch_class(ctx, runs[r].second, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters[r],
                          ctx->aux[next % kAux], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
@@ -1156,6 +1190,66 @@ void enqueue_plans(gx_context* ctx, const std::vector<std::pair<const PlanData*,
         GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
         GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
     }
+}
+
+// Enqueue the parts of a split plan and, behind each part, the copy of its
+// output range to host memory `host` on the context's copy stream: the class
+// launches of later parts keep the SMs busy while earlier ranges are copied.
+// There is no join between parts; the copy of part r waits until every
+// auxiliary stream has finished its launches of parts 0..r.  `compute_done`
+// is recorded on the context stream once every class launch has finished;
+// the context stream then also waits for the last copy.
+void enqueue_parts_with_copies(gx_context* ctx, const gx::EriDev& dev, const CachedPlan& cp, int precision,
+                               const std::vector<unsigned long long*>& counters, const double2* dout, void* host,
+                               cudaEvent_t compute_done) {
+    cudaStream_t s = ctx->stream;
+    constexpr int kAux = 32;
+    if (ctx->aux.empty()) {
+        ctx->aux.resize(kAux);
+        ctx->aux_done.resize(kAux);
+        for (int k = 0; k < kAux; ++k) {
+            GX_CUDA(cudaStreamCreateWithFlags(&ctx->aux[k], cudaStreamNonBlocking));
+            GX_CUDA(cudaEventCreateWithFlags(&ctx->aux_done[k], cudaEventDisableTiming));
+        }
+        GX_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming));
+    }
+    if (!ctx->copy_stream) {
+        GX_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        GX_CUDA(cudaEventCreateWithFlags(&ctx->copy_done, cudaEventDisableTiming));
+    }
+    for (size_t r = 0; r < cp.parts.size(); ++r)
+        if (counters[r])
+            GX_CUDA(cudaMemsetAsync(counters[r], 0, 2 * cp.parts[r]->classes.size() * sizeof(unsigned long long), s));
+    ctx->reset_status();
+    GX_CUDA(cudaEventRecord(ctx->fork, s));
+    for (int k = 0; k < kAux; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
+    GX_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->fork, 0));
+    int next = 0;
+    int64_t start = 0;
+    for (size_t r = 0; r < cp.parts.size(); ++r) {
+        const PlanData& plan = *cp.parts[r];
+        const auto& tuned = plan.tuned[precision];
+        const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
+        for (size_t ci = 0; ci < plan.classes.size(); ++ci, ++next)
+            launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
+                         gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters[r],
+                         ctx->aux[next % kAux], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
+                         (int)gs.lane[ci].second);
+        // a waited event stands for its latest record, so the events are reused per part
+        for (int k = 0; k < kAux; ++k) {
+            GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
+            GX_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->aux_done[k], 0));
+        }
+        const int64_t end = cp.part_end[r];
+        if (end > start)
+            GX_CUDA(cudaMemcpyAsync(static_cast<char*>(host) + start * sizeof(double2), dout + start,
+                                    (end - start) * sizeof(double2), cudaMemcpyDeviceToHost, ctx->copy_stream));
+        start = end;
+    }
+    for (int k = 0; k < kAux; ++k) GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
+    GX_CUDA(cudaEventRecord(compute_done, s));
+    GX_CUDA(cudaEventRecord(ctx->copy_done, ctx->copy_stream));
+    GX_CUDA(cudaStreamWaitEvent(s, ctx->copy_done, 0));
 }
 
 // Evaluate blocks of `req` into device buffer `out` (packed, C order, AO
@@ -1281,24 +1375,47 @@ std::unique_ptr<gx_basis> new_basis(gx_context* ctx, int nshell, const double* c
     return b;
 }
 
-// Most recently used cached plan of basis `b` for a request list identified
-// by (h1, h2, count, entries); `make()` returns the request list on a miss.
+// Cached plan of basis `b` for a request list identified by (h1, h2, count,
+// entries), split into up to `nparts` contiguous input ranges of about equal
+// output size (empty ranges dropped); `make()` returns the request list
+// (increasing output offsets) on a miss.
 template <class Make>
-PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
-                      Make&& make) {
+CachedPlan& lookup_parts(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
+                         int nparts, Make&& make) {
     auto& cache = plan_cache(ctx);
     auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
-        return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == entries;
+        return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == entries &&
+               c.nparts == nparts;
     });
     if (hit == cache.end()) {
         const std::vector<QuartetRequest> req = make();
-        auto plan = std::make_unique<PlanData>();
-        build_plan(ctx, b, req, *plan);
-        cache.push_front({b, h1, h2, count, entries, std::move(plan)});
+        CachedPlan c{b, h1, h2, count, entries, nparts, {}, {}};
+        // contiguous input ranges of about entries / nparts output elements
+        size_t first = 0;
+        for (int k = 0; k < nparts; ++k) {
+            size_t last = req.size();
+            if (k + 1 < nparts) {
+                const int64_t goal = entries / nparts * (k + 1);
+                last = std::lower_bound(req.begin() + first, req.end(), goal,
+                                        [](const QuartetRequest& r, int64_t v) { return r.out_off < v; }) -
+                       req.begin();
+            }
+            if (nparts > 1 && last == first) continue;
+            auto plan = std::make_unique<PlanData>();
+            plan->spread_parts = nparts;
+            if (nparts == 1)
+                build_plan(ctx, b, req, *plan);
+            else
+                build_plan(ctx, b, std::vector<QuartetRequest>(req.begin() + first, req.begin() + last), *plan);
+            c.parts.push_back(std::move(plan));
+            c.part_end.push_back(last < req.size() ? req[last].out_off : entries);
+            first = last;
+        }
+        cache.push_front(std::move(c));
         size_t bytes = 0;
         int kept_plans = 0;
         for (auto it = cache.begin(); it != cache.end();) {
-            bytes += it->plan->tasks.bytes;
+            for (const auto& p : it->parts) bytes += p->tasks.bytes;
             if (++kept_plans > 4 || (kept_plans > 1 && bytes > (size_t(2) << 30)))
                 it = cache.erase(it);
             else
@@ -1307,8 +1424,22 @@ PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, in
     } else {
         cache.splice(cache.begin(), cache, hit);  // most recently used first
     }
-    return *cache.front().plan;
+    return cache.front();
 }
+
+template <typename Make>
+PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
+                      Make&& make) {
+    return *lookup_parts(ctx, b, h1, h2, count, entries, 1, std::forward<Make>(make)).parts[0];
+}
+
+// Host-output calls of at least kOverlapEntries complex elements into
+// page-locked memory are evaluated as up to kMaxCopyParts input ranges of
+// about kOverlapEntries elements or more each, the copy of one range
+// overlapping the evaluation of the next (gx_context_set_copy_parts overrides
+// the count).
+constexpr int64_t kOverlapEntries = int64_t(1) << 25;
+constexpr int64_t kMaxCopyParts = 8;
 
 int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
                    int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
@@ -1402,7 +1533,19 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         double prepare_ms = 0.0;
         int64_t nprim = 0, evaluated[2] = {0, 0};
         if (count) {
-            PlanData& plan = lookup_plan(ctx, b, h1, h2, count, off, [&] {
+            // host output in page-locked memory: the copy of each output range
+            // overlaps the evaluation of the next ones
+            int nparts = 1;
+            if (!out_is_device && off >= kOverlapEntries) {
+                cudaPointerAttributes attr{};
+                if (cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost)
+                    nparts = ctx->copy_parts > 0
+                                 ? ctx->copy_parts
+                                 : (int)std::min<int64_t>(kMaxCopyParts, off / kOverlapEntries);
+                else
+                    (void)cudaGetLastError();
+            }
+            CachedPlan& cp = lookup_parts(ctx, b, h1, h2, count, off, nparts, [&] {
                 pass2();
                 std::vector<QuartetRequest> req((size_t)count);
 #pragma omp parallel for schedule(static)
@@ -1417,13 +1560,17 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                 }
                 return req;
             });
-            apply_recorded_tuning(ctx, b, precision, plan);
+            const size_t np = cp.parts.size();
             cudaStream_t s = ctx->stream;
-            nprim = plan.primitive_quartets;
-            unsigned long long* counters = nullptr;
-            if (stats) {
-                plan.counters.reserve(std::max<size_t>(2 * plan.classes.size(), 2) * sizeof(unsigned long long));
-                counters = plan.counters.as<unsigned long long>();
+            std::vector<unsigned long long*> counters(np, nullptr);
+            for (size_t r = 0; r < np; ++r) {
+                PlanData& plan = *cp.parts[r];
+                apply_recorded_tuning(ctx, b, precision, plan);
+                nprim += plan.primitive_quartets;
+                if (stats) {
+                    plan.counters.reserve(std::max<size_t>(2 * plan.classes.size(), 2) * sizeof(unsigned long long));
+                    counters[r] = plan.counters.as<unsigned long long>();
+                }
             }
             struct Ev {
                 cudaEvent_t a = nullptr, b = nullptr, c = nullptr;
@@ -1438,10 +1585,16 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             GX_CUDA(cudaEventCreate(&ev.c));
             prepare_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             GX_CUDA(cudaEventRecord(ev.a, s));
-            execute_plan(ctx, b, B, O, plan, dout, precision, mixed_cutoff, counters);
-            GX_CUDA(cudaEventRecord(ev.b, s));
-            if (!out_is_device && off)
-                GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            if (np == 1) {
+                execute_plan(ctx, b, B, O, *cp.parts[0], dout, precision, mixed_cutoff, counters[0]);
+                GX_CUDA(cudaEventRecord(ev.b, s));
+                if (!out_is_device && off)
+                    GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
+            } else {
+                FieldPairs& fp = field_pairs(b, B, O);
+                const gx::EriDev dev = make_dev(ctx, b, fp, dout, precision, mixed_cutoff);
+                enqueue_parts_with_copies(ctx, dev, cp, precision, counters, dout, out, ev.b);
+            }
             GX_CUDA(cudaEventRecord(ev.c, s));
             pass2();  // overlaps the device work
             GX_CUDA(cudaEventSynchronize(ev.c));
@@ -1449,13 +1602,16 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             GX_CUDA(cudaEventElapsedTime(&copy_ms, ev.b, ev.c));
             check_status(ctx);
             if (stats) {
-                std::vector<unsigned long long> c(2 * plan.classes.size());
-                if (!c.empty())
-                    GX_CUDA(cudaMemcpy(c.data(), counters, c.size() * sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToHost));
-                for (size_t i = 0; i < plan.classes.size(); ++i) {
-                    evaluated[0] += (int64_t)c[2 * i];
-                    evaluated[1] += (int64_t)c[2 * i + 1];
+                for (size_t r = 0; r < np; ++r) {
+                    const PlanData& plan = *cp.parts[r];
+                    std::vector<unsigned long long> c(2 * plan.classes.size());
+                    if (!c.empty())
+                        GX_CUDA(cudaMemcpy(c.data(), counters[r], c.size() * sizeof(unsigned long long),
+                                           cudaMemcpyDeviceToHost));
+                    for (size_t i = 0; i < plan.classes.size(); ++i) {
+                        evaluated[0] += (int64_t)c[2 * i];
+                        evaluated[1] += (int64_t)c[2 * i + 1];
+                    }
                 }
             }
         } else {
@@ -1643,7 +1799,16 @@ extern "C" int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* b
     });
 }
 
-extern "C" int gx_context_set_stable_launch(gx_context* ctx, int stable) {
+extern "C" int gx_context_set_copy_parts(gx_context* ctx, int parts) {
+    return guarded([&] {
+        if (!ctx) raise(GX_EINVAL, "null context");
+        if (parts < 0 || parts > 64) raise(GX_EINVAL, "copy parts must be in [0, 64]");
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        ctx->copy_parts = parts;
+    });
+}
+
+int gx_context_set_stable_launch(gx_context* ctx, int stable) {
     return guarded([&] {
         if (!ctx) raise(GX_EINVAL, "null context");
         std::lock_guard<std::mutex> lock(ctx->mu);
@@ -2280,6 +2445,8 @@ void gx_context_destroy(gx_context* ctx) {
     for (auto st : ctx->aux) cudaStreamDestroy(st);
     for (auto ev : ctx->aux_done) cudaEventDestroy(ev);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -3914,7 +4081,7 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
         std::vector<int> b1(nc), wpb(nc), tiles(3 * nc, 0);
         GX_CUDA(cudaEventRecord(ev[0], s));
         for (size_t ci = 0; ci < nc; ++ci) {
-            launch_class(ctx, dev, pd, ci, tuned.valid ? tuned.conf[ci] : ClassConf{},
+            launch_class(ctx, dev, pd, ci, tuned.valid ? tuned.conf[ci] : pd.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, &b1[ci],
                          &wpb[ci], &tiles[3 * ci], gs.dev.as<int2>() + gs.lane[ci].first, (int)gs.lane[ci].second);
             GX_CUDA(cudaEventRecord(ev[ci + 1], s));
@@ -3937,14 +4104,15 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
             float ms = 0.0f;
             GX_CUDA(cudaEventElapsedTime(&ms, ev[ci], ev[ci + 1]));
             o.ms = ms;
-            o.per_group = tuned.valid ? tuned.conf[ci].per_group : 0;
+            const ClassConf& used = tuned.valid ? tuned.conf[ci] : pd.defconf[ci];
+            o.per_group = used.per_group;
             o.warps_per_block = wpb[ci];
             o.batch = b1[ci];
             o.groups = (int64_t)gs.range[ci].second;
             o.kt = tiles[3 * ci];
             o.ct = tiles[3 * ci + 1];
             o.min_blocks = tiles[3 * ci + 2];
-            o.stream = tuned.valid ? tuned.conf[ci].stream : 0;
+            o.stream = used.stream;
         }
         for (auto& e : ev) cudaEventDestroy(e);
         check_status(ctx);
@@ -3959,7 +4127,7 @@ int gx_eri_plan_get_config(gx_eri_plan* plan, int precision, gx_class_config* ou
         const PlanData& pd = plan->data;
         const auto& tuned = pd.tuned[precision];
         for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
-            const ClassConf c = tuned.valid ? tuned.conf[ci] : ClassConf{};
+            const ClassConf c = tuned.valid ? tuned.conf[ci] : pd.defconf[ci];
             out[ci] = gx_class_config{c.per_group, c.wpb, c.b1, c.kt, c.ct, c.minb, c.nostage, c.stream, c.nolane};
         }
     });
@@ -4015,15 +4183,18 @@ int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, in
         cudaEvent_t e0, e1;
         GX_CUDA(cudaEventCreate(&e0));
         GX_CUDA(cudaEventCreate(&e1));
-        std::vector<ClassConf> best(nc);
+        std::vector<ClassConf> best = pd.defconf;
         double tot_default = 0.0, tot_best = 0.0;
         DeviceBuffer tmp;
         for (size_t ci = 0; ci < nc; ++ci) {
             const auto& k = pd.classes[ci].key;
-            std::vector<ClassConf> cands{ClassConf{}};
+            // the untuned configuration first (kept unless another is clearly
+            // faster), then the previous built-in default and the sweep
+            std::vector<ClassConf> cands{pd.defconf[ci]};
             if (gx::small_class(k[0], k[1], k[2], k[3])) {
                 for (int per : {256, 4096}) cands.push_back(ClassConf{per, 0, 0});
             } else {
+                cands.push_back(ClassConf{});
                 for (int per : {16, 32, 64, 128, 256, 512, 1024})
                     for (int w : {2, 4})
                         for (int b1 : {16, 32})

@@ -376,6 +376,12 @@ int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* bases, const
  * requests). */
 int gx_context_set_stable_launch(gx_context* ctx, int stable);
 
+/* Host-output gx_eri_batch calls into page-locked memory of at least 2^25
+ * complex elements run as `parts` contiguous input ranges, the copy of each
+ * range to the host overlapping the evaluation of the later ones (0, the
+ * default: one range per 2^25 elements, at most 8; 1: no overlap). */
+int gx_context_set_copy_parts(gx_context* ctx, int parts);
+
 /* A plan fixes a quartet list (its class-sorted task list and packed
  * offsets, offsets[nq+1]) so that it can be evaluated for many fields
  * without host work: the persistent batched form of
@@ -431,8 +437,10 @@ int gx_eri_plan_profile(gx_eri_plan* plan, const double* B, const double* O, int
 int gx_eri_plan_autotune(gx_eri_plan* plan, const double* B, const double* O, int precision, double mixed_cutoff,
                          void* out_device, int repeats, double* default_ms, double* tuned_ms);
 
-/* Launch configuration of one class (zeros: the default), as the
- * autotuner chooses it: primitive quartets per warp unit, warps per block
+/* Launch configuration of one class, as the autotuner chooses it (a zero
+ * field: the kernel's fixed fallback for that knob; an untuned plan runs
+ * the per-class configuration that gx_eri_plan_get_config reports, by
+ * angular-momentum class): primitive quartets per warp unit, warps per block
  * cap (<= 4), phase-1 batch cap (<= 32), ket-transform rows per lane (1, 2,
  * 4), bra-transform components per lane (1-4), register-budget variant (2
  * or 4 resident blocks), 1 = no shared staging, 1 = stream mode (per-entry

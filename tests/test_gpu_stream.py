@@ -119,3 +119,41 @@ def test_stream_validation():
     rc = nat.lib().gx_eri_for_each(nat.default_context().handle, basis._device(nat.default_context()), None, None,
                                    None, 0, 0, 0.0, 0.0, nat.QUARTET_CONSUMER(), None, None)
     assert rc == -1 and "must not be null" in nat.last_error()
+
+
+def test_overlapped_host_copies_equal_one_range():
+    # host output in page-locked memory, split into input ranges whose copies
+    # overlap the evaluation of later ranges: with size-independent launch
+    # configurations the values are bit for bit those of one range
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    recs, basis, field = _molecule(12, 2026)
+    q = gi.canonical_quartets(len(recs))
+    sizes = np.array([s.ao_count for s in basis.shells])
+    widest = np.argsort(-np.prod(sizes[q.astype(np.int64)], axis=1), kind="stable")[:100_000]
+    q = np.ascontiguousarray(q[np.sort(widest)])
+    total = int(np.prod(sizes[q.astype(np.int64)], axis=1).sum())
+    assert total >= 1 << 25
+    ctx = nat.Context(0)
+    lib = nat.lib()
+    nat.check(lib.gx_context_set_stable_launch(ctx.handle, 1))
+    from giaoint_gb300._types import field_arrays
+
+    Bv, Ov = field_arrays(field)
+    results = []
+    for parts in (1, 3):
+        nat.check(lib.gx_context_set_copy_parts(ctx.handle, parts))
+        host = torch.zeros(2 * total, dtype=torch.float64, pin_memory=True)
+        off = np.zeros(len(q) + 1, dtype=np.int64)
+        st = nat.GxStats()
+        nat.check(lib.gx_eri_batch(ctx.handle, basis._device(ctx), nat.dptr(Bv), nat.dptr(Ov), nat.u32ptr(q),
+                                   len(q), 1, 1e-6, 0.0, None, nat.i64ptr(off),
+                                   ctypes.cast(host.data_ptr(), ctypes.POINTER(ctypes.c_double)), total,
+                                   ctypes.byref(st)))
+        assert st.computed == len(q) and int(off[-1]) == total
+        results.append(host.numpy().copy())
+    assert np.array_equal(results[0], results[1])
+    with pytest.raises(ValueError):
+        nat.check(lib.gx_context_set_copy_parts(ctx.handle, -1))
+    ctx.close()
