@@ -161,7 +161,7 @@ SIGNATURES = {
                                            ctypes.c_int, ctypes.c_double, ctypes.POINTER(_i64), ctypes.POINTER(_d),
                                            _i64, _d]),
     "gx_context_set_stable_launch": (ctypes.c_int, [_vp, ctypes.c_int]),
-    "gx_context_set_copy_parts": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "gx_context_set_copy_parts": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double]),
     "gx_context_set_stream": (ctypes.c_int, [_vp, _vp]),
     "gx_context_synchronize": (ctypes.c_int, [_vp]),
     "gx_eri_plan_create": (ctypes.c_int, [_vp, _vp, _u32, ctypes.c_int64, _i64, ctypes.POINTER(_vp)]),

@@ -233,6 +233,7 @@ struct gx_context {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_done = nullptr;
     int copy_parts = 0;
+    double copy_first = 0.0;  // share of the output in the first range (0: equal ranges)
 
     PairClassHost& pair_class(int la, int lb) {
         auto key = std::make_pair(la, lb);
@@ -537,23 +538,31 @@ struct ClassConf {
 };
 
 // Configuration of a class before any tuning, from the autotuner's choices on
-// s/p/d molecules in both precision modes: two-warp blocks under the
-// four-resident-block register budget for every generic class; from L = 5
-// on, stream mode with 16-primitive-quartet units; below, 64-quartet units,
-// tables read from global memory at L = 3.  Small classes keep their own.
+// s/p/d molecules in both precision modes and on an s-g atom: two-warp blocks
+// for every generic class; below L = 5, 64-primitive-quartet units under the
+// four-resident-block register budget (tables read from global memory at
+// L = 3); from L = 5 on, stream mode with 16-quartet units, four Hermite
+// rows per lane in the ket transform from L = 8, and from L = 12 the
+// two-block register budget with phase-1 batches of 16.  Small classes keep
+// their own.
 ClassConf default_conf(const std::array<int, 4>& k) {
     ClassConf c{};
     if (gx::small_class(k[0], k[1], k[2], k[3])) return c;
     const int L = k[0] + k[1] + k[2] + k[3];
     c.wpb = 2;
     c.minb = 4;
-    if (L >= 5) {
-        c.stream = 1;
-        c.per_group = 16;
-        c.b1 = 32;
-    } else {
+    if (L < 5) {
         c.per_group = 64;
         c.nostage = L == 3 ? 1 : 0;
+        return c;
+    }
+    c.stream = 1;
+    c.per_group = 16;
+    c.b1 = 32;
+    if (L >= 8) c.kt = 4;
+    if (L >= 12) {
+        c.minb = 2;
+        c.b1 = 16;
     }
     return c;
 }
@@ -612,6 +621,7 @@ struct CachedPlan {
     uint64_t h1, h2;
     int64_t count, entries;
     int nparts;
+    double first_share;
     // the plan of each contiguous input range (one part: the whole list) and
     // the output element at which each part's blocks end
     std::vector<std::unique_ptr<PlanData>> parts;
@@ -1192,16 +1202,22 @@ void enqueue_plans(gx_context* ctx, const std::vector<std::pair<const PlanData*,
     }
 }
 
+// Blocks of the SM copy to page-locked host memory: a few dozen saturate the
+// host link; the rest of the GPU keeps evaluating.
+constexpr int kHostCopyBlocks = 64;
+
 // Enqueue the parts of a split plan and, behind each part, the copy of its
-// output range to host memory `host` on the context's copy stream: the class
-// launches of later parts keep the SMs busy while earlier ranges are copied.
+// output range to host memory `host` on the context's copy stream (by the SMs
+// through `host_mapped` when that is given, else by the copy engine): the
+// class launches of later parts keep the SMs busy while earlier ranges are
+// copied.
 // There is no join between parts; the copy of part r waits until every
 // auxiliary stream has finished its launches of parts 0..r.  `compute_done`
 // is recorded on the context stream once every class launch has finished;
 // the context stream then also waits for the last copy.
 void enqueue_parts_with_copies(gx_context* ctx, const gx::EriDev& dev, const CachedPlan& cp, int precision,
                                const std::vector<unsigned long long*>& counters, const double2* dout, void* host,
-                               cudaEvent_t compute_done) {
+                               void* host_mapped, cudaEvent_t compute_done) {
     cudaStream_t s = ctx->stream;
     constexpr int kAux = 32;
     if (ctx->aux.empty()) {
@@ -1241,9 +1257,15 @@ void enqueue_parts_with_copies(gx_context* ctx, const gx::EriDev& dev, const Cac
             GX_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->aux_done[k], 0));
         }
         const int64_t end = cp.part_end[r];
-        if (end > start)
-            GX_CUDA(cudaMemcpyAsync(static_cast<char*>(host) + start * sizeof(double2), dout + start,
-                                    (end - start) * sizeof(double2), cudaMemcpyDeviceToHost, ctx->copy_stream));
+        if (end > start) {
+            const int64_t bytes = (end - start) * (int64_t)sizeof(double2);
+            if (host_mapped)
+                GX_CUDA(gx::launch_host_copy(static_cast<char*>(host_mapped) + start * sizeof(double2), dout + start,
+                                             bytes, kHostCopyBlocks, ctx->copy_stream));
+            else
+                GX_CUDA(cudaMemcpyAsync(static_cast<char*>(host) + start * sizeof(double2), dout + start, bytes,
+                                        cudaMemcpyDeviceToHost, ctx->copy_stream));
+        }
         start = end;
     }
     for (int k = 0; k < kAux; ++k) GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
@@ -1381,21 +1403,24 @@ std::unique_ptr<gx_basis> new_basis(gx_context* ctx, int nshell, const double* c
 // (increasing output offsets) on a miss.
 template <class Make>
 CachedPlan& lookup_parts(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
-                         int nparts, Make&& make) {
+                         int nparts, Make&& make, double first_share = 0.0) {
     auto& cache = plan_cache(ctx);
     auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
         return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == entries &&
-               c.nparts == nparts;
+               c.nparts == nparts && c.first_share == first_share;
     });
     if (hit == cache.end()) {
         const std::vector<QuartetRequest> req = make();
-        CachedPlan c{b, h1, h2, count, entries, nparts, {}, {}};
-        // contiguous input ranges of about entries / nparts output elements
+        CachedPlan c{b, h1, h2, count, entries, nparts, first_share, {}, {}};
+        // contiguous input ranges: the first holds first_share of the output
+        // elements (0: an equal share), the others equal shares of the rest
+        const double f0 = first_share > 0.0 ? first_share : 1.0 / nparts;
         size_t first = 0;
         for (int k = 0; k < nparts; ++k) {
             size_t last = req.size();
             if (k + 1 < nparts) {
-                const int64_t goal = entries / nparts * (k + 1);
+                const int64_t goal =
+                    (int64_t)((double)entries * (f0 + (1.0 - f0) * k / std::max(1, nparts - 1)));
                 last = std::lower_bound(req.begin() + first, req.end(), goal,
                                         [](const QuartetRequest& r, int64_t v) { return r.out_off < v; }) -
                        req.begin();
@@ -1433,13 +1458,17 @@ PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, in
     return *lookup_parts(ctx, b, h1, h2, count, entries, 1, std::forward<Make>(make)).parts[0];
 }
 
-// Host-output calls of at least kOverlapEntries complex elements into
-// page-locked memory are evaluated as up to kMaxCopyParts input ranges of
-// about kOverlapEntries elements or more each, the copy of one range
-// overlapping the evaluation of the next (gx_context_set_copy_parts overrides
-// the count).
-constexpr int64_t kOverlapEntries = int64_t(1) << 25;
-constexpr int64_t kMaxCopyParts = 8;
+// Host-output calls of at least kOverlapEntries complex elements (1 GiB)
+// into page-locked memory are evaluated as kAutoCopyParts input ranges, the
+// first holding kAutoFirstShare of the output, its copy overlapping the
+// evaluation of the second.  Measured on the 12-atom molecule (4.2 GB, calls
+// of 77.7 ms unsplit): two equal ranges 75.9 ms, first share 0.6 / 0.7 / 0.8
+// 74.2 / 73.5 / 74.1 ms, three or four ranges 75-77 ms (the split costs
+// kernel time, the overlapped copy a little more).  gx_context_set_copy_parts
+// overrides both.
+constexpr int64_t kOverlapEntries = int64_t(1) << 26;
+constexpr int kAutoCopyParts = 2;
+constexpr double kAutoFirstShare = 0.7;
 
 int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
                    int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
@@ -1535,15 +1564,20 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
         if (count) {
             // host output in page-locked memory: the copy of each output range
             // overlaps the evaluation of the next ones
+            // page-locked host output: copied by the SMs through its mapped
+            // address (16-byte aligned), in ranges that overlap the evaluation
             int nparts = 1;
-            if (!out_is_device && off >= kOverlapEntries) {
+            void* mapped = nullptr;
+            if (!out_is_device && off > 0) {
                 cudaPointerAttributes attr{};
-                if (cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost)
-                    nparts = ctx->copy_parts > 0
-                                 ? ctx->copy_parts
-                                 : (int)std::min<int64_t>(kMaxCopyParts, off / kOverlapEntries);
-                else
+                if (cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
+                    if (attr.devicePointer && !(reinterpret_cast<uintptr_t>(attr.devicePointer) & 15))
+                        mapped = attr.devicePointer;
+                    if (ctx->copy_parts > 1 || (ctx->copy_parts == 0 && off >= kOverlapEntries))
+                        nparts = ctx->copy_parts > 0 ? ctx->copy_parts : kAutoCopyParts;
+                } else {
                     (void)cudaGetLastError();
+                }
             }
             CachedPlan& cp = lookup_parts(ctx, b, h1, h2, count, off, nparts, [&] {
                 pass2();
@@ -1559,7 +1593,7 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                     }
                 }
                 return req;
-            });
+            }, nparts == 1 ? 0.0 : (ctx->copy_parts == 0 ? kAutoFirstShare : ctx->copy_first));
             const size_t np = cp.parts.size();
             cudaStream_t s = ctx->stream;
             std::vector<unsigned long long*> counters(np, nullptr);
@@ -1588,12 +1622,14 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             if (np == 1) {
                 execute_plan(ctx, b, B, O, *cp.parts[0], dout, precision, mixed_cutoff, counters[0]);
                 GX_CUDA(cudaEventRecord(ev.b, s));
-                if (!out_is_device && off)
+                if (mapped)
+                    GX_CUDA(gx::launch_host_copy(mapped, dout, off * (int64_t)sizeof(double2), kHostCopyBlocks, s));
+                else if (!out_is_device && off)
                     GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
             } else {
                 FieldPairs& fp = field_pairs(b, B, O);
                 const gx::EriDev dev = make_dev(ctx, b, fp, dout, precision, mixed_cutoff);
-                enqueue_parts_with_copies(ctx, dev, cp, precision, counters, dout, out, ev.b);
+                enqueue_parts_with_copies(ctx, dev, cp, precision, counters, dout, out, mapped, ev.b);
             }
             GX_CUDA(cudaEventRecord(ev.c, s));
             pass2();  // overlaps the device work
@@ -1799,12 +1835,14 @@ extern "C" int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* b
     });
 }
 
-extern "C" int gx_context_set_copy_parts(gx_context* ctx, int parts) {
+extern "C" int gx_context_set_copy_parts(gx_context* ctx, int parts, double first_share) {
     return guarded([&] {
         if (!ctx) raise(GX_EINVAL, "null context");
         if (parts < 0 || parts > 64) raise(GX_EINVAL, "copy parts must be in [0, 64]");
+        if (!(first_share >= 0.0 && first_share < 1.0)) raise(GX_EINVAL, "first_share must be in [0, 1)");
         std::lock_guard<std::mutex> lock(ctx->mu);
         ctx->copy_parts = parts;
+        ctx->copy_first = first_share;
     });
 }
 
@@ -3658,7 +3696,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             cs.rank_limit = (int)std::min<int64_t>(limit, f.cap_rows);
             GX_CUDA(cudaMemcpyAsync(d_state.ptr, &cs, sizeof cs, cudaMemcpyHostToDevice, st));
             // the chain's launches replayed as one CUDA graph per (length,
-            // factor buffer, rank-chunk count): one launch instead of six per step
+            // factor buffer, rank-chunk count): one launch instead of three per step
             const int rank_hi = (int)rank + 1 + chain_k;
             const int nblk = (int)((N + 127) / 128);
             const int nchunks = rank_hi >= 64 ? std::max(1, std::min({kGemvChunks, (8 * ctx->sm_count) /
@@ -3672,16 +3710,16 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             if (!capturable) {
                 GX_CUDA(gx::launch_chol_chain(real, f.L.ptr, N, (int)n, rank_hi, chain_k,
                                               d_state.as<gx::ChainState>(), d_slot_of.as<int>(),
-                                              d_log.as<long long>(), pool.buf.ptr, d_work.ptr, d_res.as<double>(),
-                                              d_scale.as<double>(), d_partial.ptr, d_red.ptr, d_gemv.ptr,
-                                              kGemvChunks, ctx->sm_count, tol, psd, st));
+                                              d_log.as<long long>(), pool.buf.ptr, d_res.as<double>(),
+                                              d_partial.ptr, d_red.ptr, d_gemv.ptr, kGemvChunks, ctx->sm_count, tol,
+                                              psd, st));
             } else if (git == chain_graphs.end()) {
                 cudaGraph_t graph = nullptr;
                 GX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                 const cudaError_t le = gx::launch_chol_chain(
                     real, f.L.ptr, N, (int)n, rank_hi, chain_k, d_state.as<gx::ChainState>(), d_slot_of.as<int>(),
-                    d_log.as<long long>(), pool.buf.ptr, d_work.ptr, d_res.as<double>(), d_scale.as<double>(),
-                    d_partial.ptr, d_red.ptr, d_gemv.ptr, kGemvChunks, ctx->sm_count, tol, psd, st);
+                    d_log.as<long long>(), pool.buf.ptr, d_res.as<double>(), d_partial.ptr, d_red.ptr, d_gemv.ptr,
+                    kGemvChunks, ctx->sm_count, tol, psd, st);
                 const cudaError_t ce = cudaStreamEndCapture(st, &graph);
                 GX_CUDA(le);
                 GX_CUDA(ce);

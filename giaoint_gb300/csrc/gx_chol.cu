@@ -337,10 +337,10 @@ cudaError_t launch_chol_step(bool real, const void* L, long long ld, int rank, l
 // below read the pivot, rank and column from that state and return at once
 // when the chain has stopped.
 
-__global__ void chain_select_kernel(ChainState* st, const Red* red, int* slot_of, long long* log, double tol,
-                                    double psd) {
-    if (!st->active) return;
-    const Red r = *red;
+// Select logic shared by the chain's first step and the fused end of every
+// step: stop the chain, or take the argmax as the next pivot (its column
+// slot, its scale 1/sqrt(residual), its place in the log).
+__device__ void chain_select(ChainState* st, const Red& r, int* slot_of, long long* log, double tol, double psd) {
     int stop = 0;
     int slot = -1;
     if (r.minv < -psd)
@@ -358,8 +358,15 @@ __global__ void chain_select_kernel(ChainState* st, const Red* red, int* slot_of
     }
     st->pivot = r.idx;
     st->slot = slot;
+    st->scale = rsqrt(r.maxv);  // r.maxv is the stored residual of the pivot
     slot_of[r.idx] = -1;
     log[st->rank] = r.idx;
+}
+
+__global__ void chain_select_kernel(ChainState* st, const Red* red, int* slot_of, long long* log, double tol,
+                                    double psd) {
+    if (!st->active) return;
+    chain_select(st, *red, slot_of, log, tol, psd);
 }
 
 template <typename T>
@@ -398,46 +405,45 @@ __global__ void chain_gemv_split_kernel(const T* L, long long ld, const ChainSta
     if (j < N) partials[(long long)blockIdx.y * N + j] = acc;
 }
 
+// Updated column entry j: the cached raw column minus the rank-chunk partial
+// sums, in chunk order.
 template <typename T>
-__global__ void chain_gemv_sum_kernel(const T* pool, const ChainState* st, const T* partials, int nchunks, long long N,
-                                      T* col_out) {
-    if (!st->active) return;
-    const T* col_in = pool + (long long)st->slot * N;
-    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
-        T acc = col_in[j];
-        for (int y = 0; y < nchunks; ++y) {
-            if constexpr (sizeof(T) == 8) {
-                acc -= partials[(long long)y * N + j];
-            } else {
-                acc = csub(acc, partials[(long long)y * N + j]);
-            }
+__device__ __forceinline__ T chain_column(const T* col_in, const T* partials, int nchunks, long long N, long long j) {
+    T acc = col_in[j];
+    for (int y = 0; y < nchunks; ++y) {
+        if constexpr (sizeof(T) == 8) {
+            acc -= partials[(long long)y * N + j];
+        } else {
+            acc = csub(acc, partials[(long long)y * N + j]);
         }
-        col_out[j] = acc;
     }
+    return acc;
 }
 
-__global__ void chain_scale_kernel(const ChainState* st, const double* res, double* scale) {
-    if (st->active) *scale = rsqrt(res[st->pivot]);
-}
-
+// The new factor row (the updated column times the pivot's scale; the real
+// path symmetrises (mu nu) with (nu mu)), the residual update and its
+// per-block argmax/minimum.
 template <typename T>
-__global__ void chain_update_kernel(const ChainState* st, const T* col, int n, const double* scale, T* L, double* res,
-                                    Red* partial) {
+__global__ void chain_update_kernel(const ChainState* st, const T* pool, const T* partials, int nchunks, int n, T* L,
+                                    double* res, Red* partial) {
     if (!st->active) return;
     const long long N = (long long)n * n;
     const long long piv = st->pivot;
+    const T* col_in = pool + (long long)st->slot * N;
     T* Lrow = L + (long long)st->rank * N;
-    const double sc = *scale;
+    const double sc = st->scale;
     Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
     for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < N; j += (long long)gridDim.x * blockDim.x) {
         double mag2;
         if constexpr (sizeof(T) == 8) {
             const long long mu = j / n, nu = j - mu * n;
-            const double c = (col[j] + col[nu * n + mu]) * 0.5 * sc;
+            const double wj = chain_column(col_in, partials, nchunks, N, j);
+            const double wt = chain_column(col_in, partials, nchunks, N, nu * n + mu);
+            const double c = (wj + wt) * 0.5 * sc;
             Lrow[j] = c;
             mag2 = c * c;
         } else {
-            const double2 c = cscale(col[j], sc);
+            const double2 c = cscale(chain_column(col_in, partials, nchunks, N, j), sc);
             Lrow[j] = c;
             mag2 = c.x * c.x + c.y * c.y;
         }
@@ -450,7 +456,10 @@ __global__ void chain_update_kernel(const ChainState* st, const T* col, int n, c
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
 
-__global__ void chain_final_kernel(ChainState* st, const Red* partial, int np, Red* out) {
+// End of a step: the residual's argmax and minimum, the rank count, and
+// (unless this is the chain's last step) the selection of the next pivot.
+__global__ void chain_final_kernel(ChainState* st, const Red* partial, int np, Red* out, int* slot_of, long long* log,
+                                   double tol, double psd, int select_next) {
     if (!st->active) return;
     Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
     for (int i = threadIdx.x; i < np; i += blockDim.x) red_merge(r, partial[i]);
@@ -459,45 +468,36 @@ __global__ void chain_final_kernel(ChainState* st, const Red* partial, int np, R
         *out = r;
         st->rank += 1;
         st->steps += 1;
+        if (select_next) chain_select(st, r, slot_of, log, tol, psd);
     }
 }
 
 cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_hi, int steps, ChainState* st,
-                              int* slot_of, long long* log, const void* pool, void* work, double* res, double* scale,
-                              void* partial, void* out, void* gemv_partials, int max_chunks, int sms, double tol,
-                              double psd, cudaStream_t s) {
+                              int* slot_of, long long* log, const void* pool, double* res, void* partial, void* out,
+                              void* gemv_partials, int max_chunks, int sms, double tol, double psd, cudaStream_t s) {
     const int blocks = (int)((N + 127) / 128);
     int nchunks = 1;
     if (gemv_partials && max_chunks > 1 && rank_hi >= 64 && sms > 0)
         nchunks = std::max(1, std::min({max_chunks, (8 * sms) / std::max(blocks, 1), (rank_hi + 31) / 32}));
     const dim3 grid(blocks, nchunks);
-    const int sblocks = (int)std::min<long long>((N + 255) / 256, 8LL * sms);
     Red* red = static_cast<Red*>(out);
+    if (steps > 0) chain_select_kernel<<<1, 1, 0, s>>>(st, red, slot_of, log, tol, psd);
     for (int k = 0; k < steps; ++k) {
-        chain_select_kernel<<<1, 1, 0, s>>>(st, red, slot_of, log, tol, psd);
         if (real) {
             chain_gemv_split_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(L), N, st, nchunks,
                                                                  static_cast<double*>(gemv_partials), N);
-            chain_gemv_sum_kernel<double><<<sblocks, 256, 0, s>>>(static_cast<const double*>(pool), st,
-                                                                  static_cast<const double*>(gemv_partials), nchunks,
-                                                                  N, static_cast<double*>(work));
+            chain_update_kernel<double><<<RED_BLOCKS, 256, 0, s>>>(
+                st, static_cast<const double*>(pool), static_cast<const double*>(gemv_partials), nchunks, n,
+                static_cast<double*>(L), res, static_cast<Red*>(partial));
         } else {
             chain_gemv_split_kernel<double2><<<grid, 128, 0, s>>>(static_cast<const double2*>(L), N, st, nchunks,
                                                                   static_cast<double2*>(gemv_partials), N);
-            chain_gemv_sum_kernel<double2><<<sblocks, 256, 0, s>>>(static_cast<const double2*>(pool), st,
-                                                                   static_cast<const double2*>(gemv_partials),
-                                                                   nchunks, N, static_cast<double2*>(work));
+            chain_update_kernel<double2><<<RED_BLOCKS, 256, 0, s>>>(
+                st, static_cast<const double2*>(pool), static_cast<const double2*>(gemv_partials), nchunks, n,
+                static_cast<double2*>(L), res, static_cast<Red*>(partial));
         }
-        chain_scale_kernel<<<1, 1, 0, s>>>(st, res, scale);
-        if (real)
-            chain_update_kernel<double><<<RED_BLOCKS, 256, 0, s>>>(st, static_cast<const double*>(work), n, scale,
-                                                                   static_cast<double*>(L), res,
-                                                                   static_cast<Red*>(partial));
-        else
-            chain_update_kernel<double2><<<RED_BLOCKS, 256, 0, s>>>(st, static_cast<const double2*>(work), n, scale,
-                                                                    static_cast<double2*>(L), res,
-                                                                    static_cast<Red*>(partial));
-        chain_final_kernel<<<1, 256, 0, s>>>(st, static_cast<const Red*>(partial), RED_BLOCKS, red);
+        chain_final_kernel<<<1, 256, 0, s>>>(st, static_cast<const Red*>(partial), RED_BLOCKS, red, slot_of, log, tol,
+                                             psd, k + 1 < steps ? 1 : 0);
     }
     return cudaGetLastError();
 }

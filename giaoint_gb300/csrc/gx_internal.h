@@ -133,6 +133,10 @@ cudaError_t launch_quartets(const EriDev& dev, const QuartetClass& qc, int warps
                             cudaStream_t s);
 cudaError_t launch_offset_copy(int* dst, const int* src, long long n, int off, cudaStream_t s);
 cudaError_t launch_offset_copy(long long* dst, const long long* src, long long n, long long off, cudaStream_t s);
+// bytes (a multiple of 16, both addresses 16-byte aligned) from device memory
+// to page-locked host memory through its mapped device address, by at most
+// `blocks` blocks of 512 threads
+cudaError_t launch_host_copy(void* dst_mapped, const void* src, long long bytes, int blocks, cudaStream_t s);
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
                                 long long n, double2* full, cudaStream_t s);
 
@@ -239,14 +243,17 @@ struct ChainState {
     int steps;        // steps taken by this chain
     int stop;         // why it stopped: 1 column not cached, 2 converged, 3 rank limit, 4 PSD check
     int rank_limit;   // rows the factor buffer (and the caller's limit) allows
+    double scale;     // 1 / sqrt(residual) of the current pivot
 };
 // Enqueue `steps` chained pivot steps (each returns at once after the chain
 // stopped): pool holds the cached raw columns (slot_of[flat index] = slot,
-// -1 if absent), log receives the pivot of every step at its rank.
+// -1 if absent), log receives the pivot of every step at its rank.  Three
+// launches per step: the rank-chunked GEMV, the row/residual update (which
+// sums the chunks and applies the scale chosen at selection) and the
+// reduction that also selects the next pivot.
 cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_hi, int steps, ChainState* st,
-                              int* slot_of, long long* log, const void* pool, void* work, double* res, double* scale,
-                              void* partial, void* out, void* gemv_partials, int max_chunks, int sms, double tol,
-                              double psd, cudaStream_t s);
+                              int* slot_of, long long* log, const void* pool, double* res, void* partial, void* out,
+                              void* gemv_partials, int max_chunks, int sms, double tol, double psd, cudaStream_t s);
 size_t chol_red_bytes();
 size_t chol_partial_bytes();
 

@@ -20,6 +20,7 @@
 // on the primitive pair, so it is computed once per (basis, field) by
 // pair_kernel; per primitive quartet only Rh (C(L+3,3) entries) and the two
 // contractions remain.
+#include <cstdint>
 #include <algorithm>
 #include <cstdio>
 
@@ -1363,6 +1364,29 @@ cudaError_t launch_offset_copy(int* dst, const int* src, long long n, int off, c
 cudaError_t launch_offset_copy(long long* dst, const long long* src, long long n, long long off, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     offset_copy_kernel<long long><<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, s>>>(dst, src, n, off);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Output copy to page-locked host memory by the SMs (stores through the
+// mapped device address, streaming loads): 16-byte words, grid-stride.  On
+// the coherent host link a few dozen blocks reach the link bandwidth, and
+// unlike copy-engine transfers issued right after heavy kernels the copy
+// keeps that rate from call to call.
+// ---------------------------------------------------------------------------
+
+__global__ void host_copy_kernel(uint4* __restrict__ dst, const uint4* __restrict__ src, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = __ldcs(src + i);
+}
+
+cudaError_t launch_host_copy(void* dst_mapped, const void* src, long long bytes, int blocks, cudaStream_t s) {
+    if (bytes <= 0) return cudaSuccess;
+    if ((bytes & 15) || (reinterpret_cast<uintptr_t>(dst_mapped) & 15) || (reinterpret_cast<uintptr_t>(src) & 15))
+        return cudaErrorInvalidValue;
+    const long long n = bytes / 16;
+    const int grid = (int)std::max<long long>(1, std::min<long long>((n + 511) / 512, blocks));
+    host_copy_kernel<<<grid, 512, 0, s>>>(static_cast<uint4*>(dst_mapped), static_cast<const uint4*>(src), n);
     return cudaGetLastError();
 }
 

@@ -376,11 +376,14 @@ int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* bases, const
  * requests). */
 int gx_context_set_stable_launch(gx_context* ctx, int stable);
 
-/* Host-output gx_eri_batch calls into page-locked memory of at least 2^25
- * complex elements run as `parts` contiguous input ranges, the copy of each
- * range to the host overlapping the evaluation of the later ones (0, the
- * default: one range per 2^25 elements, at most 8; 1: no overlap). */
-int gx_context_set_copy_parts(gx_context* ctx, int parts);
+/* Host-output gx_eri_batch calls into page-locked memory run as `parts`
+ * contiguous input ranges, the copy of each range to the host overlapping
+ * the evaluation of the later ones (1: no overlap).  first_share in [0, 1):
+ * the first range's share of the output elements (0: equal ranges); the
+ * other ranges share the rest equally.  parts = 0, the default: two ranges,
+ * the first with 0.7 of the output, for outputs of at least 2^26 complex
+ * elements; one below. */
+int gx_context_set_copy_parts(gx_context* ctx, int parts, double first_share);
 
 /* A plan fixes a quartet list (its class-sorted task list and packed
  * offsets, offsets[nq+1]) so that it can be evaluated for many fields

@@ -142,8 +142,8 @@ def test_overlapped_host_copies_equal_one_range():
 
     Bv, Ov = field_arrays(field)
     results = []
-    for parts in (1, 3):
-        nat.check(lib.gx_context_set_copy_parts(ctx.handle, parts))
+    for parts, share in ((1, 0.0), (3, 0.0), (2, 0.7)):
+        nat.check(lib.gx_context_set_copy_parts(ctx.handle, parts, share))
         host = torch.zeros(2 * total, dtype=torch.float64, pin_memory=True)
         off = np.zeros(len(q) + 1, dtype=np.int64)
         st = nat.GxStats()
@@ -154,6 +154,7 @@ def test_overlapped_host_copies_equal_one_range():
         assert st.computed == len(q) and int(off[-1]) == total
         results.append(host.numpy().copy())
     assert np.array_equal(results[0], results[1])
+    assert np.array_equal(results[0], results[2])
     with pytest.raises(ValueError):
-        nat.check(lib.gx_context_set_copy_parts(ctx.handle, -1))
+        nat.check(lib.gx_context_set_copy_parts(ctx.handle, -1, 0.0))
     ctx.close()
