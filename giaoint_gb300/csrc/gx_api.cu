@@ -3389,6 +3389,34 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     };
     std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
     DeviceBuffer column_info;
+    // Column evaluations replayed as CUDA graphs.  Pivot shell pairs of the
+    // same kind (angular momenta and primitive counts) give column plans of
+    // the same shape: the same classes, task counts and work units, only the
+    // task records differ.  One graph per shape runs the class launches on
+    // task and unit arrays of its own, which each evaluation refills from its
+    // plan (two device copies) before the replay: one launch instead of one
+    // per class.
+    struct ShapeGraph {
+        PlanData plan;  // the shape's classes and units over buffers of its own
+        DeviceBuffer counters;
+        cudaGraphExec_t exec = nullptr;
+        ~ShapeGraph() {
+            if (exec) cudaGraphExecDestroy(exec);
+        }
+    };
+    std::map<std::vector<long long>, std::unique_ptr<ShapeGraph>> shape_graphs;
+    auto plan_shape = [](const PlanData& pd, const void* out, const void* pairs) {
+        std::vector<long long> sig{(long long)pd.classes.size(), pd.ntask, (long long)pd.base.dev.bytes,
+                                   (long long)(uintptr_t)out, (long long)(uintptr_t)pairs};
+        for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
+            const auto& pc = pd.classes[ci];
+            sig.insert(sig.end(), {pc.key[0], pc.key[1], pc.key[2], pc.key[3], (long long)pc.first,
+                                   (long long)pc.count, (long long)pd.base.range[ci].first,
+                                   (long long)pd.base.range[ci].second, (long long)pd.base.lane[ci].first,
+                                   (long long)pd.base.lane[ci].second});
+        }
+        return sig;
+    };
     {
         // largest column batch: all (x, y) blocks against the largest pivot pair
         int64_t sum_xy = 0, max_ao = 0;
@@ -3622,7 +3650,49 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                                                             GX_PRECISION_FP64, 0.0)});
                 std::vector<unsigned long long*> ctr;
                 for (auto* cp : cps) ctr.push_back(cp->counters.as<unsigned long long>());
-                enqueue_plans(ctx, runs, GX_PRECISION_FP64, ctr);
+                // (the legacy default stream cannot be captured: launch directly there)
+                const bool capturable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
+                const PlanData& pd = cps[0]->plan;
+                if (blocks.size() == 1 && capturable && pd.ntask > 0) {
+                    const auto key = plan_shape(pd, runs[0].second.out, runs[0].second.pairs.F);
+                    auto& sg = shape_graphs[key];
+                    if (!sg) {
+                        sg = std::make_unique<ShapeGraph>();
+                        PlanData& sp = sg->plan;
+                        sp.classes = pd.classes;
+                        sp.defconf = pd.defconf;
+                        sp.stable = pd.stable;
+                        sp.ntask = pd.ntask;
+                        sp.spread_parts = pd.spread_parts;
+                        sp.base.range = pd.base.range;
+                        sp.base.lane = pd.base.lane;
+                        sp.tasks.reserve(pd.tasks.bytes);
+                        sp.base.dev.reserve(pd.base.dev.bytes);
+                        sg->counters.reserve(std::max<size_t>(2 * pd.classes.size(), 2) * sizeof(unsigned long long));
+                        GX_CUDA(cudaMemsetAsync(sg->counters.ptr, 0, sg->counters.bytes, st));
+                        cudaGraph_t graph = nullptr;
+                        GX_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                        try {
+                            enqueue_plans(ctx, {{&sp, runs[0].second}}, GX_PRECISION_FP64,
+                                          {sg->counters.as<unsigned long long>()});
+                        } catch (...) {
+                            cudaStreamEndCapture(st, &graph);
+                            if (graph) cudaGraphDestroy(graph);
+                            throw;
+                        }
+                        GX_CUDA(cudaStreamEndCapture(st, &graph));
+                        const cudaError_t ie = cudaGraphInstantiate(&sg->exec, graph, 0);
+                        cudaGraphDestroy(graph);
+                        GX_CUDA(ie);
+                    }
+                    GX_CUDA(cudaMemcpyAsync(sg->plan.tasks.ptr, pd.tasks.ptr, sizeof(gx::Task) * pd.ntask,
+                                            cudaMemcpyDeviceToDevice, st));
+                    GX_CUDA(cudaMemcpyAsync(sg->plan.base.dev.ptr, pd.base.dev.ptr, pd.base.dev.bytes,
+                                            cudaMemcpyDeviceToDevice, st));
+                    GX_CUDA(cudaGraphLaunch(sg->exec, st));
+                } else {
+                    enqueue_plans(ctx, runs, GX_PRECISION_FP64, ctr);
+                }
             }
             int64_t coff = 0;
             for (size_t k = 0; k < blocks.size(); ++k) {
@@ -3783,18 +3853,20 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         final_max = std::max(red.maxv, 0.0);
     }
     // primitive quartets of the column evaluations and their FP64 FLOP model
-    for (const auto& kv : column_plans) {
-        const ColumnPlan& cp = *kv.second;
-        std::vector<unsigned long long> c(2 * cp.plan.classes.size());
-        if (c.empty()) continue;
-        GX_CUDA(cudaMemcpyAsync(c.data(), cp.counters.ptr, c.size() * sizeof(unsigned long long),
+    // (counted per plan when launched directly, per shape when replayed)
+    auto add_counts = [&](const PlanData& pd, const DeviceBuffer& counters) {
+        std::vector<unsigned long long> c(2 * pd.classes.size());
+        if (c.empty()) return;
+        GX_CUDA(cudaMemcpyAsync(c.data(), counters.ptr, c.size() * sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, st));
         GX_CUDA(cudaStreamSynchronize(st));
-        for (size_t i = 0; i < cp.plan.classes.size(); ++i) {
+        for (size_t i = 0; i < pd.classes.size(); ++i) {
             stats.column_primitive_quartets += (int64_t)c[2 * i];
-            stats.column_model_flops += (double)c[2 * i] * cp.plan.classes[i].flops_per_primitive_quartet;
+            stats.column_model_flops += (double)c[2 * i] * pd.classes[i].flops_per_primitive_quartet;
         }
-    }
+    };
+    for (const auto& kv : column_plans) add_counts(kv.second->plan, kv.second->counters);
+    for (const auto& kv : shape_graphs) add_counts(kv.second->plan, kv.second->counters);
     f.rank = rank;
     f.max_residual = final_max;
     stats.rank = rank;
