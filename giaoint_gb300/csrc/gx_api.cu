@@ -582,6 +582,8 @@ struct PlanData {
     std::vector<int> task_part;     // per task: its part (request) of a packed plan; empty for one part
     bool stable = false;            // launch configuration independent of the plan's size (see launch_class)
     std::vector<ClassConf> defconf; // per class: the configuration used before any tuning
+    std::vector<int> order;         // launch order: largest model work first, so the longest
+                                    // classes start before the short ones fill in around them
     int spread_parts = 1;           // one of this many input ranges run back to back: work units are
                                     // sized for the classes of the whole list
     int64_t ntask = 0, primitive_quartets = 0;
@@ -935,6 +937,13 @@ void build_plan_parts(gx_context* ctx, const std::vector<PlanPart>& parts, PlanD
     if (T) GX_CUDA(cudaMemcpyAsync(plan.tasks.ptr, all.get(), sizeof(gx::Task) * T, cudaMemcpyHostToDevice, ctx->stream));
     plan.defconf.resize(plan.classes.size());
     for (size_t ci = 0; ci < plan.classes.size(); ++ci) plan.defconf[ci] = default_conf(plan.classes[ci].key);
+    plan.order.resize(plan.classes.size());
+    std::iota(plan.order.begin(), plan.order.end(), 0);
+    std::stable_sort(plan.order.begin(), plan.order.end(), [&](int x, int y) {
+        const PlanClass &a = plan.classes[x], &c = plan.classes[y];
+        return (double)a.primitive_quartets * a.flops_per_primitive_quartet >
+               (double)c.primitive_quartets * c.flops_per_primitive_quartet;
+    });
     make_group_set(ctx, plan, plan.defconf, plan.base);
     // (a copy from pageable memory is staged before cudaMemcpyAsync returns,
     // so the host task array may be freed now)
@@ -1148,11 +1157,13 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
         }
         GX_CUDA(cudaEventRecord(ctx->fork, s));
         for (int k = 0; k < K; ++k) GX_CUDA(cudaStreamWaitEvent(ctx->aux[k], ctx->fork, 0));
-        for (size_t ci = 0; ci < nc; ++ci)
+        for (size_t oi = 0; oi < nc; ++oi) {
+            const size_t ci = plan.order.empty() ? oi : (size_t)plan.order[oi];
             launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters,
-                         ctx->aux[ci % K], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
+                         ctx->aux[oi % K], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
+        }
         for (int k = 0; k < K; ++k) {
             GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
             GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
@@ -1190,11 +1201,13 @@ void enqueue_plans(gx_context* ctx, const std::vector<std::pair<const PlanData*,
         const PlanData& plan = *runs[r].first;
         const auto& tuned = plan.tuned[precision];
         const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
-        for (size_t ci = 0; ci < plan.classes.size(); ++ci, ++next)
+        for (size_t oi = 0; oi < plan.classes.size(); ++oi, ++next) {
+            const size_t ci = plan.order.empty() ? oi : (size_t)plan.order[oi];
             launch_class(ctx, runs[r].second, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters[r],
                          ctx->aux[next % kAux], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
+        }
     }
     for (int k = 0; k < kAux; ++k) {
         GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
@@ -1246,11 +1259,13 @@ void enqueue_parts_with_copies(gx_context* ctx, const gx::EriDev& dev, const Cac
         const PlanData& plan = *cp.parts[r];
         const auto& tuned = plan.tuned[precision];
         const GroupSet& gs = tuned.valid ? tuned.groups : plan.base;
-        for (size_t ci = 0; ci < plan.classes.size(); ++ci, ++next)
+        for (size_t oi = 0; oi < plan.classes.size(); ++oi, ++next) {
+            const size_t ci = plan.order.empty() ? oi : (size_t)plan.order[oi];
             launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters[r],
                          ctx->aux[next % kAux], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
+        }
         // a waited event stands for its latest record, so the events are reused per part
         for (int k = 0; k < kAux; ++k) {
             GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
@@ -3661,6 +3676,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                         PlanData& sp = sg->plan;
                         sp.classes = pd.classes;
                         sp.defconf = pd.defconf;
+                        sp.order = pd.order;
                         sp.stable = pd.stable;
                         sp.ntask = pd.ntask;
                         sp.spread_parts = pd.spread_parts;
