@@ -52,9 +52,9 @@ DTYPE = "f64+f32 (mixed: FP32 primitive quartets under the cutoff, FP64 elsewher
 #   ncu --nvtx --nvtx-include "step/" --cache-control none --clock-control none
 #       --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 #       python bench.py --profile-step {mixed,fp64} --no-autotune --warmup 0 --no-cpu
-TRAFFIC_PER_STEP: dict = {"mixed": 649.9e6 + 4578.7e6, "fp64": 580.9e6 + 4367.9e6}
+TRAFFIC_PER_STEP: dict = {"mixed": 914.9e6 + 4949.6e6, "fp64": 778.4e6 + 4782.2e6}
 TRAFFIC_BASIS = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every class launch of one step "
-                 "(default launch configurations, L2 kept across launches); algorithmic output 4.20 GB per step")
+                 "(untuned launch configurations, L2 kept across launches); algorithmic output 4.20 GB per step")
 
 
 def _measured_peaks() -> dict:
@@ -969,7 +969,7 @@ def run_gpu(args):
                                        "ms_per_step": ms64},
                          "traffic": TRAFFIC_PER_STEP.get(args.precision) if args.natoms == 12 else None,
                          "traffic_basis": TRAFFIC_BASIS,
-                         "kernel": "one plan execution: quartet_kernel + small_kernel launches of the 81 classes",
+                         "kernel": "one plan execution: quartet_kernel, small_kernel and (mixed) lane32_kernel launches of the 81 classes",
                          "achieved_basis": "FLOP model per primitive quartet (reference-structured MD count) x "
                                            "primitive quartets evaluated per precision / event-timed step; "
                                            "frac = FLOPs_fp64/(t P64) + FLOPs_fp32/(t P32)",
