@@ -3398,7 +3398,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     // primitive-quartet counters (accumulated over its evaluations).
     struct ColumnPlan {
         PlanData plan;
-        DeviceBuffer boff, counters;
+        DeviceBuffer boff, flip, counters;
         int nblocks = 0;
         int64_t entries = 0;
     };
@@ -3612,15 +3612,28 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                     cp = std::make_unique<ColumnPlan>();
                     std::vector<QuartetRequest> req;
                     std::vector<long long> boff;
+                    std::vector<int> flip;
                     int64_t off = 0;
+                    // (x y | sb sa), or (sb sa | x y) when (x, y) has the
+                    // higher angular momentum: the kernels spread the ket
+                    // components of a shell quartet over warps, so the wide
+                    // pair goes to the ket (a low-L pivot against high-L bra
+                    // pairs otherwise leaves a few warps on the long tasks)
+                    const int lpiv = b->l[sa] + b->l[sb];
                     for (int x = 0; x < ns; ++x)
                         for (int y = real ? x : 0; y < ns; ++y) {
-                            req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
+                            const bool fl = b->l[x] + b->l[y] > lpiv;
+                            if (fl)
+                                req.push_back({(uint32_t)sb, (uint32_t)sa, (uint32_t)x, (uint32_t)y, off});
+                            else
+                                req.push_back({(uint32_t)x, (uint32_t)y, (uint32_t)sb, (uint32_t)sa, off});
                             boff.push_back(off);
+                            flip.push_back(fl ? 1 : 0);
                             off += b->nao_of(x) * b->nao_of(y) * b->nao_of(sb) * b->nao_of(sa);
                         }
                     build_plan(ctx, b, req, cp->plan);
                     upload(cp->boff, boff, st);
+                    upload(cp->flip, flip, st);
                     cp->nblocks = (int)req.size();
                     cp->entries = off;
                     cp->counters.reserve(std::max<size_t>(2 * cp->plan.classes.size(), 2) *
@@ -3715,7 +3728,8 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                 const int ncand = (int)blocks[k].cols.size();
                 if (ncand)
                     GX_CUDA(gx::launch_chol_cols(real, ctx->scratch_a.as<double2>() + sbase[k], cps[k]->boff.as<long long>(),
-                                                 column_info.as<int>(), cps[k]->nblocks, d_cand.as<int>() + 2 * coff,
+                                                 column_info.as<int>(), cps[k]->flip.as<int>(), cps[k]->nblocks,
+                                                 d_cand.as<int>() + 2 * coff,
                                                  ncand, (int)b->nao_of(blocks[k].sb), (int)b->nao_of(blocks[k].sa),
                                                  (int)n, d_dst.as<void*>() + coff, st));
                 coff += ncand;
@@ -3896,13 +3910,12 @@ void copy_factors(const gx_cholesky_factors& f, double* vectors) {
     cudaStream_t st = f.ctx->stream;
     const int64_t N = f.n * f.n;
     if (f.real) {
-        std::vector<double> tmp(f.rank * N);
-        GX_CUDA(cudaMemcpyAsync(tmp.data(), f.L.ptr, f.rank * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        // widened to complex128 on the device, then one copy
+        DeviceBuffer wide;
+        wide.reserve((size_t)f.rank * N * sizeof(double2));
+        GX_CUDA(gx::launch_widen_real(f.L.as<double>(), wide.as<double2>(), f.rank * N, f.ctx->sm_count, st));
+        GX_CUDA(cudaMemcpyAsync(vectors, wide.ptr, f.rank * N * sizeof(double2), cudaMemcpyDeviceToHost, st));
         GX_CUDA(cudaStreamSynchronize(st));
-        for (int64_t j = 0; j < f.rank * N; ++j) {
-            vectors[2 * j] = tmp[j];
-            vectors[2 * j + 1] = 0.0;
-        }
     } else {
         GX_CUDA(cudaMemcpyAsync(vectors, f.L.ptr, f.rank * N * sizeof(double2), cudaMemcpyDeviceToHost, st));
         GX_CUDA(cudaStreamSynchronize(st));

@@ -46,25 +46,33 @@ cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const
 // ---- columns ---------------------------------------------------------------
 
 // info per block: ao_a, ao_b, na, nb, same_shell; cand[2*k] = (c, d) local
-// indices in shells (sb, sa); dst[k] = column k (n*n values).
+// indices in shells (sb, sa); dst[k] = column k (n*n values).  flip[block]
+// (may be null): the block was evaluated as (sb sa | a b), laid out
+// (nc, nd, na, nb), which equals (a b | sb sa) by the exchange of the two
+// electrons.
 template <bool REAL>
-__global__ void chol_cols_kernel(const double2* packed, const long long* boff, const int* info, int nblocks,
-                                 const int* cand, int ncand, int nc, int nd, int n, void* const* dst) {
+__global__ void chol_cols_kernel(const double2* packed, const long long* boff, const int* info, const int* flip,
+                                 int nblocks, const int* cand, int ncand, int nc, int nd, int n, void* const* dst) {
     const int bi = blockIdx.x;
     if (bi >= nblocks) return;
     const int oa = info[5 * bi], ob = info[5 * bi + 1], na = info[5 * bi + 2], nb = info[5 * bi + 3];
     const bool same = info[5 * bi + 4] != 0;
+    const bool flipped = flip != nullptr && flip[bi] != 0;
     const double2* blk = packed + boff[bi];
     const int per = na * nb;
+    auto at = [&](int i, int j, int c, int d) -> double2 {
+        return flipped ? blk[(((long long)c * nd + d) * na + i) * nb + j]
+                       : blk[(((long long)i * nb + j) * nc + c) * nd + d];
+    };
     for (int e = threadIdx.x; e < per * ncand; e += blockDim.x) {
         const int k = e / per, r = e - k * per;
         const int i = r / nb, j = r - i * nb;
         const int c = cand[2 * k], d = cand[2 * k + 1];
-        const double2 v = blk[(((long long)i * nb + j) * nc + c) * nd + d];
+        const double2 v = at(i, j, c, d);
         const long long mu = oa + i, nu = ob + j;
         if (REAL) {
             double s = v.x;
-            if (same) s = (s + blk[(((long long)j * nb + i) * nc + c) * nd + d].x) * 0.5;
+            if (same) s = (s + at(j, i, c, d).x) * 0.5;
             double* out = static_cast<double*>(dst[k]);
             out[mu * n + nu] = s;
             if (!same) out[nu * n + mu] = s;
@@ -75,13 +83,16 @@ __global__ void chol_cols_kernel(const double2* packed, const long long* boff, c
     }
 }
 
-cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info, int nblocks,
-                             const int* cand, int ncand, int nc, int nd, int n, void* const* dst, cudaStream_t s) {
+cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info,
+                             const int* flip, int nblocks, const int* cand, int ncand, int nc, int nd, int n,
+                             void* const* dst, cudaStream_t s) {
     if (nblocks <= 0) return cudaSuccess;
     if (real)
-        chol_cols_kernel<true><<<nblocks, 256, 0, s>>>(packed, boff, info, nblocks, cand, ncand, nc, nd, n, dst);
+        chol_cols_kernel<true><<<nblocks, 256, 0, s>>>(packed, boff, info, flip, nblocks, cand, ncand, nc, nd, n,
+                                                       dst);
     else
-        chol_cols_kernel<false><<<nblocks, 256, 0, s>>>(packed, boff, info, nblocks, cand, ncand, nc, nd, n, dst);
+        chol_cols_kernel<false><<<nblocks, 256, 0, s>>>(packed, boff, info, flip, nblocks, cand, ncand, nc, nd, n,
+                                                        dst);
     return cudaGetLastError();
 }
 
@@ -422,10 +433,14 @@ __device__ __forceinline__ T chain_column(const T* col_in, const T* partials, in
 
 // The new factor row (the updated column times the pivot's scale; the real
 // path symmetrises (mu nu) with (nu mu)), the residual update and its
-// per-block argmax/minimum.
+// argmax/minimum.  Each block reduces its entries into partial[block]; the
+// last block to finish (counted in st->done) merges the partials in block
+// order, as a separate reduction kernel would, ends the step (rank, step
+// count) and, unless this is the chain's last step, selects the next pivot.
 template <typename T>
-__global__ void chain_update_kernel(const ChainState* st, const T* pool, const T* partials, int nchunks, int n, T* L,
-                                    double* res, Red* partial) {
+__global__ void chain_update_kernel(ChainState* st, const T* pool, const T* partials, int nchunks, int n, T* L,
+                                    double* res, Red* partial, Red* out, int* slot_of, long long* log, double tol,
+                                    double psd, int select_next) {
     if (!st->active) return;
     const long long N = (long long)n * n;
     const long long piv = st->pivot;
@@ -453,22 +468,25 @@ __global__ void chain_update_kernel(const ChainState* st, const T* pool, const T
         red_merge(r, Red{kept, j, nr});
     }
     r = block_reduce(r);
-    if (threadIdx.x == 0) partial[blockIdx.x] = r;
-}
-
-// End of a step: the residual's argmax and minimum, the rank count, and
-// (unless this is the chain's last step) the selection of the next pivot.
-__global__ void chain_final_kernel(ChainState* st, const Red* partial, int np, Red* out, int* slot_of, long long* log,
-                                   double tol, double psd, int select_next) {
-    if (!st->active) return;
-    Red r{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
-    for (int i = threadIdx.x; i < np; i += blockDim.x) red_merge(r, partial[i]);
-    r = block_reduce(r);
+    __shared__ int last;
     if (threadIdx.x == 0) {
-        *out = r;
+        partial[blockIdx.x] = r;
+        __threadfence();
+        last = atomicAdd(&st->done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    Red q{-1.0 / 0.0, (long long)1 << 62, 1.0 / 0.0};
+    const volatile Red* vp = partial;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) red_merge(q, Red{vp[i].maxv, vp[i].idx, vp[i].minv});
+    q = block_reduce(q);
+    if (threadIdx.x == 0) {
+        *out = q;
+        st->done = 0;
         st->rank += 1;
         st->steps += 1;
-        if (select_next) chain_select(st, r, slot_of, log, tol, psd);
+        if (select_next) chain_select(st, q, slot_of, log, tol, psd);
     }
 }
 
@@ -483,22 +501,35 @@ cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_h
     Red* red = static_cast<Red*>(out);
     if (steps > 0) chain_select_kernel<<<1, 1, 0, s>>>(st, red, slot_of, log, tol, psd);
     for (int k = 0; k < steps; ++k) {
+        const int select_next = k + 1 < steps ? 1 : 0;
         if (real) {
             chain_gemv_split_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(L), N, st, nchunks,
                                                                  static_cast<double*>(gemv_partials), N);
             chain_update_kernel<double><<<RED_BLOCKS, 256, 0, s>>>(
                 st, static_cast<const double*>(pool), static_cast<const double*>(gemv_partials), nchunks, n,
-                static_cast<double*>(L), res, static_cast<Red*>(partial));
+                static_cast<double*>(L), res, static_cast<Red*>(partial), red, slot_of, log, tol, psd, select_next);
         } else {
             chain_gemv_split_kernel<double2><<<grid, 128, 0, s>>>(static_cast<const double2*>(L), N, st, nchunks,
                                                                   static_cast<double2*>(gemv_partials), N);
             chain_update_kernel<double2><<<RED_BLOCKS, 256, 0, s>>>(
                 st, static_cast<const double2*>(pool), static_cast<const double2*>(gemv_partials), nchunks, n,
-                static_cast<double2*>(L), res, static_cast<Red*>(partial));
+                static_cast<double2*>(L), res, static_cast<Red*>(partial), red, slot_of, log, tol, psd, select_next);
         }
-        chain_final_kernel<<<1, 256, 0, s>>>(st, static_cast<const Red*>(partial), RED_BLOCKS, red, slot_of, log, tol,
-                                             psd, k + 1 < steps ? 1 : 0);
     }
+    return cudaGetLastError();
+}
+
+// Real factor rows widened to complex128 (imaginary parts zero), for the
+// copy to the caller.
+__global__ void widen_real_kernel(const double* __restrict__ src, double2* __restrict__ dst, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = make_double2(src[i], 0.0);
+}
+
+cudaError_t launch_widen_real(const double* src, double2* dst, long long n, int sms, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8LL * std::max(sms, 1)));
+    widen_real_kernel<<<grid, 256, 0, s>>>(src, dst, n);
     return cudaGetLastError();
 }
 

@@ -224,8 +224,10 @@ cudaError_t launch_small(int la, int lb, int lc, int ld, const EriDev& d, const 
 // Cholesky (gx_chol.cu)
 cudaError_t launch_chol_diag(const double2* packed, const long long* boff, const int* info, int nblocks, int n,
                              double* D, cudaStream_t s);
-cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info, int nblocks,
-                             const int* cand, int ncand, int nc, int nd, int n, void* const* dst, cudaStream_t s);
+// flip (may be null): per block, 1 when it was evaluated as (sb sa | a b)
+cudaError_t launch_chol_cols(bool real, const double2* packed, const long long* boff, const int* info,
+                             const int* flip, int nblocks, const int* cand, int ncand, int nc, int nd, int n,
+                             void* const* dst, cudaStream_t s);
 cudaError_t launch_chol_scan(const double* res, long long N, void* partial, void* out, cudaStream_t s);
 // gemv_partials (max_chunks x n^2 values, may be null): splits the factor
 // update over rank chunks when that gives more blocks; sms: SM count.
@@ -244,17 +246,20 @@ struct ChainState {
     int stop;         // why it stopped: 1 column not cached, 2 converged, 3 rank limit, 4 PSD check
     int rank_limit;   // rows the factor buffer (and the caller's limit) allows
     double scale;     // 1 / sqrt(residual) of the current pivot
+    unsigned int done;  // blocks of the current update that have finished (0 between steps)
 };
 // Enqueue `steps` chained pivot steps (each returns at once after the chain
 // stopped): pool holds the cached raw columns (slot_of[flat index] = slot,
-// -1 if absent), log receives the pivot of every step at its rank.  Three
-// launches per step: the rank-chunked GEMV, the row/residual update (which
-// sums the chunks and applies the scale chosen at selection) and the
-// reduction that also selects the next pivot.
+// -1 if absent), log receives the pivot of every step at its rank.  Two
+// launches per step: the rank-chunked GEMV, and the row/residual update,
+// which sums the chunks, applies the scale chosen at selection, and whose
+// last block reduces the residual and selects the next pivot.
 cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_hi, int steps, ChainState* st,
                               int* slot_of, long long* log, const void* pool, double* res, void* partial, void* out,
                               void* gemv_partials, int max_chunks, int sms, double tol, double psd, cudaStream_t s);
 size_t chol_red_bytes();
+// dst[i] = (src[i], 0) for i < n
+cudaError_t launch_widen_real(const double* src, double2* dst, long long n, int sms, cudaStream_t s);
 size_t chol_partial_bytes();
 
 // record a failure for gx_last_error() and return its code (gx_api.cu)
