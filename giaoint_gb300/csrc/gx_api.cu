@@ -185,6 +185,8 @@ struct SharedTables {
     double boys_table_agreement = 0.0;
 };
 
+struct ShapeGraph;  // a column-evaluation CUDA graph (see cholesky_core)
+
 // Page-locked host memory that grows on demand.
 struct PinnedHost {
     void* p = nullptr;
@@ -233,6 +235,12 @@ struct gx_context {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_done = nullptr;
     int copy_parts = 0;
+    // Cholesky column-evaluation graphs by plan shape and device view, kept
+    // across factorisations (cleared beyond kMaxShapeGraphs)
+    std::map<std::vector<long long>, std::shared_ptr<ShapeGraph>> shape_graphs;
+    // page-locked staging of the Cholesky host loop (chain state, reduction,
+    // status, chain log; the column-slot map), so its small copies never stall
+    PinnedHost chol_mail, chol_slots;
     double copy_first = 0.0;  // share of the output in the first range (0: equal ranges)
 
     PairClassHost& pair_class(int la, int lb) {
@@ -3179,6 +3187,54 @@ struct gx_cholesky_factors {
 
 namespace {
 
+// Column evaluations replayed as CUDA graphs.  Pivot shell pairs of the
+// same kind (angular momenta and primitive counts) give column plans of the
+// same shape: the same classes, task counts and work units, only the task
+// records differ.  One graph per shape and device view (the basis, pair
+// records, tables and output it reads) runs the class launches on task and
+// unit arrays of its own, which each evaluation refills from its plan (two
+// device copies) before the replay: one launch instead of one per class, and
+// no capture again for later factorisations of the same basis and field.
+}  // namespace
+
+struct ShapeGraph {
+    PlanData plan;  // the shape's classes and units over buffers of its own
+    DeviceBuffer counters;
+    cudaGraphExec_t exec = nullptr;
+    ~ShapeGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+namespace {
+
+constexpr size_t kMaxShapeGraphs = 256;
+
+// Key of a column plan's graph: its shape and every address its launches read.
+std::vector<long long> plan_shape(const PlanData& pd, const gx::EriDev& dev) {
+    auto p = [](const void* x) { return (long long)(uintptr_t)x; };
+    std::vector<long long> sig{(long long)pd.classes.size(), pd.ntask, (long long)pd.base.dev.bytes,
+                               dev.basis.ns, p(dev.basis.center), p(dev.basis.l), p(dev.basis.nprim),
+                               p(dev.basis.primoff), p(dev.basis.exps), p(dev.basis.coefs), p(dev.basis.raw),
+                               p(dev.basis.sp_off), dev.pairs.npp, p(dev.pairs.p), p(dev.pairs.Pr),
+                               p(dev.pairs.Pi), p(dev.pairs.F), p(dev.pairs.Eoff), p(dev.pairs.Epool),
+                               p(dev.pairs.bound), p(dev.pairs.Epool32), p(dev.pairs.order), p(dev.pairs.sbound),
+                               p(dev.pairs.g32), p(dev.boys.S), p(dev.boys.E0), p(dev.gl), p(dev.herm_xyz),
+                               p(dev.rec_plan), p(dev.rec_plan_off), p(dev.out), p(dev.status)};
+    uint32_t cuts[2];
+    std::memcpy(&cuts[0], &dev.skip_cut, 4);
+    std::memcpy(&cuts[1], &dev.fp32_cut, 4);
+    sig.push_back(cuts[0]);
+    sig.push_back(cuts[1]);
+    for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
+        const auto& pc = pd.classes[ci];
+        sig.insert(sig.end(), {pc.key[0], pc.key[1], pc.key[2], pc.key[3], (long long)pc.first, (long long)pc.count,
+                               (long long)pd.base.range[ci].first, (long long)pd.base.range[ci].second,
+                               (long long)pd.base.lane[ci].first, (long long)pd.base.lane[ci].second});
+    }
+    return sig;
+}
+
 // The pivot loop of python/giao_integrals/cholesky.py:60-297 on the device:
 // residual diagonal, argmax (lowest flat index on ties), column generation,
 // factor update and PSD check stay resident; the host sees one reduction
@@ -3309,12 +3365,24 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     GX_CUDA(cudaMemcpyAsync(d_res.ptr, d_D.ptr, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
     CholRed red;
     int status_code = 0;
+    // page-locked mailbox of the loop's small transfers (asynchronous both ways)
+    constexpr int kMailLog = 256;
+    struct Mail {
+        gx::ChainState cs_in, cs_out;
+        CholRed red;
+        int status, pad;
+        long long log[kMailLog];
+    };
+    ctx->chol_mail.reserve(sizeof(Mail));
+    Mail* mail = static_cast<Mail*>(ctx->chol_mail.p);
     auto fetch_red = [&] {
         // the reduction result and the kernels' status word in one wait (a
         // failure in a column batch is reported before the next pivot)
-        GX_CUDA(cudaMemcpyAsync(&red, d_red.ptr, sizeof red, cudaMemcpyDeviceToHost, st));
-        GX_CUDA(cudaMemcpyAsync(&status_code, ctx->status.ptr, sizeof status_code, cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaMemcpyAsync(&mail->red, d_red.ptr, sizeof(CholRed), cudaMemcpyDeviceToHost, st));
+        GX_CUDA(cudaMemcpyAsync(&mail->status, ctx->status.ptr, sizeof(int), cudaMemcpyDeviceToHost, st));
         GX_CUDA(cudaStreamSynchronize(st));
+        red = mail->red;
+        status_code = mail->status;
         collect_times();
         if (status_code) check_status(ctx);
     };
@@ -3368,6 +3436,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         d_slot_of.reserve(N * sizeof(int));
         d_state.reserve(sizeof(gx::ChainState));
         d_log.reserve(std::max<int64_t>(limit, 1) * sizeof(long long));
+        ctx->chol_slots.reserve(N * sizeof(int));
     }
     struct GraphSet {  // instantiated chain graphs, destroyed with the factorisation
         std::map<std::tuple<int, void*, int>, cudaGraphExec_t> m;
@@ -3404,34 +3473,11 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     };
     std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
     DeviceBuffer column_info;
-    // Column evaluations replayed as CUDA graphs.  Pivot shell pairs of the
-    // same kind (angular momenta and primitive counts) give column plans of
-    // the same shape: the same classes, task counts and work units, only the
-    // task records differ.  One graph per shape runs the class launches on
-    // task and unit arrays of its own, which each evaluation refills from its
-    // plan (two device copies) before the replay: one launch instead of one
-    // per class.
-    struct ShapeGraph {
-        PlanData plan;  // the shape's classes and units over buffers of its own
-        DeviceBuffer counters;
-        cudaGraphExec_t exec = nullptr;
-        ~ShapeGraph() {
-            if (exec) cudaGraphExecDestroy(exec);
-        }
-    };
-    std::map<std::vector<long long>, std::unique_ptr<ShapeGraph>> shape_graphs;
-    auto plan_shape = [](const PlanData& pd, const void* out, const void* pairs) {
-        std::vector<long long> sig{(long long)pd.classes.size(), pd.ntask, (long long)pd.base.dev.bytes,
-                                   (long long)(uintptr_t)out, (long long)(uintptr_t)pairs};
-        for (size_t ci = 0; ci < pd.classes.size(); ++ci) {
-            const auto& pc = pd.classes[ci];
-            sig.insert(sig.end(), {pc.key[0], pc.key[1], pc.key[2], pc.key[3], (long long)pc.first,
-                                   (long long)pc.count, (long long)pd.base.range[ci].first,
-                                   (long long)pd.base.range[ci].second, (long long)pd.base.lane[ci].first,
-                                   (long long)pd.base.lane[ci].second});
-        }
-        return sig;
-    };
+    // Column evaluations replayed as CUDA graphs (ShapeGraph), cached in the
+    // context across factorisations.
+    auto& shape_graphs = ctx->shape_graphs;
+    // counts of the evaluations replayed here, per shape (for the stats)
+    std::map<ShapeGraph*, std::vector<unsigned long long>> shape_base;
     {
         // largest column batch: all (x, y) blocks against the largest pivot pair
         int64_t sum_xy = 0, max_ao = 0;
@@ -3682,10 +3728,11 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                 const bool capturable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
                 const PlanData& pd = cps[0]->plan;
                 if (blocks.size() == 1 && capturable && pd.ntask > 0) {
-                    const auto key = plan_shape(pd, runs[0].second.out, runs[0].second.pairs.F);
+                    const auto key = plan_shape(pd, runs[0].second);
+                    if (shape_graphs.size() >= kMaxShapeGraphs && !shape_graphs.count(key)) shape_graphs.clear();
                     auto& sg = shape_graphs[key];
                     if (!sg) {
-                        sg = std::make_unique<ShapeGraph>();
+                        sg = std::make_shared<ShapeGraph>();
                         PlanData& sp = sg->plan;
                         sp.classes = pd.classes;
                         sp.defconf = pd.defconf;
@@ -3718,6 +3765,14 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                                             cudaMemcpyDeviceToDevice, st));
                     GX_CUDA(cudaMemcpyAsync(sg->plan.base.dev.ptr, pd.base.dev.ptr, pd.base.dev.bytes,
                                             cudaMemcpyDeviceToDevice, st));
+                    if (!shape_base.count(sg.get())) {
+                        // the counters accumulate across factorisations: note where this one starts
+                        std::vector<unsigned long long> c(2 * pd.classes.size());
+                        GX_CUDA(cudaMemcpyAsync(c.data(), sg->counters.ptr, c.size() * sizeof(unsigned long long),
+                                                cudaMemcpyDeviceToHost, st));
+                        GX_CUDA(cudaStreamSynchronize(st));
+                        shape_base.emplace(sg.get(), std::move(c));
+                    }
                     GX_CUDA(cudaGraphLaunch(sg->exec, st));
                 } else {
                     enqueue_plans(ctx, runs, GX_PRECISION_FP64, ctr);
@@ -3784,9 +3839,14 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         const bool chained = chain_ok && !lru.empty() && rank + 1 < std::min<int64_t>(limit, f.cap_rows);
         gx::ChainState cs_out{};
         std::vector<long long> chain_log;
+        int64_t nlog = 0;
         if (chained) {
             if (slot_dirty) {
-                GX_CUDA(cudaMemcpyAsync(d_slot_of.ptr, slot_of_h.data(), N * sizeof(int), cudaMemcpyHostToDevice, st));
+                // (the previous upload from the staging copy ended with the
+                // previous iteration's synchronisation)
+                std::memcpy(ctx->chol_slots.p, slot_of_h.data(), N * sizeof(int));
+                GX_CUDA(cudaMemcpyAsync(d_slot_of.ptr, ctx->chol_slots.p, N * sizeof(int), cudaMemcpyHostToDevice,
+                                        st));
                 slot_dirty = false;
             }
             gx::ChainState cs{};
@@ -3794,15 +3854,15 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             cs.rank = (int)rank + 1;
             cs.active = 1;
             cs.rank_limit = (int)std::min<int64_t>(limit, f.cap_rows);
-            GX_CUDA(cudaMemcpyAsync(d_state.ptr, &cs, sizeof cs, cudaMemcpyHostToDevice, st));
+            mail->cs_in = cs;
+            GX_CUDA(cudaMemcpyAsync(d_state.ptr, &mail->cs_in, sizeof cs, cudaMemcpyHostToDevice, st));
             // the chain's launches replayed as one CUDA graph per (length,
             // factor buffer, rank-chunk count): one launch instead of three per step
             const int rank_hi = (int)rank + 1 + chain_k;
             const int nblk = (int)((N + 127) / 128);
-            const int nchunks = rank_hi >= 64 ? std::max(1, std::min({kGemvChunks, (8 * ctx->sm_count) /
-                                                                                       std::max(nblk, 1),
-                                                                      (rank_hi + 31) / 32}))
-                                              : 1;
+            // (fixed once the rank reaches 64, so that few graphs are captured)
+            const int nchunks =
+                rank_hi >= 64 ? std::max(1, std::min(kGemvChunks, (8 * ctx->sm_count) / std::max(nblk, 1))) : 1;
             const auto gkey = std::make_tuple(chain_k, f.L.ptr, nchunks);
             // (the legacy default stream cannot be captured: launch directly there)
             const bool capturable = st != nullptr && st != cudaStreamLegacy && st != cudaStreamPerThread;
@@ -3830,11 +3890,10 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                 git = chain_graphs.emplace(gkey, exec).first;
             }
             if (capturable) GX_CUDA(cudaGraphLaunch(git->second, st));
-            GX_CUDA(cudaMemcpyAsync(&cs_out, d_state.ptr, sizeof cs_out, cudaMemcpyDeviceToHost, st));
+            GX_CUDA(cudaMemcpyAsync(&mail->cs_out, d_state.ptr, sizeof cs_out, cudaMemcpyDeviceToHost, st));
             // the log holds `limit` entries; the chain writes at most up to rank_limit <= limit
-            const int64_t nlog = std::min<int64_t>(chain_k, limit - (rank + 1));
-            chain_log.resize(nlog);
-            GX_CUDA(cudaMemcpyAsync(chain_log.data(), d_log.as<long long>() + rank + 1, nlog * sizeof(long long),
+            nlog = std::min<int64_t>(std::min<int64_t>(chain_k, kMailLog), limit - (rank + 1));
+            GX_CUDA(cudaMemcpyAsync(mail->log, d_log.as<long long>() + rank + 1, nlog * sizeof(long long),
                                     cudaMemcpyDeviceToHost, st));
         }
         GX_CUDA(cudaEventRecord(ev_upd.b, st));
@@ -3844,6 +3903,10 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         stats.update_bytes += (double)col_bytes * (rank + 2) + 16.0 * N;
         stats.update_flops += (real ? 2.0 : 8.0) * (double)rank * N;
         fetch_red();
+        if (chained) {
+            cs_out = mail->cs_out;
+            chain_log.assign(mail->log, mail->log + nlog);
+        }
         f.pivots.push_back(pivot / n);
         f.pivots.push_back(pivot % n);
         ++rank;
@@ -3884,19 +3947,20 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     }
     // primitive quartets of the column evaluations and their FP64 FLOP model
     // (counted per plan when launched directly, per shape when replayed)
-    auto add_counts = [&](const PlanData& pd, const DeviceBuffer& counters) {
+    auto add_counts = [&](const PlanData& pd, const DeviceBuffer& counters, const std::vector<unsigned long long>* base) {
         std::vector<unsigned long long> c(2 * pd.classes.size());
         if (c.empty()) return;
         GX_CUDA(cudaMemcpyAsync(c.data(), counters.ptr, c.size() * sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, st));
         GX_CUDA(cudaStreamSynchronize(st));
         for (size_t i = 0; i < pd.classes.size(); ++i) {
-            stats.column_primitive_quartets += (int64_t)c[2 * i];
-            stats.column_model_flops += (double)c[2 * i] * pd.classes[i].flops_per_primitive_quartet;
+            const unsigned long long v = c[2 * i] - (base ? (*base)[2 * i] : 0ull);
+            stats.column_primitive_quartets += (int64_t)v;
+            stats.column_model_flops += (double)v * pd.classes[i].flops_per_primitive_quartet;
         }
     };
-    for (const auto& kv : column_plans) add_counts(kv.second->plan, kv.second->counters);
-    for (const auto& kv : shape_graphs) add_counts(kv.second->plan, kv.second->counters);
+    for (const auto& kv : column_plans) add_counts(kv.second->plan, kv.second->counters, nullptr);
+    for (const auto& kv : shape_base) add_counts(kv.first->plan, kv.first->counters, &kv.second);
     f.rank = rank;
     f.max_residual = final_max;
     stats.rank = rank;

@@ -496,7 +496,7 @@ cudaError_t launch_chol_chain(bool real, void* L, long long N, int n, int rank_h
     const int blocks = (int)((N + 127) / 128);
     int nchunks = 1;
     if (gemv_partials && max_chunks > 1 && rank_hi >= 64 && sms > 0)
-        nchunks = std::max(1, std::min({max_chunks, (8 * sms) / std::max(blocks, 1), (rank_hi + 31) / 32}));
+        nchunks = std::max(1, std::min(max_chunks, (8 * sms) / std::max(blocks, 1)));
     const dim3 grid(blocks, nchunks);
     Red* red = static_cast<Red*>(out);
     if (steps > 0) chain_select_kernel<<<1, 1, 0, s>>>(st, red, slot_of, log, tol, psd);
