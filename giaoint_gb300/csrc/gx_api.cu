@@ -1426,12 +1426,21 @@ std::unique_ptr<gx_basis> new_basis(gx_context* ctx, int nshell, const double* c
 // (increasing output offsets) on a miss.
 template <class Make>
 CachedPlan& lookup_parts(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, int64_t count, int64_t entries,
-                         int nparts, Make&& make, double first_share = 0.0) {
+                         int nparts, Make&& make, double first_share = 0.0, CachedPlan* transient = nullptr) {
     auto& cache = plan_cache(ctx);
     auto hit = std::find_if(cache.begin(), cache.end(), [&](const CachedPlan& c) {
         return c.basis == b && c.h1 == h1 && c.h2 == h2 && c.count == count && c.entries == entries &&
                c.nparts == nparts && c.first_share == first_share;
     });
+    if (hit == cache.end() && transient) {
+        // built for this call only (the cache keeps the lists that recur)
+        const std::vector<QuartetRequest> req = make();
+        *transient = CachedPlan{b, h1, h2, count, entries, 1, 0.0, {}, {}};
+        transient->parts.push_back(std::make_unique<PlanData>());
+        build_plan(ctx, b, req, *transient->parts[0]);
+        transient->part_end.push_back(entries);
+        return *transient;
+    }
     if (hit == cache.end()) {
         const std::vector<QuartetRequest> req = make();
         CachedPlan c{b, h1, h2, count, entries, nparts, first_share, {}, {}};
@@ -1495,7 +1504,8 @@ constexpr double kAutoFirstShare = 0.7;
 
 int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* O, const uint32_t* quartets,
                    int64_t nq, int precision, double mixed_cutoff, double screening, uint32_t* kept,
-                   int64_t* offsets, void* out, bool out_is_device, int64_t capacity, gx_eri_stats* stats) {
+                   int64_t* offsets, void* out, bool out_is_device, int64_t capacity, gx_eri_stats* stats,
+                   bool cache_plan = true) {
     return guarded([&] {
         if (precision != GX_PRECISION_FP64 && precision != GX_PRECISION_MIXED && precision != GX_PRECISION_FP64_EXACT)
             raise(GX_EINVAL, "precision must be GX_PRECISION_FP64, GX_PRECISION_MIXED or GX_PRECISION_FP64_EXACT");
@@ -1602,6 +1612,7 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                     (void)cudaGetLastError();
                 }
             }
+            CachedPlan transient;  // the plan of a call that does not cache it
             CachedPlan& cp = lookup_parts(ctx, b, h1, h2, count, off, nparts, [&] {
                 pass2();
                 std::vector<QuartetRequest> req((size_t)count);
@@ -1616,7 +1627,8 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                     }
                 }
                 return req;
-            }, nparts == 1 ? 0.0 : (ctx->copy_parts == 0 ? kAutoFirstShare : ctx->copy_first));
+            }, nparts == 1 ? 0.0 : (ctx->copy_parts == 0 ? kAutoFirstShare : ctx->copy_first),
+            cache_plan ? nullptr : &transient);
             const size_t np = cp.parts.size();
             cudaStream_t s = ctx->stream;
             std::vector<unsigned long long*> counters(np, nullptr);
@@ -2653,9 +2665,10 @@ int gx_eri_for_each(gx_context* ctx, gx_basis* b, const double* B, const double*
             const int64_t cnt = first[k + 1] - first[k];
             c.offsets.assign((size_t)cnt + 1, 0);
             c.st = gx_eri_stats{};
+            // (the chunks of a long list do not displace the cached plans of other calls)
             c.rc = eri_batch_impl(ctx, b, B, O, q + 4 * first[k], cnt, precision, mixed_cutoff, 0.0, nullptr,
                                   c.offsets.data(), ctx->stream_host[slot].p, false,
-                                  (int64_t)(ctx->stream_host[slot].n / sizeof(double2)), &c.st);
+                                  (int64_t)(ctx->stream_host[slot].n / sizeof(double2)), &c.st, nchunk <= 2);
             if (c.rc) c.msg = g_error;
         };
         gx_eri_stats total{};
