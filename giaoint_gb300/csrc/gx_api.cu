@@ -3489,8 +3489,9 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     // Column evaluations replayed as CUDA graphs (ShapeGraph), cached in the
     // context across factorisations.
     auto& shape_graphs = ctx->shape_graphs;
-    // counts of the evaluations replayed here, per shape (for the stats)
-    std::map<ShapeGraph*, std::vector<unsigned long long>> shape_base;
+    // the graphs this factorisation replayed (held, so that clearing the
+    // context's cache cannot free them) and their counters when it began
+    std::map<ShapeGraph*, std::pair<std::shared_ptr<ShapeGraph>, std::vector<unsigned long long>>> shape_base;
     {
         // largest column batch: all (x, y) blocks against the largest pivot pair
         int64_t sum_xy = 0, max_ao = 0;
@@ -3674,14 +3675,20 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                     std::vector<int> flip;
                     int64_t off = 0;
                     // (x y | sb sa), or (sb sa | x y) when (x, y) has the
-                    // higher angular momentum: the kernels spread the ket
-                    // components of a shell quartet over warps, so the wide
-                    // pair goes to the ket (a low-L pivot against high-L bra
-                    // pairs otherwise leaves a few warps on the long tasks)
+                    // higher angular momentum and at least as many primitive
+                    // pairs: the kernels spread the ket components of a shell
+                    // quartet over warps, so the wide pair goes to the ket (a
+                    // low-L pivot against high-L bra pairs otherwise leaves a
+                    // few warps on the long tasks), but they contract each
+                    // bra primitive pair once over all its ket primitive
+                    // pairs, so a contracted pivot pair stays in the ket (on
+                    // the 12-atom molecule, flipping against contracted s
+                    // pivots made the column evaluations 18% slower)
                     const int lpiv = b->l[sa] + b->l[sb];
+                    const int kpiv = b->nprim[sa] * b->nprim[sb];
                     for (int x = 0; x < ns; ++x)
                         for (int y = real ? x : 0; y < ns; ++y) {
-                            const bool fl = b->l[x] + b->l[y] > lpiv;
+                            const bool fl = b->l[x] + b->l[y] > lpiv && b->nprim[x] * b->nprim[y] >= kpiv;
                             if (fl)
                                 req.push_back({(uint32_t)sb, (uint32_t)sa, (uint32_t)x, (uint32_t)y, off});
                             else
@@ -3784,7 +3791,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                         GX_CUDA(cudaMemcpyAsync(c.data(), sg->counters.ptr, c.size() * sizeof(unsigned long long),
                                                 cudaMemcpyDeviceToHost, st));
                         GX_CUDA(cudaStreamSynchronize(st));
-                        shape_base.emplace(sg.get(), std::move(c));
+                        shape_base.emplace(sg.get(), std::make_pair(sg, std::move(c)));
                     }
                     GX_CUDA(cudaGraphLaunch(sg->exec, st));
                 } else {
@@ -3973,7 +3980,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
         }
     };
     for (const auto& kv : column_plans) add_counts(kv.second->plan, kv.second->counters, nullptr);
-    for (const auto& kv : shape_base) add_counts(kv.first->plan, kv.first->counters, &kv.second);
+    for (const auto& kv : shape_base) add_counts(kv.first->plan, kv.first->counters, &kv.second.second);
     f.rank = rank;
     f.max_residual = final_max;
     stats.rank = rank;
