@@ -186,6 +186,7 @@ struct SharedTables {
 };
 
 struct ShapeGraph;  // a column-evaluation CUDA graph (see cholesky_core)
+struct ColumnPlan;  // the column-evaluation plan of one pivot shell pair (see cholesky_core)
 
 // Page-locked host memory that grows on demand.
 struct PinnedHost {
@@ -241,6 +242,11 @@ struct gx_context {
     // page-locked staging of the Cholesky host loop (chain state, reduction,
     // status, chain log; the column-slot map), so its small copies never stall
     PinnedHost chol_mail, chol_slots;
+    // Cholesky column plans by (basis, pivot shell pair, real path), kept
+    // across factorisations of the same basis (fields change only the pair
+    // records); dropped with the basis, cleared beyond kMaxColumnPlanBytes
+    std::map<std::tuple<const gx_basis*, int, int, bool>, std::shared_ptr<ColumnPlan>> column_plans;
+    size_t column_plan_bytes = 0;
     double copy_first = 0.0;  // share of the output in the first range (0: equal ranges)
 
     PairClassHost& pair_class(int la, int lb) {
@@ -1887,6 +1893,8 @@ int gx_context_set_stable_launch(gx_context* ctx, int stable) {
         std::lock_guard<std::mutex> lock(ctx->mu);
         ctx->stable_launch = stable != 0;
         drop_cached_plans(ctx, nullptr);  // cached plans were built under the other setting
+        ctx->column_plans.clear();
+        ctx->column_plan_bytes = 0;
     });
 }
 
@@ -2548,6 +2556,11 @@ void gx_basis_destroy(gx_basis* b) {
         if (owned[i]->bound) owned.push_back(owned[i]->bound.get());
     }
     for (const gx_basis* o : owned) drop_cached_plans(b->ctx, o);
+    // (its Cholesky column plans go too; the byte count is a soft cap and is
+    // only reset when no plan is left)
+    for (auto it = b->ctx->column_plans.begin(); it != b->ctx->column_plans.end();)
+        it = std::get<0>(it->first) == b ? b->ctx->column_plans.erase(it) : std::next(it);
+    if (b->ctx->column_plans.empty()) b->ctx->column_plan_bytes = 0;
     delete b;
 }
 
@@ -3219,9 +3232,20 @@ struct ShapeGraph {
     }
 };
 
+// Column evaluation of one pivot shell pair: its plan, block offsets and
+// orientations, and primitive-quartet counters (accumulated over its
+// evaluations when launched directly).
+struct ColumnPlan {
+    PlanData plan;
+    DeviceBuffer boff, flip, counters;
+    int nblocks = 0;
+    int64_t entries = 0;
+};
+
 namespace {
 
 constexpr size_t kMaxShapeGraphs = 256;
+constexpr size_t kMaxColumnPlanBytes = size_t(1) << 30;
 
 // Key of a column plan's graph: its shape and every address its launches read.
 std::vector<long long> plan_shape(const PlanData& pd, const gx::EriDev& dev) {
@@ -3476,15 +3500,9 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
     std::vector<int64_t> ref_cands, block_cands;
     KeyOrder ref_cache;
     std::vector<double> hostblk;
-    // Column evaluation of one pivot shell pair: its plan, block offsets and
-    // primitive-quartet counters (accumulated over its evaluations).
-    struct ColumnPlan {
-        PlanData plan;
-        DeviceBuffer boff, flip, counters;
-        int nblocks = 0;
-        int64_t entries = 0;
-    };
-    std::map<std::pair<int, int>, std::unique_ptr<ColumnPlan>> column_plans;
+    // the context's column plans this factorisation used (held) and their
+    // counters when it began
+    std::map<ColumnPlan*, std::pair<std::shared_ptr<ColumnPlan>, std::vector<unsigned long long>>> plan_base;
     DeviceBuffer column_info;
     // Column evaluations replayed as CUDA graphs (ShapeGraph), cached in the
     // context across factorisations.
@@ -3667,9 +3685,14 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             int64_t stot = 0;
             for (const auto& bl : blocks) {
                 const int sa = bl.sa, sb = bl.sb;
-                auto& cp = column_plans[{sa, sb}];
+                const auto pkey = std::make_tuple(static_cast<const gx_basis*>(b), sa, sb, real);
+                if (ctx->column_plan_bytes > kMaxColumnPlanBytes && !ctx->column_plans.count(pkey)) {
+                    ctx->column_plans.clear();  // (the plans in use here are held by plan_base)
+                    ctx->column_plan_bytes = 0;
+                }
+                auto& cp = ctx->column_plans[pkey];
                 if (!cp) {
-                    cp = std::make_unique<ColumnPlan>();
+                    cp = std::make_shared<ColumnPlan>();
                     std::vector<QuartetRequest> req;
                     std::vector<long long> boff;
                     std::vector<int> flip;
@@ -3705,6 +3728,16 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
                     cp->counters.reserve(std::max<size_t>(2 * cp->plan.classes.size(), 2) *
                                          sizeof(unsigned long long));
                     GX_CUDA(cudaMemsetAsync(cp->counters.ptr, 0, cp->counters.bytes, st));
+                    ctx->column_plan_bytes += cp->plan.tasks.bytes + cp->plan.base.dev.bytes + cp->boff.bytes;
+                }
+                if (!plan_base.count(cp.get())) {
+                    std::vector<unsigned long long> c(2 * cp->plan.classes.size());
+                    if (!c.empty()) {
+                        GX_CUDA(cudaMemcpyAsync(c.data(), cp->counters.ptr, c.size() * sizeof(unsigned long long),
+                                                cudaMemcpyDeviceToHost, st));
+                        GX_CUDA(cudaStreamSynchronize(st));
+                    }
+                    plan_base.emplace(cp.get(), std::make_pair(cp, std::move(c)));
                 }
                 cps.push_back(cp.get());
                 sbase.push_back(stot);
@@ -3979,7 +4012,7 @@ void cholesky_core(gx_context* ctx, gx_basis* b, const double* Bf, const double*
             stats.column_model_flops += (double)v * pd.classes[i].flops_per_primitive_quartet;
         }
     };
-    for (const auto& kv : column_plans) add_counts(kv.second->plan, kv.second->counters, nullptr);
+    for (const auto& kv : plan_base) add_counts(kv.first->plan, kv.first->counters, &kv.second.second);
     for (const auto& kv : shape_base) add_counts(kv.first->plan, kv.first->counters, &kv.second.second);
     f.rank = rank;
     f.max_residual = final_max;
