@@ -551,8 +551,11 @@ struct WarpSmem {
 // Per-warp shared layout.  Batched mode: R columns of all B1 entries
 // (stride B1 + 1) and one seed area; stream mode: a two-column R buffer and
 // the seeds and X' of every batch entry (L + 4 slots each).
+// stage32: the E~ staging also holds the FP32 copy of a record (mixed
+// precision when this kernel takes FP32 entries; otherwise only the FP64
+// record is staged and the FP32 half is not allocated)
 __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, bool mixed, int stage_e, int stream,
-                                              int L) {
+                                              int L, bool stage32) {
     WarpSmem w;
     const size_t B1p = B1 + 1;
     w.R = 0;
@@ -564,7 +567,7 @@ __host__ __device__ inline WarpSmem warp_smem(int NL, int B1, int Nab, int CH, b
     w.seed = w.eoff + (((size_t)B1 * 8 + 15) / 16) * 16;
     w.stage = w.seed + (stream ? (size_t)B1 * (L + 4) : (size_t)(BOYS_MAX_ORDER + 1 + 3)) * 16;
     // FP64 record (16 B per word) followed by its FP32 copy (8 B per word)
-    w.total = w.stage + (((size_t)stage_e * 24 + 15) / 16) * 16;
+    w.total = w.stage + (((size_t)stage_e * (stage32 ? 24 : 16) + 15) / 16) * 16;
     return w;
 }
 
@@ -984,7 +987,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
     // with the FP32 lane kernel in charge of the FP32 entries, this kernel
     // takes only the entries at or above the FP32 cutoff
     const float skip64 = qc.no32 ? fmaxf(skip, cut32) : skip;
-    const WarpSmem lay = warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e, qc.stream, qc.L);
+    const WarpSmem lay =
+        warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, cut32 > 0.0f, qc.stage_e, qc.stream, qc.L, cut32 > 0.0f && !qc.no32);
     const size_t tab_bytes = (((size_t)qc.tab_words * 4 + 15) / 16) * 16;
     char* base = reinterpret_cast<char*>(sm) + tab_bytes + (size_t)wib * lay.total;
     double2* R = reinterpret_cast<double2*>(base + lay.R);
@@ -1253,7 +1257,8 @@ __global__ void __launch_bounds__(128, MINB) quartet_kernel(EriDev d, QuartetCla
 
 size_t quartet_smem_bytes(const QuartetClass& qc, int warps_per_block, bool mixed) {
     return (((size_t)qc.tab_words * 4 + 15) / 16) * 16 +
-           (size_t)warps_per_block * warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed, qc.stage_e, qc.stream, qc.L).total;
+           (size_t)warps_per_block *
+               warp_smem(qc.NL, qc.B1, qc.Nab, qc.CH, mixed, qc.stage_e, qc.stream, qc.L, mixed && !qc.no32).total;
 }
 
 static bool g_const_ready = false;
