@@ -236,6 +236,11 @@ struct gx_context {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_done = nullptr;
     int copy_parts = 0;
+    // per-class host copies: streams that trail the class streams (so a copy
+    // never holds back the next class on its stream) and their join events
+    std::vector<cudaStream_t> class_copy;
+    std::vector<cudaEvent_t> class_copy_done;
+    cudaEvent_t class_done = nullptr;
     // Cholesky column-evaluation graphs by plan shape and device view, kept
     // across factorisations (cleared beyond kMaxShapeGraphs)
     std::map<std::vector<long long>, std::shared_ptr<ShapeGraph>> shape_graphs;
@@ -1132,21 +1137,52 @@ void launch_class(gx_context* ctx, gx::EriDev dev, const PlanData& plan, size_t 
 // the autotuned configuration of the precision mode when there is one.
 // counters: 2 per class (FP64, FP32 primitive quartets evaluated) or null;
 // zeroed first unless `accumulate`.
+// host_mapped (may be null): page-locked host output, its mapped address;
+// each class's blocks are copied there by the SMs right after the class.
 int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, int precision,
-                 unsigned long long* counters, bool accumulate);
+                 unsigned long long* counters, bool accumulate, void* host_mapped = nullptr);
 
 int execute_plan(gx_context* ctx, gx_basis* b, const double* B, const double* O, const PlanData& plan,
                  double2* out, int precision = GX_PRECISION_FP64, double mixed_cutoff = 0.0,
-                 unsigned long long* counters = nullptr, bool accumulate = false) {
+                 unsigned long long* counters = nullptr, bool accumulate = false, void* host_mapped = nullptr) {
     FieldPairs& fp = field_pairs(b, B, O);
     const gx::EriDev dev = make_dev(ctx, b, fp, out, precision, mixed_cutoff);
-    return enqueue_plan(ctx, dev, plan, precision, counters, accumulate);
+    return enqueue_plan(ctx, dev, plan, precision, counters, accumulate, host_mapped);
 }
 
 // Enqueue every class launch of `plan` for the evaluation view `dev`.
 int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, int precision,
-                 unsigned long long* counters, bool accumulate) {
+                 unsigned long long* counters, bool accumulate, void* host_mapped) {
     cudaStream_t s = ctx->stream;
+    // host copies on streams of their own, each waiting for its class (a
+    // waited event stands for its latest record, so one event serves all)
+    constexpr int kCopyStreams = 8;
+    if (host_mapped && ctx->class_copy.empty()) {
+        ctx->class_copy.resize(kCopyStreams);
+        ctx->class_copy_done.resize(kCopyStreams);
+        for (int k = 0; k < kCopyStreams; ++k) {
+            GX_CUDA(cudaStreamCreateWithFlags(&ctx->class_copy[k], cudaStreamNonBlocking));
+            GX_CUDA(cudaEventCreateWithFlags(&ctx->class_copy_done[k], cudaEventDisableTiming));
+        }
+        GX_CUDA(cudaEventCreateWithFlags(&ctx->class_done, cudaEventDisableTiming));
+    }
+    int ncopies = 0;
+    auto copy_class = [&](size_t ci, cudaStream_t cs) {
+        if (!host_mapped) return;
+        const PlanClass& pc = plan.classes[ci];
+        cudaStream_t cp = ctx->class_copy[ncopies++ % kCopyStreams];
+        GX_CUDA(cudaEventRecord(ctx->class_done, cs));
+        GX_CUDA(cudaStreamWaitEvent(cp, ctx->class_done, 0));
+        GX_CUDA(gx::launch_class_copy(plan.tasks.as<gx::Task>() + pc.first, (int)pc.count, pc.key[0], pc.key[1],
+                                      pc.key[2], pc.key[3], dev.out, host_mapped, ctx->sm_count, cp));
+    };
+    auto join_copies = [&] {
+        if (!host_mapped) return;
+        for (int k = 0; k < std::min(ncopies, kCopyStreams); ++k) {
+            GX_CUDA(cudaEventRecord(ctx->class_copy_done[k], ctx->class_copy[k]));
+            GX_CUDA(cudaStreamWaitEvent(s, ctx->class_copy_done[k], 0));
+        }
+    };
     if (counters && !accumulate) GX_CUDA(cudaMemsetAsync(counters, 0, 2 * plan.classes.size() * sizeof(unsigned long long), s));
     ctx->reset_status();
     const auto& tuned = plan.tuned[precision];
@@ -1177,16 +1213,21 @@ int enqueue_plan(gx_context* ctx, const gx::EriDev& dev, const PlanData& plan, i
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters,
                          ctx->aux[oi % K], nullptr, nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first,
                          (int)gs.lane[ci].second);
+            copy_class(ci, ctx->aux[oi % K]);
         }
         for (int k = 0; k < K; ++k) {
             GX_CUDA(cudaEventRecord(ctx->aux_done[k], ctx->aux[k]));
             GX_CUDA(cudaStreamWaitEvent(s, ctx->aux_done[k], 0));
         }
+        join_copies();
     } else {
-        for (size_t ci = 0; ci < nc; ++ci)
+        for (size_t ci = 0; ci < nc; ++ci) {
             launch_class(ctx, dev, plan, ci, tuned.valid ? tuned.conf[ci] : plan.defconf[ci],
                          gs.dev.as<int2>() + gs.range[ci].first, (int)gs.range[ci].second, counters, s, nullptr,
                          nullptr, nullptr, gs.dev.as<int2>() + gs.lane[ci].first, (int)gs.lane[ci].second);
+            copy_class(ci, s);
+        }
+        join_copies();
     }
     return 1 + (int)nc;
 }
@@ -1612,12 +1653,15 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
                 if (cudaPointerGetAttributes(&attr, out) == cudaSuccess && attr.type == cudaMemoryTypeHost) {
                     if (attr.devicePointer && !(reinterpret_cast<uintptr_t>(attr.devicePointer) & 15))
                         mapped = attr.devicePointer;
-                    if (ctx->copy_parts > 1 || (ctx->copy_parts == 0 && off >= kOverlapEntries))
+                    if (ctx->copy_parts > 1 || (ctx->copy_parts == 0 && !mapped && off >= kOverlapEntries))
                         nparts = ctx->copy_parts > 0 ? ctx->copy_parts : kAutoCopyParts;
                 } else {
                     (void)cudaGetLastError();
                 }
             }
+            // the default with a mapped output: every class's blocks copied
+            // right after the class, overlapping the other classes
+            const bool class_copies = mapped && ctx->copy_parts == 0;
             CachedPlan transient;  // the plan of a call that does not cache it
             CachedPlan& cp = lookup_parts(ctx, b, h1, h2, count, off, nparts, [&] {
                 pass2();
@@ -1661,12 +1705,16 @@ int eri_batch_impl(gx_context* ctx, gx_basis* b, const double* B, const double* 
             prepare_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             GX_CUDA(cudaEventRecord(ev.a, s));
             if (np == 1) {
-                execute_plan(ctx, b, B, O, *cp.parts[0], dout, precision, mixed_cutoff, counters[0]);
+                execute_plan(ctx, b, B, O, *cp.parts[0], dout, precision, mixed_cutoff, counters[0], false,
+                             class_copies ? mapped : nullptr);
                 GX_CUDA(cudaEventRecord(ev.b, s));
-                if (mapped)
+                if (class_copies) {
+                    // (copied with the classes)
+                } else if (mapped) {
                     GX_CUDA(gx::launch_host_copy(mapped, dout, off * (int64_t)sizeof(double2), kHostCopyBlocks, s));
-                else if (!out_is_device && off)
+                } else if (!out_is_device && off) {
                     GX_CUDA(cudaMemcpyAsync(out, dout, off * sizeof(double2), cudaMemcpyDeviceToHost, s));
+                }
             } else {
                 FieldPairs& fp = field_pairs(b, B, O);
                 const gx::EriDev dev = make_dev(ctx, b, fp, dout, precision, mixed_cutoff);
@@ -2528,6 +2576,9 @@ void gx_context_destroy(gx_context* ctx) {
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->copy_done) cudaEventDestroy(ctx->copy_done);
+    for (auto st : ctx->class_copy) cudaStreamDestroy(st);
+    for (auto ev : ctx->class_copy_done) cudaEventDestroy(ev);
+    if (ctx->class_done) cudaEventDestroy(ctx->class_done);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }

@@ -137,6 +137,11 @@ cudaError_t launch_offset_copy(long long* dst, const long long* src, long long n
 // to page-locked host memory through its mapped device address, by at most
 // `blocks` blocks of 512 threads
 cudaError_t launch_host_copy(void* dst_mapped, const void* src, long long bytes, int blocks, cudaStream_t s);
+// the entries of the `ntask` tasks of class (la, lb, lc, ld) from the packed
+// device output `src` to page-locked host memory (mapped address, 16-byte
+// aligned) at the same offsets
+cudaError_t launch_class_copy(const Task* tasks, int ntask, int la, int lb, int lc, int ld, const double2* src,
+                              void* dst_mapped, int sms, cudaStream_t s);
 cudaError_t launch_scatter_full(const double2* packed, const long long* block_off, const int* block_info, int nblocks,
                                 long long n, double2* full, cudaStream_t s);
 

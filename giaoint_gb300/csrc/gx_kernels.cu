@@ -1395,6 +1395,44 @@ cudaError_t launch_host_copy(void* dst_mapped, const void* src, long long bytes,
     return cudaGetLastError();
 }
 
+// The blocks of one class copied to page-locked host memory by the SMs
+// right after the class's kernels, on their stream: one warp per task, its
+// entries (ca, cb, cc, cd) at out_off + ca st0 + cb st1 + cc st2 + cd st3
+// (the entries the class kernels wrote), so the copy of the whole output
+// overlaps the evaluation of the other classes.
+__global__ void class_copy_kernel(const Task* __restrict__ tasks, int ntask, int na, int nb, int nc, int nd,
+                                  const double2* __restrict__ src, double2* __restrict__ dst) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * (size_t)blockDim.x) >> 5);
+    const int ncd = nc * nd;
+    const int per = na * nb * ncd;
+    for (int t = warp; t < ntask; t += nwarps) {
+        const Task tk = tasks[t];
+        for (int e = lane; e < per; e += 32) {
+            const int ab = e / ncd, cd = e - ab * ncd;
+            const int ca = ab / nb, cb = ab - ca * nb, cc = cd / nd, cdd = cd - cc * nd;
+            const long long o = tk.out_off + (long long)ca * tk.st[0] + (long long)cb * tk.st[1] +
+                                (long long)cc * tk.st[2] + (long long)cdd * tk.st[3];
+            dst[o] = __ldcs(src + o);
+        }
+    }
+}
+
+cudaError_t launch_class_copy(const Task* tasks, int ntask, int la, int lb, int lc, int ld, const double2* src,
+                              void* dst_mapped, int sms, cudaStream_t s) {
+    if (ntask <= 0) return cudaSuccess;
+    if (reinterpret_cast<uintptr_t>(dst_mapped) & 15) return cudaErrorInvalidValue;
+    // a few blocks per class: the copies trail the evaluation on streams of
+    // their own and are bound by the host link, so they should take few SMs
+    // from the classes still running
+    const int warps = 8;
+    const int grid = (int)std::max(1, std::min((ntask + warps - 1) / warps, std::max(sms, 1) / 8));
+    class_copy_kernel<<<grid, 32 * warps, 0, s>>>(tasks, ntask, ncart(la), ncart(lb), ncart(lc), ncart(ld), src,
+                                                  static_cast<double2*>(dst_mapped));
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // FMA throughput probes (FP64 and FP32): 8 independent dependent-FMA chains
 // per thread, 8 resident blocks of 256 threads per SM.

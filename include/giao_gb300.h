@@ -62,7 +62,9 @@ typedef struct gx_eri_stats {
     double kernel_ms;   /* device time of the quartet kernels                  */
     double prepare_ms;  /* host time from entry to the first launch (hashing,
                            screening, plan lookup or build)                     */
-    double copy_ms;     /* device time of the output copy to host memory       */
+    double copy_ms;     /* device time of the output copy to host memory after
+                           the quartet kernels (copies made while the classes
+                           run are in kernel_ms)                                */
     double call_ms;     /* wall time of the call                               */
 } gx_eri_stats;
 
@@ -376,13 +378,14 @@ int gx_eri_batch_packed(gx_context* ctx, int nreq, gx_basis* const* bases, const
  * requests). */
 int gx_context_set_stable_launch(gx_context* ctx, int stable);
 
-/* Host-output gx_eri_batch calls into page-locked memory run as `parts`
- * contiguous input ranges, the copy of each range to the host overlapping
- * the evaluation of the later ones (1: no overlap).  first_share in [0, 1):
- * the first range's share of the output elements (0: equal ranges); the
- * other ranges share the rest equally.  parts = 0, the default: two ranges,
- * the first with 0.7 of the output, for outputs of at least 2^26 complex
- * elements; one below. */
+/* How host-output gx_eri_batch calls copy the blocks to page-locked host
+ * memory.  parts = 0, the default: the SMs copy each class's blocks right
+ * after the class's kernels, through the buffer's mapped address, so the
+ * copy overlaps the evaluation of the other classes.  parts = 1: one copy
+ * after the whole evaluation.  parts >= 2: `parts` contiguous input ranges,
+ * the copy of each range overlapping the evaluation of the later ones;
+ * first_share in [0, 1) is the first range's share of the output elements
+ * (0: equal ranges), the other ranges share the rest equally. */
 int gx_context_set_copy_parts(gx_context* ctx, int parts, double first_share);
 
 /* A plan fixes a quartet list (its class-sorted task list and packed
