@@ -1537,14 +1537,15 @@ PlanData& lookup_plan(gx_context* ctx, gx_basis* b, uint64_t h1, uint64_t h2, in
     return *lookup_parts(ctx, b, h1, h2, count, entries, 1, std::forward<Make>(make)).parts[0];
 }
 
-// Host-output calls of at least kOverlapEntries complex elements (1 GiB)
-// into page-locked memory are evaluated as kAutoCopyParts input ranges, the
-// first holding kAutoFirstShare of the output, its copy overlapping the
-// evaluation of the second.  Measured on the 12-atom molecule (4.2 GB, calls
-// of 77.7 ms unsplit): two equal ranges 75.9 ms, first share 0.6 / 0.7 / 0.8
+// Host-output calls into page-locked memory copy each class's blocks as the
+// class finishes (through the mapped address).  Where the buffer has no
+// usable mapped address, outputs of at least kOverlapEntries complex elements
+// (1 GiB) are evaluated as kAutoCopyParts input ranges instead, the first
+// holding kAutoFirstShare of the output, its copy overlapping the evaluation
+// of the second.  Ranges measured on the 12-atom molecule (4.2 GB, calls of
+// 77.7 ms unsplit): two equal ranges 75.9 ms, first share 0.6 / 0.7 / 0.8
 // 74.2 / 73.5 / 74.1 ms, three or four ranges 75-77 ms (the split costs
-// kernel time, the overlapped copy a little more).  gx_context_set_copy_parts
-// overrides both.
+// kernel time); per-class copies 67.8 ms.  gx_context_set_copy_parts chooses.
 constexpr int64_t kOverlapEntries = int64_t(1) << 26;
 constexpr int kAutoCopyParts = 2;
 constexpr double kAutoFirstShare = 0.7;
