@@ -86,6 +86,11 @@ def test_api_validation_before_device_work():
     # the streaming entry point refuses a null consumer before it needs a device
     rc = nat.lib().gx_eri_for_each(None, None, None, None, None, 0, 0, 0.0, 0.0, nat.QUARTET_CONSUMER(), None, None)
     assert rc == -1 and "must not be null" in nat.last_error()
+    consumer = nat.QUARTET_CONSUMER(lambda blk, user: 0)
+    rc = nat.lib().gx_eri_for_each(None, None, None, None, None, 0, 0, 0.0, 0.0, consumer, None, None)
+    assert rc == -1 and "null context or basis" in nat.last_error()
+    # host-output copy modes: argument checks before any device work
+    assert nat.lib().gx_context_set_copy_parts(None, 0, 0.0) == -1
 
 
 def test_no_cpu_fallback_without_a_device():
