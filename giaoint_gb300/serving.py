@@ -12,7 +12,11 @@ fields of different sizes with continuous batching:
   footprint fits in what the in-flight requests leave of the HBM budget;
   requests that arrive while others run are admitted the moment a slot and
   memory free up, in arrival order (a request that cannot fit even an empty
-  budget fails with ``MemoryError``);
+  budget fails with ``MemoryError``), with one exception: long requests
+  (Cholesky factorisations, seconds for large molecules) hold at most
+  ``long_slots`` slots (default ``slots - 1``), and while they do, ERI
+  requests pass the Cholesky requests queued ahead of them, so a burst of
+  factorisations cannot block the short ERI requests behind it;
 * ERI requests waiting together are packed: the slot that takes an ERI
   request also takes the ERI requests queued right behind it (up to ``pack``
   requests and ``pack_entries`` entries, each fitting the budget) and runs
@@ -113,11 +117,17 @@ class Server:
     def __init__(self, slots: int = 4, *, hbm_budget: int | None = None, precision: str = "fp64",
                  mixed_cutoff: float = 1e-6, device: int = 0, runner=None, bases_per_slot: int = 32,
                  max_request_bytes: int | None = None, pack: int = 8, pack_entries: int = 1 << 26,
-                 pack_runner=None):
+                 pack_runner=None, long_slots: int | None = None):
         if slots < 1:
             raise ValueError("slots must be a positive integer")
         if pack < 1:
             raise ValueError("pack must be a positive integer")
+        # slots that Cholesky requests may hold at once (the rest stay free for
+        # ERI requests, which then pass queued Cholesky requests)
+        self.long_slots = max(1, slots - 1) if long_slots is None else int(long_slots)
+        if not 1 <= self.long_slots <= slots:
+            raise ValueError("long_slots must be in [1, slots]")
+        self._long = 0  # Cholesky requests in flight
         # ERI requests waiting together are packed into one class-sorted
         # execution: up to `pack` requests and `pack_entries` complex entries
         self.pack = int(pack)
@@ -217,26 +227,44 @@ class Server:
         self.close()
 
     # ---- scheduling -----------------------------------------------------------
+    def _pick(self) -> int | None:
+        """Queue index of the request to admit now, or None: the oldest
+        request once it fits, unless it is a Cholesky request while Cholesky
+        requests already hold ``long_slots`` slots; then the oldest ERI
+        request, once it fits (called with the lock held)."""
+        if not self._queue:
+            return None
+        i = 0
+        if self._queue[0].request.kind != "eri" and self._long >= self.long_slots:
+            i = next((k for k, p in enumerate(self._queue) if p.request.kind == "eri"), None)
+            if i is None:
+                return None
+        return i if self._reserved + self._queue[i].footprint <= self.hbm_budget else None
+
     def _take(self) -> list[_Pending] | None:
-        """Admit the oldest request once it fits, and with an ERI request the
+        """Admit the request ``_pick`` chooses, and with an ERI request the
         ERI requests queued right behind it that fit too, up to the pack
         limits (called with the lock held)."""
         while True:
-            if self._queue and self._reserved + self._queue[0].footprint <= self.hbm_budget:
-                batch = [self._queue.popleft()]
+            i = self._pick()
+            if i is not None:
+                batch = [self._queue[i]]
+                del self._queue[i]
                 entries = _entries(batch[0].request)
-                while (batch[0].request.kind == "eri" and len(batch) < self.pack and self._queue
-                       and self._queue[0].request.kind == "eri"
-                       and entries + _entries(self._queue[0].request) <= self.pack_entries
-                       and self._reserved + sum(b.footprint for b in batch) + self._queue[0].footprint
+                while (batch[0].request.kind == "eri" and len(batch) < self.pack and i < len(self._queue)
+                       and self._queue[i].request.kind == "eri"
+                       and entries + _entries(self._queue[i].request) <= self.pack_entries
+                       and self._reserved + sum(b.footprint for b in batch) + self._queue[i].footprint
                        <= self.hbm_budget):
-                    entries += _entries(self._queue[0].request)
-                    batch.append(self._queue.popleft())
+                    entries += _entries(self._queue[i].request)
+                    batch.append(self._queue[i])
+                    del self._queue[i]
                 now = self.now()
                 for p in batch:
                     p.admitted = now
                     self._reserved += p.footprint
                     self._inflight += 1
+                    self._long += p.request.kind != "eri"
                 self.max_inflight = max(self.max_inflight, self._inflight)
                 self.max_reserved = max(self.max_reserved, self._reserved)
                 self.max_pack = max(self.max_pack, len(batch))
@@ -270,6 +298,7 @@ class Server:
                     c.finished = finished
                     self._reserved -= p.footprint
                     self._inflight -= 1
+                    self._long -= p.request.kind != "eri"
                 self._cv.notify_all()
             for c, p in zip(cs, batch):
                 if c.error is not None:

@@ -1,5 +1,6 @@
 """Host logic of the serving loop (no GPU): admission by device footprint,
-arrival-order admission, overlap up to the slot count, rejection of requests
+arrival-order admission, overlap up to the slot count, the slot kept for ERI
+requests while Cholesky requests hold the others, rejection of requests
 larger than the whole budget, latency summary."""
 
 from __future__ import annotations
@@ -40,7 +41,7 @@ def test_admission_respects_budget_slots_and_arrival_order():
             live["bytes"] -= fp
         return req.kind, 10
 
-    with Server(slots=3, hbm_budget=budget, runner=runner) as srv:
+    with Server(slots=3, hbm_budget=budget, runner=runner, long_slots=3) as srv:  # no slot kept for ERIs
         done = srv.run(reqs)
     assert all(c.error is None for c in done)
     assert live["max_bytes"] <= budget
@@ -139,3 +140,28 @@ def test_waiting_eri_requests_are_packed_cholesky_never():
     # arrival order is kept across packs
     kinds = [k for p in packs for k in p]
     assert kinds == [r.kind for r in reqs]
+
+
+def test_eri_requests_pass_cholesky_requests_beyond_the_long_slots():
+    """With two slots, Cholesky requests hold at most one: a second Cholesky
+    request waits, and an ERI request queued behind it is admitted at once on
+    the free slot and finishes first."""
+    reqs = syn.serving_requests(count=16, rate=400.0, seed=5, atoms=(3, 5), max_entries=1 << 16,
+                                cholesky_fraction=0.5, cholesky_atoms=(3, 3))
+    chol = [r for r in reqs if r.kind == "cholesky"][:2]
+    eri = [r for r in reqs if r.kind == "eri"][:1]
+    assert len(chol) == 2 and len(eri) == 1
+
+    def runner(slot, r):
+        time.sleep(0.3 if r.kind == "cholesky" else 0.0)
+        return r.kind, 1
+
+    with Server(slots=2, hbm_budget=1 << 50, runner=runner) as srv:
+        assert srv.long_slots == 1
+        futs = [srv.submit(chol[0], 0), srv.submit(chol[1], 1), srv.submit(eri[0], 2)]
+        a, b, c = (f.result(timeout=10) for f in futs)
+    assert c.admitted < b.admitted  # the ERI request passed the waiting Cholesky request
+    assert c.finished < a.finished
+    assert b.admitted >= a.finished - 1e-3  # the second Cholesky request waited for the first
+    with pytest.raises(ValueError, match="long_slots"):
+        Server(slots=2, long_slots=3, runner=lambda s_, r: (None, 0))
