@@ -41,7 +41,7 @@ def test_admission_respects_budget_slots_and_arrival_order():
             live["bytes"] -= fp
         return req.kind, 10
 
-    with Server(slots=3, hbm_budget=budget, runner=runner, long_slots=3) as srv:  # no slot kept for ERIs
+    with Server(slots=3, hbm_budget=budget, runner=runner) as srv:
         done = srv.run(reqs)
     assert all(c.error is None for c in done)
     assert live["max_bytes"] <= budget
@@ -156,7 +156,7 @@ def test_eri_requests_pass_cholesky_requests_beyond_the_long_slots():
         time.sleep(0.3 if r.kind == "cholesky" else 0.0)
         return r.kind, 1
 
-    with Server(slots=2, hbm_budget=1 << 50, runner=runner) as srv:
+    with Server(slots=2, hbm_budget=1 << 50, runner=runner, long_slots=1) as srv:
         assert srv.long_slots == 1
         futs = [srv.submit(chol[0], 0), srv.submit(chol[1], 1), srv.submit(eri[0], 2)]
         a, b, c = (f.result(timeout=10) for f in futs)
