@@ -1409,6 +1409,11 @@ __global__ void class_copy_kernel(const Task* __restrict__ tasks, int ntask, int
     const int per = na * nb * ncd;
     for (int t = warp; t < ntask; t += nwarps) {
         const Task tk = tasks[t];
+        if (tk.st[3] == 1 && tk.st[2] == nd && tk.st[1] == ncd && tk.st[0] == nb * ncd) {
+            // the task's entries are one contiguous run (an unsegmented block)
+            for (int e = lane; e < per; e += 32) dst[tk.out_off + e] = __ldcs(src + tk.out_off + e);
+            continue;
+        }
         for (int e = lane; e < per; e += 32) {
             const int ab = e / ncd, cd = e - ab * ncd;
             const int ca = ab / nb, cb = ab - ca * nb, cc = cd / nd, cdd = cd - cc * nd;
