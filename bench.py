@@ -893,6 +893,7 @@ def run_gpu(args):
                "cold_call_seconds": cold_s, "cold_h2d_bytes": int(ntask.value * 48 + 48),
                "d2h_copy_seconds": d2h_s, "d2h_gb_per_s": total * 16 / d2h_s / 1e9,
                "api": "gx_eri_batch (C ABI, pinned host buffers)", "max_abs_diff_vs_device_path": e2e_diff,
+               "copy": "each class's blocks copied by the SMs to the page-locked output as the class finishes",
                "call_seconds": times, "call_seconds_median": float(statistics.median(times)),
                "call_kernel_ms": kernel_ms,
                "call_prepare_ms": prepare_ms,
