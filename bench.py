@@ -97,6 +97,8 @@ def parse():
     p.add_argument("--serving-requests", type=int, default=32)
     p.add_argument("--serving-request-gib", type=float, default=6.0,
                    help="per-request device-memory limit of the serving leg (estimated footprint; GiB)")
+    p.add_argument("--profile-e2e", action="store_true",
+                   help="three gx_eri_batch host-output calls, the third inside an NVTX range 'call', then exit")
     p.add_argument("--profile-step", default="", choices=["", "fp64", "mixed", "fp64_exact"],
                    help="run warm-up steps and one step of this mode inside an NVTX range, then exit (profiling)")
     p.add_argument("--sweep", type=int, default=64,
@@ -785,6 +787,30 @@ def run_gpu(args):
                                          ctypes.byref(f32)))
         return ms, clock_info, (n64.value, n32.value, f64.value, f32.value)
 
+    if args.profile_e2e:
+        # three host-output calls through the C ABI into page-locked memory,
+        # the third inside an NVTX range "call" (for an ncu capture of every
+        # launch of one end-to-end call: --nvtx --nvtx-include "call/")
+        nat.check(lib.gx_context_set_stream(ctx.handle, None))
+        host = torch.empty(2 * total, dtype=torch.float64, pin_memory=True)
+        hq = torch.from_numpy(quartets.view(np.int32)).pin_memory()
+        off2 = np.zeros(nq + 1, dtype=np.int64)
+        prec = {"fp64": 0, "mixed": 1}[args.precision]
+
+        def call():
+            nat.check(lib.gx_eri_batch(ctx.handle, bh, nat.dptr(Bv), nat.dptr(Ov),
+                                       ctypes.cast(hq.data_ptr(), ctypes.POINTER(ctypes.c_uint32)), nq, prec,
+                                       args.mixed_cutoff, 0.0, None, nat.i64ptr(off2),
+                                       ctypes.cast(host.data_ptr(), ctypes.POINTER(ctypes.c_double)), total, None))
+
+        call()
+        call()
+        torch.cuda.nvtx.range_push("call")
+        call()
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"profile_e2e": args.precision}), flush=True)
+        lib.gx_eri_plan_destroy(plan)
+        return
     if args.profile_step:
         # one step of one mode inside an NVTX range "step" (for an ncu capture
         # of every class launch of the step: --nvtx --nvtx-include "step/")
