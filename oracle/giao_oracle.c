@@ -391,7 +391,13 @@ static int ws_raux(ws_t* w, size_t n) {
     return 0;
 }
 
-static int eri_kernel(const prim_t* pr, const pair_t* ab, const pair_t* cd, int real_zero, ws_t* w, cplx* result) {
+/* hin (may be NULL): the 1-D Hermite coefficients of the six axes (bra x, y,
+ * z, then ket x, y, z) computed beforehand by hermite_1d with the same
+ * arguments, so that callers looping over primitive and Cartesian
+ * combinations compute each once (the reference keeps them in a cache,
+ * src/eri.cpp:107-160). */
+static int eri_kernel_h(const prim_t* pr, const pair_t* ab, const pair_t* cd, int real_zero, ws_t* w,
+                        const double* const* hin, cplx* result) {
     int maxima[6];
     for (int i = 0; i < 3; ++i) {
         maxima[i] = pr[0].ang[i] + pr[1].ang[i];
@@ -412,14 +418,21 @@ static int eri_kernel(const prim_t* pr, const pair_t* ab, const pair_t* cd, int 
         const prim_t* l = &pr[2 * pi];
         const prim_t* r = &pr[2 * pi + 1];
         const pair_t* pd = pi ? cd : ab;
-        for (int ax = 0; ax < 3; ++ax)
-            hermite_1d(l->ang[ax], r->ang[ax], l->center[ax], r->center[ax], pd->P[ax], pd->p, herm[3 * pi + ax]);
+        const double* hx[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            if (hin) {
+                hx[ax] = hin[3 * pi + ax];
+            } else {
+                hermite_1d(l->ang[ax], r->ang[ax], l->center[ax], r->center[ax], pd->P[ax], pd->p, herm[3 * pi + ax]);
+                hx[ax] = herm[3 * pi + ax];
+            }
+        }
         const int xe = maxima[3 * pi] + 1, ye = maxima[3 * pi + 1] + 1, ze = maxima[3 * pi + 2] + 1;
         prod[pi] = prodbuf[pi];
         for (int x = 0; x < xe; ++x)
             for (int y = 0; y < ye; ++y)
                 for (int zz = 0; zz < ze; ++zz)
-                    prod[pi][(x * ye + y) * ze + zz] = herm[3 * pi][x] * herm[3 * pi + 1][y] * herm[3 * pi + 2][zz];
+                    prod[pi][(x * ye + y) * ze + zz] = hx[0][x] * hx[1][y] * hx[2][zz];
     }
 
     const double p = ab->p, q = cd->p;
@@ -556,6 +569,25 @@ static int eri_kernel(const prim_t* pr, const pair_t* ab, const pair_t* cd, int 
     return 0;
 }
 
+static int eri_kernel(const prim_t* pr, const pair_t* ab, const pair_t* cd, int real_zero, ws_t* w, cplx* result) {
+    return eri_kernel_h(pr, ab, cd, real_zero, w, NULL, result);
+}
+
+/* 1-D Hermite coefficients of a primitive pair for every pair of axis powers
+ * (a <= la, b <= lb) on each axis: h[((ax * (la + 1) + a) * (lb + 1) + b) *
+ * (la + lb + 1) + t]. */
+static double* pair_hermite_cache(int la, int lb, const double* A, const double* Bc, const pair_t* pd) {
+    const size_t stride = (size_t)(la + lb + 1);
+    double* h = (double*)malloc(sizeof(double) * 3 * (size_t)(la + 1) * (size_t)(lb + 1) * stride);
+    if (!h) return NULL;
+    for (int ax = 0; ax < 3; ++ax)
+        for (int a = 0; a <= la; ++a)
+            for (int b = 0; b <= lb; ++b)
+                hermite_1d(a, b, A[ax], Bc[ax], pd->P[ax], pd->p,
+                           h + (((size_t)ax * (la + 1) + a) * (lb + 1) + b) * stride);
+    return h;
+}
+
 /* primitive_eri (src/eri.cpp:438-452) with the primitive's own coefficient
  * and optional normalisation (src/eri.cpp:371-383). */
 int or_primitive_eri(const double* exps, const double* centers, const int* angular, const double* coefs,
@@ -677,14 +709,26 @@ static int shell_quartet(const basis_t* bs, const int* sh, const field_t* f, ws_
     const double* D = bs->centers + 3 * sd;
     int rc = 0;
     w->boys_valid = 0;
+    const int la = bs->ls[sa], lb = bs->ls[sb], lc = bs->ls[sc], ld = bs->ls[sd];
+    const size_t sab = (size_t)(la + lb + 1), scd = (size_t)(lc + ld + 1);
     for (int pa = 0; pa < bs->nprims[sa] && !rc; ++pa)
         for (int pb = 0; pb < bs->nprims[sb] && !rc; ++pb) {
             pair_t ab;
             gaussian_product(bs->exps[bs->eoff[sa] + pa], A, bs->exps[bs->eoff[sb] + pb], Bc, f, &ab);
+            double* hab = pair_hermite_cache(la, lb, A, Bc, &ab);
+            if (!hab) {
+                rc = set_err(-3, "out of memory");
+                break;
+            }
             for (int pc = 0; pc < bs->nprims[sc] && !rc; ++pc)
                 for (int pd = 0; pd < bs->nprims[sd] && !rc; ++pd) {
                     pair_t cd;
                     gaussian_product(bs->exps[bs->eoff[sc] + pc], C, bs->exps[bs->eoff[sd] + pd], D, f, &cd);
+                    double* hcd = pair_hermite_cache(lc, ld, C, D, &cd);
+                    if (!hcd) {
+                        rc = set_err(-3, "out of memory");
+                        break;
+                    }
                     const int pidx[4] = {pa, pb, pc, pd};
                     for (int ca = 0; ca < nc[0] && !rc; ++ca)
                         for (int cb = 0; cb < nc[1] && !rc; ++cb)
@@ -700,8 +744,15 @@ static int shell_quartet(const basis_t* bs, const int* sh, const field_t* f, ws_
                                             pr[k].ang[x] = comps[k][cix[k]][x];
                                         }
                                     }
+                                    const double* hin[6];
+                                    for (int ax = 0; ax < 3; ++ax) {
+                                        hin[ax] = hab + (((size_t)ax * (la + 1) + comps[0][ca][ax]) * (lb + 1) +
+                                                         comps[1][cb][ax]) * sab;
+                                        hin[3 + ax] = hcd + (((size_t)ax * (lc + 1) + comps[2][cc][ax]) * (ld + 1) +
+                                                             comps[3][cdd][ax]) * scd;
+                                    }
                                     cplx val;
-                                    rc = eri_kernel(pr, &ab, &cd, real_zero, w, &val);
+                                    rc = eri_kernel_h(pr, &ab, &cd, real_zero, w, hin, &val);
                                     if (rc) break;
                                     for (int k = 0; k < 4; ++k)
                                         val *= norms[k][cix[k] * bs->nprims[sh[k]] + pidx[k]];
@@ -726,7 +777,9 @@ static int shell_quartet(const basis_t* bs, const int* sh, const field_t* f, ws_
                                         }
                                     }
                                 }
+                    free(hcd);
                 }
+            free(hab);
         }
     for (int k = 0; k < 4; ++k) free(norms[k]);
     return rc;
